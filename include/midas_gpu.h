@@ -1,0 +1,198 @@
+/*
+ * midas_gpu.h -- C ABI of the GB300 (sm_103a) MIDAS VIE-MoM / CBFM hot path.
+ *
+ * This library replaces the solver layer of nasa-jpl/MIDAS: the subroutines
+ * Compute_EFields_MoM (src/Compute_EFields_MoM.f90:1) and
+ * Compute_EFields_CBFME / Compute_EFields_CBFME_ACA
+ * (src/Compute_EFields_CBFME.f90:1, src/Compute_EFields_CBFME_ACA.f90:1),
+ * together with the kernels they call (src/Green_functions.f90,
+ * src/Incident_Field.f90, src/Calcul_ACA_matrices.f90,
+ * src/getParameters_CBFM.f90) and the MKL ScaLAPACK / PARDISO / GESVD / ZGEMM
+ * calls they make.  Each entry point below names the reference interface it
+ * stands in for.
+ *
+ * Conventions (identical to the reference's Fortran arrays):
+ *   - complex numbers are interleaved (re, im) doubles, i.e. C `double _Complex`
+ *     or Fortran `complex(c_double_complex)`;
+ *   - matrices are column-major; the unknown index of cell c and component
+ *     p in {x, y, z} is 3c + p (3(c-1)+p, 1-based, in Fortran);
+ *   - RHS / field column t is the V polarisation of incident direction t and
+ *     column t + ntr its H polarisation (src/Compute_EFields_MoM.f90:557-563);
+ *   - angles are in degrees, measured as the reference does: the incident
+ *     wave vector is k0 (cos th, sin th cos ph, sin th sin ph)
+ *     (src/Incident_Field.f90:32-34);
+ *   - index arrays (cell lists, block offsets) use the base given in
+ *     midas_gpu_opts.index_base (1 for Fortran callers);
+ *   - array arguments may be host or device pointers; the library detects
+ *     device memory and then copies nothing;
+ *   - every call is synchronous, returns a MIDAS_* status and never aborts
+ *     the process (the reference stops with `stop 1` / MPI_ERRORS_ARE_FATAL).
+ * One host thread per context; the context owns its CUDA stream.
+ */
+#ifndef MIDAS_GPU_H
+#define MIDAS_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum midas_status {
+    MIDAS_OK = 0,
+    MIDAS_ERR_ARG = 1,            /* invalid argument (size, pointer, option) */
+    MIDAS_ERR_CUDA = 2,           /* CUDA runtime / library failure */
+    MIDAS_ERR_ALLOC = 3,          /* device allocation failed */
+    MIDAS_ERR_SINGULAR = 4,       /* zero pivot ("SINGULAR MATRIX", src/Compute_EFields_MoM.f90:178-181) */
+    MIDAS_ERR_NOT_CONVERGED = 5,  /* iterative refinement did not reach ir_tol */
+    MIDAS_ERR_STATE = 6,          /* call order: e.g. solve before midas_gpu_set_cells */
+    MIDAS_ERR_DEVICE_TIMEOUT = 7, /* a bounded device-side wait expired (kernel returned early) */
+    MIDAS_ERR_UNSUPPORTED = 8     /* device is not sm_103 / feature unavailable */
+};
+
+/* Dense-solve arithmetic. */
+enum midas_solve_mode {
+    MIDAS_SOLVE_MIXED = 0,  /* TF32 tensor-core LU (tcgen05) + FP64-residual iterative refinement */
+    MIDAS_SOLVE_FP64 = 1    /* plain FP64 LU with partial pivoting (cuSOLVER zgetrf/zgetrs): the baseline */
+};
+
+/* Arithmetic of the complex(4)-local fills (Green_s_tr_partial & co). */
+enum midas_fill_mode {
+    MIDAS_FILL_FAITHFUL = 0, /* reference rounding: FP64 internals rounded to float where the reference rounds */
+    MIDAS_FILL_FAST = 1      /* lattice-offset table when the cells lie on one uniform grid */
+};
+
+typedef struct midas_gpu_ctx midas_gpu_ctx;
+
+typedef struct {
+    int struct_size;   /* sizeof(midas_gpu_opts) */
+    int device;        /* CUDA device ordinal (default 0) */
+    int index_base;    /* 0 (C) or 1 (Fortran) */
+    int solve_mode;    /* enum midas_solve_mode (default MIXED) */
+    int fill_mode;     /* enum midas_fill_mode (default FAITHFUL) */
+    int ir_max_iter;   /* refinement cap (default 30) */
+    double ir_tol;     /* refinement stops when ||b - Z x||_inf <= ir_tol * (||Z||_inf ||x||_inf + ||b||_inf)
+                          (default 1e-13) */
+    int verbose;       /* 0: silent */
+} midas_gpu_opts;
+
+typedef struct {
+    int status;             /* same as the return value */
+    int ir_iters;           /* refinement steps of the last dense solve */
+    double backward_error;  /* final normwise backward error of the last dense solve */
+    double anorm;           /* ||Z||_inf (PZLANGE 'I', src/Compute_EFields_MoM.f90:168) */
+    int k_total;            /* CBFM: total number of CBFs (K_total, src/Compute_EFields_CBFME.f90:472) */
+    int n_far_aca;          /* CBFM+ACA: block pairs represented by ACA factors */
+    double t_fill_ms;       /* device time of the fills */
+    double t_factor_ms;     /* device time of the factorisations */
+    double t_solve_ms;      /* device time of solves + refinement */
+    double t_total_ms;      /* wall time of the call */
+} midas_gpu_info;
+
+/* Fill *o with the defaults listed above. */
+void midas_gpu_default_opts(midas_gpu_opts *o);
+
+/* Create a context on opts->device (NULL opts = defaults).  Replaces the MPI /
+ * BLACS set-up of the reference (src/Main_Scattering.f90:226, src/Compute_EFields_MoM.f90:112-123). */
+int midas_gpu_init(const midas_gpu_opts *opts, midas_gpu_ctx **ctx);
+int midas_gpu_free(midas_gpu_ctx *ctx);
+/* Message of the last failure on this context ("" when none). */
+const char *midas_gpu_last_error(const midas_gpu_ctx *ctx);
+
+/* Cells of the scatterer for one frequency: centroids, edge Sc, relative
+ * permittivity, and k0 = 2 pi / lambda.  Computes a_n, Che = eps - 1, Znnpp and
+ * kappa on the device exactly as SetCellsParams (src/SetCellsParams.f90:31-49). */
+int midas_gpu_set_cells(midas_gpu_ctx *ctx, int n, const double *xc, const double *yc, const double *zc,
+                        const double *sc, const double *eps_re, const double *eps_im, double k0);
+/* Read back the per-cell parameters (any output may be NULL); che/znnpp are complex (2n doubles). */
+int midas_gpu_get_cell_params(midas_gpu_ctx *ctx, double *a_n, double *che, double *znnpp, double *kappa);
+
+/* Rows [r0, r0+nr) x columns [c0, c0+nc) (0-based unknown indices) of the FP64
+ * MoM matrix, column-major nr x nc: compute_Green_s_tr_single_element
+ * (src/Compute_EFields_MoM.f90:433-523). */
+int midas_gpu_mom_fill(midas_gpu_ctx *ctx, int r0, int nr, int c0, int nc, double *Z);
+/* FP64 right-hand sides, 3n x 2ntr: Incident_Field_single_element
+ * (src/Compute_EFields_MoM.f90:529-598). */
+int midas_gpu_mom_rhs(midas_gpu_ctx *ctx, int ntr, const double *theta, const double *phi, double *V);
+/* Incident field with the reference's complex(4) locals on the cells idx[0..ncell)
+ * (idx NULL = all cells), 3ncell x 2ntr: Incident_Field (src/Incident_Field.f90:1-63). */
+int midas_gpu_incident_field(midas_gpu_ctx *ctx, int ncell, const int *idx, int ntr, const double *theta,
+                             const double *phi, double *E);
+/* Block-pair interaction matrix 3n1 x 3n2 (complex(4)-rounded values stored in
+ * complex(8)): Green_s_tr_partial (src/Green_functions.f90:96-173). */
+int midas_gpu_block_fill(midas_gpu_ctx *ctx, int n1, const int *idx1, int n2, const int *idx2, double *Z);
+/* Dense form of the thresholded extended-block matrix handed to PARDISO:
+ * SR_Green_s_tr_partial (src/Green_functions.f90:290-562).  Z (3s x 3s) may be
+ * NULL; *nnz receives the kept-entry count and *fn (may be NULL) the Frobenius
+ * norm of the kept entries (SR_Green_s_tr_partial_FN, :564-806). */
+int midas_gpu_sr_fill(midas_gpu_ctx *ctx, int s, const int *idx, double fsr, int homog, double *Z,
+                      long long *nnz, double *fn);
+/* fSR ladder of setfSR (src/getParameters_CBFM.f90:113-168). */
+int midas_gpu_set_fsr(midas_gpu_ctx *ctx, int s, const int *idx, int homog, double res_sr, double *fsr,
+                      long long *nnz);
+/* Partial-pivot ACA of the unknown block [row0,row0+nrows) x [col0,col0+ncols)
+ * (0-based, multiples of 3): Calcul_MatrixZij_ACA (src/Calcul_ACA_matrices.f90:6-219).
+ * U is nrows x itmax, V is itmax x ncols (column-major); *rank = nb_iter_out. */
+int midas_gpu_aca(midas_gpu_ctx *ctx, int row0, int nrows, int col0, int ncols, double eps, int itmax,
+                  double *U, double *V, int *rank);
+
+/* Dense complex solve A X = B (A n x n, B n x nrhs, column-major; B is
+ * overwritten by X) with the context's solve_mode.  Stands in for PZGESV
+ * (src/Compute_EFields_MoM.f90:173, src/Compute_EFields_CBFME.f90:912). */
+int midas_gpu_dense_solve(midas_gpu_ctx *ctx, int n, int nrhs, const double *A, double *B,
+                          midas_gpu_info *info);
+
+/* Plain MoM: fill, solve, internal field E (3n x 2ntr).  The field part of
+ * Compute_EFields_MoM (src/Compute_EFields_MoM.f90:66-229). */
+int midas_gpu_mom_solve(midas_gpu_ctx *ctx, int ntr, const double *theta, const double *phi, double *E,
+                        midas_gpu_info *info);
+
+/* CBFM-E flags. */
+enum midas_cbfm_flags {
+    MIDAS_CBFM_SR = 1,      /* threshold the extended-block matrices (SR = 1, the reference default) */
+    MIDAS_CBFM_HOMOG = 2,   /* homogeneous scatterer (homogs = 1): PARDISO mtype 6 symmetric storage */
+    MIDAS_CBFM_ACA = 4,     /* off-diagonal reduced blocks from ACA factors (Use_ACA = 1) */
+    MIDAS_CBFM_FAST_CBF = 8 /* CBF block solves refined with an FP32-grade residual instead of double-float */
+};
+
+/* CBFM-E solve: Compute_EFields_CBFME (src/Compute_EFields_CBFME.f90:1-1006) or,
+ * with MIDAS_CBFM_ACA, Compute_EFields_CBFME_ACA.
+ *   cells are ordered by block: block b owns cells blk_offsets[b]..blk_offsets[b+1]-1;
+ *   ext_offsets (nblocks+1) / ext_idx list the extension cells of each block
+ *   (CBFM_Blocks_Ext, src/Extend_blocks.f90:134);
+ *   ncbf directions (cbf_theta/cbf_phi) are the CBF excitations
+ *   (getTransmitters_CBFM, src/getParameters_CBFM.f90:1-110);
+ *   thr_cbf is Threshold_CBFM (<= 0: the reference rule of :286-288);
+ *   res_sr is res_SR (<= 0: the reference default);
+ *   E (3n x 2ntr) receives the internal field, K (nblocks, may be NULL) the CBF counts. */
+int midas_gpu_cbfm_solve(midas_gpu_ctx *ctx, int nblocks, const int *blk_offsets, const int *ext_offsets,
+                         const int *ext_idx, int ncbf, const double *cbf_theta, const double *cbf_phi,
+                         double thr_cbf, double res_sr, int flags, double eps_aca, int aca_itmax, int ntr,
+                         const double *theta, const double *phi, double *E, int *K, midas_gpu_info *info);
+
+/* Extinction and absorption cross sections from the internal field
+ * (Compute_ExtAbsCsec_fromIntField, src/Compute_ExtAbsCsec_fromIntField.f90:45-64). */
+int midas_gpu_cext_cabs(midas_gpu_ctx *ctx, int ntr, const double *theta, const double *phi, const double *E,
+                        double *cext, double *cabs);
+/* Far-field scattering matrix, nrx x 4ntr (Vv, Vh, Hv, Hh per direction):
+ * GetFFieldCoeff + projection (src/Green_functions.f90:1399-1438,
+ * src/Compute_EFields_MoM.f90:306-369). */
+int midas_gpu_smatrix(midas_gpu_ctx *ctx, int nrx, const double *rx_theta, const double *rx_phi, int ntr,
+                      const double *E, double *S);
+
+/* Diagnostics (no counterpart in the reference). */
+/* Device self-test of the tensor-core GEMM engine against a CUDA-core GEMM on a
+ * ragged problem; returns MIDAS_OK when they agree to TF32 accuracy. */
+int midas_gpu_gemm_selftest(midas_gpu_ctx *ctx);
+/* Name of the GEMM engine in use ("tcgen05"). */
+const char *midas_gpu_gemm_engine(void);
+/* Average device time (CUDA events on the context stream) of `iters` launches of
+ * the tensor-core GEMM D[M x N] -= A[M x K] Bt[N x K]^T on internal buffers (fp32). */
+int midas_gpu_bench_gemm(midas_gpu_ctx *ctx, int M, int N, int K, int iters, double *ms);
+/* Number of kernels this context has launched so far. */
+long long midas_gpu_launch_count(const midas_gpu_ctx *ctx);
+/* The context's CUDA stream (a cudaStream_t): every kernel of the context runs on it. */
+void *midas_gpu_stream(const midas_gpu_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MIDAS_GPU_H */

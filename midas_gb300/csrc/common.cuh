@@ -1,0 +1,109 @@
+// common.cuh -- shared definitions of the GB300 MIDAS library (internal).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/midas_gpu.h"
+
+namespace midas {
+
+// ---------------------------------------------------------------------------
+// status plumbing: every internal call returns a midas_status; the first
+// failure message is kept on the context.
+// ---------------------------------------------------------------------------
+struct Err {
+    int code = MIDAS_OK;
+    std::string msg;
+    int set(int c, const std::string &m) {
+        if (code == MIDAS_OK) { code = c; msg = m; }
+        return c;
+    }
+};
+
+#define MIDAS_CUDA(ctx, expr)                                                                      \
+    do {                                                                                           \
+        cudaError_t _e = (expr);                                                                   \
+        if (_e != cudaSuccess)                                                                     \
+            return (ctx)->err.set(_e == cudaErrorMemoryAllocation ? MIDAS_ERR_ALLOC : MIDAS_ERR_CUDA, \
+                                  std::string(#expr) + ": " + cudaGetErrorString(_e));             \
+    } while (0)
+
+#define MIDAS_TRY(expr)                  \
+    do {                                 \
+        int _s = (expr);                 \
+        if (_s != MIDAS_OK) return _s;   \
+    } while (0)
+
+// Device error flags (written by kernels that hit a bounded wait or a bad pivot).
+enum DevErr : int { DEV_OK = 0, DEV_TIMEOUT = 1, DEV_ZERO_PIVOT = 2, DEV_BAD_ARG = 4 };
+
+// Reference Pi = Acos(-1.) evaluated in single precision (src/Initialization.f90:39).
+inline double ref_pi_host() { return (double)acosf(-1.0f); }
+
+// ---------------------------------------------------------------------------
+// device buffers
+// ---------------------------------------------------------------------------
+struct DBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+};
+
+}  // namespace midas
+
+// The context (opaque in the C ABI).
+struct midas_gpu_ctx {
+    midas_gpu_opts opts;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    midas::Err err;
+    double pi = 0;
+    // cells
+    int n = 0;
+    double k0 = 0;
+    double *x = nullptr, *y = nullptr, *z = nullptr, *sc = nullptr, *an = nullptr, *kappa = nullptr;
+    double2 *eps = nullptr, *che = nullptr, *znnpp = nullptr;
+    float2 *fk4 = nullptr;   // f_kapChe rounded to complex(4), per cell
+    double2 *fk8 = nullptr;  // f_kapChe in complex(8), per cell
+    // uniform-lattice description of the cells (fast fills)
+    int lattice = 0;         // 1 when all cells sit on one grid of pitch d
+    double lat_d = 0, lat_o[3] = {0, 0, 0};
+    int lat_lo[3] = {0, 0, 0}, lat_hi[3] = {0, 0, 0};
+    int *lat_ijk = nullptr;  // 3 ints per cell
+    float2 *lat_tab4 = nullptr;    // complex(4) dyad table per lattice offset (6 comps)
+    double2 *lat_tab8 = nullptr;   // FP64 dyad table per lattice offset (6 comps)
+    int lat_dim[3] = {0, 0, 0};
+    // scratch pool (grow-only, reused across calls)
+    std::vector<midas::DBuf> pool;
+    int *d_flag = nullptr;   // device error flag
+    long long launches = 0;  // kernels launched on this context
+    void *cusolver = nullptr;
+    void *cublas = nullptr;
+};
+
+namespace midas {
+
+// Scratch allocation helpers (pool slot i grows as needed).
+int ensure(midas_gpu_ctx *ctx, int slot, size_t bytes, void **out);
+
+// Is p a device (or managed) pointer?
+bool is_device_ptr(const void *p);
+
+// Copy-in helper: returns a device pointer holding `bytes` of p (p itself when it
+// already lives on the device); uses pool slot `slot`.
+int to_device(midas_gpu_ctx *ctx, const void *p, size_t bytes, int slot, const void **out);
+
+// Device error flag check after a kernel sequence.
+int check_flag(midas_gpu_ctx *ctx, const char *where);
+
+// Pool slots (fixed roles).
+enum Slot : int {
+    S_IN0 = 0, S_IN1, S_IN2, S_IN3, S_IN4, S_IN5, S_OUT0, S_OUT1,
+    S_Z32, S_Z64, S_LINV, S_UINV, S_BEXP, S_BEXP2, S_RHS64, S_X64, S_R64, S_T32, S_T32B, S_RED,
+    S_CBF0, S_CBF1, S_CBF2, S_CBF3, S_CBF4, S_CBF5, S_CBF6, S_CBF7, S_CBF8, S_CBF9,
+    S_NSLOTS
+};
+
+}  // namespace midas

@@ -1,0 +1,593 @@
+// fill.cu -- impedance fills and incident fields of the MIDAS VIE-MoM (sm_103a).
+//
+// The element arithmetic follows the reference routines cited at each kernel.
+// Two arithmetic families:
+//   * FP64 (MoM path): compute_Green_s_tr_single_element,
+//     Incident_Field_single_element (src/Compute_EFields_MoM.f90:433-598);
+//   * "complex(4) locals" (CBFM path): Green_s_tr_partial, SR_Green_s_tr_partial,
+//     computeBlockRow/Col (src/Green_functions.f90:96-1225) and Incident_Field
+//     (src/Incident_Field.f90:1-63): FP64 intermediates rounded to float exactly
+//     where the Fortran assigns to a Complex (kind 4) local, single-precision
+//     3.*Tau and complex(4) products evaluated without FMA (the reference's
+//     ifort -O3 x86-64 build has no FMA).
+//
+// When the cells sit on one uniform lattice (every configuration built by a
+// voxeliser does), the dyad F depends only on the integer lattice offset
+// between observation and source cell.  The "lattice" kernels evaluate F once
+// per offset into a table (FP64 and complex(4)-rounded) and the fills become a
+// gather plus one complex product per element, which turns the fill from
+// FP64/SFU-bound into HBM-bound on GB300.
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace midas {
+
+// ---------------------------------------------------------------------------
+// complex helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double2 zmul8(double2 a, double2 b)
+{
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// complex(8) product with every operation separately rounded (no FMA)
+__device__ __forceinline__ double2 zmul8_rn(double2 a, double2 b)
+{
+    return make_double2(__dsub_rn(__dmul_rn(a.x, b.x), __dmul_rn(a.y, b.y)),
+                        __dadd_rn(__dmul_rn(a.x, b.y), __dmul_rn(a.y, b.x)));
+}
+// complex(4) product with every float operation separately rounded (no FMA)
+__device__ __forceinline__ float2 zmul4_rn(float2 a, float2 b)
+{
+    return make_float2(__fsub_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)),
+                       __fadd_rn(__fmul_rn(a.x, b.y), __fmul_rn(a.y, b.x)));
+}
+
+// ---------------------------------------------------------------------------
+// a1: SetCellsParams (src/SetCellsParams.f90:31-49)
+// ---------------------------------------------------------------------------
+__global__ void k_set_cells(int n, const double *sc, const double2 *eps, double k0, double Pi, double *an,
+                            double2 *che, double2 *znnpp, double *kappa, double2 *fk8, float2 *fk4)
+{
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    const double third = (double)(1.0f / 3.0f);
+    const double two3 = (double)(2.0f / 3.0f);
+    double a = sc[c] * pow(0.75 / Pi, third);
+    double2 ch = make_double2(eps[c].x - 1.0, eps[c].y);
+    double ka = k0 * a;
+    double s, co;
+    sincos(ka, &s, &co);
+    double2 t = make_double2(two3 * co, two3 * s);
+    t = zmul8(t, make_double2(1.0, -ka));
+    t.x -= 1.0;
+    double2 zn = zmul8(t, ch);
+    double kap = 4 * Pi * (s - ka * co) / pow(k0, 3.0);
+    an[c] = a;
+    che[c] = ch;
+    znnpp[c] = zn;
+    kappa[c] = kap;
+    double2 f = make_double2(kap * ch.x, kap * ch.y);   // f_kapChe = Kappa_n*Che_n
+    fk8[c] = f;
+    fk4[c] = make_float2((float)f.x, (float)f.y);
+}
+
+// ---------------------------------------------------------------------------
+// dyads.  Component order of the six unique entries: xx, yy, zz, xy, yz, xz.
+// ---------------------------------------------------------------------------
+// FP64 F (before the -f_kapChe factor): src/Compute_EFields_MoM.f90:474-519.
+__device__ __forceinline__ void dyadF8(double rx, double ry, double rz, double k0, double Pi, double2 F[6])
+{
+    double r = sqrt(rx * rx + ry * ry + rz * rz);
+    double s, co;
+    sincos(k0 * r, &s, &co);
+    double den = 4 * Pi * (r * r);
+    double2 Gr = make_double2(co / den, s / den);
+    double2 Tau = make_double2(-(1 / r), k0);
+    double k2 = k0 * k0;
+    double d[3] = {rx, ry, rz};
+#pragma unroll
+    for (int p = 0; p < 3; ++p) {
+        double sv = 3. * (d[p] * d[p]) / (r * r);
+        double2 in = make_double2((Tau.x + k2 * (r - d[p] * d[p] / r)) - sv * Tau.x, Tau.y - sv * Tau.y);
+        F[p] = zmul8(Gr, in);
+    }
+    double2 w = make_double2(-k2 - (3. * Tau.x) / r, -((3. * Tau.y) / r));
+    double2 g;
+    g = make_double2((Gr.x / r) * (rx * ry), (Gr.y / r) * (rx * ry)); F[3] = zmul8(g, w);
+    g = make_double2((Gr.x / r) * (ry * rz), (Gr.y / r) * (ry * rz)); F[4] = zmul8(g, w);
+    g = make_double2((Gr.x / r) * (rx * rz), (Gr.y / r) * (rx * rz)); F[5] = zmul8(g, w);
+}
+
+// complex(4)-rounded F: Green_s_tr_partial (src/Green_functions.f90:139-157).
+__device__ __forceinline__ void dyadF4(double rx, double ry, double rz, double k0, double Pi, float2 F[6])
+{
+    double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(rx, rx), __dmul_rn(ry, ry)), __dmul_rn(rz, rz)));
+    double s, co;
+    sincos(__dmul_rn(k0, r), &s, &co);
+    double den = __dmul_rn(__dmul_rn(4.0, Pi), __dmul_rn(r, r));
+    float2 Gr4 = make_float2((float)__ddiv_rn(co, den), (float)__ddiv_rn(s, den));
+    float2 Tau4 = make_float2((float)(-__ddiv_rn(1.0, r)), (float)k0);
+    double2 Gr = make_double2(Gr4.x, Gr4.y), Tau = make_double2(Tau4.x, Tau4.y);
+    double k2 = __dmul_rn(k0, k0);
+    double r2 = __dmul_rn(r, r);
+    double d[3] = {rx, ry, rz};
+#pragma unroll
+    for (int p = 0; p < 3; ++p) {
+        double dd = __dmul_rn(d[p], d[p]);
+        double sv = __ddiv_rn(__dmul_rn(3., dd), r2);
+        double re = __dsub_rn(__dadd_rn(Tau.x, __dmul_rn(k2, __dsub_rn(r, __ddiv_rn(dd, r)))), __dmul_rn(sv, Tau.x));
+        double im = __dsub_rn(Tau.y, __dmul_rn(sv, Tau.y));
+        double2 f = zmul8_rn(Gr, make_double2(re, im));
+        F[p] = make_float2((float)f.x, (float)f.y);
+    }
+    // 3.*Tau_mn is a single-precision complex(4) product
+    float t3r = __fmul_rn(3.0f, Tau4.x), t3i = __fmul_rn(3.0f, Tau4.y);
+    double2 w = make_double2(__dsub_rn(-k2, __ddiv_rn((double)t3r, r)), -__ddiv_rn((double)t3i, r));
+    double gr = __ddiv_rn(Gr.x, r), gi = __ddiv_rn(Gr.y, r);
+    double pr[3] = {__dmul_rn(rx, ry), __dmul_rn(ry, rz), __dmul_rn(rx, rz)};
+#pragma unroll
+    for (int t = 0; t < 3; ++t) {
+        double2 f = zmul8_rn(make_double2(__dmul_rn(gr, pr[t]), __dmul_rn(gi, pr[t])), w);
+        F[3 + t] = make_float2((float)f.x, (float)f.y);
+    }
+}
+
+// index (p,q) -> unique component
+__device__ __forceinline__ int comp6(int p, int q)
+{
+    return p == q ? p : ((p + q == 1) ? 3 : ((p + q == 3) ? 4 : 5));
+}
+
+// lattice offset -> table slot (offsets stored for every (di,dj,dk) in range)
+struct Lat {
+    const int *ijk;
+    int dim0, dim1, dim2;     // table extents (2*span+1)
+    int sp0, sp1, sp2;        // spans
+    __device__ __forceinline__ size_t slot(int o, int s) const
+    {
+        int di = ijk[3 * o] - ijk[3 * s] + sp0;
+        int dj = ijk[3 * o + 1] - ijk[3 * s + 1] + sp1;
+        int dk = ijk[3 * o + 2] - ijk[3 * s + 2] + sp2;
+        return ((size_t)dk * dim1 + dj) * dim0 + di;
+    }
+};
+
+// Table of F per lattice offset: tab8 (FP64) and tab4 (complex(4)-rounded).
+__global__ void k_lat_table(int dim0, int dim1, int dim2, int sp0, int sp1, int sp2, double d, double k0,
+                            double Pi, double2 *tab8, float2 *tab4)
+{
+    size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    size_t tot = (size_t)dim0 * dim1 * dim2;
+    if (t >= tot) return;
+    int di = (int)(t % dim0) - sp0;
+    int dj = (int)((t / dim0) % dim1) - sp1;
+    int dk = (int)(t / ((size_t)dim0 * dim1)) - sp2;
+    if (di == 0 && dj == 0 && dk == 0) {
+        for (int c = 0; c < 6; ++c) { tab8[6 * t + c] = make_double2(0, 0); tab4[6 * t + c] = make_float2(0, 0); }
+        return;
+    }
+    double rx = di * d, ry = dj * d, rz = dk * d;
+    double2 F8[6];
+    float2 F4[6];
+    dyadF8(rx, ry, rz, k0, Pi, F8);
+    dyadF4(rx, ry, rz, k0, Pi, F4);
+    for (int c = 0; c < 6; ++c) { tab8[6 * t + c] = F8[c]; tab4[6 * t + c] = F4[c]; }
+}
+
+// ---------------------------------------------------------------------------
+// a2: FP64 MoM fill.  Writes the nine entries of each cell pair (io, is) that
+// fall inside rows [r0,r0+nr) x cols [c0,c0+nc) to out[(row-r0)*rs + (col-c0)*cs];
+// out32 (optional) receives the same values rounded to complex64.
+// Threads run along the source cell so row-major outputs are coalesced.
+// ---------------------------------------------------------------------------
+template <bool LAT>
+__global__ void k_mom_fill(int r0, int nr, int c0, int nc, const double *x, const double *y, const double *z,
+                           const double2 *znnpp, const double2 *fk8, double k0, double Pi, Lat lat,
+                           const double2 *tab8, double2 *out, float2 *out32, size_t rs, size_t cs)
+{
+    int is = c0 / 3 + blockIdx.x * blockDim.x + threadIdx.x;
+    int io = r0 / 3 + blockIdx.y * blockDim.y + threadIdx.y;
+    if (3 * is >= c0 + nc || 3 * io >= r0 + nr) return;
+    double2 D[9];
+    if (io == is) {
+        double2 dg = make_double2(1 - znnpp[is].x, -znnpp[is].y);
+#pragma unroll
+        for (int p = 0; p < 3; ++p)
+#pragma unroll
+            for (int q = 0; q < 3; ++q) D[p * 3 + q] = (p == q) ? dg : make_double2(0, 0);
+    } else {
+        double2 F[6];
+        if (LAT) {
+            size_t sl = lat.slot(io, is);
+#pragma unroll
+            for (int c = 0; c < 6; ++c) F[c] = tab8[6 * sl + c];
+        } else {
+            dyadF8(x[io] - x[is], y[io] - y[is], z[io] - z[is], k0, Pi, F);
+        }
+        double2 fk = fk8[is];
+#pragma unroll
+        for (int p = 0; p < 3; ++p)
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                double2 v = zmul8(F[comp6(p, q)], fk);
+                D[p * 3 + q] = make_double2(-v.x, -v.y);
+            }
+    }
+#pragma unroll
+    for (int p = 0; p < 3; ++p) {
+        int row = 3 * io + p;
+        if (row < r0 || row >= r0 + nr) continue;
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            int col = 3 * is + q;
+            if (col < c0 || col >= c0 + nc) continue;
+            size_t o = (size_t)(row - r0) * rs + (size_t)(col - c0) * cs;
+            if (out) out[o] = D[p * 3 + q];
+            if (out32) out32[o] = make_float2((float)D[p * 3 + q].x, (float)D[p * 3 + q].y);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// a3: FP64 incident field (Incident_Field_single_element).  V[(3c+p)*rs + col*cs]
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ T mkz(double re, double im);
+template <>
+__device__ __forceinline__ double2 mkz<double2>(double re, double im) { return make_double2(re, im); }
+template <>
+__device__ __forceinline__ float2 mkz<float2>(double re, double im) { return make_float2((float)re, (float)im); }
+
+template <typename T>
+__global__ void k_mom_rhs(int n, const double *x, const double *y, const double *z, double k0, double Pi, int ntr,
+                          const double *th, const double *ph, T *V, size_t rs, size_t cs)
+{
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    int col = blockIdx.y;
+    if (c >= n) return;
+    int vh = col >= ntr;
+    int t = vh ? col - ntr : col;
+    double tr = th[t] * Pi / 180., pr = ph[t] * Pi / 180.;
+    double st, ct, sp, cp;
+    sincos(tr, &st, &ct);
+    sincos(pr, &sp, &cp);
+    double kx = k0 * ct, ky = k0 * st * cp, kz = k0 * st * sp;
+    double s1, c1, s2, c2, s3, c3;
+    sincos(kx * x[c], &s1, &c1);
+    sincos(ky * y[c], &s2, &c2);
+    sincos(kz * z[c], &s3, &c3);
+    double2 e = zmul8(zmul8(make_double2(c1, s1), make_double2(c2, s2)), make_double2(c3, s3));
+    double2 o[3];
+    if (!vh) {
+        o[0] = make_double2(-(e.x * st), -(e.y * st));
+        o[1] = make_double2((e.x * ct) * cp, (e.y * ct) * cp);
+        o[2] = make_double2((e.x * ct) * sp, (e.y * ct) * sp);
+    } else {
+        o[0] = make_double2(0, 0);
+        o[1] = make_double2(-(e.x * sp), -(e.y * sp));
+        o[2] = make_double2(e.x * cp, e.y * cp);
+    }
+    for (int p = 0; p < 3; ++p) V[(size_t)(3 * c + p) * rs + (size_t)col * cs] = mkz<T>(o[p].x, o[p].y);
+}
+
+// ---------------------------------------------------------------------------
+// a8: Incident_Field with complex(4) locals, on cells idx[0..ncell).
+// E[(3c+p)*rs + col*cs]; column t = V, t + ntr = H.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_incident4(int ncell, const int *idx, const double *x, const double *y, const double *z, double k0,
+                            double Pi, int ntr, const double *th, const double *ph, T *E, size_t rs, size_t cs)
+{
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    int t = blockIdx.y;
+    if (c >= ncell) return;
+    int g = idx ? idx[c] : c;
+    double tr = th[t] * Pi / 180., pr = ph[t] * Pi / 180.;
+    double st = sin(tr), ct = cos(tr), sp = sin(pr), cp = cos(pr);
+    float kx = (float)(k0 * ct);
+    float ky = (float)((k0 * st) * cp);
+    float kz = (float)((k0 * st) * sp);
+    double s1, c1, s2, c2, s3, c3;
+    sincos((double)kx * x[g], &s1, &c1);
+    sincos((double)ky * y[g], &s2, &c2);
+    sincos((double)kz * z[g], &s3, &c3);
+    double2 e = zmul8_rn(zmul8_rn(make_double2(c1, s1), make_double2(c2, s2)), make_double2(c3, s3));
+    float2 ex = make_float2((float)(-__dmul_rn(e.x, st)), (float)(-__dmul_rn(e.y, st)));
+    float2 ey = make_float2((float)__dmul_rn(__dmul_rn(e.x, ct), cp), (float)__dmul_rn(__dmul_rn(e.y, ct), cp));
+    float2 ez = make_float2((float)__dmul_rn(__dmul_rn(e.x, ct), sp), (float)__dmul_rn(__dmul_rn(e.y, ct), sp));
+    float2 hy = make_float2((float)(-__dmul_rn(e.x, sp)), (float)(-__dmul_rn(e.y, sp)));
+    float2 hz = make_float2((float)__dmul_rn(e.x, cp), (float)__dmul_rn(e.y, cp));
+    size_t rv = (size_t)t * cs, rh = (size_t)(t + ntr) * cs;
+    E[(size_t)(3 * c) * rs + rv] = mkz<T>(ex.x, ex.y);
+    E[(size_t)(3 * c + 1) * rs + rv] = mkz<T>(ey.x, ey.y);
+    E[(size_t)(3 * c + 2) * rs + rv] = mkz<T>(ez.x, ez.y);
+    E[(size_t)(3 * c) * rs + rh] = mkz<T>(0, 0);
+    E[(size_t)(3 * c + 1) * rs + rh] = mkz<T>(hy.x, hy.y);
+    E[(size_t)(3 * c + 2) * rs + rh] = mkz<T>(hz.x, hz.y);
+}
+
+// ---------------------------------------------------------------------------
+// a4/a6: complex(4)-local block fill over cell lists idx1 (rows) x idx2 (cols).
+//   mode 0: Green_s_tr_partial (all entries; self 3x3 = diag(1 - Znnpp)).
+//   mode 1: SR_Green_s_tr_partial dense form: keep |g| > thr (float abs), self
+//           3x3 keeps its diagonal; homog mirrors the upper triangle (PARDISO
+//           mtype 6 reads only Is > Io).  idx1 == idx2 (extended block).
+// out[(3 io + p) * rs + (3 is + q) * cs].
+// ---------------------------------------------------------------------------
+template <bool LAT, typename T>
+__global__ void k_block_fill4(int n1, const int *idx1, int n2, const int *idx2, const double *x, const double *y,
+                              const double *z, const double2 *znnpp, const float2 *fk4, double k0, double Pi,
+                              Lat lat, const float2 *tab4, int mode, double thr, int homog, T *out, size_t rs,
+                              size_t cs)
+{
+    int js = blockIdx.x * blockDim.x + threadIdx.x;
+    int io = blockIdx.y * blockDim.y + threadIdx.y;
+    if (js >= n2 || io >= n1) return;
+    int o = idx1[io], s = idx2[js];
+    T V[9];
+    if (o == s) {
+        T dg = mkz<T>(1 - znnpp[s].x, -znnpp[s].y);
+#pragma unroll
+        for (int p = 0; p < 3; ++p)
+#pragma unroll
+            for (int q = 0; q < 3; ++q) V[p * 3 + q] = (p == q) ? dg : mkz<T>(0, 0);
+    } else {
+        // homog SR: the lower triangle is the transposed mirror of the pair (s -> o)
+        bool mirror = (mode == 1 && homog && js < io);
+        int oo = mirror ? s : o, ss = mirror ? o : s;
+        float2 F[6];
+        if (LAT) {
+            size_t sl = lat.slot(oo, ss);
+#pragma unroll
+            for (int c = 0; c < 6; ++c) F[c] = tab4[6 * sl + c];
+        } else {
+            dyadF4(x[oo] - x[ss], y[oo] - y[ss], z[oo] - z[ss], k0, Pi, F);
+        }
+        float2 fk = fk4[ss];
+#pragma unroll
+        for (int p = 0; p < 3; ++p)
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                float2 g = zmul4_rn(F[comp6(p, q)], fk);
+                g = make_float2(-g.x, -g.y);
+                if (mode == 1) {
+                    float a = hypotf(g.x, g.y);
+                    if (!((double)a > thr)) g = make_float2(0.f, 0.f);
+                }
+                // the mirror transposes the 3x3: entry (p,q) of (o,s) is (q,p) of (s,o); F is symmetric
+                V[p * 3 + q] = mkz<T>(g.x, g.y);
+            }
+    }
+#pragma unroll
+    for (int p = 0; p < 3; ++p)
+#pragma unroll
+        for (int q = 0; q < 3; ++q) out[(size_t)(3 * io + p) * rs + (size_t)(3 * js + q) * cs] = V[p * 3 + q];
+}
+
+// ---------------------------------------------------------------------------
+// setfSR scan: one pass over the extended block computes
+//   fnz   -- Green_s_tr_partial_FN (src/Green_functions.f90:176-287), and
+//   for each fSR of the ladder j: nnz_j and sum |g|^2 of SR_Green_s_tr_partial_FN
+//   (:564-806).  Per-CTA partials: part[cta * (1 + 2 * NL) + ...].
+// ---------------------------------------------------------------------------
+constexpr int NLAD = 11;
+template <bool LAT>
+__global__ void k_sr_scan(int s_n, const int *idx, const double *x, const double *y, const double *z,
+                          const double2 *znnpp, const float2 *fk4, double k0, double Pi, Lat lat, const float2 *tab4,
+                          int homog, const double *thr, double *part)
+{
+    __shared__ double sh[32][1 + 2 * NLAD];
+    double acc[1 + 2 * NLAD];
+#pragma unroll
+    for (int j = 0; j < 1 + 2 * NLAD; ++j) acc[j] = 0;
+    size_t npair = (size_t)s_n * s_n;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < npair; t += (size_t)gridDim.x * blockDim.x) {
+        int io = (int)(t / s_n), is = (int)(t % s_n);
+        int o = idx[io], s = idx[is];
+        if (io == is) {
+            double a = hypot(1 - znnpp[s].x, -znnpp[s].y);
+            acc[0] += 3. * (a * a);                       // FN of Z (self term)
+            for (int j = 0; j < NLAD; ++j) { acc[1 + j] += 3; acc[1 + NLAD + j] += 3. * (a * a); }
+            continue;
+        }
+        float2 F[6];
+        if (LAT) {
+            size_t sl = lat.slot(o, s);
+            for (int c = 0; c < 6; ++c) F[c] = tab4[6 * sl + c];
+        } else {
+            dyadF4(x[o] - x[s], y[o] - y[s], z[o] - z[s], k0, Pi, F);
+        }
+        float2 fk = fk4[s];
+        // Green_s_tr_partial_FN: homog scans Io >= Is; term is a real(4) expression
+        if (!homog || io >= is) {
+            float aF[6];
+            for (int c = 0; c < 6; ++c) aF[c] = hypotf(F[c].x, F[c].y);
+            float afk = hypotf(fk.x, fk.y);
+            float tt = __fadd_rn(__fmul_rn(aF[0], aF[0]), __fmul_rn(2.f, __fmul_rn(aF[3], aF[3])));
+            tt = __fadd_rn(tt, __fmul_rn(2.f, __fmul_rn(aF[5], aF[5])));
+            tt = __fadd_rn(tt, __fmul_rn(aF[1], aF[1]));
+            tt = __fadd_rn(tt, __fmul_rn(2.f, __fmul_rn(aF[4], aF[4])));
+            tt = __fadd_rn(tt, __fmul_rn(aF[2], aF[2]));
+            acc[0] += (double)__fmul_rn(tt, __fmul_rn(afk, afk));
+        }
+        // SR: homog keeps only Is > Io
+        if (!homog || is > io) {
+            for (int p = 0; p < 3; ++p)
+                for (int q = 0; q < 3; ++q) {
+                    float2 g = zmul4_rn(F[comp6(p, q)], fk);
+                    float a = hypotf(g.x, g.y);
+                    double a2 = (double)__fmul_rn(a, a);
+                    for (int j = 0; j < NLAD; ++j)
+                        if ((double)a > thr[j]) { acc[1 + j] += 1; acc[1 + NLAD + j] += a2; }
+                }
+        }
+    }
+    // block reduction (fixed order)
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int j = 0; j < 1 + 2 * NLAD; ++j) {
+        double v = acc[j];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) sh[wid][j] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 1 + 2 * NLAD) {
+        double v = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += sh[w][threadIdx.x];
+        part[(size_t)blockIdx.x * (1 + 2 * NLAD) + threadIdx.x] = v;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host launchers
+// ---------------------------------------------------------------------------
+static Lat make_lat(const midas_gpu_ctx *c)
+{
+    Lat l;
+    l.ijk = c->lat_ijk;
+    l.dim0 = c->lat_dim[0]; l.dim1 = c->lat_dim[1]; l.dim2 = c->lat_dim[2];
+    l.sp0 = (c->lat_dim[0] - 1) / 2; l.sp1 = (c->lat_dim[1] - 1) / 2; l.sp2 = (c->lat_dim[2] - 1) / 2;
+    return l;
+}
+
+static bool use_lat(const midas_gpu_ctx *c) { return c->lattice && c->lat_tab4 != nullptr; }
+
+int launch_set_cells(midas_gpu_ctx *c)
+{
+    int n = c->n;
+    ++c->launches;
+    k_set_cells<<<(n + 127) / 128, 128, 0, c->stream>>>(n, c->sc, c->eps, c->k0, c->pi, c->an, c->che, c->znnpp,
+                                                        c->kappa, c->fk8, c->fk4);
+    MIDAS_CUDA(c, cudaGetLastError());
+    return MIDAS_OK;
+}
+
+int launch_lat_table(midas_gpu_ctx *c)
+{
+    size_t tot = (size_t)c->lat_dim[0] * c->lat_dim[1] * c->lat_dim[2];
+    ++c->launches;
+    k_lat_table<<<(unsigned)((tot + 127) / 128), 128, 0, c->stream>>>(
+        c->lat_dim[0], c->lat_dim[1], c->lat_dim[2], (c->lat_dim[0] - 1) / 2, (c->lat_dim[1] - 1) / 2,
+        (c->lat_dim[2] - 1) / 2, c->lat_d, c->k0, c->pi, c->lat_tab8, c->lat_tab4);
+    MIDAS_CUDA(c, cudaGetLastError());
+    return MIDAS_OK;
+}
+
+int launch_mom_fill(midas_gpu_ctx *c, int r0, int nr, int c0, int nc, double2 *out, float2 *out32, size_t rs,
+                    size_t cs)
+{
+    int ci0 = c0 / 3, ci1 = (c0 + nc - 1) / 3, ri0 = r0 / 3, ri1 = (r0 + nr - 1) / 3;
+    dim3 blk(64, 4);
+    dim3 grd((ci1 - ci0 + 1 + 63) / 64, (ri1 - ri0 + 1 + 3) / 4);
+    // the fill kernel indexes cells from r0/3, c0/3: pass the aligned starts
+    Lat l = make_lat(c);
+    ++c->launches;
+    if (c->opts.fill_mode == MIDAS_FILL_FAST && c->lattice && c->lat_tab8)
+        k_mom_fill<true><<<grd, blk, 0, c->stream>>>(r0, nr, c0, nc, c->x, c->y, c->z, c->znnpp, c->fk8, c->k0, c->pi,
+                                                     l, c->lat_tab8, out, out32, rs, cs);
+    else
+        k_mom_fill<false><<<grd, blk, 0, c->stream>>>(r0, nr, c0, nc, c->x, c->y, c->z, c->znnpp, c->fk8, c->k0,
+                                                      c->pi, l, nullptr, out, out32, rs, cs);
+    MIDAS_CUDA(c, cudaGetLastError());
+    return MIDAS_OK;
+}
+
+template <typename T>
+int launch_mom_rhs(midas_gpu_ctx *c, int ntr, const double *th, const double *ph, T *V, size_t rs, size_t cs)
+{
+    dim3 grd((c->n + 127) / 128, 2 * ntr);
+    ++c->launches;
+    k_mom_rhs<T><<<grd, 128, 0, c->stream>>>(c->n, c->x, c->y, c->z, c->k0, c->pi, ntr, th, ph, V, rs, cs);
+    MIDAS_CUDA(c, cudaGetLastError());
+    return MIDAS_OK;
+}
+template int launch_mom_rhs<double2>(midas_gpu_ctx *, int, const double *, const double *, double2 *, size_t, size_t);
+
+template <typename T>
+int launch_incident4(midas_gpu_ctx *c, int ncell, const int *idx, int ntr, const double *th, const double *ph, T *E,
+                     size_t rs, size_t cs)
+{
+    dim3 grd((ncell + 127) / 128, ntr);
+    ++c->launches;
+    k_incident4<T><<<grd, 128, 0, c->stream>>>(ncell, idx, c->x, c->y, c->z, c->k0, c->pi, ntr, th, ph, E, rs, cs);
+    MIDAS_CUDA(c, cudaGetLastError());
+    return MIDAS_OK;
+}
+template int launch_incident4<double2>(midas_gpu_ctx *, int, const int *, int, const double *, const double *,
+                                       double2 *, size_t, size_t);
+template int launch_incident4<float2>(midas_gpu_ctx *, int, const int *, int, const double *, const double *,
+                                      float2 *, size_t, size_t);
+
+template <typename T>
+int launch_block_fill4(midas_gpu_ctx *c, int n1, const int *idx1, int n2, const int *idx2, int mode, double thr,
+                       int homog, T *out, size_t rs, size_t cs)
+{
+    dim3 blk(64, 2);
+    dim3 grd((n2 + 63) / 64, (n1 + 1) / 2);
+    Lat l = make_lat(c);
+    ++c->launches;
+    if (c->opts.fill_mode == MIDAS_FILL_FAST && use_lat(c))
+        k_block_fill4<true, T><<<grd, blk, 0, c->stream>>>(n1, idx1, n2, idx2, c->x, c->y, c->z, c->znnpp, c->fk4,
+                                                           c->k0, c->pi, l, c->lat_tab4, mode, thr, homog, out, rs, cs);
+    else
+        k_block_fill4<false, T><<<grd, blk, 0, c->stream>>>(n1, idx1, n2, idx2, c->x, c->y, c->z, c->znnpp, c->fk4,
+                                                            c->k0, c->pi, l, nullptr, mode, thr, homog, out, rs, cs);
+    MIDAS_CUDA(c, cudaGetLastError());
+    return MIDAS_OK;
+}
+template int launch_block_fill4<double2>(midas_gpu_ctx *, int, const int *, int, const int *, int, double, int,
+                                         double2 *, size_t, size_t);
+template int launch_block_fill4<float2>(midas_gpu_ctx *, int, const int *, int, const int *, int, double, int,
+                                        float2 *, size_t, size_t);
+
+// setfSR ladder (src/getParameters_CBFM.f90:140-162).  vmax = |1 - Znnpp(first cell)|.
+int sr_ladder(midas_gpu_ctx *c, int s_n, const int *d_idx, int first_cell, int homog, double res_sr, double *fsr_out,
+              long long *nnz_out, int want_all, double *all_nnz, double *all_fn, double *fnz_out)
+{
+    static const double ladder[NLAD] = {1e2, 1e3, 2e3, 3e3, 4e3, 5e3, 6e3, 7e3, 8e3, 9e3, 1e4};
+    double2 zn;
+    MIDAS_CUDA(c, cudaMemcpyAsync(&zn, c->znnpp + first_cell, sizeof(double2), cudaMemcpyDeviceToHost, c->stream));
+    MIDAS_CUDA(c, cudaStreamSynchronize(c->stream));
+    double vmax = hypot(1 - zn.x, -zn.y);
+    double thr[NLAD];
+    for (int j = 0; j < NLAD; ++j) thr[j] = vmax / ladder[j];
+    const int nblk = 2 * 152, nv = 1 + 2 * NLAD;
+    void *buf;
+    MIDAS_TRY(ensure(c, S_RED, sizeof(double) * (nblk * nv + NLAD), &buf));
+    double *part = (double *)buf, *dthr = part + nblk * nv;
+    MIDAS_CUDA(c, cudaMemcpyAsync(dthr, thr, sizeof(thr), cudaMemcpyHostToDevice, c->stream));
+    Lat l = make_lat(c);
+    ++c->launches;
+    if (c->opts.fill_mode == MIDAS_FILL_FAST && use_lat(c))
+        k_sr_scan<true><<<nblk, 256, 0, c->stream>>>(s_n, d_idx, c->x, c->y, c->z, c->znnpp, c->fk4, c->k0, c->pi, l,
+                                                     c->lat_tab4, homog, dthr, part);
+    else
+        k_sr_scan<false><<<nblk, 256, 0, c->stream>>>(s_n, d_idx, c->x, c->y, c->z, c->znnpp, c->fk4, c->k0, c->pi,
+                                                      l, nullptr, homog, dthr, part);
+    MIDAS_CUDA(c, cudaGetLastError());
+    std::vector<double> h((size_t)nblk * nv);
+    MIDAS_CUDA(c, cudaMemcpyAsync(h.data(), part, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, c->stream));
+    MIDAS_CUDA(c, cudaStreamSynchronize(c->stream));
+    double tot[1 + 2 * NLAD] = {0};
+    for (int b = 0; b < nblk; ++b)
+        for (int j = 0; j < nv; ++j) tot[j] += h[(size_t)b * nv + j];
+    double norm_z = sqrt(tot[0]);
+    if (fnz_out) *fnz_out = norm_z;
+    if (want_all) {
+        for (int j = 0; j < NLAD; ++j) { all_nnz[j] = tot[1 + j]; all_fn[j] = sqrt(tot[1 + NLAD + j]); }
+    }
+    int jj = 0;
+    double res = 1e3, fsr = ladder[0];
+    long long nnz = 0;
+    while (jj < NLAD && res > res_sr) {
+        fsr = ladder[jj];
+        nnz = (long long)tot[1 + jj];
+        double fn = sqrt(tot[1 + NLAD + jj]);
+        res = fabs(norm_z - fn) / norm_z * 100.;
+        jj++;
+    }
+    if (fsr_out) *fsr_out = fsr;
+    if (nnz_out) *nnz_out = nnz;
+    return MIDAS_OK;
+}
+
+}  // namespace midas

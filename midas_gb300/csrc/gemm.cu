@@ -1,0 +1,476 @@
+// gemm.cu -- FP32-in / FP32-accumulate GEMM for the MIDAS dense solves (sm_103a).
+//
+//   D[M x N] = alpha * A[M x K] * Bt[N x K]^T + beta * D        (row-major, K contiguous)
+//
+// Complex matrices use the real embedding: an interleaved complex row of length
+// k is a real row of length 2k; the complex right operand is expanded by
+// expand_b() into Bt rows (Br, -Bi) / (Bi, Br), so one real GEMM computes the
+// complex product with 8mnk flops (the 4M count) and no separate planes.
+//
+// Engine "tcgen05": TMA (cp.async.bulk.tensor, 128B swizzle) feeds a 4-stage
+// shared-memory ring; one elected thread issues tcgen05.mma.kind::tf32 with the
+// 128 x BN accumulator in tensor memory; four epilogue warps drain TMEM with
+// tcgen05.ld and apply alpha/beta.  Every mbarrier wait is bounded: on expiry
+// the kernel raises DEV_TIMEOUT in the context flag and unwinds (TMEM freed).
+// Engine "simt": a register-tiled CUDA-core kernel used to validate the tensor
+// path on the device (gemm_selftest) and selectable with MIDAS_GEMM=simt.
+#include <cuda.h>
+#include <cstdlib>
+#include <cstring>
+
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace midas {
+
+// ---------------------------------------------------------------------------
+// SIMT engine: 64 x 64 tile, 256 threads, 4 x 4 outputs per thread.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_gemm_simt(GemmArgs g)
+{
+    __shared__ float As[16][64 + 4];
+    __shared__ float Bs[16][64 + 4];
+    int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+    int m0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
+    float acc[4][4] = {};
+    for (int k0 = 0; k0 < g.K; k0 += 16) {
+        for (int i = threadIdx.x; i < 64 * 16; i += 256) {
+            int r = i / 16, kk = i % 16;
+            int gm = m0 + r, gn = n0 + r, gk = k0 + kk;
+            As[kk][r] = (gm < g.M && gk < g.K) ? g.A[(long long)gm * g.lda + gk] : 0.f;
+            Bs[kk][r] = (gn < g.N && gk < g.K) ? g.Bt[(long long)gn * g.ldb + gk] : 0.f;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < 16; ++kk) {
+            float a[4], b[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) { a[i] = As[kk][ty * 4 + i]; b[i] = Bs[kk][tx * 4 + i]; }
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            int gm = m0 + ty * 4 + i, gn = n0 + tx * 4 + j;
+            if (gm < g.M && gn < g.N) {
+                float *d = g.D + (long long)gm * g.ldd + gn;
+                *d = g.alpha * acc[i][j] + (g.beta != 0.f ? g.beta * *d : 0.f);
+            }
+        }
+}
+
+// ---------------------------------------------------------------------------
+// tcgen05 engine
+// ---------------------------------------------------------------------------
+constexpr int TC_BM = 128;
+constexpr int TC_BN = 128;
+constexpr int TC_BK = 32;          // 32 fp32 = 128 B = one 128B-swizzle row
+constexpr int TC_STAGES = 4;
+constexpr int TC_THREADS = 192;    // warp0 TMA, warp1 MMA/TMEM, warps2-5 epilogue
+constexpr int TC_A_BYTES = TC_BM * TC_BK * 4;
+constexpr int TC_B_BYTES = TC_BN * TC_BK * 4;
+constexpr int TC_STAGE_BYTES = TC_A_BYTES + TC_B_BYTES;
+constexpr int TC_SMEM = TC_STAGES * TC_STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+constexpr uint32_t TC_SPIN_LIMIT = 1u << 26;   // bounded waits (~seconds with backoff)
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ bool mbar_try(uint64_t *bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n.reg .pred p;\n"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// bounded wait: returns false (and raises the abort flag) when the limit expires
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag, int *gflag)
+{
+    for (uint32_t i = 0; i < TC_SPIN_LIMIT; ++i) {
+        if (mbar_try(bar, parity)) return true;
+        if (*abort_flag) return false;
+        if (i > 64) __nanosleep(64);
+    }
+    *abort_flag = 1;
+    atomicOr(gflag, DEV_TIMEOUT);
+    return false;
+}
+
+__device__ __forceinline__ void mbar_arrive_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar, int x, int y)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::
+            "r"(smem_u32(dst)),
+        "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(x), "r"(y)
+        : "memory");
+}
+
+// shared-memory matrix descriptor: K-major, 128B swizzle, 8-row atoms 1024 B apart
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+    d |= (uint64_t)(16 >> 4) << 16;          // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;        // stride byte offset: 8 rows x 128 B
+    d |= (uint64_t)1 << 46;                  // descriptor version (tcgen05)
+    d |= (uint64_t)2 << 61;                  // SWIZZLE_128B
+    return d;
+}
+
+// instruction descriptor: kind::tf32, D f32, A/B tf32, K-major both, M x N
+__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N)
+{
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate)
+{
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t *bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                     smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float v[32])
+{
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int M, int N, int K,
+              float *D, long long ldd, float alpha, float beta, int *gflag)
+{
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t *full = (uint64_t *)(smem + TC_STAGES * TC_STAGE_BYTES);
+    uint64_t *empty = full + TC_STAGES;
+    uint64_t *accf = empty + TC_STAGES;
+    volatile uint32_t *tmem_slot = (volatile uint32_t *)(accf + 1);
+    volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
+
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * TC_BN;
+    const int nk = (K + TC_BK - 1) / TC_BK;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < TC_STAGES; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
+        mbar_init(accf, 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmA) : "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmB) : "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32((const void *)tmem_slot)),
+                     "r"(TC_BN));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            for (int kb = 0; kb < nk; ++kb) {
+                int s = kb % TC_STAGES;
+                if (!mbar_wait(&empty[s], ((kb / TC_STAGES) + 1) & 1, abort_flag, gflag)) break;
+                uint8_t *sa = smem + s * TC_STAGE_BYTES;
+                uint8_t *sb = sa + TC_A_BYTES;
+                mbar_arrive_tx(&full[s], TC_STAGE_BYTES);
+                tma_load_2d(sa, &tmA, &full[s], kb * TC_BK, m0);
+                tma_load_2d(sb, &tmB, &full[s], kb * TC_BK, n0);
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            const uint32_t idesc = idesc_tf32(TC_BM, TC_BN);
+            for (int kb = 0; kb < nk; ++kb) {
+                int s = kb % TC_STAGES;
+                if (!mbar_wait(&full[s], (kb / TC_STAGES) & 1, abort_flag, gflag)) break;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                uint32_t sa = smem_u32(smem + s * TC_STAGE_BYTES);
+                uint32_t sb = sa + TC_A_BYTES;
+#pragma unroll
+                for (int k4 = 0; k4 < TC_BK / 8; ++k4) {
+                    uint64_t ad = smem_desc_sw128(sa + k4 * 32);
+                    uint64_t bd = smem_desc_sw128(sb + k4 * 32);
+                    mma_tf32(tmem, ad, bd, idesc, (kb > 0 || k4 > 0) ? 1u : 0u);
+                }
+                mma_commit(&empty[s]);
+            }
+            mma_commit(accf);
+        }
+    } else {
+        // epilogue: warp w reads TMEM lanes 32*(w%4) .. +31
+        const int lg = warp % 4;
+        const int row = m0 + lg * 32 + lane;
+        bool ok = mbar_wait(accf, 0, abort_flag, gflag);
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        if (ok) {
+            for (int c = 0; c < TC_BN / 32; ++c) {
+                float v[32];
+                tmem_ld32(tmem + ((uint32_t)(lg * 32) << 16) + (uint32_t)(c * 32), v);
+                if (row < M) {
+                    float *d = D + (long long)row * ldd + n0 + c * 32;
+                    int ncol = N - (n0 + c * 32);
+                    if (ncol >= 32 && (((uintptr_t)d) & 15) == 0) {
+#pragma unroll
+                        for (int j = 0; j < 32; j += 4) {
+                            float4 o;
+                            if (beta != 0.f) {
+                                float4 p = *(float4 *)(d + j);
+                                o = make_float4(alpha * v[j] + beta * p.x, alpha * v[j + 1] + beta * p.y,
+                                                alpha * v[j + 2] + beta * p.z, alpha * v[j + 3] + beta * p.w);
+                            } else {
+                                o = make_float4(alpha * v[j], alpha * v[j + 1], alpha * v[j + 2], alpha * v[j + 3]);
+                            }
+                            *(float4 *)(d + j) = o;
+                        }
+                    } else {
+                        for (int j = 0; j < 32 && j < ncol; ++j)
+                            d[j] = alpha * v[j] + (beta != 0.f ? beta * d[j] : 0.f);
+                    }
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (warp == 1)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_BN));
+}
+
+// ---------------------------------------------------------------------------
+// tensor-map creation through the driver entry point (no libcuda link needed)
+// ---------------------------------------------------------------------------
+typedef CUresult (*PFN_encodeTiled)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                    const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                    CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static PFN_encodeTiled g_encode = nullptr;
+
+static int get_encode(midas_gpu_ctx *c)
+{
+    if (g_encode) return MIDAS_OK;
+    cudaDriverEntryPointQueryResult q;
+    void *fn = nullptr;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn)
+        return c->err.set(MIDAS_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled entry point unavailable");
+    g_encode = (PFN_encodeTiled)fn;
+    return MIDAS_OK;
+}
+
+static int make_map(midas_gpu_ctx *c, CUtensorMap *m, const float *base, int rows, int K, long long ld, int box_rows)
+{
+    cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)ld * 4};
+    cuuint32_t box[2] = {(cuuint32_t)TC_BK, (cuuint32_t)box_rows};
+    cuuint32_t es[2] = {1, 1};
+    CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)base, dims, strides, box, es,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return c->err.set(MIDAS_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+    return MIDAS_OK;
+}
+
+static int g_engine = -1;   // 0 simt, 1 tcgen05
+
+const char *gemm_engine() { return g_engine == 0 ? "simt" : "tcgen05"; }
+
+static int pick_engine()
+{
+    if (g_engine < 0) {
+        const char *e = getenv("MIDAS_GEMM");
+        g_engine = (e && strcmp(e, "simt") == 0) ? 0 : 1;
+    }
+    return g_engine;
+}
+
+static int gemm_simt(midas_gpu_ctx *c, const GemmArgs &g)
+{
+    dim3 grd((g.N + 63) / 64, (g.M + 63) / 64);
+    ++c->launches;
+    k_gemm_simt<<<grd, 256, 0, c->stream>>>(g);
+    MIDAS_CUDA(c, cudaGetLastError());
+    return MIDAS_OK;
+}
+
+static int gemm_tc(midas_gpu_ctx *c, const GemmArgs &g)
+{
+    MIDAS_TRY(get_encode(c));
+    if ((((uintptr_t)g.A) & 15) || (((uintptr_t)g.Bt) & 15) || (g.lda & 3) || (g.ldb & 3))
+        return c->err.set(MIDAS_ERR_ARG, "gemm_tf32: operands must be 16-byte aligned with ld % 4 == 0");
+    static bool attr = false;
+    if (!attr) {
+        MIDAS_CUDA(c, cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
+        attr = true;
+    }
+    CUtensorMap ma, mb;
+    MIDAS_TRY(make_map(c, &ma, g.A, g.M, g.K, g.lda, TC_BM));
+    MIDAS_TRY(make_map(c, &mb, g.Bt, g.N, g.K, g.ldb, TC_BN));
+    dim3 grd((g.N + TC_BN - 1) / TC_BN, (g.M + TC_BM - 1) / TC_BM);
+    ++c->launches;
+    k_gemm_tc<<<grd, TC_THREADS, TC_SMEM, c->stream>>>(ma, mb, g.M, g.N, g.K, g.D, g.ldd, g.alpha, g.beta,
+                                                       c->d_flag);
+    MIDAS_CUDA(c, cudaGetLastError());
+    return MIDAS_OK;
+}
+
+int gemm_tf32(midas_gpu_ctx *c, const GemmArgs &g)
+{
+    if (g.M <= 0 || g.N <= 0) return MIDAS_OK;
+    if (g.K <= 0) return c->err.set(MIDAS_ERR_ARG, "gemm_tf32: K must be positive");
+    return pick_engine() ? gemm_tc(c, g) : gemm_simt(c, g);
+}
+
+// ---------------------------------------------------------------------------
+// complex operand expansion
+// ---------------------------------------------------------------------------
+__global__ void k_expand_b(int k, int n, const float2 *B, long long rsb, long long csb, float *Bt, long long ldt)
+{
+    int p = blockIdx.x * blockDim.x + threadIdx.x;   // along k (contiguous in Bt rows)
+    int j = blockIdx.y;
+    if (p >= k) return;
+    float2 b = B[(long long)p * rsb + (long long)j * csb];
+    float *r0 = Bt + (long long)(2 * j) * ldt + 2 * p;
+    float *r1 = r0 + ldt;
+    r0[0] = b.x; r0[1] = -b.y;
+    r1[0] = b.y; r1[1] = b.x;
+}
+
+int expand_b(midas_gpu_ctx *c, int k, int n, const float2 *B, long long rsb, long long csb, float *Bt, long long ldt)
+{
+    if (k <= 0 || n <= 0) return MIDAS_OK;
+    dim3 grd((k + 127) / 128, n);
+    ++c->launches;
+    k_expand_b<<<grd, 128, 0, c->stream>>>(k, n, B, rsb, csb, Bt, ldt);
+    MIDAS_CUDA(c, cudaGetLastError());
+    return MIDAS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// device self-test: tcgen05 vs SIMT on a ragged problem (called by tests)
+// ---------------------------------------------------------------------------
+__global__ void k_fill_pattern(float *p, long long n, uint32_t seed)
+{
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t h = (uint32_t)i * 2654435761u ^ seed;
+    h ^= h >> 13; h *= 0x5bd1e995u; h ^= h >> 15;
+    p[i] = ((h & 0xFFFF) / 32768.0f) - 1.0f;
+}
+
+int gemm_selftest(midas_gpu_ctx *c)
+{
+    const int M = 300, N = 200, K = 136;   // ragged in every dimension
+    size_t na = (size_t)M * K, nb = (size_t)N * K, nd = (size_t)M * N;
+    void *buf;
+    MIDAS_TRY(ensure(c, S_T32, sizeof(float) * (na + nb + 2 * nd), &buf));
+    float *A = (float *)buf, *B = A + na, *D0 = B + nb, *D1 = D0 + nd;
+    ++c->launches;
+    k_fill_pattern<<<(unsigned)((na + 255) / 256), 256, 0, c->stream>>>(A, (long long)na, 1u);
+    ++c->launches;
+    k_fill_pattern<<<(unsigned)((nb + 255) / 256), 256, 0, c->stream>>>(B, (long long)nb, 7u);
+    ++c->launches;
+    k_fill_pattern<<<(unsigned)((nd + 255) / 256), 256, 0, c->stream>>>(D0, (long long)nd, 11u);
+    MIDAS_CUDA(c, cudaMemcpyAsync(D1, D0, sizeof(float) * nd, cudaMemcpyDeviceToDevice, c->stream));
+    GemmArgs g{M, N, K, A, K, B, K, D0, N, -1.0f, 1.0f};
+    MIDAS_TRY(gemm_simt(c, g));
+    g.D = D1;
+    MIDAS_TRY(gemm_tc(c, g));
+    std::vector<float> h0(nd), h1(nd);
+    MIDAS_CUDA(c, cudaMemcpyAsync(h0.data(), D0, sizeof(float) * nd, cudaMemcpyDeviceToHost, c->stream));
+    MIDAS_CUDA(c, cudaMemcpyAsync(h1.data(), D1, sizeof(float) * nd, cudaMemcpyDeviceToHost, c->stream));
+    MIDAS_CUDA(c, cudaStreamSynchronize(c->stream));
+    MIDAS_TRY(check_flag(c, "gemm_selftest"));
+    double md = 0;
+    for (size_t i = 0; i < nd; ++i) md = fmax(md, fabs((double)h0[i] - (double)h1[i]));
+    // TF32 operands: |err| <= K * 2^-10 * max|a||b| ~ 0.13 worst case; typical << 0.05
+    if (!(md < 0.05)) {
+        char msg[128];
+        snprintf(msg, sizeof msg, "tcgen05 GEMM self-test mismatch: max |diff| = %g", md);
+        return c->err.set(MIDAS_ERR_CUDA, msg);
+    }
+    return MIDAS_OK;
+}
+
+// Time `iters` launches of one M x N x K GEMM (D = D - A Bt^T) with CUDA events on
+// the context stream; returns the average device time per launch in *ms.
+int gemm_bench(midas_gpu_ctx *c, int M, int N, int K, int iters, double *ms)
+{
+    if (M <= 0 || N <= 0 || K <= 0 || iters <= 0) return c->err.set(MIDAS_ERR_ARG, "bench_gemm: bad sizes");
+    size_t na = (size_t)M * K, nb = (size_t)N * K, nd = (size_t)M * N;
+    void *buf;
+    MIDAS_TRY(ensure(c, S_T32, sizeof(float) * (na + nb + nd) + 256, &buf));
+    float *A = (float *)buf, *B = A + na, *D = B + nb;
+    ++c->launches;
+    k_fill_pattern<<<(unsigned)((na + 255) / 256), 256, 0, c->stream>>>(A, (long long)na, 3u);
+    ++c->launches;
+    k_fill_pattern<<<(unsigned)((nb + 255) / 256), 256, 0, c->stream>>>(B, (long long)nb, 5u);
+    MIDAS_CUDA(c, cudaMemsetAsync(D, 0, sizeof(float) * nd, c->stream));
+    GemmArgs g{M, N, K, A, K, B, K, D, N, -1.0f, 1.0f};
+    MIDAS_TRY(gemm_tf32(c, g));   // warm-up
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, c->stream);
+    for (int i = 0; i < iters; ++i) MIDAS_TRY(gemm_tf32(c, g));
+    cudaEventRecord(e1, c->stream);
+    cudaEventSynchronize(e1);
+    float t = 0;
+    cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    MIDAS_TRY(check_flag(c, "bench_gemm"));
+    *ms = t / iters;
+    return MIDAS_OK;
+}
+
+}  // namespace midas

@@ -1,0 +1,62 @@
+// kernels.cuh -- internal launcher prototypes shared between translation units.
+#pragma once
+#include "common.cuh"
+
+namespace midas {
+
+// fill.cu
+int launch_set_cells(midas_gpu_ctx *c);
+int launch_lat_table(midas_gpu_ctx *c);
+int launch_mom_fill(midas_gpu_ctx *c, int r0, int nr, int c0, int nc, double2 *out, float2 *out32, size_t rs,
+                    size_t cs);
+template <typename T>
+int launch_mom_rhs(midas_gpu_ctx *c, int ntr, const double *th, const double *ph, T *V, size_t rs, size_t cs);
+template <typename T>
+int launch_incident4(midas_gpu_ctx *c, int ncell, const int *idx, int ntr, const double *th, const double *ph, T *E,
+                     size_t rs, size_t cs);
+template <typename T>
+int launch_block_fill4(midas_gpu_ctx *c, int n1, const int *idx1, int n2, const int *idx2, int mode, double thr,
+                       int homog, T *out, size_t rs, size_t cs);
+int sr_ladder(midas_gpu_ctx *c, int s_n, const int *d_idx, int first_cell, int homog, double res_sr, double *fsr_out,
+              long long *nnz_out, int want_all, double *all_nnz, double *all_fn, double *fnz_out);
+
+// gemm.cu : D[M x N] = alpha * A[M x K] * Bt[N x K]^T + beta * D   (all fp32, row-major,
+// K contiguous for A and Bt).  Complex products use the real embedding: A is the
+// interleaved complex matrix (K = 2k), Bt the expanded operand (N = 2n, see expand_b).
+struct GemmArgs {
+    int M, N, K;
+    const float *A; long long lda;
+    const float *Bt; long long ldb;
+    float *D; long long ldd;
+    float alpha, beta;
+};
+int gemm_tf32(midas_gpu_ctx *c, const GemmArgs &g);
+// expand a complex k x n operand B (element (p,j) at B[p*rsb + j*csb], complex64) into
+// Bt (2n x 2k floats, row stride ldt): rows 2j = (Br, -Bi), 2j+1 = (Bi, Br) along p.
+int expand_b(midas_gpu_ctx *c, int k, int n, const float2 *B, long long rsb, long long csb, float *Bt,
+             long long ldt);
+// which GEMM engine is active ("tcgen05" or "simt")
+const char *gemm_engine();
+int gemm_selftest(midas_gpu_ctx *c);
+int gemm_bench(midas_gpu_ctx *c, int M, int N, int K, int iters, double *ms);
+
+// dense.cu
+struct DenseLU {
+    int n = 0, nb = 64, nblk = 0;
+    float2 *A = nullptr;     // n x n row-major, overwritten by L\U
+    long long lda = 0;
+    float2 *Linv = nullptr;  // nblk blocks of nb x nb (row-major), unit-lower inverses
+    float2 *Uinv = nullptr;  // nblk blocks of nb x nb, upper inverses
+};
+int lu_factor_nopiv(midas_gpu_ctx *c, DenseLU &lu);
+// solve LU X = R in place; R is n x nrhs column-major complex64 (ld = n)
+int lu_solve(midas_gpu_ctx *c, const DenseLU &lu, float2 *R, int nrhs);
+// mixed-precision solve of Z x = b: Z64 row-major FP64 (for residuals), lu factored;
+// b/x are n x nrhs column-major FP64.
+int ir_solve(midas_gpu_ctx *c, const DenseLU &lu, const double2 *Z64, long long ldz, const double2 *b, double2 *x,
+             int nrhs, midas_gpu_info *info);
+int zgesv_fp64(midas_gpu_ctx *c, int n, int nrhs, double2 *Acol, double2 *Bcol, midas_gpu_info *info);
+void destroy_cusolver(void *h);
+int inf_norm_rows(midas_gpu_ctx *c, const double2 *Z, long long ldz, int n, double *out);
+
+}  // namespace midas

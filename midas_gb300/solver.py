@@ -1,0 +1,229 @@
+"""Host-side mirror of the reference's solver interface, driving the GPU library.
+
+``Context`` wraps one ``midas_gpu_ctx``.  Its methods follow the reference's
+subroutines (same names, argument meaning and layout, reference file:line in
+each docstring); arrays are numpy (host) or torch tensors (device) and are
+passed to the C ABI by address.  Failures raise ``MidasError`` carrying the
+MIDAS_* status -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from ._lib import Info, MidasError, Opts, addr
+
+
+def _c(a, dtype):
+    return np.ascontiguousarray(a, dtype=dtype)
+
+
+@dataclass
+class CellsIn:
+    """type Cell inputs (src/Initialization.f90:22-26): centroids, edge, eps."""
+
+    xyz: np.ndarray
+    sc: np.ndarray
+    eps: np.ndarray
+    k0: float
+
+
+class Context:
+    def __init__(self, device: int = 0, solve_mode: int = _lib.SOLVE_MIXED, fill_mode: int = _lib.FILL_FAITHFUL,
+                 index_base: int = 0, ir_tol: float = 1e-13, ir_max_iter: int = 30):
+        self.L = _lib.load()
+        o = Opts()
+        self.L.midas_gpu_default_opts(ctypes.byref(o))
+        o.device, o.solve_mode, o.fill_mode, o.index_base = device, solve_mode, fill_mode, index_base
+        o.ir_tol, o.ir_max_iter = ir_tol, ir_max_iter
+        h = ctypes.c_void_p()
+        st = self.L.midas_gpu_init(ctypes.byref(o), ctypes.byref(h))
+        if st != 0:
+            raise MidasError(st, "midas_gpu_init failed")
+        self.h = h
+        self.n = 0
+        self.info = Info()
+        self._keep = []
+
+    def close(self):
+        if self.h:
+            self.L.midas_gpu_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, st):
+        if st != 0:
+            raise MidasError(st, self.L.midas_gpu_last_error(self.h).decode())
+
+    # -- cells -------------------------------------------------------------
+    def set_cells(self, xyz, sc, eps, k0: float):
+        """SetCellsParams (src/SetCellsParams.f90:31-49) for the given cells."""
+        xyz = np.asarray(xyz, dtype=np.float64).reshape(-1, 3)
+        n = xyz.shape[0]
+        x, y, z = (_c(xyz[:, i], np.float64) for i in range(3))
+        scv = _c(np.broadcast_to(sc, (n,)), np.float64)
+        ev = np.broadcast_to(np.asarray(eps, dtype=np.complex128), (n,))
+        er, ei = _c(ev.real, np.float64), _c(ev.imag, np.float64)
+        self._ck(self.L.midas_gpu_set_cells(self.h, n, addr(x), addr(y), addr(z), addr(scv), addr(er), addr(ei),
+                                            float(k0)))
+        self.n = n
+        return self
+
+    def cell_params(self):
+        n = self.n
+        an, kap = np.zeros(n), np.zeros(n)
+        che, zn = np.zeros(n, np.complex128), np.zeros(n, np.complex128)
+        self._ck(self.L.midas_gpu_get_cell_params(self.h, addr(an), addr(che), addr(zn), addr(kap)))
+        return {"a_n": an, "che": che, "znnpp": zn, "kappa": kap}
+
+    # -- element-level entry points ----------------------------------------
+    def mom_fill(self, r0=0, nr=None, c0=0, nc=None):
+        """compute_Green_s_tr_single_element over a block (src/Compute_EFields_MoM.f90:433-523)."""
+        N = 3 * self.n
+        nr = N - r0 if nr is None else nr
+        nc = N - c0 if nc is None else nc
+        Z = np.zeros((nc, nr), np.complex128)
+        self._ck(self.L.midas_gpu_mom_fill(self.h, r0, nr, c0, nc, addr(Z)))
+        return Z.T
+
+    def mom_rhs(self, th, ph):
+        """Incident_Field_single_element (src/Compute_EFields_MoM.f90:529-598)."""
+        th, ph = _c(th, np.float64), _c(ph, np.float64)
+        V = np.zeros((2 * len(th), 3 * self.n), np.complex128)
+        self._ck(self.L.midas_gpu_mom_rhs(self.h, len(th), addr(th), addr(ph), addr(V)))
+        return V.T
+
+    def incident_field(self, th, ph, idx=None):
+        """Incident_Field with complex(4) locals (src/Incident_Field.f90:1-63)."""
+        th, ph = _c(th, np.float64), _c(ph, np.float64)
+        if idx is not None:
+            idx = _c(idx, np.int32)
+        nc = self.n if idx is None else len(idx)
+        E = np.zeros((2 * len(th), 3 * nc), np.complex128)
+        self._ck(self.L.midas_gpu_incident_field(self.h, nc, addr(idx), len(th), addr(th), addr(ph), addr(E)))
+        return E.T
+
+    def block_fill(self, idx1, idx2):
+        """Green_s_tr_partial (src/Green_functions.f90:96-173)."""
+        idx1, idx2 = _c(idx1, np.int32), _c(idx2, np.int32)
+        Z = np.zeros((3 * len(idx2), 3 * len(idx1)), np.complex128)
+        self._ck(self.L.midas_gpu_block_fill(self.h, len(idx1), addr(idx1), len(idx2), addr(idx2), addr(Z)))
+        return Z.T
+
+    def sr_fill(self, idx, fsr: float, homog: int, want_matrix=True):
+        """SR_Green_s_tr_partial in dense form (src/Green_functions.f90:290-562)."""
+        idx = _c(idx, np.int32)
+        s = len(idx)
+        Z = np.zeros((3 * s, 3 * s), np.complex128) if want_matrix else None
+        nnz, fn = ctypes.c_longlong(0), ctypes.c_double(0)
+        self._ck(self.L.midas_gpu_sr_fill(self.h, s, addr(idx), float(fsr), int(homog), addr(Z), ctypes.byref(nnz),
+                                          ctypes.byref(fn)))
+        return (Z.T if want_matrix else None), nnz.value, fn.value
+
+    def set_fsr(self, idx, homog: int, res_sr: float = 0.0):
+        """setfSR (src/getParameters_CBFM.f90:113-168)."""
+        idx = _c(idx, np.int32)
+        f, nnz = ctypes.c_double(0), ctypes.c_longlong(0)
+        self._ck(self.L.midas_gpu_set_fsr(self.h, len(idx), addr(idx), int(homog), float(res_sr), ctypes.byref(f),
+                                          ctypes.byref(nnz)))
+        return f.value, nnz.value
+
+    def aca(self, row0, nrows, col0, ncols, eps=float(np.float32(1e-4)), itmax=50):
+        """Calcul_MatrixZij_ACA (src/Calcul_ACA_matrices.f90:6-219)."""
+        U = np.zeros((itmax, nrows), np.complex128)
+        V = np.zeros((ncols, itmax), np.complex128)
+        k = ctypes.c_int(0)
+        self._ck(self.L.midas_gpu_aca(self.h, row0, nrows, col0, ncols, float(eps), itmax, addr(U), addr(V),
+                                      ctypes.byref(k)))
+        return k.value, U.T, V.T
+
+    # -- solves ------------------------------------------------------------
+    def dense_solve(self, A, B):
+        """PZGESV stand-in: solve A X = B (column-major complex)."""
+        A = np.asfortranarray(A, dtype=np.complex128)
+        X = np.asfortranarray(B, dtype=np.complex128).copy()
+        n, nrhs = X.shape
+        self._ck(self.L.midas_gpu_dense_solve(self.h, n, nrhs, addr(A), addr(X), ctypes.byref(self.info)))
+        return X
+
+    def mom_solve(self, th, ph, out=None):
+        """Field part of Compute_EFields_MoM (src/Compute_EFields_MoM.f90:66-229): E (3n x 2NTr)."""
+        th, ph = _c(th, np.float64), _c(ph, np.float64)
+        E = np.zeros((2 * len(th), 3 * self.n), np.complex128) if out is None else out
+        self._ck(self.L.midas_gpu_mom_solve(self.h, len(th), addr(th), addr(ph), addr(E), ctypes.byref(self.info)))
+        return E.T if out is None else E
+
+    def cbfm_solve(self, blk_offsets, ext_lists, cbf_th, cbf_ph, th, ph, flags=_lib.CBFM_SR, thr_cbf=0.0,
+                   res_sr=0.0, eps_aca=float(np.float32(1e-4)), aca_itmax=50, out=None):
+        """Compute_EFields_CBFME(_ACA) (src/Compute_EFields_CBFME.f90:1-1006): (E, K)."""
+        bo = _c(blk_offsets, np.int32)
+        nb = len(bo) - 1
+        eo = _c(np.concatenate([[0], np.cumsum([len(e) for e in ext_lists])]), np.int32)
+        ei = _c(np.concatenate([np.asarray(e, np.int32) for e in ext_lists]) if eo[-1] > 0 else np.zeros(1),
+                np.int32)
+        cth, cph = _c(cbf_th, np.float64), _c(cbf_ph, np.float64)
+        th, ph = _c(th, np.float64), _c(ph, np.float64)
+        K = np.zeros(nb, np.int32)
+        E = np.zeros((2 * len(th), 3 * self.n), np.complex128) if out is None else out
+        self._ck(self.L.midas_gpu_cbfm_solve(self.h, nb, addr(bo), addr(eo), addr(ei), len(cth), addr(cth),
+                                             addr(cph), float(thr_cbf), float(res_sr), int(flags), float(eps_aca),
+                                             int(aca_itmax), len(th), addr(th), addr(ph), addr(E), addr(K),
+                                             ctypes.byref(self.info)))
+        return (E.T if out is None else E), K
+
+    # -- post-processing ---------------------------------------------------
+    def cext_cabs(self, th, ph, E):
+        """Compute_ExtAbsCsec_fromIntField (src/Compute_ExtAbsCsec_fromIntField.f90:45-64)."""
+        th, ph = _c(th, np.float64), _c(ph, np.float64)
+        Ef = np.asfortranarray(E, dtype=np.complex128)
+        ce, ca = np.zeros(len(th)), np.zeros(len(th))
+        self._ck(self.L.midas_gpu_cext_cabs(self.h, len(th), addr(th), addr(ph), addr(Ef), addr(ce), addr(ca)))
+        return ce, ca
+
+    def smatrix(self, rth, rph, E):
+        """S matrix (src/Green_functions.f90:1399-1438, src/Compute_EFields_MoM.f90:306-369)."""
+        rth, rph = _c(rth, np.float64), _c(rph, np.float64)
+        Ef = np.asfortranarray(E, dtype=np.complex128)
+        ntr = Ef.shape[1] // 2
+        S = np.zeros((4 * ntr, len(rth)), np.complex128)
+        self._ck(self.L.midas_gpu_smatrix(self.h, len(rth), addr(rth), addr(rph), ntr, addr(Ef), addr(S)))
+        return S.T
+
+    def launch_count(self) -> int:
+        return int(self.L.midas_gpu_launch_count(self.h))
+
+    def stream_handle(self) -> int:
+        """cudaStream_t of the context (wrap with torch.cuda.ExternalStream to time on it)."""
+        return int(self.L.midas_gpu_stream(self.h) or 0)
+
+    def bench_gemm(self, M, N, K, iters=20) -> float:
+        """Average ms per launch of one tensor-core GEMM (CUDA events on the context stream)."""
+        ms = ctypes.c_double(0)
+        self._ck(self.L.midas_gpu_bench_gemm(self.h, M, N, K, iters, ctypes.byref(ms)))
+        return ms.value
+
+    def gemm_selftest(self):
+        self._ck(self.L.midas_gpu_gemm_selftest(self.h))
+        return self.L.midas_gpu_gemm_engine().decode()
+
+
+def compute_efields_mom(ctx: Context, th, ph, rth, rph):
+    """Compute_EFields_MoM (src/Compute_EFields_MoM.f90:1-427): returns
+    (E_total, S_total, C_ext, C_abs) with the reference's layouts."""
+    E = ctx.mom_solve(th, ph)
+    S = ctx.smatrix(rth, rph, E)
+    ce, ca = ctx.cext_cabs(th, ph, E)
+    return E, S, ce, ca
+
+
+def compute_efields_cbfme(ctx: Context, blk_offsets, ext_lists, cbf_th, cbf_ph, th, ph, **kw):
+    """Compute_EFields_CBFME (src/Compute_EFields_CBFME.f90:1-1006): (E_total, K_patchs)."""
+    return ctx.cbfm_solve(blk_offsets, ext_lists, cbf_th, cbf_ph, th, ph, **kw)

@@ -1,0 +1,103 @@
+"""GPU fills and incident fields against the oracle (through the C ABI)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ULP32 = 2.0 ** -23
+
+
+def scene(oracle, sc=0.2, m=1.5 + 0.01j, k0=2.0, inhom=False, seed=0):
+    xyz = oracle.sphere_cells(2.0, sc)
+    if inhom:
+        rng = np.random.default_rng(seed)
+        eps = rng.uniform(1.5, 3.5, len(xyz)) + 1j * rng.uniform(0, 0.2, len(xyz))
+    else:
+        eps = np.full(len(xyz), m * m)
+    return xyz, sc, eps, k0
+
+
+@pytest.fixture(scope="module", params=["faithful", "fast"])
+def pair(request, gpulib, oracle):
+    from midas_gb300 import _lib
+    from midas_gb300.solver import Context
+    xyz, sc, eps, k0 = scene(oracle, inhom=True)
+    mode = _lib.FILL_FAITHFUL if request.param == "faithful" else _lib.FILL_FAST
+    ctx = Context(fill_mode=mode).set_cells(xyz, sc, eps, k0)
+    cells = oracle.Cells(xyz, sc, eps, k0)
+    yield ctx, cells, request.param
+    ctx.close()
+
+
+def ulps32(a, b):
+    """Per-element difference in units of the float32 ulp of the larger magnitude."""
+    scale = np.maximum(np.abs(a), np.abs(b))
+    d = np.abs(a - b)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        u = np.where(scale > 0, d / (scale * ULP32), 0.0)
+    return u
+
+
+def test_cell_params(pair):
+    ctx, cells, _ = pair
+    p = ctx.cell_params()
+    assert np.array_equal(p["che"], cells.che)
+    assert np.max(np.abs(p["a_n"] - cells.a_n) / cells.a_n) < 4e-16
+    assert np.max(np.abs(p["znnpp"] - cells.znnpp) / np.abs(cells.znnpp)) < 1e-14
+    assert np.max(np.abs(p["kappa"] - cells.kappa) / np.abs(cells.kappa)) < 1e-14
+
+
+def test_mom_fill_fp64(pair, oracle):
+    ctx, cells, mode = pair
+    N = 3 * cells.n
+    for (r0, nr, c0, nc) in [(0, N, 0, N), (7, 100, 301, 77)]:
+        Zg = ctx.mom_fill(r0, nr, c0, nc)
+        Zo = oracle.mom_fill(cells, r0, nr, c0, nc)
+        assert np.max(np.abs(Zg - Zo)) / np.max(np.abs(Zo)) < 1e-13
+
+
+def test_mom_rhs_fp64(pair, oracle):
+    ctx, cells, _ = pair
+    th, ph = [90.0, 33.0, 150.0], [90.0, 250.0, 10.0]
+    assert np.max(np.abs(ctx.mom_rhs(th, ph) - oracle.mom_rhs(cells, th, ph))) < 1e-14
+
+
+def test_incident_field_complex4(pair, oracle):
+    ctx, cells, _ = pair
+    th, ph = [90.0, 33.0, 150.0], [90.0, 250.0, 10.0]
+    idx = np.arange(5, cells.n, 3, dtype=np.int32)
+    Eg, Eo = ctx.incident_field(th, ph, idx), oracle.incident_c4(cells, th, ph, idx)
+    u = ulps32(Eg, Eo)
+    assert u.max() <= 1.0
+    assert np.mean(u > 0) < 1e-3
+
+
+def test_block_fill_complex4(pair, oracle):
+    ctx, cells, mode = pair
+    i1 = np.arange(0, cells.n, 2, dtype=np.int32)
+    i2 = np.arange(1, cells.n, 3, dtype=np.int32)
+    for a, b in [(i1, i2), (i1, i1)]:
+        Zg, Zo = ctx.block_fill(a, b), oracle.green_partial(cells, a, b)
+        u = ulps32(Zg, Zo)
+        assert u.max() <= 2.0, (mode, u.max())
+        assert np.mean(u > 0) < 1e-3
+
+
+@pytest.mark.parametrize("homog", [0, 1])
+def test_sr_fill_and_ladder(gpulib, oracle, homog):
+    from midas_gb300 import _lib
+    from midas_gb300.solver import Context
+    xyz, sc, eps, k0 = scene(oracle, sc=0.25, inhom=not homog)
+    cells = oracle.Cells(xyz, sc, eps, k0)
+    idx = np.arange(cells.n, dtype=np.int32)[::-1].copy()
+    for mode in (_lib.FILL_FAITHFUL, _lib.FILL_FAST):
+        ctx = Context(fill_mode=mode).set_cells(xyz, sc, eps, k0)
+        f_g, nnz_g = ctx.set_fsr(idx, homog)
+        f_o, nnz_o = oracle.set_fsr(cells, idx, homog)
+        assert f_g == f_o and nnz_g == nnz_o
+        Zg, nz, fn = ctx.sr_fill(idx, f_o, homog)
+        Zo, nzo, fno = oracle.sr_dense(cells, idx, f_o, homog)
+        assert nz == nzo and abs(fn - fno) / fno < 1e-12
+        assert np.array_equal(Zg != 0, Zo != 0)
+        assert ulps32(Zg, Zo).max() <= 2.0
+        ctx.close()

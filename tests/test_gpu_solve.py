@@ -1,0 +1,95 @@
+"""Tensor-core GEMM engine, dense mixed-precision solve and the MoM path on the GPU."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx(gpulib):
+    from midas_gb300.solver import Context
+    c = Context()
+    yield c
+    c.close()
+
+
+def test_gemm_engine_selftest(ctx):
+    assert ctx.gemm_selftest() == "tcgen05"
+
+
+@pytest.mark.parametrize("n,nrhs", [(64, 1), (200, 3), (517, 8)])
+def test_dense_solve_mixed(ctx, n, nrhs):
+    rng = np.random.default_rng(n)
+    A = (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) / np.sqrt(n) * 0.4
+    A += np.eye(n) * (1.5 + 0.3j)
+    B = rng.standard_normal((n, nrhs)) + 1j * rng.standard_normal((n, nrhs))
+    X = ctx.dense_solve(A, B)
+    Xr = np.linalg.solve(A, B)
+    assert np.linalg.norm(X - Xr) / np.linalg.norm(Xr) < 1e-12
+    assert ctx.info.backward_error <= 1e-13 and ctx.info.ir_iters >= 1
+
+
+def test_dense_solve_torch_reference(ctx):
+    """The LU/IR result against a plain PyTorch reference solve of the same system."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(3)
+    n = 384
+    A = np.eye(n) * 2 + 0.3 * (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) / np.sqrt(n)
+    B = rng.standard_normal((n, 2)) + 1j * rng.standard_normal((n, 2))
+    X = ctx.dense_solve(A, B)
+    Xt = torch.linalg.solve(torch.from_numpy(A), torch.from_numpy(B)).numpy()
+    assert np.linalg.norm(X - Xt) / np.linalg.norm(Xt) < 1e-12
+
+
+@pytest.mark.parametrize("mode", ["mixed", "fp64"])
+def test_mom_solve_matches_oracle(gpulib, oracle, mode):
+    from midas_gb300 import _lib
+    from midas_gb300.solver import Context, compute_efields_mom
+    m, sc, k0 = 1.5 + 0.01j, 0.2, 2.0
+    xyz = oracle.sphere_cells(2.0, sc)
+    cells = oracle.Cells(xyz, sc, m * m, k0)
+    th, ph = [90.0, 40.0], [90.0, 200.0]
+    rth = np.linspace(0, 180, 19)
+    rph = np.zeros_like(rth) + 90.0
+    ref = oracle.mom_solve(cells, th, ph, rth, rph)
+    sm = _lib.SOLVE_MIXED if mode == "mixed" else _lib.SOLVE_FP64
+    c = Context(solve_mode=sm).set_cells(xyz, sc, m * m, k0)
+    E, S, ce, ca = compute_efields_mom(c, th, ph, rth, rph)
+    rel = np.linalg.norm(E - ref["E"]) / np.linalg.norm(ref["E"])
+    assert rel < 1e-10, rel
+    assert np.max(np.abs(ce - ref["cext"]) / np.abs(ref["cext"])) < 1e-10
+    assert np.max(np.abs(ca - ref["cabs"]) / np.abs(ref["cabs"])) < 1e-10
+    assert np.max(np.abs(S - ref["S"])) / np.max(np.abs(ref["S"])) < 1e-10
+    if mode == "mixed":
+        assert c.info.backward_error <= 1e-13
+    c.close()
+
+
+def test_mom_solve_inhomogeneous_fast_fill(gpulib, oracle):
+    from midas_gb300 import _lib, geometry as G
+    from midas_gb300.solver import Context
+    rng = np.random.default_rng(11)
+    xyz = G.cube_cells(9, 0.1)
+    eps = rng.uniform(1.5, 3.5, len(xyz)) + 1j * rng.uniform(0, 0.2, len(xyz))
+    k0 = 2 * np.pi / (9 * 0.1 / 2)
+    cells = oracle.Cells(xyz, 0.1, eps, k0)
+    th, ph = [10.0, 70.0, 130.0], [30.0, 200.0, 300.0]
+    ref = oracle.mom_solve(cells, th, ph)
+    c = Context(fill_mode=_lib.FILL_FAST).set_cells(xyz, 0.1, eps, k0)
+    E = c.mom_solve(th, ph)
+    assert np.linalg.norm(E - ref["E"]) / np.linalg.norm(ref["E"]) < 1e-10
+    c.close()
+
+
+def test_errors_are_reported(gpulib):
+    from midas_gb300._lib import MidasError
+    from midas_gb300.solver import Context
+    c = Context()
+    with pytest.raises(MidasError) as e:
+        c.mom_solve([0.0], [0.0])
+    assert e.value.status == 6   # MIDAS_ERR_STATE: no cells
+    c.set_cells(np.zeros((2, 3)) + [[0, 0, 0], [0.1, 0, 0]], 0.1, 2.0, 1.0)
+    with pytest.raises(MidasError) as e:
+        c.mom_fill(0, 7, 0, 6)
+    assert e.value.status == 1   # block outside the matrix
+    c.close()
