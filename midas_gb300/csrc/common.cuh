@@ -31,9 +31,9 @@ struct Err {
                                   std::string(#expr) + ": " + cudaGetErrorString(_e));             \
     } while (0)
 
-#define MIDAS_TRY(expr)                  \
+#define MIDAS_TRY(...)                   \
     do {                                 \
-        int _s = (expr);                 \
+        int _s = (__VA_ARGS__);          \
         if (_s != MIDAS_OK) return _s;   \
     } while (0)
 

@@ -431,6 +431,29 @@ int zgesv_fp64(midas_gpu_ctx *c, int n, int nrhs, double2 *A, double2 *B, midas_
     return MIDAS_OK;
 }
 
+
+
+// Mixed solve of a system whose FP64 row-major matrix Z64 and complex64 copy Z32
+// (np x np, padded) are already in the pool slots; b/x are np x nrhs (ld np).
+int mixed_solve(midas_gpu_ctx *c, int np, float2 *Z32, const double2 *Z64, const double2 *b, double2 *x,
+                              int nrhs, midas_gpu_info *info)
+{
+    DenseLU lu;
+    lu.n = np;
+    lu.A = Z32;
+    lu.lda = np;
+    Timer tf(c->stream);
+    MIDAS_TRY(lu_factor_nopiv(c, lu));
+    MIDAS_TRY(check_flag(c, "lu_factor"));
+    float tfac = tf.stop();
+    Timer ts(c->stream);
+    int st = ir_solve(c, lu, Z64, np, b, x, nrhs, info);
+    float tsol = ts.stop();
+    if (info) { info->t_factor_ms = tfac; info->t_solve_ms = tsol; }
+    return st;
+}
+
+
 void destroy_cusolver(void *h) { cusolverDnDestroy((cusolverDnHandle_t)h); }
 
 }  // namespace midas

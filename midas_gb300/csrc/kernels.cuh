@@ -4,6 +4,23 @@
 
 namespace midas {
 
+// CUDA-event timer on a stream (device time between construction and stop()).
+struct Timer {
+    cudaEvent_t a, b;
+    cudaStream_t s;
+    explicit Timer(cudaStream_t st) : s(st) { cudaEventCreate(&a); cudaEventCreate(&b); cudaEventRecord(a, s); }
+    float stop()
+    {
+        float ms = 0;
+        cudaEventRecord(b, s);
+        cudaEventSynchronize(b);
+        cudaEventElapsedTime(&ms, a, b);
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        return ms;
+    }
+};
+
 // fill.cu
 int launch_set_cells(midas_gpu_ctx *c);
 int launch_lat_table(midas_gpu_ctx *c);
@@ -57,6 +74,10 @@ int ir_solve(midas_gpu_ctx *c, const DenseLU &lu, const double2 *Z64, long long 
              int nrhs, midas_gpu_info *info);
 int zgesv_fp64(midas_gpu_ctx *c, int n, int nrhs, double2 *Acol, double2 *Bcol, midas_gpu_info *info);
 void destroy_cusolver(void *h);
+// Mixed solve of a system whose FP64 row-major matrix Z64 and complex64 copy Z32
+// (np x np, padded to 64) are filled; b/x are np x nrhs column-major (ld np).
+int mixed_solve(midas_gpu_ctx *c, int np, float2 *Z32, const double2 *Z64, const double2 *b, double2 *x, int nrhs,
+                midas_gpu_info *info);
 int inf_norm_rows(midas_gpu_ctx *c, const double2 *Z, long long ldz, int n, double *out);
 
 }  // namespace midas

@@ -526,42 +526,6 @@ __global__ void k_copy_unpad(const double2 *src, int n, int np, int nrhs, double
     dst[i] = src[(long long)k * np + r];
 }
 
-struct Timer {
-    cudaEvent_t a, b;
-    cudaStream_t s;
-    explicit Timer(cudaStream_t st) : s(st) { cudaEventCreate(&a); cudaEventCreate(&b); cudaEventRecord(a, s); }
-    float stop()
-    {
-        float ms = 0;
-        cudaEventRecord(b, s);
-        cudaEventSynchronize(b);
-        cudaEventElapsedTime(&ms, a, b);
-        cudaEventDestroy(a);
-        cudaEventDestroy(b);
-        return ms;
-    }
-};
-
-// Mixed solve of a system whose FP64 row-major matrix Z64 and complex64 copy Z32
-// (np x np, padded) are already in the pool slots; b/x are np x nrhs (ld np).
-static int mixed_solve_filled(midas_gpu_ctx *c, int np, float2 *Z32, const double2 *Z64, const double2 *b, double2 *x,
-                              int nrhs, midas_gpu_info *info)
-{
-    DenseLU lu;
-    lu.n = np;
-    lu.A = Z32;
-    lu.lda = np;
-    Timer tf(c->stream);
-    MIDAS_TRY(lu_factor_nopiv(c, lu));
-    MIDAS_TRY(check_flag(c, "lu_factor"));
-    float tfac = tf.stop();
-    Timer ts(c->stream);
-    int st = ir_solve(c, lu, Z64, np, b, x, nrhs, info);
-    float tsol = ts.stop();
-    if (info) { info->t_factor_ms = tfac; info->t_solve_ms = tsol; }
-    return st;
-}
-
 }  // namespace midas
 
 extern "C" {
@@ -606,7 +570,7 @@ int midas_gpu_dense_solve(midas_gpu_ctx *c, int n, int nrhs, const double *A, do
         k_copy_pad<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>((const double2 *)pbin, n, np, nrhs,
                                                                          (double2 *)pb);
         MIDAS_CUDA(c, cudaGetLastError());
-        st = mixed_solve_filled(c, np, (float2 *)p32, (const double2 *)p64, (const double2 *)pb, (double2 *)px, nrhs,
+        st = mixed_solve(c, np, (float2 *)p32, (const double2 *)p64, (const double2 *)pb, (double2 *)px, nrhs,
                                 info);
         if (st == MIDAS_OK) {
             void *pout;
@@ -674,7 +638,7 @@ int midas_gpu_mom_solve(midas_gpu_ctx *c, int ntr, const double *theta, const do
         MIDAS_TRY(launch_mom_rhs<double2>(c, ntr, (const double *)th, (const double *)ph, (double2 *)pb, 1, np));
         float tfill = tf.stop();
         if (info) info->t_fill_ms = tfill;
-        st = mixed_solve_filled(c, np, (float2 *)p32, (const double2 *)p64, (const double2 *)pb, (double2 *)px, nrhs,
+        st = mixed_solve(c, np, (float2 *)p32, (const double2 *)p64, (const double2 *)pb, (double2 *)px, nrhs,
                                 info);
         if (st == MIDAS_OK) {
             void *pout;

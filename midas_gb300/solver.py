@@ -149,7 +149,7 @@ class Context:
     def dense_solve(self, A, B):
         """PZGESV stand-in: solve A X = B (column-major complex)."""
         A = np.asfortranarray(A, dtype=np.complex128)
-        X = np.asfortranarray(B, dtype=np.complex128).copy()
+        X = np.array(B, dtype=np.complex128, order="F", copy=True)
         n, nrhs = X.shape
         self._ck(self.L.midas_gpu_dense_solve(self.h, n, nrhs, addr(A), addr(X), ctypes.byref(self.info)))
         return X
