@@ -184,6 +184,13 @@ int midas_gpu_smatrix(midas_gpu_ctx *ctx, int nrx, const double *rx_theta, const
 int midas_gpu_gemm_selftest(midas_gpu_ctx *ctx);
 /* Name of the GEMM engine in use ("tcgen05"). */
 const char *midas_gpu_gemm_engine(void);
+/* Hermitian eigen-decomposition on the device (the CBF singular-value step):
+ * A is m x m row-major complex; W receives the eigenvalues in descending order and
+ * V (row-major m x m) the eigenvectors as columns. */
+int midas_gpu_heev(midas_gpu_ctx *ctx, int m, const double *A, double *W, double *V);
+/* FP32-grade complex product D = A B on the tensor cores (the split-TF32 GEMM of
+ * the reduced-matrix assembly); A (M x K), B (K x N), D (M x N) row-major complex. */
+int midas_gpu_zgemm_x3(midas_gpu_ctx *ctx, int M, int N, int K, const double *A, const double *B, double *D);
 /* Average device time (CUDA events on the context stream) of `iters` launches of
  * the tensor-core GEMM D[M x N] -= A[M x K] Bt[N x K]^T on internal buffers (fp32). */
 int midas_gpu_bench_gemm(midas_gpu_ctx *ctx, int M, int N, int K, int iters, double *ms);

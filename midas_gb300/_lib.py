@@ -28,7 +28,7 @@ EXPORTS = [
     "midas_gpu_block_fill", "midas_gpu_sr_fill", "midas_gpu_set_fsr", "midas_gpu_aca", "midas_gpu_dense_solve",
     "midas_gpu_mom_solve", "midas_gpu_cbfm_solve", "midas_gpu_cext_cabs", "midas_gpu_smatrix",
     "midas_gpu_gemm_selftest", "midas_gpu_gemm_engine", "midas_gpu_launch_count", "midas_gpu_stream",
-    "midas_gpu_bench_gemm",
+    "midas_gpu_bench_gemm", "midas_gpu_heev", "midas_gpu_zgemm_x3",
 ]
 
 
@@ -93,6 +93,8 @@ def load(path: str = LIB_PATH):
         "midas_gpu_launch_count": (ctypes.c_longlong, [vp]),
         "midas_gpu_stream": (ctypes.c_void_p, [vp]),
         "midas_gpu_bench_gemm": (i, [vp, i, i, i, i, ctypes.POINTER(ctypes.c_double)]),
+        "midas_gpu_heev": (i, [vp, i, P, P, P]),
+        "midas_gpu_zgemm_x3": (i, [vp, i, i, i, P, P, P]),
     }
     for name, (res, args) in sigs.items():
         f = getattr(L, name)

@@ -12,8 +12,8 @@
 //    double-float pair; products are exact (FMA two-product) and sums use
 //    compensated double-float accumulation, giving an FP64-grade residual
 //    without the GB300's slow FP64 pipe.
-//  * heev_jacobi : Hermitian eigen-decomposition (parallel cyclic Jacobi, FP64)
-//    of the CBF Gram matrices; one CTA per matrix.
+//  * heev_dev : Hermitian eigen-decomposition (Householder tridiagonalisation +
+//    implicit QL, FP64) of the CBF Gram matrices; one CTA per matrix.
 #include <cmath>
 
 #include "common.cuh"
@@ -104,7 +104,7 @@ int zgemm_x3(midas_gpu_ctx *c, int M, int N, int K, const TA *A, long long ars, 
     k_split_expand_b<TB><<<dim3((K + 127) / 128, N), 128, 0, c->stream>>>(K, N, B, brs, bcs, B3, K6);
     MIDAS_CUDA(c, cudaGetLastError());
     GemmArgs g{M, 2 * N, (int)K6, A3, K6, B3, K6, D, ldd, alpha, beta};
-    return gemm_tf32(c, g);
+    return gemm_tf32(c, g, true);
 }
 template int zgemm_x3<float2, double2>(midas_gpu_ctx *, int, int, int, const float2 *, long long, long long, int,
                                        const double2 *, long long, long long, float *, long long, float, float);
@@ -256,162 +256,244 @@ int residual_df32(midas_gpu_ctx *c, int n, int nrhs, const float2 *Z, long long 
 }
 
 // ---------------------------------------------------------------------------
-// Hermitian Jacobi eigen-solver (FP64), one CTA per matrix.
-// A: batch of m x m Hermitian matrices (row-major, leading dim lda, stride sa);
-// on exit W (descending eigenvalues) and V (row-major m x m, columns = vectors).
-// Parallel ordering: round-robin tournament, m/2 disjoint pairs per round.
+// Hermitian eigen-decomposition (FP64), one CTA per matrix: Householder
+// tridiagonalisation (the zhetd2 recurrence: H = I - tau v v^H, x = tau A v,
+// w = x - tau/2 (x^H v) v, A <- A - v w^H - w v^H), implicit-shift QL on the real
+// tridiagonal (one thread generates the Givens rotations of an iteration, all
+// threads apply them to their rows of Z), back-transformation V = H_0 .. H_{m-2} Z,
+// eigenpairs sorted by decreasing eigenvalue.  Backward stable: absolute errors
+// ~ eps ||A||, so the CBF threshold subspace is resolved to eps ||A|| / gap.
+// A (m x m row-major, lda) is destroyed; Hv (m x m) holds the reflectors; Z is the
+// output V (row-major m x m).  Shared memory: d, e, tau, v, x, rotation buffers.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(1024) k_heev_jacobi(int m, double2 *A, long long lda, long long sa, double2 *V,
-                                                      long long sv, double *W, int sweeps, double tol)
+__device__ double block_sum_d(double v, double *red)
 {
-    extern __shared__ double sh[];
-    int mm = m + (m & 1);    // even player count (a dummy when m is odd)
-    int *perm = (int *)sh;   // mm ints
-    double *cs = (double *)(perm + mm + (mm & 1));   // per pair: c, s*cos(phi), s*sin(phi)
-    double *red = cs + 3 * (mm / 2);
-    double2 *a = A + blockIdx.x * sa;
-    double2 *v = V + blockIdx.x * sv;
-    const int tid = threadIdx.x, nt = blockDim.x;
-    for (int t = tid; t < m * m; t += nt) v[(t / m) * m + t % m] = make_double2((t / m == t % m) ? 1.0 : 0.0, 0.0);
-    for (int t = tid; t < mm; t += nt) perm[t] = t;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     __syncthreads();
-    for (int sw = 0; sw < sweeps; ++sw) {
-        // off-diagonal norm vs diagonal norm
-        double off = 0, dia = 0;
-        for (int t = tid; t < m * m; t += nt) {
-            int i = t / m, j = t % m;
-            double2 x = a[(long long)i * lda + j];
-            double q = x.x * x.x + x.y * x.y;
-            if (i == j) dia += q; else off += q;
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            off += __shfl_down_sync(0xffffffffu, off, o);
-            dia += __shfl_down_sync(0xffffffffu, dia, o);
-        }
-        if ((tid & 31) == 0) { red[2 * (tid >> 5)] = off; red[2 * (tid >> 5) + 1] = dia; }
-        __syncthreads();
-        if (tid == 0) {
-            double so = 0, sd = 0;
-            for (int w = 0; w < nt / 32; ++w) { so += red[2 * w]; sd += red[2 * w + 1]; }
-            red[0] = so; red[1] = sd;
-        }
-        __syncthreads();
-        bool done = red[0] <= tol * tol * red[1];
-        __syncthreads();
-        if (done) break;
-        for (int round = 0; round < mm - 1; ++round) {
-            // pair t: (perm[t], perm[mm-1-t])
-            for (int t = tid; t < mm / 2; t += nt) {
-                int p = perm[t], q = perm[mm - 1 - t];
-                if (p > q) { int tmp = p; p = q; q = tmp; }
-                double c = 1, sr = 0, si = 0;
-                if (q < m) {
-                    double app = a[(long long)p * lda + p].x, aqq = a[(long long)q * lda + q].x;
-                    double2 apq = a[(long long)p * lda + q];
-                    double g = hypot(apq.x, apq.y);
-                    if (g > 1e-300) {
-                        // zero a_pq: tan(2 th) = 2|a_pq| / (a_qq - a_pp)
-                        double th = 0.5 * atan2(2.0 * g, aqq - app);
-                        double cth = cos(th), sth = sin(th);
-                        c = cth;
-                        sr = sth * apq.x / g;
-                        si = sth * apq.y / g;
-                    }
-                }
-                cs[3 * t] = c; cs[3 * t + 1] = sr; cs[3 * t + 2] = si;
-            }
-            __syncthreads();
-            // rotation J on columns (p, q): J_pp = c, J_qq = c, J_pq = s e^{i phi}... applied as
-            // A <- J^H A J, V <- V J with  col_p' = c col_p - conj(s) col_q,  col_q' = s col_p + c col_q
-            // rows: row_p' = c row_p - s row_q, row_q' = conj(s) row_p + c row_q
-            int npair = mm / 2;
-            for (int t = tid; t < npair * m; t += nt) {   // rows
-                int pr = t / m, k = t % m;
-                int p = perm[pr], q = perm[mm - 1 - pr];
-                if (p > q) { int tmp = p; p = q; q = tmp; }
-                if (q >= m) continue;
-                double c = cs[3 * pr], sr = cs[3 * pr + 1], si = cs[3 * pr + 2];
-                double2 x = a[(long long)p * lda + k], y = a[(long long)q * lda + k];
-                // row_p' = c x - s y ; row_q' = conj(s) x + c y     (s = sr + i si)
-                a[(long long)p * lda + k] = make_double2(c * x.x - (sr * y.x - si * y.y), c * x.y - (sr * y.y + si * y.x));
-                a[(long long)q * lda + k] = make_double2(sr * x.x + si * x.y + c * y.x, sr * x.y - si * x.x + c * y.y);
-            }
-            __syncthreads();
-            for (int t = tid; t < npair * m; t += nt) {   // columns of A and V
-                int pr = t / m, k = t % m;
-                int p = perm[pr], q = perm[mm - 1 - pr];
-                if (p > q) { int tmp = p; p = q; q = tmp; }
-                if (q >= m) continue;
-                double c = cs[3 * pr], sr = cs[3 * pr + 1], si = cs[3 * pr + 2];
-                // col_p' = c x - conj(s) y ; col_q' = s x + c y
-                double2 x = a[(long long)k * lda + p], y = a[(long long)k * lda + q];
-                a[(long long)k * lda + p] = make_double2(c * x.x - (sr * y.x + si * y.y), c * x.y - (sr * y.y - si * y.x));
-                a[(long long)k * lda + q] = make_double2(sr * x.x - si * x.y + c * y.x, sr * x.y + si * x.x + c * y.y);
-                x = v[(long long)k * m + p];
-                y = v[(long long)k * m + q];
-                v[(long long)k * m + p] = make_double2(c * x.x - (sr * y.x + si * y.y), c * x.y - (sr * y.y - si * y.x));
-                v[(long long)k * m + q] = make_double2(sr * x.x - si * x.y + c * y.x, sr * x.y + si * x.x + c * y.y);
-            }
-            __syncthreads();
-            // rotate the tournament (player 0 fixed)
-            if (tid == 0) {
-                int last = perm[mm - 1];
-                for (int t = mm - 1; t > 1; --t) perm[t] = perm[t - 1];
-                perm[1] = last;
-            }
-            __syncthreads();
-        }
-    }
-    // eigenvalues: diagonal, sorted descending together with the vectors (selection sort on indices)
-    double *wv = W + blockIdx.x * m;
-    for (int t = tid; t < m; t += nt) wv[t] = a[(long long)t * lda + t].x;
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
     __syncthreads();
-    if (tid == 0) {
-        for (int i = 0; i < m; ++i) perm[i] = i;
-        for (int i = 0; i < m; ++i) {
-            int b = i;
-            for (int j = i + 1; j < m; ++j)
-                if (wv[perm[j]] > wv[perm[b]]) b = j;
-            int tmp = perm[i]; perm[i] = perm[b]; perm[b] = tmp;
-        }
-    }
-    __syncthreads();
-    // permute: write sorted eigenvalues into red scratch then back; vectors into A (as scratch)
-    for (int t = tid; t < m * m; t += nt) {
-        int k = t / m, j = t % m;
-        a[(long long)k * lda + j] = v[(long long)k * m + perm[j]];
-    }
-    __syncthreads();
-    for (int t = tid; t < m * m; t += nt) {
-        int k = t / m, j = t % m;
-        v[(long long)k * m + j] = a[(long long)k * lda + j];
-    }
-    double *tmpw = red;   // red has room for >= 2*32 doubles; use W directly with a second pass
-    __syncthreads();
-    if (tid == 0) {
-        // in-place permutation of wv via V's first row is not available; use a simple O(m^2) rewrite
-        for (int i = 0; i < m; ++i) tmpw[0] = 0;
-    }
-    __syncthreads();
-    // sorted eigenvalues: read diag of the (unchanged) eigenvalue array through perm
-    // (store into A's diagonal first to avoid aliasing)
-    for (int t = tid; t < m; t += nt) a[(long long)t * lda + t].x = wv[perm[t]];
-    __syncthreads();
-    for (int t = tid; t < m; t += nt) wv[t] = a[(long long)t * lda + t].x;
+    double s = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+    return s;
 }
 
-int heev_jacobi(midas_gpu_ctx *c, int batch, int m, double2 *A, long long lda, long long sa, double2 *V,
-                long long sv, double *W)
+__global__ void __launch_bounds__(256) k_heev_tridiag(int m, double2 *Ab, long long lda, long long sa, double2 *Hb,
+                                                      double2 *Vb, long long sv, double *Wb, int *flag)
 {
-    int mm = m + (m & 1);
-    size_t sm = sizeof(int) * (mm + 2) + sizeof(double) * (3 * (mm / 2) + 64) + 64;
-    static int attr_set = 0;
-    if (sm > 48 * 1024 && !attr_set) {
-        MIDAS_CUDA(c, cudaFuncSetAttribute(k_heev_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-        attr_set = 1;
+    extern __shared__ double shm[];
+    double *d = shm, *e = d + m, *rc = e + m, *rs = rc + m, *red = rs + m;   // red: 32 doubles
+    double2 *tau = (double2 *)(red + 32), *v = tau + m, *x = v + m;
+    __shared__ int nrot;
+    __shared__ double2 s_tau, s_scale;
+    __shared__ double s_beta;
+    double2 *A = Ab + blockIdx.x * sa;
+    double2 *H = Hb + blockIdx.x * sv;
+    double2 *V = Vb + blockIdx.x * sv;
+    double *W = Wb + (long long)blockIdx.x * m;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    // ---- tridiagonalisation --------------------------------------------------
+    for (int k = 0; k < m - 1; ++k) {
+        const int L = m - k - 1;   // trailing size
+        double xn2 = 0;
+        for (int r = k + 2 + tid; r < m; r += nt) {
+            double2 a = A[(long long)r * lda + k];
+            xn2 += a.x * a.x + a.y * a.y;
+        }
+        xn2 = block_sum_d(xn2, red);
+        if (tid == 0) {
+            double2 al = A[(long long)(k + 1) * lda + k];
+            if (xn2 == 0 && al.y == 0) {
+                s_tau = make_double2(0, 0);
+                s_beta = al.x;
+            } else {
+                double beta = -copysign(sqrt(al.x * al.x + al.y * al.y + xn2), al.x);
+                s_tau = make_double2((beta - al.x) / beta, -al.y / beta);
+                double2 dnm = make_double2(al.x - beta, al.y);   // 1/(alpha - beta)
+                double q = dnm.x * dnm.x + dnm.y * dnm.y;
+                s_scale = make_double2(dnm.x / q, -dnm.y / q);
+                s_beta = beta;
+            }
+        }
+        __syncthreads();
+        const double2 t = s_tau;
+        for (int i = tid; i < L; i += nt) {
+            double2 vi;
+            if (i == 0) vi = make_double2(1, 0);
+            else {
+                double2 a = A[(long long)(k + 1 + i) * lda + k];
+                vi = make_double2(a.x * s_scale.x - a.y * s_scale.y, a.x * s_scale.y + a.y * s_scale.x);
+            }
+            v[i] = vi;
+            H[(long long)(k + 1 + i) * m + k] = vi;
+        }
+        if (tid == 0) tau[k] = t;
+        __syncthreads();
+        if (t.x != 0 || t.y != 0) {
+            // x = tau * A22 v
+            for (int i = tid; i < L; i += nt) {
+                const double2 *row = A + (long long)(k + 1 + i) * lda + (k + 1);
+                double sx = 0, sy = 0;
+                for (int j = 0; j < L; ++j) {
+                    double2 a = row[j], vj = v[j];
+                    sx += a.x * vj.x - a.y * vj.y;
+                    sy += a.x * vj.y + a.y * vj.x;
+                }
+                x[i] = make_double2(t.x * sx - t.y * sy, t.x * sy + t.y * sx);
+            }
+            __syncthreads();
+            // dot = x^H v ; alpha = -1/2 tau dot ; w = x + alpha v  (w stored in x)
+            double pr = 0, pi = 0;
+            for (int i = tid; i < L; i += nt) {
+                double2 a = x[i], b = v[i];
+                pr += a.x * b.x + a.y * b.y;
+                pi += a.x * b.y - a.y * b.x;
+            }
+            pr = block_sum_d(pr, red);
+            pi = block_sum_d(pi, red);
+            double2 al = make_double2(-0.5 * (t.x * pr - t.y * pi), -0.5 * (t.x * pi + t.y * pr));
+            __syncthreads();
+            for (int i = tid; i < L; i += nt) {
+                double2 b = v[i];
+                x[i] = make_double2(x[i].x + al.x * b.x - al.y * b.y, x[i].y + al.x * b.y + al.y * b.x);
+            }
+            __syncthreads();
+            // A22 -= v w^H + w v^H
+            for (int q = tid; q < L * L; q += nt) {
+                int i = q / L, j = q % L;
+                double2 vi = v[i], wi = x[i], vj = v[j], wj = x[j];
+                double2 *a = A + (long long)(k + 1 + i) * lda + (k + 1 + j);
+                a->x -= (vi.x * wj.x + vi.y * wj.y) + (wi.x * vj.x + wi.y * vj.y);
+                a->y -= (vi.y * wj.x - vi.x * wj.y) + (wi.y * vj.x - wi.x * vj.y);
+            }
+        }
+        if (tid == 0) {
+            e[k] = s_beta;
+            d[k] = A[(long long)k * lda + k].x;
+        }
+        __syncthreads();
     }
+    if (tid == 0) { d[m - 1] = A[(long long)(m - 1) * lda + (m - 1)].x; e[m - 1] = 0; }
+    // Z = I (real, kept in V.x; V.y = 0)
+    for (int q = tid; q < m * m; q += nt) V[q] = make_double2((q / m == q % m) ? 1.0 : 0.0, 0.0);
+    __syncthreads();
+    // ---- implicit QL on (d, e) ------------------------------------------------
+    // deflation: |e| <= eps (|d_i| + |d_i+1|), or |e| <= eps ||T|| -- eigenvalues at the
+    // roundoff level of a rank-deficient Gram matrix never pass the relative test alone
+    const double eps = 2.220446049250313e-16;
+    __shared__ double s_tn;
+    if (tid == 0) {
+        double tn = 0;
+        for (int i = 0; i < m; ++i) tn = fmax(tn, fabs(d[i]) + fabs(e[i]) + (i > 0 ? fabs(e[i - 1]) : 0.0));
+        s_tn = tn;
+    }
+    __syncthreads();
+    const double tnorm = s_tn;
+    for (int l = 0; l < m; ++l) {
+        int iter = 0;
+        while (true) {
+            __shared__ int s_mm;
+            if (tid == 0) {
+                int mm = l;
+                while (mm < m - 1) {
+                    double dd = fabs(d[mm]) + fabs(d[mm + 1]);
+                    if (fabs(e[mm]) <= eps * dd || fabs(e[mm]) <= eps * tnorm) break;
+                    ++mm;
+                }
+                s_mm = mm;
+            }
+            __syncthreads();
+            const int mm = s_mm;
+            if (mm == l) break;
+            if (++iter > 200) {
+                if (tid == 0) atomicOr(flag, DEV_BAD_ARG);
+                break;
+            }
+            if (tid == 0) {
+                double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
+                double r = hypot(g, 1.0);
+                g = d[mm] - d[l] + e[l] / (g + copysign(r, g));
+                double s = 1, c = 1, p = 0;
+                int cnt = 0, broke = 0;
+                for (int i = mm - 1; i >= l; --i) {
+                    double f = s * e[i], b = c * e[i];
+                    r = hypot(f, g);
+                    e[i + 1] = r;
+                    if (r == 0.0) { d[i + 1] -= p; e[mm] = 0.0; broke = 1; break; }
+                    s = f / r; c = g / r;
+                    g = d[i + 1] - p;
+                    r = (d[i] - g) * s + 2.0 * c * b;
+                    p = s * r;
+                    d[i + 1] = g + p;
+                    g = c * r - b;
+                    rs[cnt] = s; rc[cnt] = c;
+                    ++cnt;
+                }
+                if (!broke) { d[l] -= p; e[l] = g; e[mm] = 0.0; }
+                nrot = cnt;
+            }
+            __syncthreads();
+            // apply the rotations (in generation order) to every row of Z
+            for (int row = tid; row < m; row += nt) {
+                double2 *z = V + (long long)row * m;
+                for (int q = 0; q < nrot; ++q) {
+                    int i = mm - 1 - q;
+                    double s = rs[q], c = rc[q];
+                    double f = z[i + 1].x;
+                    z[i + 1].x = s * z[i].x + c * f;
+                    z[i].x = c * z[i].x - s * f;
+                }
+            }
+            __syncthreads();
+        }
+    }
+    // ---- back-transformation V = H_0 H_1 ... H_{m-2} Z --------------------------
+    for (int k = m - 2; k >= 0; --k) {
+        double2 t = tau[k];
+        if (t.x == 0 && t.y == 0) continue;
+        const int L = m - k - 1;
+        for (int j = tid; j < m; j += nt) {
+            double wr = 0, wi = 0;   // w_j = sum_r conj(v_r) V[r][j]
+            for (int r = 0; r < L; ++r) {
+                double2 vr = H[(long long)(k + 1 + r) * m + k], z = V[(long long)(k + 1 + r) * m + j];
+                wr += vr.x * z.x + vr.y * z.y;
+                wi += vr.x * z.y - vr.y * z.x;
+            }
+            double2 tw = make_double2(t.x * wr - t.y * wi, t.x * wi + t.y * wr);
+            for (int r = 0; r < L; ++r) {
+                double2 vr = H[(long long)(k + 1 + r) * m + k];
+                double2 *z = V + (long long)(k + 1 + r) * m + j;
+                z->x -= vr.x * tw.x - vr.y * tw.y;
+                z->y -= vr.x * tw.y + vr.y * tw.x;
+            }
+        }
+        __syncthreads();
+    }
+    // ---- sort (descending) ------------------------------------------------------
+    __shared__ int ord[1024];
+    if (tid == 0) {
+        for (int i = 0; i < m; ++i) ord[i] = i;
+        for (int i = 0; i < m; ++i) {
+            int bst = i;
+            for (int j = i + 1; j < m; ++j)
+                if (d[ord[j]] > d[ord[bst]]) bst = j;
+            int tmp = ord[i]; ord[i] = ord[bst]; ord[bst] = tmp;
+        }
+    }
+    __syncthreads();
+    for (int i = tid; i < m; i += nt) W[i] = d[ord[i]];
+    // permute the columns of V through A (scratch)
+    for (int q = tid; q < m * m; q += nt) A[(long long)(q / m) * lda + q % m] = V[(long long)(q / m) * m + ord[q % m]];
+    __syncthreads();
+    for (int q = tid; q < m * m; q += nt) V[q] = A[(long long)(q / m) * lda + q % m];
+}
+
+int heev_dev(midas_gpu_ctx *c, int batch, int m, double2 *A, long long lda, long long sa, double2 *H, double2 *V,
+             long long sv, double *W)
+{
+    if (m > 1024) return c->err.set(MIDAS_ERR_ARG, "heev: m > 1024");
+    size_t sm = sizeof(double) * (4 * (size_t)m + 32) + sizeof(double2) * 3 * (size_t)m;
     ++c->launches;
-    k_heev_jacobi<<<batch, 1024, sm, c->stream>>>(m, A, lda, sa, V, sv, W, 30, 1e-15);
+    k_heev_tridiag<<<batch, 256, sm, c->stream>>>(m, A, lda, sa, H, V, sv, W, c->d_flag);
     MIDAS_CUDA(c, cudaGetLastError());
     return MIDAS_OK;
 }

@@ -9,7 +9,7 @@
 //      c. CBF excitations (Incident_Field, complex(4) locals) [361-369]
 //      d. solve Z_ext X = E_ref: no-pivot TF32 tensor LU + refinement with a
 //         double-float residual (PARDISO with 20 refinement steps in the reference) [396]
-//      e. SVD of X by its Gram matrix X^H X (FP64) and Hermitian Jacobi; keep
+//      e. SVD of X by its Gram matrix X^H X (FP64) and a Hermitian eigen-solver; keep
 //         sigma_i / sigma_1 >= Threshold_CBFM; C_b = (X V_K Sigma_K^-1)[rows of the
 //         non-extended block] [419-445] -- the span of the retained left singular
 //         vectors, which is all the reduced system depends on.
@@ -36,8 +36,8 @@ int zgemm_x3(midas_gpu_ctx *c, int M, int N, int K, const TA *A, long long ars, 
              const TB *B, long long brs, long long bcs, float *D, long long ldd, float alpha, float beta);
 int residual_df32(midas_gpu_ctx *c, int n, int nrhs, const float2 *Z, long long ldz, const float2 *Xh,
                   const float2 *Xl, const float2 *B, double2 *R);
-int heev_jacobi(midas_gpu_ctx *c, int batch, int m, double2 *A, long long lda, long long sa, double2 *V,
-                long long sv, double *W);
+int heev_dev(midas_gpu_ctx *c, int batch, int m, double2 *A, long long lda, long long sa, double2 *H, double2 *V,
+             long long sv, double *W);
 
 static inline int pad64(int x) { return (x + 63) / 64 * 64; }
 
@@ -207,17 +207,18 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
     MIDAS_TRY(ensure(c, S_CBF2, sizeof(float2) * (size_t)spmax * spmax, &p2));
     size_t nrm = (size_t)spmax * m;
     MIDAS_TRY(ensure(c, S_CBF3, (sizeof(float2) * 4 + sizeof(double2) * 2) * nrm + 4096, &p3));
-    MIDAS_TRY(ensure(c, S_CBF4, sizeof(double2) * (size_t)2 * m * m + sizeof(double) * m + 4096, &p4));
+    MIDAS_TRY(ensure(c, S_CBF4, sizeof(double2) * (size_t)3 * m * m + sizeof(double) * m + 4096, &p4));
     float2 *Zlu = (float2 *)p1, *Zsr = (float2 *)p2;
     Buf b3{c, 0, (char *)p3};
     float2 *Bm = b3.take<float2>(nrm), *Xh = b3.take<float2>(nrm), *Xl = b3.take<float2>(nrm),
            *d32 = b3.take<float2>(nrm);
     double2 *X64 = b3.take<double2>(nrm), *R64 = b3.take<double2>(nrm);
     Buf b4{c, 0, (char *)p4};
-    double2 *G = b4.take<double2>((size_t)m * m), *Vv = b4.take<double2>((size_t)m * m);
+    double2 *G = b4.take<double2>((size_t)m * m), *Vv = b4.take<double2>((size_t)m * m),
+            *Hh = b4.take<double2>((size_t)m * m);
     double *W = b4.take<double>(m);
     void *pred;
-    MIDAS_TRY(ensure(c, S_RED, sizeof(unsigned long long) * 2 * m + 64, &pred));
+    MIDAS_TRY(ensure(c, S_RED2, sizeof(unsigned long long) * 2 * m + 64, &pred));
     unsigned long long *red = (unsigned long long *)pred;
     std::vector<unsigned long long> hred(2 * m);
     std::vector<double> hW(m);
@@ -239,6 +240,7 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
             double2 zn;
             MIDAS_CUDA(c, cudaMemcpy(&zn, c->znnpp + bo[b], sizeof(double2), cudaMemcpyDeviceToHost));
             thr_sr = hypot(1 - zn.x, -zn.y) / fsr;
+            if (c->opts.verbose >= 2) fprintf(stderr, "[midas] cbf block %d: fSR=%g nnz=%lld thr=%.17g\n", b, fsr, nnz, thr_sr);
         }
         MIDAS_CUDA(c, cudaMemsetAsync(Zsr, 0, sizeof(float2) * (size_t)sp * sp, c->stream));
         MIDAS_TRY(launch_block_fill4<float2>(c, s, idx, s, idx, sr ? 1 : 0, thr_sr, homog, Zsr, (size_t)sp, 1));
@@ -287,10 +289,15 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
         ir_max = std::max(ir_max, it);
         // Gram G = X^H X over the 3s rows of the extended block (FP64), eigen-decomposition
         MIDAS_TRY(zgemm64(c, m, m, N3, X64, sp, 1, 1, X64, 1, sp, G, m, 1, make_double2(1, 0), make_double2(0, 0)));
-        MIDAS_TRY(heev_jacobi(c, 1, m, G, m, (long long)m * m, Vv, (long long)m * m, W));
+        MIDAS_TRY(heev_dev(c, 1, m, G, m, (long long)m * m, Hh, Vv, (long long)m * m, W));
         MIDAS_CUDA(c, cudaMemcpyAsync(hW.data(), W, sizeof(double) * m, cudaMemcpyDeviceToHost, c->stream));
         MIDAS_CUDA(c, cudaStreamSynchronize(c->stream));
         double s1 = sqrt(std::max(hW[0], 0.0));
+        if (c->opts.verbose >= 2) {
+            fprintf(stderr, "[midas] cbf block %d: s=%d refine=%d sigma/sigma1:", b, s, it);
+            for (int k = 0; k < std::min(N3, m); ++k) fprintf(stderr, " %.6e", sqrt(std::max(hW[k], 0.0)) / s1);
+            fprintf(stderr, "\n");
+        }
         int K = 0;
         for (int k = 0; k < std::min(N3, m); ++k) {
             double sk = sqrt(std::max(hW[k], 0.0));
@@ -340,7 +347,7 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
     MIDAS_TRY(ensure(c, S_Z32, sizeof(float2) * (size_t)npd * npd, &p32));
     MIDAS_TRY(ensure(c, S_RHS64, sizeof(double2) * (size_t)npd * nr, &pb));
     MIDAS_TRY(ensure(c, S_X64, sizeof(double2) * (size_t)npd * nr, &px));
-    MIDAS_TRY(ensure(c, S_T32B, sizeof(double2) * (size_t)3 * nbmax * nr, &pe));
+    MIDAS_TRY(ensure(c, S_EINC, sizeof(double2) * (size_t)3 * nbmax * nr, &pe));
     {
         long long tot = (long long)npd * npd;
         ++c->launches;

@@ -180,6 +180,15 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float v[32])
     for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// PROMOTE = true: the K loop is cut into chunks of TC_PROMOTE_KB k-blocks; each
+// chunk is accumulated by the tensor core into one of two TMEM buffers (2 x BN
+// columns) and the epilogue warps add it into IEEE FP32 register accumulators
+// while the MMA fills the other buffer.  The tensor core's own accumulation
+// (coarser than an FMA chain) then only spans 64 products, which brings long-K
+// products with cancellation (the CBF reduced matrix) to FP32-FMA accuracy.
+constexpr int TC_PROMOTE_KB = 2;
+
+template <bool PROMOTE>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int M, int N, int K,
               float *D, long long ldd, float alpha, float beta, int *gflag)
@@ -188,17 +197,22 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t *full = (uint64_t *)(smem + TC_STAGES * TC_STAGE_BYTES);
     uint64_t *empty = full + TC_STAGES;
-    uint64_t *accf = empty + TC_STAGES;
-    volatile uint32_t *tmem_slot = (volatile uint32_t *)(accf + 1);
+    uint64_t *accf = empty + TC_STAGES;     // [2]: chunk accumulated (tcgen05.commit)
+    uint64_t *acce = accf + 2;              // [2]: chunk drained (128 epilogue arrivals)
+    volatile uint32_t *tmem_slot = (volatile uint32_t *)(acce + 2);
     volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
+    constexpr uint32_t NCOL = PROMOTE ? 2 * TC_BN : TC_BN;
 
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
     const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * TC_BN;
     const int nk = (K + TC_BK - 1) / TC_BK;
+    const int KC = PROMOTE ? TC_PROMOTE_KB : (nk > 0 ? nk : 1);
+    const int nchunk = (nk + KC - 1) / KC;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < TC_STAGES; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
-        mbar_init(accf, 1);
+        mbar_init(&accf[0], 1); mbar_init(&accf[1], 1);
+        mbar_init(&acce[0], 128); mbar_init(&acce[1], 128);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmA) : "memory");
@@ -207,7 +221,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                          smem_u32((const void *)tmem_slot)),
-                     "r"(TC_BN));
+                     "r"(NCOL));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -230,51 +244,93 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     } else if (warp == 1) {
         if (lane == 0) {
             const uint32_t idesc = idesc_tf32(TC_BM, TC_BN);
-            for (int kb = 0; kb < nk; ++kb) {
-                int s = kb % TC_STAGES;
-                if (!mbar_wait(&full[s], (kb / TC_STAGES) & 1, abort_flag, gflag)) break;
+            bool ok = true;
+            for (int ch = 0; ch < nchunk && ok; ++ch) {
+                const int buf = PROMOTE ? (ch & 1) : 0;
+                if (PROMOTE && ch >= 2)
+                    if (!mbar_wait(&acce[buf], ((ch >> 1) - 1) & 1, abort_flag, gflag)) break;
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                uint32_t sa = smem_u32(smem + s * TC_STAGE_BYTES);
-                uint32_t sb = sa + TC_A_BYTES;
+                const uint32_t dst = tmem + (uint32_t)(buf * TC_BN);
+                const int kb1 = min(nk, (ch + 1) * KC);
+                for (int kb = ch * KC; kb < kb1; ++kb) {
+                    int s = kb % TC_STAGES;
+                    if (!mbar_wait(&full[s], (kb / TC_STAGES) & 1, abort_flag, gflag)) { ok = false; break; }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    uint32_t sa = smem_u32(smem + s * TC_STAGE_BYTES);
+                    uint32_t sb = sa + TC_A_BYTES;
 #pragma unroll
-                for (int k4 = 0; k4 < TC_BK / 8; ++k4) {
-                    uint64_t ad = smem_desc_sw128(sa + k4 * 32);
-                    uint64_t bd = smem_desc_sw128(sb + k4 * 32);
-                    mma_tf32(tmem, ad, bd, idesc, (kb > 0 || k4 > 0) ? 1u : 0u);
+                    for (int k4 = 0; k4 < TC_BK / 8; ++k4) {
+                        uint64_t ad = smem_desc_sw128(sa + k4 * 32);
+                        uint64_t bd = smem_desc_sw128(sb + k4 * 32);
+                        mma_tf32(dst, ad, bd, idesc, (kb > ch * KC || k4 > 0) ? 1u : 0u);
+                    }
+                    mma_commit(&empty[s]);
                 }
-                mma_commit(&empty[s]);
+                mma_commit(&accf[buf]);
             }
-            mma_commit(accf);
         }
     } else {
         // epilogue: warp w reads TMEM lanes 32*(w%4) .. +31
         const int lg = warp % 4;
         const int row = m0 + lg * 32 + lane;
-        bool ok = mbar_wait(accf, 0, abort_flag, gflag);
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        if (ok) {
-            for (int c = 0; c < TC_BN / 32; ++c) {
-                float v[32];
-                tmem_ld32(tmem + ((uint32_t)(lg * 32) << 16) + (uint32_t)(c * 32), v);
-                if (row < M) {
+        const uint32_t lane_base = (uint32_t)(lg * 32) << 16;
+        if (PROMOTE) {
+            float acc[TC_BN];
+#pragma unroll
+            for (int j = 0; j < TC_BN; ++j) acc[j] = 0.f;
+            bool ok = true;
+            for (int ch = 0; ch < nchunk && ok; ++ch) {
+                const int buf = ch & 1;
+                ok = mbar_wait(&accf[buf], (ch >> 1) & 1, abort_flag, gflag);
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                if (!ok) break;
+#pragma unroll
+                for (int c = 0; c < TC_BN / 32; ++c) {
+                    float v[32];
+                    tmem_ld32(tmem + lane_base + (uint32_t)(buf * TC_BN + c * 32), v);
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) acc[c * 32 + j] += v[j];
+                }
+                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acce[buf])) : "memory");
+            }
+            if (ok && row < M) {
+#pragma unroll
+                for (int c = 0; c < TC_BN / 32; ++c) {
                     float *d = D + (long long)row * ldd + n0 + c * 32;
                     int ncol = N - (n0 + c * 32);
-                    if (ncol >= 32 && (((uintptr_t)d) & 15) == 0) {
 #pragma unroll
-                        for (int j = 0; j < 32; j += 4) {
-                            float4 o;
-                            if (beta != 0.f) {
-                                float4 p = *(float4 *)(d + j);
-                                o = make_float4(alpha * v[j] + beta * p.x, alpha * v[j + 1] + beta * p.y,
-                                                alpha * v[j + 2] + beta * p.z, alpha * v[j + 3] + beta * p.w);
-                            } else {
-                                o = make_float4(alpha * v[j], alpha * v[j + 1], alpha * v[j + 2], alpha * v[j + 3]);
+                    for (int j = 0; j < 32; ++j)
+                        if (j < ncol) d[j] = alpha * acc[c * 32 + j] + (beta != 0.f ? beta * d[j] : 0.f);
+                }
+            }
+        } else {
+            bool ok = mbar_wait(&accf[0], 0, abort_flag, gflag);
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            if (ok) {
+                for (int c = 0; c < TC_BN / 32; ++c) {
+                    float v[32];
+                    tmem_ld32(tmem + lane_base + (uint32_t)(c * 32), v);
+                    if (row < M) {
+                        float *d = D + (long long)row * ldd + n0 + c * 32;
+                        int ncol = N - (n0 + c * 32);
+                        if (ncol >= 32 && (((uintptr_t)d) & 15) == 0) {
+#pragma unroll
+                            for (int j = 0; j < 32; j += 4) {
+                                float4 o;
+                                if (beta != 0.f) {
+                                    float4 p = *(float4 *)(d + j);
+                                    o = make_float4(alpha * v[j] + beta * p.x, alpha * v[j + 1] + beta * p.y,
+                                                    alpha * v[j + 2] + beta * p.z, alpha * v[j + 3] + beta * p.w);
+                                } else {
+                                    o = make_float4(alpha * v[j], alpha * v[j + 1], alpha * v[j + 2], alpha * v[j + 3]);
+                                }
+                                *(float4 *)(d + j) = o;
                             }
-                            *(float4 *)(d + j) = o;
+                        } else {
+                            for (int j = 0; j < 32 && j < ncol; ++j)
+                                d[j] = alpha * v[j] + (beta != 0.f ? beta * d[j] : 0.f);
                         }
-                    } else {
-                        for (int j = 0; j < 32 && j < ncol; ++j)
-                            d[j] = alpha * v[j] + (beta != 0.f ? beta * d[j] : 0.f);
                     }
                 }
             }
@@ -284,7 +340,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (warp == 1)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_BN));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(NCOL));
 }
 
 // ---------------------------------------------------------------------------
@@ -342,14 +398,15 @@ static int gemm_simt(midas_gpu_ctx *c, const GemmArgs &g)
     return MIDAS_OK;
 }
 
-static int gemm_tc(midas_gpu_ctx *c, const GemmArgs &g)
+static int gemm_tc(midas_gpu_ctx *c, const GemmArgs &g, bool precise)
 {
     MIDAS_TRY(get_encode(c));
     if ((((uintptr_t)g.A) & 15) || (((uintptr_t)g.Bt) & 15) || (g.lda & 3) || (g.ldb & 3))
         return c->err.set(MIDAS_ERR_ARG, "gemm_tf32: operands must be 16-byte aligned with ld % 4 == 0");
     static bool attr = false;
     if (!attr) {
-        MIDAS_CUDA(c, cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
+        MIDAS_CUDA(c, cudaFuncSetAttribute(k_gemm_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
+        MIDAS_CUDA(c, cudaFuncSetAttribute(k_gemm_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
         attr = true;
     }
     CUtensorMap ma, mb;
@@ -357,17 +414,21 @@ static int gemm_tc(midas_gpu_ctx *c, const GemmArgs &g)
     MIDAS_TRY(make_map(c, &mb, g.Bt, g.N, g.K, g.ldb, TC_BN));
     dim3 grd((g.N + TC_BN - 1) / TC_BN, (g.M + TC_BM - 1) / TC_BM);
     ++c->launches;
-    k_gemm_tc<<<grd, TC_THREADS, TC_SMEM, c->stream>>>(ma, mb, g.M, g.N, g.K, g.D, g.ldd, g.alpha, g.beta,
-                                                       c->d_flag);
+    if (precise)
+        k_gemm_tc<true><<<grd, TC_THREADS, TC_SMEM, c->stream>>>(ma, mb, g.M, g.N, g.K, g.D, g.ldd, g.alpha, g.beta,
+                                                                 c->d_flag);
+    else
+        k_gemm_tc<false><<<grd, TC_THREADS, TC_SMEM, c->stream>>>(ma, mb, g.M, g.N, g.K, g.D, g.ldd, g.alpha, g.beta,
+                                                                  c->d_flag);
     MIDAS_CUDA(c, cudaGetLastError());
     return MIDAS_OK;
 }
 
-int gemm_tf32(midas_gpu_ctx *c, const GemmArgs &g)
+int gemm_tf32(midas_gpu_ctx *c, const GemmArgs &g, bool precise)
 {
     if (g.M <= 0 || g.N <= 0) return MIDAS_OK;
     if (g.K <= 0) return c->err.set(MIDAS_ERR_ARG, "gemm_tf32: K must be positive");
-    return pick_engine() ? gemm_tc(c, g) : gemm_simt(c, g);
+    return pick_engine() ? gemm_tc(c, g, precise) : gemm_simt(c, g);
 }
 
 // ---------------------------------------------------------------------------
@@ -424,7 +485,7 @@ int gemm_selftest(midas_gpu_ctx *c)
     GemmArgs g{M, N, K, A, K, B, K, D0, N, -1.0f, 1.0f};
     MIDAS_TRY(gemm_simt(c, g));
     g.D = D1;
-    MIDAS_TRY(gemm_tc(c, g));
+    MIDAS_TRY(gemm_tc(c, g, false));
     std::vector<float> h0(nd), h1(nd);
     MIDAS_CUDA(c, cudaMemcpyAsync(h0.data(), D0, sizeof(float) * nd, cudaMemcpyDeviceToHost, c->stream));
     MIDAS_CUDA(c, cudaMemcpyAsync(h1.data(), D1, sizeof(float) * nd, cudaMemcpyDeviceToHost, c->stream));

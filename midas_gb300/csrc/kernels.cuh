@@ -47,7 +47,8 @@ struct GemmArgs {
     float *D; long long ldd;
     float alpha, beta;
 };
-int gemm_tf32(midas_gpu_ctx *c, const GemmArgs &g);
+// precise = periodic promotion of the tensor-core partial sums to FP32 registers
+int gemm_tf32(midas_gpu_ctx *c, const GemmArgs &g, bool precise = false);
 // expand a complex k x n operand B (element (p,j) at B[p*rsb + j*csb], complex64) into
 // Bt (2n x 2k floats, row stride ldt): rows 2j = (Br, -Bi), 2j+1 = (Bi, Br) along p.
 int expand_b(midas_gpu_ctx *c, int k, int n, const float2 *B, long long rsb, long long csb, float *Bt,

@@ -13,6 +13,11 @@ int launch_cext_cabs(midas_gpu_ctx *c, int ntr, const double *th, const double *
                      double *cabs);
 int launch_smatrix(midas_gpu_ctx *c, int nrx, const double *rth, const double *rph, int ntr, const double2 *E,
                    double2 *S);
+template <typename TA, typename TB>
+int zgemm_x3(midas_gpu_ctx *c, int M, int N, int K, const TA *A, long long ars, long long acs, int conjA,
+             const TB *B, long long brs, long long bcs, float *D, long long ldd, float alpha, float beta);
+int heev_dev(midas_gpu_ctx *c, int batch, int m, double2 *A, long long lda, long long sa, double2 *H, double2 *V,
+             long long sv, double *W);
 int cbfm_run(midas_gpu_ctx *c, int nblocks, const int *blk_offsets, const int *ext_offsets, const int *ext_idx,
              int ncbf, const double *cbf_theta, const double *cbf_phi, double thr_cbf, double res_sr, int flags,
              double eps_aca, int aca_itmax, int ntr, const double *theta, const double *phi, double2 *E, int *K,
@@ -724,6 +729,41 @@ int midas_gpu_gemm_selftest(midas_gpu_ctx *c)
 }
 
 const char *midas_gpu_gemm_engine(void) { return gemm_engine(); }
+
+int midas_gpu_heev(midas_gpu_ctx *c, int m, const double *A, double *W, double *V)
+{
+    if (!c || m <= 0 || !A || !W || !V) return MIDAS_ERR_ARG;
+    c->err = Err();
+    void *p;
+    MIDAS_TRY(ensure(c, S_OUT0, sizeof(double2) * 3 * (size_t)m * m + sizeof(double) * m + 512, &p));
+    double2 *dA = (double2 *)p, *dV = dA + (size_t)m * m, *dH = dV + (size_t)m * m;
+    double *dW = (double *)(dH + (size_t)m * m);
+    MIDAS_CUDA(c, cudaMemcpyAsync(dA, A, sizeof(double2) * (size_t)m * m, cudaMemcpyDefault, c->stream));
+    MIDAS_TRY(heev_dev(c, 1, m, dA, m, (long long)m * m, dH, dV, (long long)m * m, dW));
+    MIDAS_CUDA(c, cudaMemcpyAsync(W, dW, sizeof(double) * m, cudaMemcpyDefault, c->stream));
+    MIDAS_CUDA(c, cudaMemcpyAsync(V, dV, sizeof(double2) * (size_t)m * m, cudaMemcpyDefault, c->stream));
+    MIDAS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return check_flag(c, "heev");
+}
+
+int midas_gpu_zgemm_x3(midas_gpu_ctx *c, int M, int N, int K, const double *A, const double *B, double *D)
+{
+    if (!c || M <= 0 || N <= 0 || K <= 0 || !A || !B || !D) return MIDAS_ERR_ARG;
+    c->err = Err();
+    void *p;
+    size_t na = (size_t)M * K, nb = (size_t)K * N, nd = (size_t)M * N;
+    MIDAS_TRY(ensure(c, S_OUT0, sizeof(double2) * (na + nb) + sizeof(float2) * nd + 1024, &p));
+    double2 *dA = (double2 *)p, *dB = dA + na;
+    float2 *dD = (float2 *)(dB + nb);
+    MIDAS_CUDA(c, cudaMemcpyAsync(dA, A, sizeof(double2) * na, cudaMemcpyDefault, c->stream));
+    MIDAS_CUDA(c, cudaMemcpyAsync(dB, B, sizeof(double2) * nb, cudaMemcpyDefault, c->stream));
+    MIDAS_TRY(zgemm_x3<double2, double2>(c, M, N, K, dA, K, 1, 0, dB, N, 1, (float *)dD, 2LL * N, 1.f, 0.f));
+    std::vector<float2> h(nd);
+    MIDAS_CUDA(c, cudaMemcpyAsync(h.data(), dD, sizeof(float2) * nd, cudaMemcpyDeviceToHost, c->stream));
+    MIDAS_CUDA(c, cudaStreamSynchronize(c->stream));
+    for (size_t i = 0; i < nd; ++i) { D[2 * i] = h[i].x; D[2 * i + 1] = h[i].y; }
+    return check_flag(c, "zgemm_x3");
+}
 
 int midas_gpu_bench_gemm(midas_gpu_ctx *c, int M, int N, int K, int iters, double *ms)
 {

@@ -33,12 +33,12 @@ class CellsIn:
 
 class Context:
     def __init__(self, device: int = 0, solve_mode: int = _lib.SOLVE_MIXED, fill_mode: int = _lib.FILL_FAITHFUL,
-                 index_base: int = 0, ir_tol: float = 1e-13, ir_max_iter: int = 30):
+                 index_base: int = 0, ir_tol: float = 1e-13, ir_max_iter: int = 30, verbose: int = 0):
         self.L = _lib.load()
         o = Opts()
         self.L.midas_gpu_default_opts(ctypes.byref(o))
         o.device, o.solve_mode, o.fill_mode, o.index_base = device, solve_mode, fill_mode, index_base
-        o.ir_tol, o.ir_max_iter = ir_tol, ir_max_iter
+        o.ir_tol, o.ir_max_iter, o.verbose = ir_tol, ir_max_iter, verbose
         h = ctypes.c_void_p()
         st = self.L.midas_gpu_init(ctypes.byref(o), ctypes.byref(h))
         if st != 0:
@@ -209,6 +209,23 @@ class Context:
         ms = ctypes.c_double(0)
         self._ck(self.L.midas_gpu_bench_gemm(self.h, M, N, K, iters, ctypes.byref(ms)))
         return ms.value
+
+    def heev(self, A):
+        """Hermitian eigen-decomposition on the device: (W descending, V columns)."""
+        A = np.ascontiguousarray(A, dtype=np.complex128)
+        m = A.shape[0]
+        W = np.zeros(m)
+        V = np.zeros((m, m), np.complex128)
+        self._ck(self.L.midas_gpu_heev(self.h, m, addr(A), addr(W), addr(V)))
+        return W, V
+
+    def zgemm_x3(self, A, B):
+        """FP32-grade complex product on the tensor cores (split TF32)."""
+        A = np.ascontiguousarray(A, dtype=np.complex128)
+        B = np.ascontiguousarray(B, dtype=np.complex128)
+        D = np.zeros((A.shape[0], B.shape[1]), np.complex128)
+        self._ck(self.L.midas_gpu_zgemm_x3(self.h, A.shape[0], B.shape[1], A.shape[1], addr(A), addr(B), addr(D)))
+        return D
 
     def gemm_selftest(self):
         self._ck(self.L.midas_gpu_gemm_selftest(self.h))

@@ -29,12 +29,17 @@ def test_cbfm_matches_oracle(gpulib, oracle, nbx, inhom, fill):
     niws = 91
     homog = 0 if inhom else 1
     cells = oracle.Cells(xyz, sc, eps, k0)
-    ref = oracle.cbfm_solve(cells, oracle.Partition(offs, ext), th, ph, niws, homog=homog)
+    keep = {}
+    ref = oracle.cbfm_solve(cells, oracle.Partition(offs, ext), th, ph, niws, homog=homog, keep=keep)
+    ref["sv"] = keep["sv"]
     cth, cph = G.transmitters_un(niws)
     mode = _lib.FILL_FAITHFUL if fill == "faithful" else _lib.FILL_FAST
-    ctx = Context(fill_mode=mode).set_cells(xyz, sc, eps, k0)
+    ctx = Context(fill_mode=mode, verbose=2).set_cells(xyz, sc, eps, k0)
     flags = _lib.CBFM_SR | (_lib.CBFM_HOMOG if homog else 0)
     E, K = ctx.cbfm_solve(offs, ext, cth, cph, th, ph, flags=flags)
+    print("oracle fsr", keep["fsr"], "nnz", keep["nnz"])
+    for b, sv in enumerate(ref["sv"]):
+        print(f"oracle block {b}: sigma/sigma1:", " ".join(f"{v:.6e}" for v in sv / sv[0]))
     assert np.array_equal(K, ref["K"]), (K, ref["K"])
     rel = np.linalg.norm(E - ref["E"]) / np.linalg.norm(ref["E"])
     assert rel < 1e-6, rel

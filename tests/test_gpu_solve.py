@@ -93,3 +93,33 @@ def test_errors_are_reported(gpulib):
         c.mom_fill(0, 7, 0, 6)
     assert e.value.status == 1   # block outside the matrix
     c.close()
+
+
+@pytest.mark.parametrize("m", [7, 64, 182])
+def test_heev_jacobi(ctx, m):
+    """Graded spectrum (singular values 1 .. 1e-9), as the Gram matrices of the CBF step."""
+    rng = np.random.default_rng(m)
+    U, _ = np.linalg.qr(rng.standard_normal((3 * m, m)) + 1j * rng.standard_normal((3 * m, m)))
+    Q, _ = np.linalg.qr(rng.standard_normal((m, m)) + 1j * rng.standard_normal((m, m)))
+    X = (U * np.logspace(0, -9, m)) @ Q
+    A = X.conj().T @ X
+    W, V = ctx.heev(A)
+    ref = np.sort(np.linalg.eigvalsh(A))[::-1]
+    assert np.all(np.diff(W) <= 0)
+    assert np.max(np.abs(W - ref)) <= 1e-13 * ref[0]
+    sel = ref > 1e-8 * ref[0]       # the range the CBF threshold (sigma ratio >= 1e-4) uses
+    assert np.max(np.abs(W[sel] - ref[sel]) / ref[sel]) < 1e-8
+    assert np.max(np.abs(V.conj().T @ A @ V - np.diag(W))) <= 1e-12 * ref[0]
+
+
+@pytest.mark.parametrize("M,N,K", [(130, 65, 828), (300, 40, 2000)])
+def test_zgemm_x3_fp32_grade(ctx, M, N, K):
+    """Split-TF32 product against FP64: error at the FP32 level, not the TF32 level."""
+    rng = np.random.default_rng(K)
+    A = rng.standard_normal((M, K)) + 1j * rng.standard_normal((M, K))
+    B = rng.standard_normal((K, N)) + 1j * rng.standard_normal((K, N))
+    D = ctx.zgemm_x3(A, B)
+    ref = A @ B
+    scale = np.abs(A) @ np.abs(B)
+    err = np.max(np.abs(D - ref) / scale)
+    assert err < 2e-7, err   # IEEE FP32 (numpy complex64) reaches ~4e-8 here
