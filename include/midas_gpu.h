@@ -178,6 +178,23 @@ int midas_gpu_cext_cabs(midas_gpu_ctx *ctx, int ntr, const double *theta, const 
 int midas_gpu_smatrix(midas_gpu_ctx *ctx, int nrx, const double *rx_theta, const double *rx_phi, int ntr,
                       const double *E, double *S);
 
+/* Dense complex solve that allocates no device memory (no counterpart in the
+ * reference).  For callers that cannot call cudaMalloc -- code running while a
+ * stream is captured into a CUDA graph, plug-ins whose host application owns and
+ * caps all device memory, latency-critical paths -- it solves A X = B (A n x n,
+ * B n x nrhs, column-major complex, host or device memory; B is overwritten by X)
+ * with the same mixed-precision LU + FP64 refinement as midas_gpu_dense_solve,
+ * on `stream` (a cudaStream_t; NULL = the legacy default stream) of `device`.
+ * No context is needed.  All scratch comes from one static 16 MiB device array
+ * inside the library, which every GPU that loads the library holds until exit.
+ * Limits: n <= 512, nrhs <= 32 (larger sizes return MIDAS_ERR_ARG).  All calls
+ * share the array: calls that overlap on the GPU race, so serialise them.  The
+ * first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make it before any stream capture starts.
+ * *backward_error (may be NULL) receives the final normwise backward error. */
+int midas_gpu_dense_solve_noalloc(int device, void *stream, int n, int nrhs, const double *A, double *B,
+                                  double *backward_error);
+
 /* Diagnostics (no counterpart in the reference). */
 /* Device self-test of the tensor-core GEMM engine against a CUDA-core GEMM on a
  * ragged problem; returns MIDAS_OK when they agree to TF32 accuracy. */

@@ -26,7 +26,7 @@ EXPORTS = [
     "midas_gpu_default_opts", "midas_gpu_init", "midas_gpu_free", "midas_gpu_last_error", "midas_gpu_set_cells",
     "midas_gpu_get_cell_params", "midas_gpu_mom_fill", "midas_gpu_mom_rhs", "midas_gpu_incident_field",
     "midas_gpu_block_fill", "midas_gpu_sr_fill", "midas_gpu_set_fsr", "midas_gpu_aca", "midas_gpu_dense_solve",
-    "midas_gpu_mom_solve", "midas_gpu_cbfm_solve", "midas_gpu_cext_cabs", "midas_gpu_smatrix",
+    "midas_gpu_mom_solve", "midas_gpu_cbfm_solve", "midas_gpu_dense_solve_noalloc", "midas_gpu_cext_cabs", "midas_gpu_smatrix",
     "midas_gpu_gemm_selftest", "midas_gpu_gemm_engine", "midas_gpu_launch_count", "midas_gpu_stream",
     "midas_gpu_bench_gemm", "midas_gpu_heev", "midas_gpu_zgemm_x3",
 ]
@@ -85,6 +85,7 @@ def load(path: str = LIB_PATH):
         "midas_gpu_aca": (i, [vp, i, i, i, i, d, i, P, P, ctypes.POINTER(ctypes.c_int)]),
         "midas_gpu_dense_solve": (i, [vp, i, i, P, P, ctypes.POINTER(Info)]),
         "midas_gpu_mom_solve": (i, [vp, i, P, P, P, ctypes.POINTER(Info)]),
+        "midas_gpu_dense_solve_noalloc": (i, [i, vp, i, i, P, P, ctypes.POINTER(ctypes.c_double)]),
         "midas_gpu_cbfm_solve": (i, [vp, i, P, P, P, i, P, P, d, d, i, d, i, i, P, P, P, P, ctypes.POINTER(Info)]),
         "midas_gpu_cext_cabs": (i, [vp, i, P, P, P, P, P]),
         "midas_gpu_smatrix": (i, [vp, i, P, P, i, P, P]),
