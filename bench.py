@@ -48,7 +48,32 @@ def workload_mom_c1():
             "method": "mom"}
 
 
-WORKLOADS = {"mom_c1": workload_mom_c1}
+def workload_cbfm_c2():
+    """CBFM-E on a seeded Gaussian random sphere: x = 6, m = 1.55 + 0.005i, log-radius
+    std 0.15, correlation angle 20 deg, voxel a/21.1 (~41k cells, ~123k unknowns),
+    3x3x3 bounding-box blocks with a 15 % (of the block edge) extension, CBF
+    excitations from the reference's Niws table ('un'), 24 seeded incident
+    directions x 2 polarisations."""
+    from midas_gb300 import geometry as G
+    a, x, m = 1.0, 6.0, 1.55 + 0.005j
+    k0 = x / a
+    sc = a / 21.1
+    xyz = G.gaussian_sphere(a, 0.15, 20.0, sc, seed=2026)
+    perm, offs = G.box_partition(xyz, 3, 3, 3)
+    xyz = np.ascontiguousarray(xyz[perm])
+    box, sph = G.block_contours(xyz, offs)
+    edge = float((box[:, 1] - box[:, 0]).max(axis=1).mean())
+    ext = G.extend_blocks(xyz, offs, 0.15 * edge, sc)
+    lam = 2 * math.pi / k0
+    niws = G.init_nipws(float(sph[:, 3].max()) / (lam / abs(m)))
+    cth, cph = G.transmitters_un(niws)
+    th, ph = G.random_directions(24, seed=7)
+    return {"name": "cbfm_c2_gaussian_sphere_x6_m1.55+0.005i", "xyz": xyz, "sc": sc,
+            "eps": np.full(len(xyz), m * m), "k0": k0, "th": th, "ph": ph, "method": "cbfm",
+            "offs": offs, "ext": ext, "cth": cth, "cph": cph, "homog": 1, "niws": niws}
+
+
+WORKLOADS = {"mom_c1": workload_mom_c1, "cbfm_c2": workload_cbfm_c2}
 
 
 # ---------------------------------------------------------------------------
@@ -146,6 +171,71 @@ def allmax(pg, v):
 # ---------------------------------------------------------------------------
 # reference arm: CPU restatement on the host cores
 # ---------------------------------------------------------------------------
+def cbfm_cpu_sample(wl):
+    """Bounded CPU sample of the CBFM workload, extrapolated per phase.
+
+    Times the oracle on (a) the CBF generation of the median-size extended block
+    (SR threshold scan + thresholded fill, then the dense FP64 solve + SVD that
+    stand in for PARDISO + GESVD), (b) the reduced-matrix assembly of one
+    median-size block pair (FP64 fill + the two ZGEMMs) and (c) a reduced solve of
+    the extrapolated K_total.  Each phase is scaled to the whole partition by its
+    own order: block fills by s_b^2, block solves by s_b^3, pair fills by n_i n_j,
+    pair products by n_i n_j K.  Returns (seconds per step, description)."""
+    from oracle import oracle as O
+    import scipy.linalg as sla
+    O.build()
+    cells = O.Cells(wl["xyz"], wl["sc"], wl["eps"], wl["k0"])
+    offs = np.asarray(wl["offs"])
+    nbk = np.diff(offs).astype(float)
+    s = nbk + np.array([len(e) for e in wl["ext"]], float)
+    part = O.Partition(offs, wl["ext"])
+    b = int(np.argsort(s)[len(s) // 2])
+    idx = part.extended(b)
+    homog = int(wl.get("homog", 0))
+    thr = O.cbf_threshold(cells)
+    t0 = time.perf_counter()
+    Eref = O.incident_c4(cells, wl["cth"], wl["cph"], idx=idx)
+    fsr, _ = O.set_fsr(cells, idx, homog, O.RES_SR_DEFAULT)
+    Zb = O.sr_dense(cells, idx, fsr, homog)[0]
+    t1 = time.perf_counter()
+    Ep = O._solve(Zb, Eref)
+    U, S, _ = np.linalg.svd(Ep, full_matrices=False)
+    K = int(np.count_nonzero(S / S[0] >= thr))
+    t2 = time.perf_counter()
+    del Zb
+    order = np.argsort(nbk)
+    i, j = int(order[len(order) // 2]), int(order[len(order) // 2 + 1])
+    rng = np.random.default_rng(0)
+    t3 = time.perf_counter()
+    Zij = O.green_partial(cells, part.block(i), part.block(j))
+    t4 = time.perf_counter()
+    Ci = rng.standard_normal((Zij.shape[0], K)) + 1j * rng.standard_normal((Zij.shape[0], K))
+    Cj = rng.standard_normal((Zij.shape[1], K)) + 1j * rng.standard_normal((Zij.shape[1], K))
+    t4b = time.perf_counter()
+    Zc_ij = (Ci.T @ Zij) @ Cj
+    t5 = time.perf_counter()
+    nblocks = len(nbk)
+    kt = K * nblocks
+    A = rng.standard_normal((kt, kt)) + 1j * rng.standard_normal((kt, kt))
+    B = rng.standard_normal((kt, 2 * len(wl["th"]))) + 0j
+    t6 = time.perf_counter()
+    sla.solve(A, B, check_finite=False)
+    t7 = time.perf_counter()
+    del Zc_ij
+    sb = s[b]
+    pair = np.outer(nbk, nbk)
+    scale_fill_b = float(np.sum((s / sb) ** 2))
+    scale_solve_b = float(np.sum((s / sb) ** 3))
+    scale_pair = float(pair.sum() / (nbk[i] * nbk[j]))
+    T = ((t1 - t0) * scale_fill_b + (t2 - t1) * scale_solve_b + (t4 - t3) * scale_pair + (t5 - t4b) * scale_pair
+         + (t7 - t6))
+    desc = (f"oracle (C + OpenMP fills, LAPACK via scipy) on block {b} (extended {int(sb)} cells, K={K}), pair "
+            f"({i},{j}) and a {kt}-unknown reduced solve; {t2 - t0 + t4 - t3 + t5 - t4b + t7 - t6:.1f} s "
+            f"measured, extrapolated x{scale_fill_b:.1f} (block fills, s^2), x{scale_solve_b:.1f} (block solves, "
+            f"s^3), x{scale_pair:.0f} (pair fills and products, n_i n_j) to all {nblocks} blocks")
+    return T, desc
+
+
 def run_reference(args, wl, world, rank, pg):
     if rank != 0:
         return 0
@@ -153,17 +243,20 @@ def run_reference(args, wl, world, rank, pg):
     O.build()
     cells = O.Cells(wl["xyz"], wl["sc"], wl["eps"], wl["k0"])
     times = []
+    desc = None
     for it in range(args.warmup + args.steps):
         t0 = time.perf_counter()
         if wl["method"] == "mom":
             O.mom_solve(cells, wl["th"], wl["ph"])
-        dt = time.perf_counter() - t0
+            dt = time.perf_counter() - t0
+        else:
+            dt, desc = cbfm_cpu_sample(wl)
         if it >= args.warmup:
             times.append(dt)
     per = float(np.mean(times))
     value = len(wl["th"]) / per
     cores = os.cpu_count()
-    sample = f"full {wl['name']} solve per step (C fills with OpenMP + LAPACK zgesv via scipy)"
+    sample = desc or f"full {wl['name']} solve per step (C fills with OpenMP + LAPACK zgesv via scipy)"
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c128 (fp64)", "data": "synthetic",
@@ -200,12 +293,30 @@ def run_ours(args, wl, world, rank, local, pg):
     torch.cuda.synchronize()
     L = ctx.L
 
+    cbfm = wl["method"] == "cbfm"
+    if cbfm:
+        from midas_gb300 import _lib as LB
+        bo = np.ascontiguousarray(wl["offs"], np.int32)
+        eo = np.ascontiguousarray(np.concatenate([[0], np.cumsum([len(e) for e in wl["ext"]])]), np.int32)
+        ei = np.ascontiguousarray(np.concatenate(wl["ext"]), np.int32)
+        cth, cph = np.ascontiguousarray(wl["cth"]), np.ascontiguousarray(wl["cph"])
+        flags = LB.CBFM_SR | (LB.CBFM_HOMOG if wl.get("homog") else 0) | (LB.CBFM_ACA if wl.get("aca") else 0)
+        Kb = np.zeros(len(bo) - 1, np.int32)
+
+    def solve(thp, php, Ep):
+        if cbfm:
+            ctx._ck(L.midas_gpu_cbfm_solve(ctx.h, len(bo) - 1, bo.ctypes.data, eo.ctypes.data, ei.ctypes.data,
+                                           len(cth), cth.ctypes.data, cph.ctypes.data, 0.0, 0.0, flags,
+                                           float(np.float32(1e-4)), 50, ntr, thp, php, Ep, Kb.ctypes.data,
+                                           ctypes_byref(ctx.info)))
+        else:
+            ctx._ck(L.midas_gpu_mom_solve(ctx.h, ntr, thp, php, Ep, ctypes_byref(ctx.info)))
+
     def step_resident():
         ctx._ck(L.midas_gpu_set_cells(ctx.h, n, xyz_d[0].data_ptr(), xyz_d[1].data_ptr(), xyz_d[2].data_ptr(),
                                       sc_d.data_ptr(), er_d.data_ptr(), ei_d.data_ptr(), float(wl["k0"])))
         ctx.n = n
-        ctx._ck(L.midas_gpu_mom_solve(ctx.h, ntr, th_d.data_ptr(), ph_d.data_ptr(), E_d.data_ptr(),
-                                      ctypes_byref(ctx.info)))
+        solve(th_d.data_ptr(), ph_d.data_ptr(), E_d.data_ptr())
 
     # host buffers for the end-to-end leg
     xs = [np.ascontiguousarray(wl["xyz"][:, i]) for i in range(3)]
@@ -217,14 +328,14 @@ def run_ours(args, wl, world, rank, local, pg):
         ctx._ck(L.midas_gpu_set_cells(ctx.h, n, xs[0].ctypes.data, xs[1].ctypes.data, xs[2].ctypes.data,
                                       sch.ctypes.data, erh.ctypes.data, eih.ctypes.data, float(wl["k0"])))
         ctx.n = n
-        ctx._ck(L.midas_gpu_mom_solve(ctx.h, ntr, wl["th"].ctypes.data, wl["ph"].ctypes.data, Eh.ctypes.data,
-                                      ctypes_byref(ctx.info)))
+        solve(wl["th"].ctypes.data, wl["ph"].ctypes.data, Eh.ctypes.data)
 
     for _ in range(args.warmup):
         step_resident()
     torch.cuda.synchronize()
     barrier(pg)
     l0 = ctx.launch_count()
+    ctx.profile(True)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
         torch.cuda.synchronize()
@@ -236,6 +347,8 @@ def run_ours(args, wl, world, rank, local, pg):
         torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1)
     launches = ctx.launch_count() - l0
+    kprof = ctx.profile_query()
+    ctx.profile(False)
     phases = ctx.info.as_dict()
     barrier(pg)
     ms = allmax(pg, ms)
@@ -255,73 +368,133 @@ def run_ours(args, wl, world, rank, local, pg):
     e2e_s = allmax(pg, e2e_s)
     e2e_value = world * ntr * args.steps / e2e_s
     h2d = 6 * 8 * n + 2 * 8 * ntr
-    d2h = 16 * N * 2 * ntr
+    if cbfm:
+        h2d += 4 * (bo.size + eo.size + ei.size) + 8 * (cth.size + cph.size)
+    d2h = 16 * N * 2 * ntr + (4 * Kb.size if cbfm else 0)
 
-    # roofline of the dominant kernel (largest trailing update of the LU: M x 2M x 128)
+    # roofline of the dominant kernel class, timed live over the timed region
     peaks = load_peaks()
-    np_ = (N + 63) // 64 * 64
-    M_ = np_ - 64
-    gms = ctx.bench_gemm(M_, 2 * M_, 128, iters=10)
-    flops = 2.0 * M_ * (2 * M_) * 128
-    algo_bytes = 4.0 * (M_ * 128 + 2 * M_ * 128 + 2 * M_ * (2 * M_))
-    tf_ach = flops / (gms * 1e-3) / 1e12
-    gb_ach = algo_bytes / (gms * 1e-3) / 1e9
-    tf_peak = peaks["bf16_tflops"] / 2.0
+    tf_peak = peaks["bf16_tflops"] / 2.0     # dense TF32 = half the bf16 rate
     hb_peak = peaks["hbm_gbs"]
-    if gb_ach / hb_peak >= tf_ach / tf_peak:
+    top = max(kprof, key=lambda k: kprof[k]["ms"])
+    kp = kprof[top]
+    sec = kp["ms"] * 1e-3
+    gb_ach = kp["bytes"] / sec / 1e9 if sec > 0 else 0.0
+    tf_ach = kp["flops"] / sec / 1e12 if sec > 0 else 0.0
+    ridge = tf_peak * 1e12 / (hb_peak * 1e9)
+    ai = kp["flops"] / kp["bytes"] if kp["bytes"] > 0 else float("inf")
+    if ai < ridge:
         roof = {"bound": "hbm", "achieved": gb_ach, "peak": hb_peak, "unit": "GB/s", "frac": gb_ach / hb_peak,
-                "traffic": None, "kernel": f"k_gemm_tc trailing update M={M_} N={2 * M_} K=128 (fp32/tf32)",
-                "peak_src": peaks["src"], "tflops": tf_ach}
+                "peak_src": peaks["src"] + " hbm_gbs"}
     else:
         roof = {"bound": "tensor", "achieved": tf_ach, "peak": tf_peak, "unit": "TFLOP/s", "frac": tf_ach / tf_peak,
-                "traffic": None, "kernel": f"k_gemm_tc trailing update M={M_} N={2 * M_} K=128",
-                "peak_src": peaks["src"] + " bf16 / 2 (tf32)", "gbs": gb_ach}
+                "peak_src": peaks["src"] + " bf16_tflops / 2 (tf32 rate)"}
+    roof.update({"traffic": None, "kernel_class": top, "launches": kp["launches"],
+                 "ms_per_launch": kp["ms"] / max(1, kp["launches"]),
+                 "algorithmic_bytes_per_launch": kp["bytes"] / max(1, kp["launches"]),
+                 "algorithmic_flops_per_launch": kp["flops"] / max(1, kp["launches"]),
+                 "share_of_step": kp["ms"] / ms if ms > 0 else None, "tflops": tf_ach, "gbs": gb_ach})
+    classes = {k: {"ms_per_step": v["ms"] / args.steps, "launches_per_step": v["launches"] / args.steps,
+                   "gbs": v["bytes"] / (v["ms"] * 1e-3) / 1e9 if v["ms"] > 0 else None,
+                   "tflops": v["flops"] / (v["ms"] * 1e-3) / 1e12 if v["ms"] > 0 else None}
+               for k, v in kprof.items()}
 
     # the plain FP64 MoM on the same GPU (cuSOLVER zgetrf), the metric's denominator
     fp64 = None
     if rank == 0 and not args.no_fp64:
-        c64 = Context(device=local, solve_mode=_lib.SOLVE_FP64)
-        c64.set_cells(wl["xyz"], wl["sc"], wl["eps"], wl["k0"])
-        c64.mom_solve(wl["th"], wl["ph"])
-        t0 = time.perf_counter()
-        E64 = c64.mom_solve(wl["th"], wl["ph"])
-        t64 = time.perf_counter() - t0
-        E_mixed = E_d.cpu().numpy().view(np.complex128).reshape(2 * ntr, N).T
-        relerr = float(np.linalg.norm(E_mixed - E64) / np.linalg.norm(E64))
-        fp64 = {"value": ntr / t64, "unit": "solves/s", "impl": "cuSOLVER zgetrf/zgetrs FP64 + FP64 fill",
-                "speedup": value / (ntr / t64), "field_rel_err_vs_fp64": relerr}
-        c64.close()
+        if cbfm:
+            fp64 = fp64_mom_extrapolated(local, wl, value)
+        else:
+            c64 = Context(device=local, solve_mode=_lib.SOLVE_FP64)
+            c64.set_cells(wl["xyz"], wl["sc"], wl["eps"], wl["k0"])
+            c64.mom_solve(wl["th"], wl["ph"])
+            t0 = time.perf_counter()
+            E64 = c64.mom_solve(wl["th"], wl["ph"])
+            t64 = time.perf_counter() - t0
+            E_mixed = E_d.cpu().numpy().view(np.complex128).reshape(2 * ntr, N).T
+            relerr = float(np.linalg.norm(E_mixed - E64) / np.linalg.norm(E64))
+            fp64 = {"value": ntr / t64, "unit": "solves/s", "impl": "cuSOLVER zgetrf/zgetrs FP64 + FP64 fill",
+                    "speedup": value / (ntr / t64), "field_rel_err_vs_fp64": relerr}
+            c64.close()
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        from oracle import oracle as O
-        O.build()
-        cells = O.Cells(wl["xyz"], wl["sc"], wl["eps"], wl["k0"])
-        t0 = time.perf_counter()
-        O.mom_solve(cells, wl["th"], wl["ph"])
-        tc = time.perf_counter() - t0
-        cpu = {"value": ntr / tc, "unit": "solves/s", "cores": os.cpu_count(), "kind": "port",
-               "sample": f"one full {wl['name']} solve (C restatement with OpenMP + LAPACK zgesv)"}
+        if cbfm:
+            tc, desc = cbfm_cpu_sample(wl)
+            cpu = {"value": ntr / tc, "unit": "solves/s", "cores": os.cpu_count(), "kind": "port", "sample": desc}
+        else:
+            from oracle import oracle as O
+            O.build()
+            cells = O.Cells(wl["xyz"], wl["sc"], wl["eps"], wl["k0"])
+            t0 = time.perf_counter()
+            O.mom_solve(cells, wl["th"], wl["ph"])
+            tc = time.perf_counter() - t0
+            cpu = {"value": ntr / tc, "unit": "solves/s", "cores": os.cpu_count(), "kind": "port",
+                   "sample": f"one full {wl['name']} solve (C restatement with OpenMP + LAPACK zgesv)"}
 
     if rank == 0:
+        cfg = {"workload": wl["name"], "cells": n, "unknowns": N, "directions": ntr, "polarisations": 2,
+               "parallelism": f"replicas x{world}"}
+        if cbfm:
+            cfg.update({"blocks": len(bo) - 1, "cbf_excitations": int(2 * len(cth)), "K_total": int(Kb.sum()),
+                        "K_min_max": [int(Kb.min()), int(Kb.max())], "flags": flags,
+                        "l2": "inputs larger than L2 (per-block LU operands and reduced-matrix block columns of "
+                              "several GB each step)"})
+            dtype = "c64 tf32-tensor block LU + double-float refinement; split-tf32 reduced products; f64 reduced solve"
+        else:
+            np_ = (N + 63) // 64 * 64
+            cfg["l2"] = ("inputs larger than L2 (FP64 + FP32 impedance matrices = "
+                         f"{(16 + 8) * np_ * np_ / 1e9:.1f} GB per step)")
+            dtype = "c64 tf32-tensor LU + f64 refinement (FP64 fill)"
         line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "c64 tf32-tensor LU + f64 refinement (FP64 fill)",
-                "data": "synthetic (seeded voxelised scatterer, reference voxeliser)",
-                "config": {"workload": wl["name"], "cells": n, "unknowns": N, "directions": ntr,
-                           "polarisations": 2, "parallelism": f"replicas x{world}",
-                           "l2": "inputs larger than L2 (FP64 + FP32 impedance matrices = "
-                                 f"{(16 + 8) * np_ * np_ / 1e9:.1f} GB per step)"},
-                "roofline": roof, "cpu_baseline": cpu,
+                "vs_baseline": None, "dtype": dtype,
+                "data": "synthetic (seeded voxelised scatterer)",
+                "config": cfg, "roofline": roof, "cpu_baseline": cpu,
                 "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": d2h},
                 "gpu_launches": launches, "clocks": clk.summary(), "fp64_mom_gpu": fp64,
                 "phases_ms": {k: phases[k] for k in ("t_fill_ms", "t_factor_ms", "t_solve_ms", "t_total_ms")},
+                "kernel_classes": classes,
                 "ir": {"iters": phases["ir_iters"], "backward_error": phases["backward_error"]},
                 "gemm_engine": ctx.gemm_selftest()}
         print(json.dumps(line), flush=True)
     ctx.close()
     return 0
+
+
+def fp64_mom_extrapolated(local, wl, value):
+    """Plain FP64 MoM (FP64 fill + cuSOLVER zgetrf/zgetrs) timed on this GPU on the
+    sphere x = 2 scene (12,672 unknowns) and scaled to the workload's unknowns by
+    phase: fill N^2, factorisation N^3, solves N^2 x right-hand sides.  A measured
+    full-size FP64 run does not fit the benchmark's time (the FP64 LU of ~123k
+    unknowns is ~5e15 flops at the part's FP64 rate)."""
+    from midas_gb300 import _lib
+    from midas_gb300.solver import Context
+    ref = workload_mom_c1()
+    c64 = Context(device=local, solve_mode=_lib.SOLVE_FP64)
+    c64.set_cells(ref["xyz"], ref["sc"], ref["eps"], ref["k0"])
+    th = np.asarray(wl["th"], float)
+    ph = np.asarray(wl["ph"], float)
+    c64.mom_solve(th, ph)
+    t0 = time.perf_counter()
+    c64.mom_solve(th, ph)
+    t_meas = time.perf_counter() - t0
+    inf = c64.info.as_dict()
+    c64.close()
+    n0, n1 = 3 * len(ref["xyz"]), 3 * len(wl["xyz"])
+    r = n1 / n0
+    t_fill = inf["t_fill_ms"] * 1e-3 * r ** 2
+    t_fac = inf["t_factor_ms"] * 1e-3 * r ** 3
+    t_sol = inf["t_solve_ms"] * 1e-3 * r ** 2
+    t = t_fill + t_fac + t_sol
+    ntr = len(th)
+    return {"value": ntr / t, "unit": "solves/s", "impl": "cuSOLVER zgetrf/zgetrs FP64 + FP64 fill",
+            "measured_on": f"{ref['name']} ({n0} unknowns, {ntr} directions x 2 pol): {t_meas:.2f} s "
+                           f"(fill {inf['t_fill_ms']:.0f} ms, factor {inf['t_factor_ms']:.0f} ms, "
+                           f"solve {inf['t_solve_ms']:.0f} ms)",
+            "extrapolated_to_unknowns": n1, "extrapolated_s": t, "speedup": value / (ntr / t),
+            "memory_gb_fp64_matrix": 16.0 * n1 * n1 / 1e9}
 
 
 def ctypes_byref(x):
@@ -335,7 +508,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="mom_c1", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="cbfm_c2", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     args = ap.parse_args()

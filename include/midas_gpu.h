@@ -216,6 +216,28 @@ long long midas_gpu_launch_count(const midas_gpu_ctx *ctx);
 /* The context's CUDA stream (a cudaStream_t): every kernel of the context runs on it. */
 void *midas_gpu_stream(const midas_gpu_ctx *ctx);
 
+/* Kernel classes timed by the profiler below. */
+#define MIDAS_KC_GEMM_TC   0   /* tcgen05 GEMM (LU panels and trailing updates, CBFM products) */
+#define MIDAS_KC_GEMM_SIMT 1   /* CUDA-core FP32 GEMM (fallback engine) */
+#define MIDAS_KC_FILL      2   /* impedance fills (MoM element, CBFM block, SR threshold) */
+#define MIDAS_KC_SR_SCAN   3   /* setfSR ladder scan */
+#define MIDAS_KC_DIAG_LU   4   /* diagonal-block LU and inverses */
+#define MIDAS_KC_TRSV      5   /* blocked triangular solves */
+#define MIDAS_KC_RESID     6   /* refinement residuals (FP64 / double-float) */
+#define MIDAS_KC_ZGEMM64   7   /* FP64 complex GEMMs (Gram, CBF projections, Vc, E) */
+#define MIDAS_KC_EIG       8   /* Hermitian eigensolver */
+#define MIDAS_KC_OTHER     9   /* everything else that is instrumented */
+#define MIDAS_KC_COUNT     10
+/* enable = 1 clears the per-class totals and starts timing every instrumented
+ * launch with CUDA events on the context stream; 0 stops.  Timing adds one event
+ * record before and after each instrumented launch. */
+int midas_gpu_profile(midas_gpu_ctx *ctx, int enable);
+/* Totals of one kernel class since profiling was enabled: device milliseconds,
+ * algorithmic flops and bytes (the op's own counts, not hardware counters) and
+ * launches.  Waits for the recorded events. */
+int midas_gpu_profile_query(midas_gpu_ctx *ctx, int kclass, double *ms, double *flops, double *bytes,
+                            long long *launches);
+
 #ifdef __cplusplus
 }
 #endif

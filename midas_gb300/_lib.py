@@ -20,6 +20,8 @@ STATUS = {0: "MIDAS_OK", 1: "MIDAS_ERR_ARG", 2: "MIDAS_ERR_CUDA", 3: "MIDAS_ERR_
 SOLVE_MIXED, SOLVE_FP64 = 0, 1
 FILL_FAITHFUL, FILL_FAST = 0, 1
 CBFM_SR, CBFM_HOMOG, CBFM_ACA, CBFM_FAST_CBF = 1, 2, 4, 8
+# kernel classes of midas_gpu_profile_query (MIDAS_KC_* in the header)
+KCLASSES = ["gemm_tc", "gemm_simt", "fill", "sr_scan", "diag_lu", "trsv", "resid", "zgemm64", "eig", "other"]
 
 # every symbol the header declares (checked by the CPU tests)
 EXPORTS = [
@@ -28,7 +30,7 @@ EXPORTS = [
     "midas_gpu_block_fill", "midas_gpu_sr_fill", "midas_gpu_set_fsr", "midas_gpu_aca", "midas_gpu_dense_solve",
     "midas_gpu_mom_solve", "midas_gpu_cbfm_solve", "midas_gpu_dense_solve_noalloc", "midas_gpu_cext_cabs", "midas_gpu_smatrix",
     "midas_gpu_gemm_selftest", "midas_gpu_gemm_engine", "midas_gpu_launch_count", "midas_gpu_stream",
-    "midas_gpu_bench_gemm", "midas_gpu_heev", "midas_gpu_zgemm_x3",
+    "midas_gpu_bench_gemm", "midas_gpu_heev", "midas_gpu_zgemm_x3", "midas_gpu_profile", "midas_gpu_profile_query",
 ]
 
 
@@ -94,6 +96,9 @@ def load(path: str = LIB_PATH):
         "midas_gpu_launch_count": (ctypes.c_longlong, [vp]),
         "midas_gpu_stream": (ctypes.c_void_p, [vp]),
         "midas_gpu_bench_gemm": (i, [vp, i, i, i, i, ctypes.POINTER(ctypes.c_double)]),
+        "midas_gpu_profile": (i, [vp, i]),
+        "midas_gpu_profile_query": (i, [vp, i, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                                        ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong)]),
         "midas_gpu_heev": (i, [vp, i, P, P, P]),
         "midas_gpu_zgemm_x3": (i, [vp, i, i, i, P, P, P]),
     }

@@ -16,6 +16,8 @@
 //    implicit QL, FP64) of the CBF Gram matrices; one CTA per matrix.
 #include <cmath>
 
+#include <algorithm>
+
 #include "common.cuh"
 #include "kernels.cuh"
 
@@ -53,17 +55,18 @@ template <typename T>
 __global__ void k_split_a(int M, int K, const T *src, long long rs, long long cs, int conj, float *A3, long long lda3)
 {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
-    int i = blockIdx.y;
-    if (k >= K || i >= M) return;
-    double2 v = ld2<T>(src, (long long)i * rs + (long long)k * cs);
-    if (conj) v.y = -v.y;
-    float hr, lr, hi_, li;
-    split2(v.x, hr, lr);
-    split2(v.y, hi_, li);
-    float *row = A3 + (long long)i * lda3;
-    row[2 * k] = hr; row[2 * k + 1] = hi_;
-    row[2 * K + 2 * k] = hr; row[2 * K + 2 * k + 1] = hi_;
-    row[4 * K + 2 * k] = lr; row[4 * K + 2 * k + 1] = li;
+    if (k >= K) return;
+    for (int i = blockIdx.y; i < M; i += gridDim.y) {   // rows beyond the 65535 grid limit loop
+        double2 v = ld2<T>(src, (long long)i * rs + (long long)k * cs);
+        if (conj) v.y = -v.y;
+        float hr, lr, hi_, li;
+        split2(v.x, hr, lr);
+        split2(v.y, hi_, li);
+        float *row = A3 + (long long)i * lda3;
+        row[2 * k] = hr; row[2 * k + 1] = hi_;
+        row[2 * K + 2 * k] = hr; row[2 * K + 2 * k + 1] = hi_;
+        row[4 * K + 2 * k] = lr; row[4 * K + 2 * k + 1] = li;
+    }
 }
 
 // B3t rows 2j, 2j+1 for element (k, j) = src[k*rs + j*cs]
@@ -71,17 +74,18 @@ template <typename T>
 __global__ void k_split_expand_b(int K, int N, const T *src, long long rs, long long cs, float *B3, long long ldb3)
 {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
-    int j = blockIdx.y;
-    if (k >= K || j >= N) return;
-    double2 v = ld2<T>(src, (long long)k * rs + (long long)j * cs);
-    float hr, lr, hi_, li;
-    split2(v.x, hr, lr);
-    split2(v.y, hi_, li);
-    float *r0 = B3 + (long long)(2 * j) * ldb3, *r1 = r0 + ldb3;
-    // segment 0: hi, segment 1: lo, segment 2: hi
-    r0[2 * k] = hr; r0[2 * k + 1] = -hi_; r1[2 * k] = hi_; r1[2 * k + 1] = hr;
-    r0[2 * K + 2 * k] = lr; r0[2 * K + 2 * k + 1] = -li; r1[2 * K + 2 * k] = li; r1[2 * K + 2 * k + 1] = lr;
-    r0[4 * K + 2 * k] = hr; r0[4 * K + 2 * k + 1] = -hi_; r1[4 * K + 2 * k] = hi_; r1[4 * K + 2 * k + 1] = hr;
+    if (k >= K) return;
+    for (int j = blockIdx.y; j < N; j += gridDim.y) {
+        double2 v = ld2<T>(src, (long long)k * rs + (long long)j * cs);
+        float hr, lr, hi_, li;
+        split2(v.x, hr, lr);
+        split2(v.y, hi_, li);
+        float *r0 = B3 + (long long)(2 * j) * ldb3, *r1 = r0 + ldb3;
+        // segment 0: hi, segment 1: lo, segment 2: hi
+        r0[2 * k] = hr; r0[2 * k + 1] = -hi_; r1[2 * k] = hi_; r1[2 * k + 1] = hr;
+        r0[2 * K + 2 * k] = lr; r0[2 * K + 2 * k + 1] = -li; r1[2 * K + 2 * k] = li; r1[2 * K + 2 * k + 1] = lr;
+        r0[4 * K + 2 * k] = hr; r0[4 * K + 2 * k + 1] = -hi_; r1[4 * K + 2 * k] = hi_; r1[4 * K + 2 * k + 1] = hr;
+    }
 }
 
 template <typename TA, typename TB>
@@ -99,9 +103,10 @@ int zgemm_x3(midas_gpu_ctx *c, int M, int N, int K, const TA *A, long long ars, 
         MIDAS_CUDA(c, cudaMemsetAsync(B3, 0, sizeof(float) * (size_t)2 * N * K6, c->stream));
     }
     ++c->launches;
-    k_split_a<TA><<<dim3((K + 127) / 128, M), 128, 0, c->stream>>>(M, K, A, ars, acs, conjA, A3, K6);
+    k_split_a<TA><<<dim3((K + 127) / 128, std::min(M, 65535)), 128, 0, c->stream>>>(M, K, A, ars, acs, conjA, A3, K6);
     ++c->launches;
-    k_split_expand_b<TB><<<dim3((K + 127) / 128, N), 128, 0, c->stream>>>(K, N, B, brs, bcs, B3, K6);
+    k_split_expand_b<TB><<<dim3((K + 127) / 128, std::min(N, 65535)), 128, 0, c->stream>>>(K, N, B, brs, bcs, B3,
+                                                                                            K6);
     MIDAS_CUDA(c, cudaGetLastError());
     GemmArgs g{M, 2 * N, (int)K6, A3, K6, B3, K6, D, ldd, alpha, beta};
     return gemm_tf32(c, g, true);
@@ -162,7 +167,9 @@ int zgemm64(midas_gpu_ctx *c, int M, int N, int K, const double2 *A, long long a
     if (M <= 0 || N <= 0) return MIDAS_OK;
     dim3 blk(16, 16), grd((N + 15) / 16, (M + 15) / 16);
     ++c->launches;
+    int kp = kp_begin(c);
     k_zgemm64<<<grd, blk, 0, c->stream>>>(M, N, K, A, ars, acs, conjA, B, brs, bcs, C, crs, ccs, alpha, beta);
+    kp_end(c, kp, MIDAS_KC_ZGEMM64, 8.0 * M * N * K, 16.0 * ((double)M * K + (double)K * N + 2.0 * M * N));
     MIDAS_CUDA(c, cudaGetLastError());
     return MIDAS_OK;
 }
@@ -250,7 +257,9 @@ int residual_df32(midas_gpu_ctx *c, int n, int nrhs, const float2 *Z, long long 
 {
     dim3 grd((nrhs + 31) / 32, (n + 31) / 32);
     ++c->launches;
+    int kp = kp_begin(c);
     k_residual_df32<<<grd, 256, 0, c->stream>>>(n, nrhs, Z, ldz, Xh, Xl, B, R);
+    kp_end(c, kp, MIDAS_KC_RESID, 8.0 * n * n * nrhs, 8.0 * n * n + 32.0 * n * nrhs);
     MIDAS_CUDA(c, cudaGetLastError());
     return MIDAS_OK;
 }
@@ -493,7 +502,9 @@ int heev_dev(midas_gpu_ctx *c, int batch, int m, double2 *A, long long lda, long
     if (m > 1024) return c->err.set(MIDAS_ERR_ARG, "heev: m > 1024");
     size_t sm = sizeof(double) * (4 * (size_t)m + 32) + sizeof(double2) * 3 * (size_t)m;
     ++c->launches;
+    int kp = kp_begin(c);
     k_heev_tridiag<<<batch, 256, sm, c->stream>>>(m, A, lda, sa, H, V, sv, W, c->d_flag);
+    kp_end(c, kp, MIDAS_KC_EIG, 0.0, 0.0);
     MIDAS_CUDA(c, cudaGetLastError());
     return MIDAS_OK;
 }

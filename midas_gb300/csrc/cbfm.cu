@@ -15,7 +15,10 @@
 //         vectors, which is all the reduced system depends on.
 //   2. T = Z(:, block j) C_j for every block column (complex(4)-rounded fill, FP32-grade
 //      3xTF32 tensor GEMM) and Zc(i, :) = C_i^T T(rows of i) -- plain transpose as
-//      ZGEMM('T','N') [630-809]
+//      ZGEMM('T','N') [630-809].  With ACA, every off-diagonal pair first runs the
+//      partial-pivot ACA (one CTA per pair, one launch for all pairs); a pair whose
+//      rank stays below Nb_it_max contributes T(rows of i, cols of j) = U (V C_j)
+//      instead of its dense fill (src/Compute_EFields_CBFME_ACA.f90:588-635).
 //   3. Vc = C^T Einc [829-849], reduced solve (mixed LU + FP64 refinement) [873-943],
 //      E = C alpha [990-1006].
 #include <algorithm>
@@ -157,8 +160,14 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
     }
     const int m = 2 * ncbf;
     const bool sr = flags & MIDAS_CBFM_SR, homog = flags & MIDAS_CBFM_HOMOG;
-    if (flags & MIDAS_CBFM_ACA) return c->err.set(MIDAS_ERR_UNSUPPORTED, "cbfm: ACA variant not available yet");
+    const bool use_aca = flags & MIDAS_CBFM_ACA;
     if (!(res_sr > 0)) res_sr = (double)1e-2f;
+    if (!(eps_aca > 0)) eps_aca = (double)1e-4f;        // Epsilon_ACA (src/InOut_ReadWrite_Functions.f90:396)
+    if (aca_itmax <= 0) aca_itmax = 50;                 // Nb_it_max
+    if (use_aca && (aca_itmax < 2 || aca_itmax > ACA_MAX_IT))
+        return c->err.set(MIDAS_ERR_ARG, "cbfm: aca_itmax must be in [2, 128]");
+    // the ACA driver fixes Threshold_CBFM = 1e-3 (src/Compute_EFields_CBFME_ACA.f90:124)
+    if (use_aca && !(thr_cbf > 0)) thr_cbf = (double)1e-3f;
     // ---- Threshold_CBFM from max |m| (src/Compute_EFields_CBFME.f90:286-288) ----
     if (!(thr_cbf > 0)) {
         std::vector<double2> eps(n);
@@ -206,22 +215,25 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
     MIDAS_TRY(ensure(c, S_CBF1, sizeof(float2) * (size_t)spmax * spmax, &p1));
     MIDAS_TRY(ensure(c, S_CBF2, sizeof(float2) * (size_t)spmax * spmax, &p2));
     size_t nrm = (size_t)spmax * m;
-    MIDAS_TRY(ensure(c, S_CBF3, (sizeof(float2) * 4 + sizeof(double2) * 2) * nrm + 4096, &p3));
-    MIDAS_TRY(ensure(c, S_CBF4, sizeof(double2) * (size_t)3 * m * m + sizeof(double) * m + 4096, &p4));
+    // FP64 block solutions of every block are kept for the batched eigen-solve
+    std::vector<size_t> xoff(nb + 1, 0);
+    for (int b = 0; b < nb; ++b) xoff[b + 1] = xoff[b] + (size_t)pad64(3 * (xo[b + 1] - xo[b])) * m;
+    MIDAS_TRY(ensure(c, S_CBF3, sizeof(float2) * 4 * nrm + sizeof(double2) * (nrm + xoff[nb]) + 4096, &p3));
+    MIDAS_TRY(ensure(c, S_CBF4, (sizeof(double2) * (size_t)3 * m * m + sizeof(double) * m) * nb + 4096, &p4));
     float2 *Zlu = (float2 *)p1, *Zsr = (float2 *)p2;
     Buf b3{c, 0, (char *)p3};
     float2 *Bm = b3.take<float2>(nrm), *Xh = b3.take<float2>(nrm), *Xl = b3.take<float2>(nrm),
            *d32 = b3.take<float2>(nrm);
-    double2 *X64 = b3.take<double2>(nrm), *R64 = b3.take<double2>(nrm);
+    double2 *Xall = b3.take<double2>(xoff[nb]), *R64 = b3.take<double2>(nrm);
     Buf b4{c, 0, (char *)p4};
-    double2 *G = b4.take<double2>((size_t)m * m), *Vv = b4.take<double2>((size_t)m * m),
-            *Hh = b4.take<double2>((size_t)m * m);
-    double *W = b4.take<double>(m);
+    const size_t mm = (size_t)m * m;
+    double2 *Gall = b4.take<double2>(mm * nb), *Vall = b4.take<double2>(mm * nb), *Hall = b4.take<double2>(mm * nb);
+    double *Wall = b4.take<double>((size_t)m * nb);
     void *pred;
     MIDAS_TRY(ensure(c, S_RED2, sizeof(unsigned long long) * 2 * m + 64, &pred));
     unsigned long long *red = (unsigned long long *)pred;
     std::vector<unsigned long long> hred(2 * m);
-    std::vector<double> hW(m);
+    std::vector<int> srefine(nb, 0);
     const double cbf_tol = (flags & MIDAS_CBFM_FAST_CBF) ? 1e-7 : 1e-11;
     cudaEvent_t e0, e1, e2, e3;
     cudaEventCreate(&e0); cudaEventCreate(&e1); cudaEventCreate(&e2); cudaEventCreate(&e3);
@@ -232,6 +244,7 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
         const int s = xo[b + 1] - xo[b], nbc = bo[b + 1] - bo[b];
         const int N3 = 3 * s, sp = pad64(N3);
         const int *idx = d_xall + xo[b];
+        double2 *X64 = Xall + xoff[b];
         double thr_sr = 0.0;
         if (sr) {
             double fsr;
@@ -287,11 +300,25 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
         }
         if (it == 12) return c->err.set(MIDAS_ERR_NOT_CONVERGED, "cbf block solve: refinement did not converge");
         ir_max = std::max(ir_max, it);
-        // Gram G = X^H X over the 3s rows of the extended block (FP64), eigen-decomposition
-        MIDAS_TRY(zgemm64(c, m, m, N3, X64, sp, 1, 1, X64, 1, sp, G, m, 1, make_double2(1, 0), make_double2(0, 0)));
-        MIDAS_TRY(heev_dev(c, 1, m, G, m, (long long)m * m, Hh, Vv, (long long)m * m, W));
-        MIDAS_CUDA(c, cudaMemcpyAsync(hW.data(), W, sizeof(double) * m, cudaMemcpyDeviceToHost, c->stream));
-        MIDAS_CUDA(c, cudaStreamSynchronize(c->stream));
+        // Gram G = X^H X over the 3s rows of the extended block (FP64)
+        MIDAS_TRY(zgemm64(c, m, m, N3, X64, sp, 1, 1, X64, 1, sp, Gall + mm * b, m, 1, make_double2(1, 0),
+                          make_double2(0, 0)));
+        srefine[b] = it;
+    }
+    // eigen-decomposition of every block's Gram matrix in one launch (one CTA per block)
+    MIDAS_TRY(heev_dev(c, nb, m, Gall, m, (long long)mm, Hall, Vall, (long long)mm, Wall));
+    std::vector<double> hWall((size_t)m * nb);
+    MIDAS_CUDA(c, cudaMemcpyAsync(hWall.data(), Wall, sizeof(double) * m * nb, cudaMemcpyDeviceToHost, c->stream));
+    MIDAS_CUDA(c, cudaStreamSynchronize(c->stream));
+    MIDAS_TRY(check_flag(c, "cbf eigen-solve"));
+    for (int b = 0; b < nb; ++b) {
+        const int s = xo[b + 1] - xo[b], nbc = bo[b + 1] - bo[b];
+        const int N3 = 3 * s, sp = pad64(N3);
+        const double2 *X64 = Xall + xoff[b];
+        double2 *Vv = Vall + mm * b;
+        const double *W = Wall + (size_t)m * b;
+        const double *hW = hWall.data() + (size_t)m * b;
+        const int it = srefine[b];
         double s1 = sqrt(std::max(hW[0], 0.0));
         if (c->opts.verbose >= 2) {
             fprintf(stderr, "[midas] cbf block %d: s=%d refine=%d sigma/sigma1:", b, s, it);
@@ -319,6 +346,43 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
     for (int b = 0; b < nb; ++b) koff[b + 1] = koff[b] + Kb[b];
     const int Kt = koff[nb];
     const long long ldT = 2LL * Kt;   // floats per row of T (complex)
+    // ACA of every off-diagonal pair (i, j), pair index i * (nb - 1) + (j < i ? j : j - 1)
+    const int npairs = use_aca ? nb * (nb - 1) : 0;
+    std::vector<int> rank(npairs, 0);
+    std::vector<AcaPair> pairs(npairs);
+    double2 *Uaca = nullptr, *Vaca = nullptr, *Waca = nullptr;
+    int n_far = 0;
+    auto pidx = [&](int i, int j) { return i * (nb - 1) + (j < i ? j : j - 1); };
+    if (use_aca) {
+        long long uo = 0, vo = 0;
+        for (int i = 0; i < nb; ++i)
+            for (int j = 0; j < nb; ++j) {
+                if (i == j) continue;
+                AcaPair &p = pairs[pidx(i, j)];
+                p.r0 = bo[i]; p.ni = bo[i + 1] - bo[i]; p.c0 = bo[j]; p.nj = bo[j + 1] - bo[j];
+                p.uoff = uo; p.voff = vo;
+                uo += 3LL * p.ni * aca_itmax;
+                vo += 3LL * p.nj * aca_itmax;
+            }
+        const size_t need = sizeof(double2) * (size_t)(uo + vo + (size_t)aca_itmax * m) +
+                            sizeof(AcaPair) * npairs + sizeof(int) * npairs + 5 * 256;
+        void *pa;
+        MIDAS_TRY(ensure(c, S_ACA, need, &pa));
+        Buf ba{c, 0, (char *)pa};
+        Uaca = ba.take<double2>(uo);
+        Vaca = ba.take<double2>(vo);
+        Waca = ba.take<double2>((size_t)aca_itmax * m);
+        AcaPair *d_pairs = ba.take<AcaPair>(npairs);
+        int *d_rank = ba.take<int>(npairs);
+        MIDAS_CUDA(c, cudaMemcpyAsync(d_pairs, pairs.data(), sizeof(AcaPair) * npairs, cudaMemcpyHostToDevice,
+                                      c->stream));
+        MIDAS_TRY(aca_batch(c, npairs, d_pairs, eps_aca, aca_itmax, Uaca, Vaca, d_rank));
+        MIDAS_CUDA(c, cudaMemcpyAsync(rank.data(), d_rank, sizeof(int) * npairs, cudaMemcpyDeviceToHost, c->stream));
+        MIDAS_CUDA(c, cudaStreamSynchronize(c->stream));
+        for (int p = 0; p < npairs; ++p) n_far += std::min(rank[p], aca_itmax) < aca_itmax;
+        if (c->opts.verbose >= 1) fprintf(stderr, "[midas] aca: %d of %d pairs low-rank\n", n_far, npairs);
+    }
+    auto dense = [&](int i, int j) { return i == j || !use_aca || std::min(rank[pidx(i, j)], aca_itmax) >= aca_itmax; };
     void *pz, *pt;
     MIDAS_TRY(ensure(c, S_CBF6, sizeof(float2) * (size_t)3 * n * 3 * nbmax, &pz));
     MIDAS_TRY(ensure(c, S_CBF7, sizeof(float) * (size_t)3 * n * ldT + sizeof(float) * (size_t)Kt * ldT, &pt));
@@ -326,11 +390,30 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
     float *T = (float *)pt, *Zcf = T + (size_t)3 * n * ldT;
     for (int j = 0; j < nb; ++j) {
         const int nj = bo[j + 1] - bo[j];
-        // Z(:, block j): rows = all unknowns, columns = unknowns of block j (row-major, ld 3 nj)
-        MIDAS_TRY(launch_block_fill4<float2>(c, n, d_all, nj, d_all + bo[j], 0, 0.0, 0, Zcol, (size_t)3 * nj, 1));
         const double2 *Cj = Call + coff[j];
-        MIDAS_TRY(zgemm_x3<float2, double2>(c, 3 * n, Kb[j], 3 * nj, Zcol, 3 * nj, 1, 0, Cj, 1, 3 * nj,
-                                            T + 2LL * koff[j], ldT, 1.f, 0.f));
+        // dense row blocks of column j, in runs of consecutive blocks: Z(rows of the run,
+        // block j) (row-major, ld 3 nj), then T(rows of the run, cols of j) = Z C_j
+        for (int i = 0; i < nb;) {
+            if (!dense(i, j)) { ++i; continue; }
+            int i1 = i;
+            while (i1 < nb && dense(i1, j)) ++i1;
+            const int r0 = bo[i], nr = bo[i1] - bo[i];
+            MIDAS_TRY(launch_block_fill4<float2>(c, nr, d_all + r0, nj, d_all + bo[j], 0, 0.0, 0, Zcol,
+                                                 (size_t)3 * nj, 1));
+            MIDAS_TRY(zgemm_x3<float2, double2>(c, 3 * nr, Kb[j], 3 * nj, Zcol, 3 * nj, 1, 0, Cj, 1, 3 * nj,
+                                                T + (size_t)3 * r0 * ldT + 2LL * koff[j], ldT, 1.f, 0.f));
+            i = i1;
+        }
+        // low-rank pairs: T(rows of i, cols of j) = U (V C_j), FP64 products
+        for (int i = 0; i < nb && use_aca; ++i) {
+            if (dense(i, j)) continue;
+            const AcaPair &p = pairs[pidx(i, j)];
+            const int k = rank[pidx(i, j)];
+            MIDAS_TRY(zgemm64(c, k, Kb[j], 3 * nj, Vaca + p.voff, 3LL * nj, 1, 0, Cj, 1, 3LL * nj, Waca, Kb[j], 1,
+                              make_double2(1, 0), make_double2(0, 0)));
+            MIDAS_TRY(aca_uw(c, 3 * p.ni, k, Kb[j], Uaca + p.uoff, Waca,
+                             (float2 *)T + (size_t)3 * bo[i] * Kt + koff[j], Kt));
+        }
     }
     for (int i = 0; i < nb; ++i) {
         const int ni = bo[i + 1] - bo[i];
@@ -392,6 +475,7 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
     if (info) {
         info->status = MIDAS_OK;
         info->k_total = Kt;
+        info->n_far_aca = n_far;
         info->ir_iters = sinfo.ir_iters;
         info->backward_error = sinfo.backward_error;
         info->anorm = sinfo.anorm;
@@ -400,13 +484,9 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
         info->t_solve_ms = t23;   // Vc, reduced solve, E
         info->t_total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tw0).count();
     }
-    (void)eps_aca; (void)aca_itmax; (void)ir_max;
+    (void)ir_max;
     return MIDAS_OK;
 }
 
-int aca_run(midas_gpu_ctx *c, int, int, int, int, double, int, double2 *, double2 *, int *)
-{
-    return c->err.set(MIDAS_ERR_UNSUPPORTED, "aca: not available yet");
-}
 
 }  // namespace midas

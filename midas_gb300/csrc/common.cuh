@@ -51,6 +51,20 @@ struct DBuf {
     size_t bytes = 0;
 };
 
+// ---------------------------------------------------------------------------
+// per-kernel-class device timing (roofline reports): CUDA events recorded on
+// the context stream around each instrumented launch while profiling is on
+// ---------------------------------------------------------------------------
+struct KProf {
+    bool on = false;
+    std::vector<cudaEvent_t> ev;   // event pool, grown on demand
+    size_t used = 0;
+    struct Rec { int cls, e0; double flops, bytes; };
+    std::vector<Rec> rec;
+    double ms[MIDAS_KC_COUNT] = {}, flops[MIDAS_KC_COUNT] = {}, bytes[MIDAS_KC_COUNT] = {};
+    long long n[MIDAS_KC_COUNT] = {};
+};
+
 }  // namespace midas
 
 // The context (opaque in the C ABI).
@@ -79,6 +93,7 @@ struct midas_gpu_ctx {
     std::vector<midas::DBuf> pool;
     int *d_flag = nullptr;   // device error flag
     long long launches = 0;  // kernels launched on this context
+    midas::KProf kprof;
     void *cusolver = nullptr;
     void *cublas = nullptr;
 };
@@ -87,6 +102,13 @@ namespace midas {
 
 // Scratch allocation helpers (pool slot i grows as needed).
 int ensure(midas_gpu_ctx *ctx, int slot, size_t bytes, void **out);
+
+// Kernel-class timing: kp_begin records a start event (returns -1 when profiling
+// is off), kp_end the stop event with the launch's algorithmic flops and bytes;
+// kp_flush waits for the recorded events and accumulates them per class.
+int kp_begin(midas_gpu_ctx *ctx);
+void kp_end(midas_gpu_ctx *ctx, int e0, int cls, double flops, double bytes);
+int kp_flush(midas_gpu_ctx *ctx);
 
 // Is p a device (or managed) pointer?
 bool is_device_ptr(const void *p);
@@ -104,7 +126,7 @@ enum Slot : int {
     S_IN0 = 0, S_IN1, S_IN2, S_IN3, S_IN4, S_IN5, S_OUT0, S_OUT1,
     S_Z32, S_Z64, S_LINV, S_UINV, S_BEXP, S_BEXP2, S_RHS64, S_X64, S_R64, S_T32, S_T32B, S_RED,
     S_CBF0, S_CBF1, S_CBF2, S_CBF3, S_CBF4, S_CBF5, S_CBF6, S_CBF7, S_CBF8, S_CBF9, S_RED2, S_EINC,
-    S_NSLOTS
+    S_ACA, S_NSLOTS
 };
 
 }  // namespace midas

@@ -138,8 +138,10 @@ int lu_factor_nopiv(midas_gpu_ctx *c, DenseLU &lu)
         const int j0 = k * nb, rem = n - j0 - nb;
         float2 *A11 = lu.A + (long long)j0 * lda + j0;
         ++c->launches;
+        int kp = kp_begin(c);
         k_diag_lu<LU_NB><<<1, 512, smem, c->stream>>>(A11, lda, lu.Linv + (size_t)k * nb * nb,
                                                       lu.Uinv + (size_t)k * nb * nb, uexp, 1e-30f, c->d_flag);
+        kp_end(c, kp, MIDAS_KC_DIAG_LU, 8.0 * nb * nb * nb, 8.0 * nb * nb * 4);
         MIDAS_CUDA(c, cudaGetLastError());
         if (rem == 0) break;
         // L21 = A21 U11^-1 (in place: each output row tile reads only its own rows)
@@ -222,22 +224,30 @@ int lu_solve(midas_gpu_ctx *c, const DenseLU &lu, float2 *R, int nrhs)
     for (int k = 0; k < lu.nblk; ++k) {
         int r0 = k * nb;
         ++c->launches;
+        int kp = kp_begin(c);
         k_apply_inv<<<nrhs, 64, 0, c->stream>>>(lu.Linv + (size_t)k * nb * nb, nb, R, n, r0);
+        kp_end(c, kp, MIDAS_KC_TRSV, 8.0 * nb * nb * nrhs, 8.0 * nb * nb + 16.0 * nb * nrhs);
         int na = n - r0 - nb;
         if (na > 0) {
             ++c->launches;
+            kp = kp_begin(c);
             k_gemv_update<<<(na * 32 + 255) / 256, 256, 0, c->stream>>>(lu.A, lu.lda, r0 + nb, na, r0, nb, R, n,
                                                                           nrhs);
+            kp_end(c, kp, MIDAS_KC_TRSV, 8.0 * na * nb * nrhs, 8.0 * na * nb + 16.0 * na * nrhs + 8.0 * nb * nrhs);
         }
     }
     // backward: U x = y
     for (int k = lu.nblk - 1; k >= 0; --k) {
         int r0 = k * nb;
         ++c->launches;
+        int kp = kp_begin(c);
         k_apply_inv<<<nrhs, 64, 0, c->stream>>>(lu.Uinv + (size_t)k * nb * nb, nb, R, n, r0);
+        kp_end(c, kp, MIDAS_KC_TRSV, 8.0 * nb * nb * nrhs, 8.0 * nb * nb + 16.0 * nb * nrhs);
         if (r0 > 0) {
             ++c->launches;
+            kp = kp_begin(c);
             k_gemv_update<<<(r0 * 32 + 255) / 256, 256, 0, c->stream>>>(lu.A, lu.lda, 0, r0, r0, nb, R, n, nrhs);
+            kp_end(c, kp, MIDAS_KC_TRSV, 8.0 * r0 * nb * nrhs, 8.0 * r0 * nb + 16.0 * r0 * nrhs + 8.0 * nb * nrhs);
         }
     }
     MIDAS_CUDA(c, cudaGetLastError());
@@ -364,7 +374,9 @@ int ir_solve(midas_gpu_ctx *c, const DenseLU &lu, const double2 *Z64, long long 
         k_add_corr<<<(unsigned)((nn + 255) / 256), 256, 0, c->stream>>>(x, d32, (long long)nn);
         MIDAS_CUDA(c, cudaMemsetAsync(red, 0, sizeof(unsigned long long) * 2 * nrhs, c->stream));
         ++c->launches;
+        int kp = kp_begin(c);
         k_residual64<<<(n * 32 + 255) / 256, 256, 0, c->stream>>>(Z64, ldz, n, b, x, nrhs, r, r32, red);
+        kp_end(c, kp, MIDAS_KC_RESID, 8.0 * n * n * nrhs, 16.0 * n * n + 40.0 * n * nrhs);
         ++c->launches;
         k_colmax<<<dim3(64, nrhs), 256, 0, c->stream>>>(x, n, nrhs, red + nrhs);
         MIDAS_CUDA(c, cudaGetLastError());

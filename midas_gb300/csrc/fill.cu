@@ -18,29 +18,10 @@
 // gather plus one complex product per element, which turns the fill from
 // FP64/SFU-bound into HBM-bound on GB300.
 #include "common.cuh"
+#include "green.cuh"
 #include "kernels.cuh"
 
 namespace midas {
-
-// ---------------------------------------------------------------------------
-// complex helpers
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ double2 zmul8(double2 a, double2 b)
-{
-    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
-}
-// complex(8) product with every operation separately rounded (no FMA)
-__device__ __forceinline__ double2 zmul8_rn(double2 a, double2 b)
-{
-    return make_double2(__dsub_rn(__dmul_rn(a.x, b.x), __dmul_rn(a.y, b.y)),
-                        __dadd_rn(__dmul_rn(a.x, b.y), __dmul_rn(a.y, b.x)));
-}
-// complex(4) product with every float operation separately rounded (no FMA)
-__device__ __forceinline__ float2 zmul4_rn(float2 a, float2 b)
-{
-    return make_float2(__fsub_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)),
-                       __fadd_rn(__fmul_rn(a.x, b.y), __fmul_rn(a.y, b.x)));
-}
 
 // ---------------------------------------------------------------------------
 // a1: SetCellsParams (src/SetCellsParams.f90:31-49)
@@ -70,87 +51,6 @@ __global__ void k_set_cells(int n, const double *sc, const double2 *eps, double 
     fk8[c] = f;
     fk4[c] = make_float2((float)f.x, (float)f.y);
 }
-
-// ---------------------------------------------------------------------------
-// dyads.  Component order of the six unique entries: xx, yy, zz, xy, yz, xz.
-// ---------------------------------------------------------------------------
-// FP64 F (before the -f_kapChe factor): src/Compute_EFields_MoM.f90:474-519.
-__device__ __forceinline__ void dyadF8(double rx, double ry, double rz, double k0, double Pi, double2 F[6])
-{
-    double r = sqrt(rx * rx + ry * ry + rz * rz);
-    double s, co;
-    sincos(k0 * r, &s, &co);
-    double den = 4 * Pi * (r * r);
-    double2 Gr = make_double2(co / den, s / den);
-    double2 Tau = make_double2(-(1 / r), k0);
-    double k2 = k0 * k0;
-    double d[3] = {rx, ry, rz};
-#pragma unroll
-    for (int p = 0; p < 3; ++p) {
-        double sv = 3. * (d[p] * d[p]) / (r * r);
-        double2 in = make_double2((Tau.x + k2 * (r - d[p] * d[p] / r)) - sv * Tau.x, Tau.y - sv * Tau.y);
-        F[p] = zmul8(Gr, in);
-    }
-    double2 w = make_double2(-k2 - (3. * Tau.x) / r, -((3. * Tau.y) / r));
-    double2 g;
-    g = make_double2((Gr.x / r) * (rx * ry), (Gr.y / r) * (rx * ry)); F[3] = zmul8(g, w);
-    g = make_double2((Gr.x / r) * (ry * rz), (Gr.y / r) * (ry * rz)); F[4] = zmul8(g, w);
-    g = make_double2((Gr.x / r) * (rx * rz), (Gr.y / r) * (rx * rz)); F[5] = zmul8(g, w);
-}
-
-// complex(4)-rounded F: Green_s_tr_partial (src/Green_functions.f90:139-157).
-__device__ __forceinline__ void dyadF4(double rx, double ry, double rz, double k0, double Pi, float2 F[6])
-{
-    double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(rx, rx), __dmul_rn(ry, ry)), __dmul_rn(rz, rz)));
-    double s, co;
-    sincos(__dmul_rn(k0, r), &s, &co);
-    double den = __dmul_rn(__dmul_rn(4.0, Pi), __dmul_rn(r, r));
-    float2 Gr4 = make_float2((float)__ddiv_rn(co, den), (float)__ddiv_rn(s, den));
-    float2 Tau4 = make_float2((float)(-__ddiv_rn(1.0, r)), (float)k0);
-    double2 Gr = make_double2(Gr4.x, Gr4.y), Tau = make_double2(Tau4.x, Tau4.y);
-    double k2 = __dmul_rn(k0, k0);
-    double r2 = __dmul_rn(r, r);
-    double d[3] = {rx, ry, rz};
-#pragma unroll
-    for (int p = 0; p < 3; ++p) {
-        double dd = __dmul_rn(d[p], d[p]);
-        double sv = __ddiv_rn(__dmul_rn(3., dd), r2);
-        double re = __dsub_rn(__dadd_rn(Tau.x, __dmul_rn(k2, __dsub_rn(r, __ddiv_rn(dd, r)))), __dmul_rn(sv, Tau.x));
-        double im = __dsub_rn(Tau.y, __dmul_rn(sv, Tau.y));
-        double2 f = zmul8_rn(Gr, make_double2(re, im));
-        F[p] = make_float2((float)f.x, (float)f.y);
-    }
-    // 3.*Tau_mn is a single-precision complex(4) product
-    float t3r = __fmul_rn(3.0f, Tau4.x), t3i = __fmul_rn(3.0f, Tau4.y);
-    double2 w = make_double2(__dsub_rn(-k2, __ddiv_rn((double)t3r, r)), -__ddiv_rn((double)t3i, r));
-    double gr = __ddiv_rn(Gr.x, r), gi = __ddiv_rn(Gr.y, r);
-    double pr[3] = {__dmul_rn(rx, ry), __dmul_rn(ry, rz), __dmul_rn(rx, rz)};
-#pragma unroll
-    for (int t = 0; t < 3; ++t) {
-        double2 f = zmul8_rn(make_double2(__dmul_rn(gr, pr[t]), __dmul_rn(gi, pr[t])), w);
-        F[3 + t] = make_float2((float)f.x, (float)f.y);
-    }
-}
-
-// index (p,q) -> unique component
-__device__ __forceinline__ int comp6(int p, int q)
-{
-    return p == q ? p : ((p + q == 1) ? 3 : ((p + q == 3) ? 4 : 5));
-}
-
-// lattice offset -> table slot (offsets stored for every (di,dj,dk) in range)
-struct Lat {
-    const int *ijk;
-    int dim0, dim1, dim2;     // table extents (2*span+1)
-    int sp0, sp1, sp2;        // spans
-    __device__ __forceinline__ size_t slot(int o, int s) const
-    {
-        int di = ijk[3 * o] - ijk[3 * s] + sp0;
-        int dj = ijk[3 * o + 1] - ijk[3 * s + 1] + sp1;
-        int dk = ijk[3 * o + 2] - ijk[3 * s + 2] + sp2;
-        return ((size_t)dk * dim1 + dj) * dim0 + di;
-    }
-};
 
 // Table of F per lattice offset: tab8 (FP64) and tab4 (complex(4)-rounded).
 __global__ void k_lat_table(int dim0, int dim1, int dim2, int sp0, int sp1, int sp2, double d, double k0,
@@ -351,7 +251,7 @@ __global__ void k_block_fill4(int n1, const int *idx1, int n2, const int *idx2, 
                 float2 g = zmul4_rn(F[comp6(p, q)], fk);
                 g = make_float2(-g.x, -g.y);
                 if (mode == 1) {
-                    float a = hypotf(g.x, g.y);
+                    float a = absf4(g);
                     if (!((double)a > thr)) g = make_float2(0.f, 0.f);
                 }
                 // the mirror transposes the 3x3: entry (p,q) of (o,s) is (q,p) of (s,o); F is symmetric
@@ -401,8 +301,8 @@ __global__ void k_sr_scan(int s_n, const int *idx, const double *x, const double
         // Green_s_tr_partial_FN: homog scans Io >= Is; term is a real(4) expression
         if (!homog || io >= is) {
             float aF[6];
-            for (int c = 0; c < 6; ++c) aF[c] = hypotf(F[c].x, F[c].y);
-            float afk = hypotf(fk.x, fk.y);
+            for (int c = 0; c < 6; ++c) aF[c] = absf4(F[c]);
+            float afk = absf4(fk);
             float tt = __fadd_rn(__fmul_rn(aF[0], aF[0]), __fmul_rn(2.f, __fmul_rn(aF[3], aF[3])));
             tt = __fadd_rn(tt, __fmul_rn(2.f, __fmul_rn(aF[5], aF[5])));
             tt = __fadd_rn(tt, __fmul_rn(aF[1], aF[1]));
@@ -415,7 +315,7 @@ __global__ void k_sr_scan(int s_n, const int *idx, const double *x, const double
             for (int p = 0; p < 3; ++p)
                 for (int q = 0; q < 3; ++q) {
                     float2 g = zmul4_rn(F[comp6(p, q)], fk);
-                    float a = hypotf(g.x, g.y);
+                    float a = absf4(g);
                     double a2 = (double)__fmul_rn(a, a);
                     for (int j = 0; j < NLAD; ++j)
                         if ((double)a > thr[j]) { acc[1 + j] += 1; acc[1 + NLAD + j] += a2; }
@@ -481,12 +381,14 @@ int launch_mom_fill(midas_gpu_ctx *c, int r0, int nr, int c0, int nc, double2 *o
     // the fill kernel indexes cells from r0/3, c0/3: pass the aligned starts
     Lat l = make_lat(c);
     ++c->launches;
+    int kp = kp_begin(c);
     if (c->opts.fill_mode == MIDAS_FILL_FAST && c->lattice && c->lat_tab8)
         k_mom_fill<true><<<grd, blk, 0, c->stream>>>(r0, nr, c0, nc, c->x, c->y, c->z, c->znnpp, c->fk8, c->k0, c->pi,
                                                      l, c->lat_tab8, out, out32, rs, cs);
     else
         k_mom_fill<false><<<grd, blk, 0, c->stream>>>(r0, nr, c0, nc, c->x, c->y, c->z, c->znnpp, c->fk8, c->k0,
                                                       c->pi, l, nullptr, out, out32, rs, cs);
+    kp_end(c, kp, MIDAS_KC_FILL, 0.0, (double)nr * nc * ((out ? 16 : 0) + (out32 ? 8 : 0)));
     MIDAS_CUDA(c, cudaGetLastError());
     return MIDAS_OK;
 }
@@ -525,12 +427,14 @@ int launch_block_fill4(midas_gpu_ctx *c, int n1, const int *idx1, int n2, const 
     dim3 grd((n2 + 63) / 64, (n1 + 1) / 2);
     Lat l = make_lat(c);
     ++c->launches;
+    int kp = kp_begin(c);
     if (c->opts.fill_mode == MIDAS_FILL_FAST && use_lat(c))
         k_block_fill4<true, T><<<grd, blk, 0, c->stream>>>(n1, idx1, n2, idx2, c->x, c->y, c->z, c->znnpp, c->fk4,
                                                            c->k0, c->pi, l, c->lat_tab4, mode, thr, homog, out, rs, cs);
     else
         k_block_fill4<false, T><<<grd, blk, 0, c->stream>>>(n1, idx1, n2, idx2, c->x, c->y, c->z, c->znnpp, c->fk4,
                                                             c->k0, c->pi, l, nullptr, mode, thr, homog, out, rs, cs);
+    kp_end(c, kp, MIDAS_KC_FILL, 0.0, 9.0 * n1 * n2 * sizeof(T));
     MIDAS_CUDA(c, cudaGetLastError());
     return MIDAS_OK;
 }
@@ -557,12 +461,14 @@ int sr_ladder(midas_gpu_ctx *c, int s_n, const int *d_idx, int first_cell, int h
     MIDAS_CUDA(c, cudaMemcpyAsync(dthr, thr, sizeof(thr), cudaMemcpyHostToDevice, c->stream));
     Lat l = make_lat(c);
     ++c->launches;
+    int kp = kp_begin(c);
     if (c->opts.fill_mode == MIDAS_FILL_FAST && use_lat(c))
         k_sr_scan<true><<<nblk, 256, 0, c->stream>>>(s_n, d_idx, c->x, c->y, c->z, c->znnpp, c->fk4, c->k0, c->pi, l,
                                                      c->lat_tab4, homog, dthr, part);
     else
         k_sr_scan<false><<<nblk, 256, 0, c->stream>>>(s_n, d_idx, c->x, c->y, c->z, c->znnpp, c->fk4, c->k0, c->pi,
                                                       l, nullptr, homog, dthr, part);
+    kp_end(c, kp, MIDAS_KC_SR_SCAN, 0.0, 0.0);
     MIDAS_CUDA(c, cudaGetLastError());
     std::vector<double> h((size_t)nblk * nv);
     MIDAS_CUDA(c, cudaMemcpyAsync(h.data(), part, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, c->stream));

@@ -18,6 +18,8 @@
 #include <cstdlib>
 #include <cstring>
 
+#include <algorithm>
+
 #include "common.cuh"
 #include "kernels.cuh"
 
@@ -389,11 +391,19 @@ static int pick_engine()
     return g_engine;
 }
 
+// algorithmic bytes of one real GEMM: A and Bt once, D written (and read when beta != 0)
+static double gemm_bytes(const GemmArgs &g)
+{
+    return 4.0 * ((double)g.M * g.K + (double)g.N * g.K + (double)g.M * g.N * (g.beta != 0.f ? 2 : 1));
+}
+
 static int gemm_simt(midas_gpu_ctx *c, const GemmArgs &g)
 {
     dim3 grd((g.N + 63) / 64, (g.M + 63) / 64);
     ++c->launches;
+    int kp = kp_begin(c);
     k_gemm_simt<<<grd, 256, 0, c->stream>>>(g);
+    kp_end(c, kp, MIDAS_KC_GEMM_SIMT, 2.0 * g.M * g.N * g.K, gemm_bytes(g));
     MIDAS_CUDA(c, cudaGetLastError());
     return MIDAS_OK;
 }
@@ -414,12 +424,14 @@ static int gemm_tc(midas_gpu_ctx *c, const GemmArgs &g, bool precise)
     MIDAS_TRY(make_map(c, &mb, g.Bt, g.N, g.K, g.ldb, TC_BN));
     dim3 grd((g.N + TC_BN - 1) / TC_BN, (g.M + TC_BM - 1) / TC_BM);
     ++c->launches;
+    int kp = kp_begin(c);
     if (precise)
         k_gemm_tc<true><<<grd, TC_THREADS, TC_SMEM, c->stream>>>(ma, mb, g.M, g.N, g.K, g.D, g.ldd, g.alpha, g.beta,
                                                                  c->d_flag);
     else
         k_gemm_tc<false><<<grd, TC_THREADS, TC_SMEM, c->stream>>>(ma, mb, g.M, g.N, g.K, g.D, g.ldd, g.alpha, g.beta,
                                                                   c->d_flag);
+    kp_end(c, kp, MIDAS_KC_GEMM_TC, 2.0 * g.M * g.N * g.K, gemm_bytes(g));
     MIDAS_CUDA(c, cudaGetLastError());
     return MIDAS_OK;
 }
@@ -437,19 +449,20 @@ int gemm_tf32(midas_gpu_ctx *c, const GemmArgs &g, bool precise)
 __global__ void k_expand_b(int k, int n, const float2 *B, long long rsb, long long csb, float *Bt, long long ldt)
 {
     int p = blockIdx.x * blockDim.x + threadIdx.x;   // along k (contiguous in Bt rows)
-    int j = blockIdx.y;
     if (p >= k) return;
-    float2 b = B[(long long)p * rsb + (long long)j * csb];
-    float *r0 = Bt + (long long)(2 * j) * ldt + 2 * p;
-    float *r1 = r0 + ldt;
-    r0[0] = b.x; r0[1] = -b.y;
-    r1[0] = b.y; r1[1] = b.x;
+    for (int j = blockIdx.y; j < n; j += gridDim.y) {   // columns beyond the 65535 grid limit loop
+        float2 b = B[(long long)p * rsb + (long long)j * csb];
+        float *r0 = Bt + (long long)(2 * j) * ldt + 2 * p;
+        float *r1 = r0 + ldt;
+        r0[0] = b.x; r0[1] = -b.y;
+        r1[0] = b.y; r1[1] = b.x;
+    }
 }
 
 int expand_b(midas_gpu_ctx *c, int k, int n, const float2 *B, long long rsb, long long csb, float *Bt, long long ldt)
 {
     if (k <= 0 || n <= 0) return MIDAS_OK;
-    dim3 grd((k + 127) / 128, n);
+    dim3 grd((k + 127) / 128, std::min(n, 65535));
     ++c->launches;
     k_expand_b<<<grd, 128, 0, c->stream>>>(k, n, B, rsb, csb, Bt, ldt);
     MIDAS_CUDA(c, cudaGetLastError());

@@ -21,6 +21,19 @@ struct Timer {
     }
 };
 
+// aca.cu: one block pair of the ACA batch -- cells [r0, r0+ni) x [c0, c0+nj);
+// U and V of the pair start at element offsets uoff / voff of the batch arrays.
+constexpr int ACA_MAX_IT = 128;
+struct AcaPair {
+    int r0, ni, c0, nj;
+    long long uoff, voff;
+};
+int aca_batch(midas_gpu_ctx *c, int npairs, const AcaPair *d_pairs, double eps, int itmax, double2 *U, double2 *V,
+              int *d_rank);
+int aca_uw(midas_gpu_ctx *c, int nrows, int k, int ncol, const double2 *U, const double2 *W, float2 *T, long long ldt);
+int aca_run(midas_gpu_ctx *c, int row0, int nrows, int col0, int ncols, double eps, int itmax, double2 *U,
+            double2 *V, int *rank);
+
 // fill.cu
 int launch_set_cells(midas_gpu_ctx *c);
 int launch_lat_table(midas_gpu_ctx *c);

@@ -63,11 +63,53 @@ int to_device(midas_gpu_ctx *ctx, const void *p, size_t bytes, int slot, const v
     return MIDAS_OK;
 }
 
+int kp_begin(midas_gpu_ctx *c)
+{
+    KProf &k = c->kprof;
+    if (!k.on) return -1;
+    while (k.ev.size() < k.used + 2) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) { cudaGetLastError(); k.on = false; return -1; }
+        k.ev.push_back(e);
+    }
+    int i = (int)k.used;
+    k.used += 2;
+    if (cudaEventRecord(k.ev[i], c->stream) != cudaSuccess) { cudaGetLastError(); return -1; }
+    return i;
+}
+
+void kp_end(midas_gpu_ctx *c, int e0, int cls, double flops, double bytes)
+{
+    if (e0 < 0) return;
+    KProf &k = c->kprof;
+    if (cudaEventRecord(k.ev[e0 + 1], c->stream) != cudaSuccess) { cudaGetLastError(); return; }
+    k.rec.push_back({cls, e0, flops, bytes});
+}
+
+int kp_flush(midas_gpu_ctx *c)
+{
+    KProf &k = c->kprof;
+    if (k.rec.empty()) { k.used = 0; return MIDAS_OK; }
+    MIDAS_CUDA(c, cudaEventSynchronize(k.ev[k.rec.back().e0 + 1]));
+    for (const auto &r : k.rec) {
+        float ms = 0;
+        MIDAS_CUDA(c, cudaEventElapsedTime(&ms, k.ev[r.e0], k.ev[r.e0 + 1]));
+        k.ms[r.cls] += ms;
+        k.flops[r.cls] += r.flops;
+        k.bytes[r.cls] += r.bytes;
+        k.n[r.cls] += 1;
+    }
+    k.rec.clear();
+    k.used = 0;
+    return MIDAS_OK;
+}
+
 int check_flag(midas_gpu_ctx *ctx, const char *where)
 {
     int h = 0;
     MIDAS_CUDA(ctx, cudaMemcpyAsync(&h, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     MIDAS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    MIDAS_TRY(kp_flush(ctx));
     if (h == 0) return MIDAS_OK;
     MIDAS_CUDA(ctx, cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->stream));
     std::string w(where);
@@ -249,6 +291,7 @@ int midas_gpu_free(midas_gpu_ctx *c)
         if (b.p) cudaFree(b.p);
     if (c->d_flag) cudaFree(c->d_flag);
     if (c->cusolver) destroy_cusolver(c->cusolver);
+    for (cudaEvent_t e : c->kprof.ev) cudaEventDestroy(e);
     cudaStreamDestroy(c->stream);
     delete c;
     return MIDAS_OK;
@@ -469,6 +512,8 @@ int midas_gpu_aca(midas_gpu_ctx *c, int row0, int nrows, int col0, int ncols, do
     if (row0 < 0 || col0 < 0 || nrows <= 0 || ncols <= 0 || row0 % 3 || col0 % 3 || nrows % 3 || ncols % 3 ||
         row0 + nrows > N || col0 + ncols > N || itmax < 2 || !U || !V || !rank)
         return c->err.set(MIDAS_ERR_ARG, "aca: bad block");
+    cudaSetDevice(c->device);
+    MIDAS_TRY(need_tables(c));
     size_t bu = sizeof(double2) * (size_t)nrows * itmax, bv = sizeof(double2) * (size_t)itmax * ncols;
     void *pu, *pv;
     MIDAS_TRY(ensure(c, S_OUT0, bu, &pu));
@@ -773,6 +818,35 @@ int midas_gpu_bench_gemm(midas_gpu_ctx *c, int M, int N, int K, int iters, doubl
 }
 
 long long midas_gpu_launch_count(const midas_gpu_ctx *c) { return c ? c->launches : 0; }
+
+int midas_gpu_profile(midas_gpu_ctx *c, int enable)
+{
+    if (!c) return MIDAS_ERR_ARG;
+    c->err = Err();
+    cudaSetDevice(c->device);
+    MIDAS_TRY(kp_flush(c));
+    KProf &k = c->kprof;
+    if (enable) {
+        for (int i = 0; i < MIDAS_KC_COUNT; ++i) { k.ms[i] = k.flops[i] = k.bytes[i] = 0; k.n[i] = 0; }
+    }
+    k.on = enable != 0;
+    return MIDAS_OK;
+}
+
+int midas_gpu_profile_query(midas_gpu_ctx *c, int kclass, double *ms, double *flops, double *bytes,
+                            long long *launches)
+{
+    if (!c || kclass < 0 || kclass >= MIDAS_KC_COUNT) return MIDAS_ERR_ARG;
+    c->err = Err();
+    cudaSetDevice(c->device);
+    MIDAS_TRY(kp_flush(c));
+    const KProf &k = c->kprof;
+    if (ms) *ms = k.ms[kclass];
+    if (flops) *flops = k.flops[kclass];
+    if (bytes) *bytes = k.bytes[kclass];
+    if (launches) *launches = k.n[kclass];
+    return MIDAS_OK;
+}
 
 void *midas_gpu_stream(const midas_gpu_ctx *c) { return c ? (void *)c->stream : nullptr; }
 

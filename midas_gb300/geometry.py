@@ -83,36 +83,44 @@ def _real_sph_harm(l: int, m: int, ct: np.ndarray, phi: np.ndarray) -> np.ndarra
 
 
 def gaussian_sphere(a: float, sigma: float, corr_angle_deg: float, d: float, seed: int,
-                    lmax: int = 24) -> np.ndarray:
+                    lmax: int = 24, ngrid: int = 181) -> np.ndarray:
     """Voxel centroids inside r(u) = a exp(s(u) - sigma^2/2), s a Gaussian field
-    on the unit sphere with std sigma and the given correlation angle."""
+    on the unit sphere with std sigma and the given correlation angle.
+
+    s is a real spherical-harmonic series with seeded coefficients; r is
+    evaluated on an (ngrid x 2 ngrid) theta-phi grid and interpolated bilinearly
+    at each voxel direction."""
     rng = np.random.default_rng(seed)
     c = _legendre_coeffs(corr_angle_deg, lmax)
-    coef = {}
+    tg = np.linspace(0.0, np.pi, ngrid)
+    pg = np.linspace(-np.pi, np.pi, 2 * ngrid - 1)
+    T, P = np.meshgrid(tg, pg, indexing="ij")
+    ct, ph = np.cos(T).ravel(), P.ravel()
+    s = np.zeros_like(ct)
     for l in range(lmax + 1):
         if c[l] <= 0:
             continue
         sd = sigma * math.sqrt(c[l] * 4 * math.pi / (2 * l + 1))
         for m in range(-l, l + 1):
-            coef[(l, m)] = rng.normal(0.0, sd)
-
-    def radius(ct, phi):
-        s = np.zeros_like(ct)
-        for (l, m), v in coef.items():
-            s += v * _real_sph_harm(l, m, ct, phi)
-        return a * np.exp(s - sigma ** 2 / 2.0)
-
-    rmax = a * math.exp(4 * sigma)
+            s += rng.normal(0.0, sd) * _real_sph_harm(l, m, ct, ph)
+    R = (a * np.exp(s - sigma ** 2 / 2.0)).reshape(T.shape)
+    rmax = float(R.max()) * 1.001
     n = int(math.ceil(rmax / d))
     g = (np.arange(-n, n) + 0.5) * d
     X, Y, Z = np.meshgrid(g, g, g, indexing="ij")
     p = np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1)
     r = np.linalg.norm(p, axis=1)
     p, r = p[r < rmax], r[r < rmax]
-    ct = p[:, 2] / r
+    th = np.arccos(np.clip(p[:, 2] / r, -1.0, 1.0))
     phi = np.arctan2(p[:, 1], p[:, 0])
-    keep = r < radius(ct, phi)
-    return np.ascontiguousarray(p[keep])
+    fi = th / np.pi * (ngrid - 1)
+    fj = (phi + np.pi) / (2 * np.pi) * (2 * ngrid - 2)
+    i0 = np.clip(np.floor(fi).astype(int), 0, ngrid - 2)
+    j0 = np.clip(np.floor(fj).astype(int), 0, 2 * ngrid - 3)
+    wi, wj = fi - i0, fj - j0
+    rr = (R[i0, j0] * (1 - wi) * (1 - wj) + R[i0 + 1, j0] * wi * (1 - wj) + R[i0, j0 + 1] * (1 - wi) * wj
+          + R[i0 + 1, j0 + 1] * wi * wj)
+    return np.ascontiguousarray(p[r < rr])
 
 
 def cube_cells(n_side: int, d: float, n_cells: int | None = None) -> np.ndarray:

@@ -200,6 +200,21 @@ class Context:
     def launch_count(self) -> int:
         return int(self.L.midas_gpu_launch_count(self.h))
 
+    def profile(self, enable: bool = True):
+        """Start (clearing the totals) or stop per-kernel-class device timing."""
+        self._ck(self.L.midas_gpu_profile(self.h, 1 if enable else 0))
+
+    def profile_query(self) -> dict:
+        """{class: {ms, flops, bytes, launches}} since profiling was enabled."""
+        out = {}
+        for k, name in enumerate(_lib.KCLASSES):
+            ms, fl, by, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_double(), ctypes.c_longlong()
+            self._ck(self.L.midas_gpu_profile_query(self.h, k, ctypes.byref(ms), ctypes.byref(fl), ctypes.byref(by),
+                                                    ctypes.byref(n)))
+            if n.value:
+                out[name] = {"ms": ms.value, "flops": fl.value, "bytes": by.value, "launches": n.value}
+        return out
+
     def stream_handle(self) -> int:
         """cudaStream_t of the context (wrap with torch.cuda.ExternalStream to time on it)."""
         return int(self.L.midas_gpu_stream(self.h) or 0)

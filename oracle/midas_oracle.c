@@ -62,6 +62,8 @@ static inline zc8 z8(double re, double im) { zc8 z; z.re = re; z.im = im; return
 static inline zc8 z8mul(zc8 a, zc8 b) { return z8(a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re); }
 static inline zc8 z8of4(zc4 a) { return z8((double)a.re, (double)a.im); }
 static inline zc4 z4of8(zc8 a) { zc4 r; r.re = (float)a.re; r.im = (float)a.im; return r; }
+/* |z| of a complex(4) value, rounded like the GPU kernels' (see zabs below) */
+static inline float absf4(float re, float im) { return sqrtf(re * re + im * im); }
 static inline zc4 z4mul(zc4 a, zc4 b)
 {
     /* complex(4) product without FMA: every float operation rounded. */
@@ -330,7 +332,7 @@ double or_green_partial_fn(int n1, const int *idx1, int n2, const int *idx2, int
     for (int js = 0; js < n2; ++js) {
         int s = idx2[js];
         zc4 fk = fk4_of(kappa, che, s);
-        float afk = hypotf(fk.re, fk.im);
+        float afk = absf4(fk.re, fk.im);
         int io0 = homog ? js : 0;
         double part = 0;
         for (int io = io0; io < n1; ++io) {
@@ -351,7 +353,7 @@ double or_green_partial_fn(int n1, const int *idx1, int n2, const int *idx2, int
             for (int p = 0; p < 3; ++p) {
                 double sv = 3. * (d[p] * d[p]) / (r * r);
                 zc4 f = z4of8(z8mul(Gr, z8((Tau.re + k2 * (r - d[p] * d[p] / r)) - sv * Tau.re, Tau.im - sv * Tau.im)));
-                aF[p] = hypotf(f.re, f.im);
+                aF[p] = absf4(f.re, f.im);
             }
             float t3r = 3.0f * Tau4.re, t3i = 3.0f * Tau4.im;
             zc8 w = z8(-k2 - (double)t3r / r, -((double)t3i / r));
@@ -359,7 +361,7 @@ double or_green_partial_fn(int n1, const int *idx1, int n2, const int *idx2, int
             for (int t = 0; t < 3; ++t) {
                 double rr = d[pq[t][0]] * d[pq[t][1]];
                 zc4 f = z4of8(z8mul(z8((Gr.re / r) * rr, (Gr.im / r) * rr), w));
-                aF[3 + t] = hypotf(f.re, f.im);
+                aF[3 + t] = absf4(f.re, f.im);
             }
             /* (|Fxx|**2+2.*|Fxy|**2+2.*|Fxz|**2+|Fyy|**2+2.*|Fyz|**2+|Fzz|**2)*|f_kapChe|**2.: abs() of
              * a complex(4) is real(4), so the whole term is a single-precision expression (:236-237). */
@@ -421,7 +423,7 @@ long or_sr_dense(int s_n, const int *idx, double fsr, int homog,
                 for (int q = 0; q < 3; ++q) {
                     zc8 g = D[p * 3 + q];
                     /* abs(g) of a complex(4) value */
-                    float af = hypotf((float)g.re, (float)g.im);
+                    float af = absf4((float)g.re, (float)g.im);
                     double a = (double)af;
                     if (a > thr) {
                         nnz += 1; g2 += (double)(af * af);
@@ -551,7 +553,11 @@ void or_block_col(int row0, int nrows, int gcol, const double *x, const double *
     block_col(row0, nrows, gcol, x, y, z, kappa, che, k0, ref_pi(), (zc8 *)out);
 }
 
-static inline double zabs(zc8 a) { return hypot(a.re, a.im); }
+/* |z| as sqrt(re^2 + im^2) with every operation rounded: the pivot searches and
+ * threshold tests compare magnitudes, and this form evaluates bit-identically in
+ * the oracle (no FMA contraction) and on the GPU.  (The reference's Fortran ABS
+ * of a complex is a compiler intrinsic whose last-bit behaviour is unpinned.) */
+static inline double zabs(zc8 a) { return sqrt(a.re * a.re + a.im * a.im); }
 static inline zc8 zdiv(zc8 a, zc8 b)
 {
     double d = b.re * b.re + b.im * b.im;
