@@ -280,7 +280,8 @@ def run_ours(args, wl, world, rank, local, pg):
     n = len(wl["xyz"])
     ntr = len(wl["th"])
     N = 3 * n
-    ctx = Context(device=local)
+    # FAST fill: dyads from the per-lattice-offset tables (voxel scatterers sit on one lattice)
+    ctx = Context(device=local, fill_mode=_lib.FILL_FAST)
     stream = torch.cuda.ExternalStream(ctx.stream_handle(), device=dev)
     # device-resident inputs
     xyz_d = torch.from_numpy(np.ascontiguousarray(wl["xyz"].T)).to(dev)

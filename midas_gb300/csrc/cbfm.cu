@@ -50,16 +50,19 @@ __global__ void k_pad_diag32(float2 *Z, long long ld, int n0, int np)
     if (i < np) Z[(long long)i * ld + i] = make_float2(1.f, 0.f);
 }
 
-// X64 += d32 ; Xh = fp32(X64) ; Xl = fp32(X64 - Xh)   (n x m column-major, ld n)
-__global__ void k_ir_update(long long tot, double2 *X64, const float2 *d32, float2 *Xh, float2 *Xl, int first)
+// X64 += d32 ; Xh = fp32(X64) ; Xl = fp32(X64 - Xh)   (n x m column-major, ld n);
+// with rm = 1, Xh and Xl are written row-major (n x m) for the CSR residual
+__global__ void k_ir_update(long long tot, int n, int m, double2 *X64, const float2 *d32, float2 *Xh, float2 *Xl,
+                            int first, int rm)
 {
     long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i >= tot) return;
     double2 x = first ? make_double2(d32[i].x, d32[i].y) : make_double2(X64[i].x + d32[i].x, X64[i].y + d32[i].y);
     X64[i] = x;
     float2 h = make_float2((float)x.x, (float)x.y);
-    Xh[i] = h;
-    Xl[i] = make_float2((float)(x.x - h.x), (float)(x.y - h.y));
+    long long o = rm ? (i % n) * m + i / n : i;
+    Xh[o] = h;
+    Xl[o] = make_float2((float)(x.x - h.x), (float)(x.y - h.y));
 }
 
 // d32 = fp32(r); per-column max |r| and max |x| into red (bit patterns of >= 0 doubles)
@@ -211,9 +214,9 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
     std::vector<size_t> coff(nb + 1, 0);
     std::vector<int> Kb(nb, 0);
     // per-block work buffers (sized for the largest extended block)
-    void *p1, *p2, *p3, *p4;
+    void *p1, *p2 = nullptr, *p3, *p4;
     MIDAS_TRY(ensure(c, S_CBF1, sizeof(float2) * (size_t)spmax * spmax, &p1));
-    MIDAS_TRY(ensure(c, S_CBF2, sizeof(float2) * (size_t)spmax * spmax, &p2));
+    if (!sr) MIDAS_TRY(ensure(c, S_CBF2, sizeof(float2) * (size_t)spmax * spmax, &p2));
     size_t nrm = (size_t)spmax * m;
     // FP64 block solutions of every block are kept for the batched eigen-solve
     std::vector<size_t> xoff(nb + 1, 0);
@@ -255,13 +258,21 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
             thr_sr = hypot(1 - zn.x, -zn.y) / fsr;
             if (c->opts.verbose >= 2) fprintf(stderr, "[midas] cbf block %d: fSR=%g nnz=%lld thr=%.17g\n", b, fsr, nnz, thr_sr);
         }
-        MIDAS_CUDA(c, cudaMemsetAsync(Zsr, 0, sizeof(float2) * (size_t)sp * sp, c->stream));
-        MIDAS_TRY(launch_block_fill4<float2>(c, s, idx, s, idx, sr ? 1 : 0, thr_sr, homog, Zsr, (size_t)sp, 1));
+        // the thresholded block goes straight into the LU buffer; with SR its CSR
+        // form (about a sixth of the entries) serves the refinement residuals,
+        // without SR a dense copy does
+        MIDAS_CUDA(c, cudaMemsetAsync(Zlu, 0, sizeof(float2) * (size_t)sp * sp, c->stream));
+        MIDAS_TRY(launch_block_fill4<float2>(c, s, idx, s, idx, sr ? 1 : 0, thr_sr, homog, Zlu, (size_t)sp, 1));
         if (sp > N3) {
             ++c->launches;
-            k_pad_diag32<<<1, 64, 0, c->stream>>>(Zsr, sp, N3, sp);
+            k_pad_diag32<<<1, 64, 0, c->stream>>>(Zlu, sp, N3, sp);
         }
-        MIDAS_CUDA(c, cudaMemcpyAsync(Zlu, Zsr, sizeof(float2) * (size_t)sp * sp, cudaMemcpyDeviceToDevice, c->stream));
+        Csr zcsr;
+        if (sr)
+            MIDAS_TRY(csr_from_dense(c, sp, Zlu, sp, S_CSR, &zcsr));
+        else
+            MIDAS_CUDA(c, cudaMemcpyAsync(Zsr, Zlu, sizeof(float2) * (size_t)sp * sp, cudaMemcpyDeviceToDevice,
+                                          c->stream));
         MIDAS_CUDA(c, cudaMemsetAsync(Bm, 0, sizeof(float2) * (size_t)sp * m, c->stream));
         MIDAS_TRY(launch_incident4<float2>(c, s, idx, ncbf, d_cth, d_cph, Bm, 1, (size_t)sp));
         DenseLU lu;
@@ -274,10 +285,13 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
         MIDAS_TRY(lu_solve(c, lu, d32, m));
         long long tot = (long long)sp * m;
         ++c->launches;
-        k_ir_update<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(tot, X64, d32, Xh, Xl, 1);
+        k_ir_update<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(tot, sp, m, X64, d32, Xh, Xl, 1, sr);
         int it;
         for (it = 0; it < 12; ++it) {
-            MIDAS_TRY(residual_df32(c, sp, m, Zsr, sp, Xh, Xl, Bm, R64));
+            if (sr)
+                MIDAS_TRY(residual_csr_df32(c, zcsr, m, Xh, Xl, Bm, R64));
+            else
+                MIDAS_TRY(residual_df32(c, sp, m, Zsr, sp, Xh, Xl, Bm, R64));
             MIDAS_CUDA(c, cudaMemsetAsync(red, 0, sizeof(unsigned long long) * 2 * m, c->stream));
             ++c->launches;
             k_r_to32<<<dim3(32, m), 256, 0, c->stream>>>(sp, m, R64, d32, X64, red);
@@ -296,7 +310,7 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
             if (worst <= cbf_tol) break;
             MIDAS_TRY(lu_solve(c, lu, d32, m));
             ++c->launches;
-            k_ir_update<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(tot, X64, d32, Xh, Xl, 0);
+            k_ir_update<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(tot, sp, m, X64, d32, Xh, Xl, 0, sr);
         }
         if (it == 12) return c->err.set(MIDAS_ERR_NOT_CONVERGED, "cbf block solve: refinement did not converge");
         ir_max = std::max(ir_max, it);

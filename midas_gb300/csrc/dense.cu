@@ -60,11 +60,19 @@ __global__ void __launch_bounds__(512) k_diag_lu(float2 *A11, long long lda, flo
         }
         __syncthreads();
     }
-    // L^-1 (unit lower): row i of X: X[i][c] = -sum_{m=c}^{i-1} L[i][m] X[m][c], X[c][c] = 1
-    for (int t = tid; t < NB * NB; t += nt) li[t] = make_float2((t / NB == t % NB) ? 1.f : 0.f, 0.f);
+    // Triangular inverses, one column per thread (no barriers inside): threads
+    // 0..NB-1 build column c of L^-1 (unit lower) top-down,
+    //   X[c][c] = 1,  X[i][c] = -sum_{m=c}^{i-1} L[i][m] X[m][c];
+    // threads NB..2NB-1 build column c of U^-1 bottom-up,
+    //   X[c][c] = 1/U[c][c],  X[i][c] = -(sum_{m=i+1}^{c} U[i][m] X[m][c]) / U[i][i].
+    // L[i][m] / U[i][m] is the same word for the whole warp (broadcast); X[m][c]
+    // is consecutive across the warp.
+    for (int t = tid; t < NB * NB; t += nt) { li[t] = make_float2(0.f, 0.f); ui[t] = make_float2(0.f, 0.f); }
     __syncthreads();
-    for (int i = 1; i < NB; ++i) {
-        for (int cc = tid; cc < i; cc += nt) {
+    if (tid < NB) {
+        const int cc = tid;
+        li[cc * NB + cc] = make_float2(1.f, 0.f);
+        for (int i = cc + 1; i < NB; ++i) {
             float2 s = make_float2(0.f, 0.f);
             for (int m = cc; m < i; ++m) {
                 float2 l = a[i * NB + m], x = li[m * NB + cc];
@@ -73,26 +81,22 @@ __global__ void __launch_bounds__(512) k_diag_lu(float2 *A11, long long lda, flo
             }
             li[i * NB + cc] = make_float2(-s.x, -s.y);
         }
-        __syncthreads();
-    }
-    // U^-1 (upper): row i from the bottom: X[i][c] = (delta_ic - sum_{m=i+1}^{c} U[i][m] X[m][c]) / U[i][i]
-    for (int t = tid; t < NB * NB; t += nt) ui[t] = make_float2(0.f, 0.f);
-    __syncthreads();
-    for (int i = NB - 1; i >= 0; --i) {
-        float2 d = a[i * NB + i];
-        float dm = d.x * d.x + d.y * d.y;
-        float2 id = make_float2(d.x / dm, -d.y / dm);
-        for (int cc = i + tid; cc < NB; cc += nt) {
-            float2 s = make_float2(cc == i ? 1.f : 0.f, 0.f);
+    } else if (tid < 2 * NB) {
+        const int cc = tid - NB;
+        for (int i = cc; i >= 0; --i) {
+            float2 s = make_float2(i == cc ? 1.f : 0.f, 0.f);
             for (int m = i + 1; m <= cc; ++m) {
                 float2 u = a[i * NB + m], x = ui[m * NB + cc];
                 s.x -= u.x * x.x - u.y * x.y;
                 s.y -= u.x * x.y + u.y * x.x;
             }
+            float2 d = a[i * NB + i];
+            float dm = d.x * d.x + d.y * d.y;
+            float2 id = make_float2(d.x / dm, -d.y / dm);
             ui[i * NB + cc] = make_float2(s.x * id.x - s.y * id.y, s.x * id.y + s.y * id.x);
         }
-        __syncthreads();
     }
+    __syncthreads();
     for (int i = tid; i < NB * NB; i += nt) {
         A11[(long long)(i / NB) * lda + (i % NB)] = a[i];
         Linv[i] = li[i];
@@ -169,87 +173,134 @@ int lu_factor_nopiv(midas_gpu_ctx *c, DenseLU &lu)
 }
 
 // ---------------------------------------------------------------------------
-// blocked triangular solves on X (n x nrhs column-major complex64, ld = n)
+// blocked triangular solves on the tensor cores.  The right-hand sides are
+// solved in row-major form Rt (n x nrhs), so every update is one tcgen05 GEMM
+// whose A operand is the L or U panel read in place (row-major, no copy):
+//   Rt[rows below] -= L[rows below, block] * Y[block]      (forward)
+//   Rt[rows above] -= U[rows above, block] * X[block]      (backward)
+// Two levels: inside a super-block of SOLVE_SB rows the 64-row diagonal
+// blocks are applied one after the other (their inverses come from the
+// factorisation) and update only the rows of the super-block; one GEMM with
+// K = SOLVE_SB then updates every row outside it.  The right-hand-side
+// traffic per super-block is then O(n nrhs) instead of O(n nrhs) per 64 rows.
 // ---------------------------------------------------------------------------
-// X[rows r0..r0+nb) = Minv (nb x nb row-major) * X[rows]  (nb <= 64, one CTA per rhs)
-__global__ void k_apply_inv(const float2 *Minv, int nb, float2 *X, long long ldx, int r0)
+constexpr int SOLVE_SB = 512;
+
+size_t lu_solve_scratch_bytes(int n, int nrhs)
 {
-    __shared__ float2 t[64];
-    float2 *x = X + (long long)blockIdx.x * ldx + r0;
-    int i = threadIdx.x;
-    if (i < nb) t[i] = x[i];
-    __syncthreads();
-    if (i < nb) {
-        float2 s = make_float2(0.f, 0.f);
-        for (int m = 0; m < nb; ++m) {
-            float2 a = Minv[i * nb + m], v = t[m];
-            s.x += a.x * v.x - a.y * v.y;
-            s.y += a.x * v.y + a.y * v.x;
-        }
-        x[i] = s;
-    }
+    return sizeof(float2) * (size_t)n * nrhs + sizeof(float) * 4 * (size_t)nrhs * SOLVE_SB + 512;
 }
 
-// X[rows ra..ra+na) -= A[rows ra.., cols cb..cb+nb) * X[rows cb..cb+nb)  (warp per row)
-__global__ void k_gemv_update(const float2 *A, long long lda, int ra, int na, int cb, int nb, float2 *X,
-                              long long ldx, int nrhs)
+// Y = Minv * Rt[r0 .. r0+64) (in place, one CTA per right-hand side j), and the
+// expanded copy of Y for the next GEMM's B operand: rows 2j, 2j+1 of Bt hold
+// (Yr, -Yi) and (Yi, Yr) interleaved along the 64 rows, from column col0.
+__global__ void k_apply_inv_rm(const float2 *Minv, float2 *Rt, int nrhs, int r0, float *Bt, long long ldb, int col0)
 {
-    int w = (blockIdx.x * blockDim.x + threadIdx.x) / 32, lane = threadIdx.x % 32;
-    if (w >= na) return;
-    const float2 *row = A + (long long)(ra + w) * lda + cb;
-    for (int r = 0; r < nrhs; ++r) {
-        const float2 *xv = X + (long long)r * ldx + cb;
-        float sx = 0.f, sy = 0.f;
-        for (int m = lane; m < nb; m += 32) {
-            float2 a = row[m], v = xv[m];
-            sx += a.x * v.x - a.y * v.y;
-            sy += a.x * v.y + a.y * v.x;
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            sx += __shfl_down_sync(0xffffffffu, sx, o);
-            sy += __shfl_down_sync(0xffffffffu, sy, o);
-        }
-        if (lane == 0) {
-            float2 *d = X + (long long)r * ldx + ra + w;
-            d->x -= sx;
-            d->y -= sy;
-        }
+    __shared__ float2 t[64];
+    const int j = blockIdx.x, i = threadIdx.x;
+    float2 *x = Rt + (long long)r0 * nrhs + j;
+    t[i] = x[(long long)i * nrhs];
+    __syncthreads();
+    float2 s = make_float2(0.f, 0.f);
+    for (int m = 0; m < 64; ++m) {
+        float2 a = Minv[i * 64 + m], v = t[m];
+        s.x += a.x * v.x - a.y * v.y;
+        s.y += a.x * v.y + a.y * v.x;
     }
+    x[(long long)i * nrhs] = s;
+    float *b0 = Bt + (long long)(2 * j) * ldb + col0 + 2 * i, *b1 = b0 + ldb;
+    b0[0] = s.x; b0[1] = -s.y;
+    b1[0] = s.y; b1[1] = s.x;
+}
+
+// column-major R (n x nrhs, ld n) -> row-major Rt (n x nrhs), 32 x 32 tiles
+__global__ void k_cm_to_rm(const float2 *R, int n, int nrhs, float2 *Rt)
+{
+    __shared__ float2 tile[32][33];
+    const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 32, tx = threadIdx.x;
+    for (int k = threadIdx.y; k < 32; k += blockDim.y)
+        if (r0 + tx < n && c0 + k < nrhs) tile[k][tx] = R[(long long)(c0 + k) * n + r0 + tx];
+    __syncthreads();
+    for (int k = threadIdx.y; k < 32; k += blockDim.y)
+        if (r0 + k < n && c0 + tx < nrhs) Rt[(long long)(r0 + k) * nrhs + c0 + tx] = tile[tx][k];
+}
+
+// row-major Rt -> column-major R
+__global__ void k_rm_to_cm(const float2 *Rt, int n, int nrhs, float2 *R)
+{
+    __shared__ float2 tile[32][33];
+    const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 32, tx = threadIdx.x;
+    for (int k = threadIdx.y; k < 32; k += blockDim.y)
+        if (r0 + k < n && c0 + tx < nrhs) tile[k][tx] = Rt[(long long)(r0 + k) * nrhs + c0 + tx];
+    __syncthreads();
+    for (int k = threadIdx.y; k < 32; k += blockDim.y)
+        if (r0 + tx < n && c0 + k < nrhs) R[(long long)(c0 + k) * n + r0 + tx] = tile[tx][k];
+}
+
+static int apply_inv(midas_gpu_ctx *c, const float2 *Minv, float2 *Rt, int nrhs, int r0, float *Bt, long long ldb,
+                     int col0)
+{
+    ++c->launches;
+    int kp = kp_begin(c);
+    k_apply_inv_rm<<<nrhs, 64, 0, c->stream>>>(Minv, Rt, nrhs, r0, Bt, ldb, col0);
+    kp_end(c, kp, MIDAS_KC_TRSV, 8.0 * 64 * 64 * nrhs, 8.0 * 64 * 64 + 32.0 * 64 * nrhs);
+    MIDAS_CUDA(c, cudaGetLastError());
+    return MIDAS_OK;
 }
 
 int lu_solve(midas_gpu_ctx *c, const DenseLU &lu, float2 *R, int nrhs)
 {
     const int n = lu.n, nb = lu.nb;
-    // forward: L y = b  (right-looking: solve block k, then update the rows below)
-    for (int k = 0; k < lu.nblk; ++k) {
-        int r0 = k * nb;
-        ++c->launches;
-        int kp = kp_begin(c);
-        k_apply_inv<<<nrhs, 64, 0, c->stream>>>(lu.Linv + (size_t)k * nb * nb, nb, R, n, r0);
-        kp_end(c, kp, MIDAS_KC_TRSV, 8.0 * nb * nb * nrhs, 8.0 * nb * nb + 16.0 * nb * nrhs);
-        int na = n - r0 - nb;
-        if (na > 0) {
-            ++c->launches;
-            kp = kp_begin(c);
-            k_gemv_update<<<(na * 32 + 255) / 256, 256, 0, c->stream>>>(lu.A, lu.lda, r0 + nb, na, r0, nb, R, n,
-                                                                          nrhs);
-            kp_end(c, kp, MIDAS_KC_TRSV, 8.0 * na * nb * nrhs, 8.0 * na * nb + 16.0 * na * nrhs + 8.0 * nb * nrhs);
+    if (nb != 64) return c->err.set(MIDAS_ERR_ARG, "lu_solve: block size must be 64");
+    void *p;
+    MIDAS_TRY(ensure(c, S_SOLVE, lu_solve_scratch_bytes(n, nrhs), &p));
+    float2 *Rt = (float2 *)p;
+    float *Bt = (float *)((char *)p + (((sizeof(float2) * (size_t)n * nrhs) + 255) & ~(size_t)255));
+    float *Rtf = (float *)Rt;
+    const float *Af = (const float *)lu.A;
+    const long long lda = lu.lda;
+    dim3 tb(32, 8), tg((n + 31) / 32, (nrhs + 31) / 32);
+    ++c->launches;
+    k_cm_to_rm<<<tg, tb, 0, c->stream>>>(R, n, nrhs, Rt);
+    MIDAS_CUDA(c, cudaGetLastError());
+    const int nsb = (n + SOLVE_SB - 1) / SOLVE_SB;
+    // forward: L Y = B
+    for (int S = 0; S < nsb; ++S) {
+        const int K0 = S * SOLVE_SB, K1 = std::min(n, K0 + SOLVE_SB), ldb = 2 * (K1 - K0);
+        for (int r0 = K0; r0 < K1; r0 += nb) {
+            MIDAS_TRY(apply_inv(c, lu.Linv + (size_t)(r0 / nb) * nb * nb, Rt, nrhs, r0, Bt, ldb, 2 * (r0 - K0)));
+            const int rows = K1 - (r0 + nb);
+            if (rows > 0) {
+                GemmArgs g{rows, 2 * nrhs, 2 * nb, Af + 2 * ((r0 + nb) * lda + r0), 2 * lda, Bt + 2 * (r0 - K0), ldb,
+                           Rtf + 2LL * (r0 + nb) * nrhs, 2LL * nrhs, -1.f, 1.f};
+                MIDAS_TRY(gemm_tf32(c, g));
+            }
+        }
+        if (K1 < n) {
+            GemmArgs g{n - K1, 2 * nrhs, ldb, Af + 2 * (K1 * lda + K0), 2 * lda, Bt, ldb, Rtf + 2LL * K1 * nrhs,
+                       2LL * nrhs, -1.f, 1.f};
+            MIDAS_TRY(gemm_tf32(c, g));
         }
     }
-    // backward: U x = y
-    for (int k = lu.nblk - 1; k >= 0; --k) {
-        int r0 = k * nb;
-        ++c->launches;
-        int kp = kp_begin(c);
-        k_apply_inv<<<nrhs, 64, 0, c->stream>>>(lu.Uinv + (size_t)k * nb * nb, nb, R, n, r0);
-        kp_end(c, kp, MIDAS_KC_TRSV, 8.0 * nb * nb * nrhs, 8.0 * nb * nb + 16.0 * nb * nrhs);
-        if (r0 > 0) {
-            ++c->launches;
-            kp = kp_begin(c);
-            k_gemv_update<<<(r0 * 32 + 255) / 256, 256, 0, c->stream>>>(lu.A, lu.lda, 0, r0, r0, nb, R, n, nrhs);
-            kp_end(c, kp, MIDAS_KC_TRSV, 8.0 * r0 * nb * nrhs, 8.0 * r0 * nb + 16.0 * r0 * nrhs + 8.0 * nb * nrhs);
+    // backward: U X = Y
+    for (int S = nsb - 1; S >= 0; --S) {
+        const int K0 = S * SOLVE_SB, K1 = std::min(n, K0 + SOLVE_SB), ldb = 2 * (K1 - K0);
+        for (int r0 = K1 - nb; r0 >= K0; r0 -= nb) {
+            MIDAS_TRY(apply_inv(c, lu.Uinv + (size_t)(r0 / nb) * nb * nb, Rt, nrhs, r0, Bt, ldb, 2 * (r0 - K0)));
+            const int rows = r0 - K0;
+            if (rows > 0) {
+                GemmArgs g{rows, 2 * nrhs, 2 * nb, Af + 2 * (K0 * lda + r0), 2 * lda, Bt + 2 * (r0 - K0), ldb,
+                           Rtf + 2LL * K0 * nrhs, 2LL * nrhs, -1.f, 1.f};
+                MIDAS_TRY(gemm_tf32(c, g));
+            }
+        }
+        if (K0 > 0) {
+            GemmArgs g{K0, 2 * nrhs, ldb, Af + 2 * K0, 2 * lda, Bt, ldb, Rtf, 2LL * nrhs, -1.f, 1.f};
+            MIDAS_TRY(gemm_tf32(c, g));
         }
     }
+    ++c->launches;
+    k_rm_to_cm<<<tg, tb, 0, c->stream>>>(Rt, n, nrhs, R);
     MIDAS_CUDA(c, cudaGetLastError());
     return MIDAS_OK;
 }

@@ -73,12 +73,14 @@ __global__ void __launch_bounds__(256) k_gemm_simt(GemmArgs g)
 constexpr int TC_BM = 128;
 constexpr int TC_BN = 128;
 constexpr int TC_BK = 32;          // 32 fp32 = 128 B = one 128B-swizzle row
-constexpr int TC_STAGES = 4;
 constexpr int TC_THREADS = 192;    // warp0 TMA, warp1 MMA/TMEM, warps2-5 epilogue
 constexpr int TC_A_BYTES = TC_BM * TC_BK * 4;
 constexpr int TC_B_BYTES = TC_BN * TC_BK * 4;
 constexpr int TC_STAGE_BYTES = TC_A_BYTES + TC_B_BYTES;
-constexpr int TC_SMEM = TC_STAGES * TC_STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+// 4 stages for long K; 2 stages (and two CTAs per SM, so one CTA's epilogue
+// overlaps the other's loads) for the K <= 256 updates of the LU and the solves
+__host__ __device__ constexpr int tc_smem(int stages) { return stages * TC_STAGE_BYTES + 1024 /*align*/ + 256; }
+constexpr int TC_EPI_PITCH = 36;   // floats per staged row (32 + 4: conflict-free float4 access)
 constexpr uint32_t TC_SPIN_LIMIT = 1u << 26;   // bounded waits (~seconds with backoff)
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p)
@@ -190,8 +192,8 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float v[32])
 // products with cancellation (the CBF reduced matrix) to FP32-FMA accuracy.
 constexpr int TC_PROMOTE_KB = 2;
 
-template <bool PROMOTE>
-__global__ void __launch_bounds__(TC_THREADS, 1)
+template <bool PROMOTE, int TC_STAGES>
+__global__ void __launch_bounds__(TC_THREADS, TC_STAGES == 2 ? 2 : 1)
     k_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int M, int N, int K,
               float *D, long long ldd, float alpha, float beta, int *gflag)
 {
@@ -310,30 +312,45 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             bool ok = mbar_wait(&accf[0], 0, abort_flag, gflag);
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             if (ok) {
+                // Every MMA has completed, so the stage buffers are free: each warp
+                // stages its 32 rows x 32 columns in shared memory (one row per lane,
+                // as tcgen05.ld delivers them) and writes them back row-contiguous:
+                // a float4 store instruction covers 4 rows x 128 B of D.
+                float *stg = (float *)smem + lg * 32 * TC_EPI_PITCH;
+                const int rr = lane >> 3, cq = (lane & 7) * 4;
+                const bool vec = ((((uintptr_t)D) | ((uintptr_t)ldd * 4)) & 15) == 0;
                 for (int c = 0; c < TC_BN / 32; ++c) {
                     float v[32];
                     tmem_ld32(tmem + lane_base + (uint32_t)(c * 32), v);
-                    if (row < M) {
-                        float *d = D + (long long)row * ldd + n0 + c * 32;
-                        int ncol = N - (n0 + c * 32);
-                        if (ncol >= 32 && (((uintptr_t)d) & 15) == 0) {
 #pragma unroll
-                            for (int j = 0; j < 32; j += 4) {
-                                float4 o;
-                                if (beta != 0.f) {
-                                    float4 p = *(float4 *)(d + j);
-                                    o = make_float4(alpha * v[j] + beta * p.x, alpha * v[j + 1] + beta * p.y,
-                                                    alpha * v[j + 2] + beta * p.z, alpha * v[j + 3] + beta * p.w);
-                                } else {
-                                    o = make_float4(alpha * v[j], alpha * v[j + 1], alpha * v[j + 2], alpha * v[j + 3]);
-                                }
-                                *(float4 *)(d + j) = o;
+                    for (int j = 0; j < 32; j += 4)
+                        *(float4 *)(stg + lane * TC_EPI_PITCH + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+                    __syncwarp();
+                    const int col = n0 + c * 32 + cq;
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        const int r = i * 4 + rr, grow = m0 + lg * 32 + r;
+                        if (grow >= M) continue;
+                        float4 a = *(const float4 *)(stg + r * TC_EPI_PITCH + cq);
+                        float *d = D + (long long)grow * ldd + col;
+                        if (vec && col + 3 < N) {
+                            float4 o;
+                            if (beta != 0.f) {
+                                float4 p = *(const float4 *)d;
+                                o = make_float4(alpha * a.x + beta * p.x, alpha * a.y + beta * p.y,
+                                                alpha * a.z + beta * p.z, alpha * a.w + beta * p.w);
+                            } else {
+                                o = make_float4(alpha * a.x, alpha * a.y, alpha * a.z, alpha * a.w);
                             }
+                            *(float4 *)d = o;
                         } else {
-                            for (int j = 0; j < 32 && j < ncol; ++j)
-                                d[j] = alpha * v[j] + (beta != 0.f ? beta * d[j] : 0.f);
+                            const float av[4] = {a.x, a.y, a.z, a.w};
+#pragma unroll
+                            for (int e = 0; e < 4; ++e)
+                                if (col + e < N) d[e] = alpha * av[e] + (beta != 0.f ? beta * d[e] : 0.f);
                         }
                     }
+                    __syncwarp();
                 }
             }
         }
@@ -415,8 +432,12 @@ static int gemm_tc(midas_gpu_ctx *c, const GemmArgs &g, bool precise)
         return c->err.set(MIDAS_ERR_ARG, "gemm_tf32: operands must be 16-byte aligned with ld % 4 == 0");
     static bool attr = false;
     if (!attr) {
-        MIDAS_CUDA(c, cudaFuncSetAttribute(k_gemm_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
-        MIDAS_CUDA(c, cudaFuncSetAttribute(k_gemm_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
+        MIDAS_CUDA(c, cudaFuncSetAttribute(k_gemm_tc<false, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          tc_smem(4)));
+        MIDAS_CUDA(c, cudaFuncSetAttribute(k_gemm_tc<false, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          tc_smem(2)));
+        MIDAS_CUDA(c, cudaFuncSetAttribute(k_gemm_tc<true, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          tc_smem(4)));
         attr = true;
     }
     CUtensorMap ma, mb;
@@ -426,11 +447,14 @@ static int gemm_tc(midas_gpu_ctx *c, const GemmArgs &g, bool precise)
     ++c->launches;
     int kp = kp_begin(c);
     if (precise)
-        k_gemm_tc<true><<<grd, TC_THREADS, TC_SMEM, c->stream>>>(ma, mb, g.M, g.N, g.K, g.D, g.ldd, g.alpha, g.beta,
-                                                                 c->d_flag);
+        k_gemm_tc<true, 4><<<grd, TC_THREADS, tc_smem(4), c->stream>>>(ma, mb, g.M, g.N, g.K, g.D, g.ldd, g.alpha,
+                                                                       g.beta, c->d_flag);
+    else if (g.K <= 256)
+        k_gemm_tc<false, 2><<<grd, TC_THREADS, tc_smem(2), c->stream>>>(ma, mb, g.M, g.N, g.K, g.D, g.ldd, g.alpha,
+                                                                        g.beta, c->d_flag);
     else
-        k_gemm_tc<false><<<grd, TC_THREADS, TC_SMEM, c->stream>>>(ma, mb, g.M, g.N, g.K, g.D, g.ldd, g.alpha, g.beta,
-                                                                  c->d_flag);
+        k_gemm_tc<false, 4><<<grd, TC_THREADS, tc_smem(4), c->stream>>>(ma, mb, g.M, g.N, g.K, g.D, g.ldd, g.alpha,
+                                                                        g.beta, c->d_flag);
     kp_end(c, kp, MIDAS_KC_GEMM_TC, 2.0 * g.M * g.N * g.K, gemm_bytes(g));
     MIDAS_CUDA(c, cudaGetLastError());
     return MIDAS_OK;

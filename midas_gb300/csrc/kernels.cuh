@@ -34,6 +34,16 @@ int aca_uw(midas_gpu_ctx *c, int nrows, int k, int ncol, const double2 *U, const
 int aca_run(midas_gpu_ctx *c, int row0, int nrows, int col0, int ncols, double eps, int itmax, double2 *U,
             double2 *V, int *rank);
 
+// sparse.cu: CSR matrix (0-based, columns ascending within a row)
+struct Csr {
+    int n = 0, nnz = 0;
+    int *rowptr = nullptr, *col = nullptr;
+    float2 *val = nullptr;
+};
+int csr_from_dense(midas_gpu_ctx *c, int n, const float2 *Z, long long ldz, int slot, Csr *out);
+int residual_csr_df32(midas_gpu_ctx *c, const Csr &Z, int m, const float2 *Xh_rm, const float2 *Xl_rm,
+                      const float2 *B, double2 *R);
+
 // fill.cu
 int launch_set_cells(midas_gpu_ctx *c);
 int launch_lat_table(midas_gpu_ctx *c);
@@ -82,6 +92,7 @@ struct DenseLU {
 int lu_factor_nopiv(midas_gpu_ctx *c, DenseLU &lu);
 // solve LU X = R in place; R is n x nrhs column-major complex64 (ld = n)
 int lu_solve(midas_gpu_ctx *c, const DenseLU &lu, float2 *R, int nrhs);
+size_t lu_solve_scratch_bytes(int n, int nrhs);   // device scratch lu_solve takes from slot S_SOLVE
 // mixed-precision solve of Z x = b: Z64 row-major FP64 (for residuals), lu factored;
 // b/x are n x nrhs column-major FP64.
 int ir_solve(midas_gpu_ctx *c, const DenseLU &lu, const double2 *Z64, long long ldz, const double2 *b, double2 *x,
