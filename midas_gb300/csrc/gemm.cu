@@ -362,6 +362,215 @@ __global__ void __launch_bounds__(TC_THREADS, TC_STAGES == 2 ? 2 : 1)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(NCOL));
 }
 
+
+// ---------------------------------------------------------------------------
+// Persistent tcgen05 GEMM for D = alpha A Bt^T + beta D (fp32 D, TMA-able):
+// one CTA per SM walks the output tiles in groups of TCP_GROUP_M row tiles
+// (so the CTAs running together share A and B tiles in L2).  Roles:
+//   warp 0  TMA: the D tile of each output tile (4 boxes of 32 columns, 128B
+//           swizzle) into one of DBUF buffers, then the A/B k-blocks;
+//   warp 1  MMA: accumulates tile i into TMEM buffer i & 1 (2 x 128 columns),
+//           so tile i+1 is computed while tile i is drained;
+//   warps 2-5 epilogue: TMEM -> registers, alpha acc + beta D in the swizzled
+//           D buffer (conflict-free), then one thread TMA-stores the buffer.
+// Every wait is bounded; on expiry the CTA raises DEV_TIMEOUT and unwinds.
+// ---------------------------------------------------------------------------
+constexpr int TCP_GROUP_M = 16;
+constexpr int TCP_D_BYTES = TC_BM * TC_BN * 4;   // one D tile (4 boxes of 16 KB)
+__host__ __device__ constexpr int tcp_smem(int stages, int dbuf)
+{
+    return stages * TC_STAGE_BYTES + dbuf * TCP_D_BYTES + 1024 /*align*/ + 512 /*barriers*/;
+}
+
+__device__ __forceinline__ void tcp_tile(int t, int mt, int nt, int &m0, int &n0)
+{
+    const int per = TCP_GROUP_M * nt;
+    const int first = (t / per) * TCP_GROUP_M;
+    const int gsz = min(mt - first, TCP_GROUP_M);
+    const int r = t % per;
+    m0 = (first + r % gsz) * TC_BM;
+    n0 = (r / gsz) * TC_BN;
+}
+
+// named barrier 1 over the 128 epilogue threads that also ANDs a flag, so every
+// thread takes the same branch after a bounded wait
+__device__ __forceinline__ bool epi_bar_and(bool ok)
+{
+    uint32_t r;
+    asm volatile(
+        "{\n.reg .pred p, q;\nsetp.ne.u32 q, %1, 0;\nbar.red.and.pred p, 1, 128, q;\nselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(r)
+        : "r"((uint32_t)ok)
+        : "memory");
+    return r != 0;
+}
+
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, const void *src, int x, int y)
+{
+    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"((uint64_t)map),
+                 "r"(x), "r"(y), "r"(smem_u32(src))
+                 : "memory");
+}
+
+template <int STAGES, int DBUF>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_gemm_tcp(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+               const __grid_constant__ CUtensorMap tmD, int M, int N, int K, float alpha, float beta, int *gflag)
+{
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t *dsm = smem + STAGES * TC_STAGE_BYTES;                 // DBUF x 64 KB, 1024-aligned
+    uint64_t *full = (uint64_t *)(dsm + DBUF * TCP_D_BYTES);
+    uint64_t *empty = full + STAGES;
+    uint64_t *tfull = empty + STAGES;     // [2] accumulator ready
+    uint64_t *tempty = tfull + 2;         // [2] accumulator drained (128 arrivals)
+    uint64_t *dfull = tempty + 2;         // [DBUF] D tile loaded
+    uint64_t *dempty = dfull + DBUF;      // [DBUF] D buffer stored back (1 arrival)
+    volatile uint32_t *tmem_slot = (volatile uint32_t *)(dempty + DBUF);
+    volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
+
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const int mt = (M + TC_BM - 1) / TC_BM, nt = (N + TC_BN - 1) / TC_BN, ntiles = mt * nt;
+    const int nk = (K + TC_BK - 1) / TC_BK;
+    const bool use_d = beta != 0.f;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
+        for (int b = 0; b < 2; ++b) { mbar_init(&tfull[b], 1); mbar_init(&tempty[b], 128); }
+        for (int b = 0; b < DBUF; ++b) { mbar_init(&dfull[b], 1); mbar_init(&dempty[b], 1); }
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmA) : "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmB) : "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmD) : "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32((const void *)tmem_slot)),
+                     "r"(2 * TC_BN));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            long long kg = 0;
+            int li = 0;
+            bool ok = true;
+            // D of tile li goes into buffer li % DBUF once the store of tile li - DBUF has
+            // read it: with two buffers it is requested before the tile's k-blocks,
+            // with one buffer after them (so the wait overlaps this tile's MMAs)
+            auto load_d = [&](int li_, int m0_, int n0_) -> bool {
+                const int db = li_ % DBUF;
+                if (li_ >= DBUF && !mbar_wait(&dempty[db], ((li_ / DBUF) - 1) & 1, abort_flag, gflag)) return false;
+                uint8_t *dst = dsm + db * TCP_D_BYTES;
+                mbar_arrive_tx(&dfull[db], TCP_D_BYTES);
+#pragma unroll
+                for (int cch = 0; cch < TC_BN / 32; ++cch)
+                    tma_load_2d(dst + cch * (TCP_D_BYTES / 4), &tmD, &dfull[db], n0_ + cch * 32, m0_);
+                return true;
+            };
+            for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++li) {
+                int m0, n0;
+                tcp_tile(t, mt, nt, m0, n0);
+                if (use_d && DBUF > 1 && !load_d(li, m0, n0)) break;
+                for (int kb = 0; kb < nk; ++kb, ++kg) {
+                    const int s = (int)(kg % STAGES);
+                    if (!mbar_wait(&empty[s], (int)((kg / STAGES) + 1) & 1, abort_flag, gflag)) { ok = false; break; }
+                    uint8_t *sa = smem + s * TC_STAGE_BYTES;
+                    mbar_arrive_tx(&full[s], TC_STAGE_BYTES);
+                    tma_load_2d(sa, &tmA, &full[s], kb * TC_BK, m0);
+                    tma_load_2d(sa + TC_A_BYTES, &tmB, &full[s], kb * TC_BK, n0);
+                }
+                if (ok && use_d && DBUF == 1 && !load_d(li, m0, n0)) break;
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            const uint32_t idesc = idesc_tf32(TC_BM, TC_BN);
+            long long kg = 0;
+            int li = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++li) {
+                const int buf = li & 1;
+                if (li >= 2 && !mbar_wait(&tempty[buf], ((li >> 1) - 1) & 1, abort_flag, gflag)) break;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t dst = tmem + (uint32_t)(buf * TC_BN);
+                for (int kb = 0; kb < nk; ++kb, ++kg) {
+                    const int s = (int)(kg % STAGES);
+                    if (!mbar_wait(&full[s], (int)(kg / STAGES) & 1, abort_flag, gflag)) { ok = false; break; }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t sa = smem_u32(smem + s * TC_STAGE_BYTES), sb = sa + TC_A_BYTES;
+#pragma unroll
+                    for (int k4 = 0; k4 < TC_BK / 8; ++k4)
+                        mma_tf32(dst, smem_desc_sw128(sa + k4 * 32), smem_desc_sw128(sb + k4 * 32), idesc,
+                                 (kb > 0 || k4 > 0) ? 1u : 0u);
+                    mma_commit(&empty[s]);
+                }
+                if (ok) mma_commit(&tfull[buf]);
+            }
+        }
+    } else {
+        const int lg = warp % 4, et = threadIdx.x - 64;   // epilogue thread 0..127
+        const int r = lg * 32 + lane;                     // tile row of this thread
+        const uint32_t lane_base = (uint32_t)(lg * 32) << 16;
+        int li = 0;
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++li) {
+            int m0, n0;
+            tcp_tile(t, mt, nt, m0, n0);
+            const int buf = li & 1, db = li % DBUF;
+            bool ok = mbar_wait(&tfull[buf], (li >> 1) & 1, abort_flag, gflag);
+            if (ok && use_d) ok = mbar_wait(&dfull[db], (li / DBUF) & 1, abort_flag, gflag);
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            if (!epi_bar_and(ok)) break;
+            uint8_t *dbase = dsm + db * TCP_D_BYTES;
+#pragma unroll 1
+            for (int cch = 0; cch < TC_BN / 32; ++cch) {
+                float v[32];
+                tmem_ld32(tmem + lane_base + (uint32_t)(buf * TC_BN + cch * 32), v);
+                uint8_t *rowp = dbase + cch * (TCP_D_BYTES / 4) + r * 128;
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    float4 *p = (float4 *)(rowp + ((u ^ (r & 7)) << 4));
+                    float4 o;
+                    if (use_d) {
+                        float4 d = *p;
+                        o = make_float4(alpha * v[4 * u] + beta * d.x, alpha * v[4 * u + 1] + beta * d.y,
+                                        alpha * v[4 * u + 2] + beta * d.z, alpha * v[4 * u + 3] + beta * d.w);
+                    } else {
+                        o = make_float4(alpha * v[4 * u], alpha * v[4 * u + 1], alpha * v[4 * u + 2],
+                                        alpha * v[4 * u + 3]);
+                    }
+                    *p = o;
+                }
+            }
+            // the accumulator buffer is free for tile li + 2
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty[buf])) : "memory");
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            asm volatile("bar.sync 1, 128;" ::: "memory");
+            if (et == 0) {
+#pragma unroll
+                for (int cch = 0; cch < TC_BN / 32; ++cch)
+                    tma_store_2d(&tmD, dbase + cch * (TCP_D_BYTES / 4), n0 + cch * 32, m0);
+                asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+                asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&dempty[db])) : "memory");
+            }
+            asm volatile("bar.sync 1, 128;" ::: "memory");
+        }
+        if (et == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (warp == 1)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TC_BN));
+}
+
 // ---------------------------------------------------------------------------
 // tensor-map creation through the driver entry point (no libcuda link needed)
 // ---------------------------------------------------------------------------
@@ -443,6 +652,34 @@ static int gemm_tc(midas_gpu_ctx *c, const GemmArgs &g, bool precise)
     CUtensorMap ma, mb;
     MIDAS_TRY(make_map(c, &ma, g.A, g.M, g.K, g.lda, TC_BM));
     MIDAS_TRY(make_map(c, &mb, g.Bt, g.N, g.K, g.ldb, TC_BN));
+    // persistent kernel whenever D can be a TMA operand
+    if (!precise && !(((uintptr_t)g.D) & 15) && !((g.ldd * 4) & 15)) {
+        static int nsm = 0;
+        static bool pattr = false;
+        if (!nsm) MIDAS_CUDA(c, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
+        if (!pattr) {
+            MIDAS_CUDA(c, cudaFuncSetAttribute(k_gemm_tcp<2, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              tcp_smem(2, 2)));
+            MIDAS_CUDA(c, cudaFuncSetAttribute(k_gemm_tcp<4, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              tcp_smem(4, 1)));
+            pattr = true;
+        }
+        CUtensorMap md;
+        MIDAS_TRY(make_map(c, &md, g.D, g.M, g.N, g.ldd, TC_BM));
+        const long long ntiles = (long long)((g.M + TC_BM - 1) / TC_BM) * ((g.N + TC_BN - 1) / TC_BN);
+        const int grid = (int)std::min<long long>(ntiles, nsm);
+        ++c->launches;
+        int kp = kp_begin(c);
+        if (g.K <= 256)
+            k_gemm_tcp<2, 2><<<grid, TC_THREADS, tcp_smem(2, 2), c->stream>>>(ma, mb, md, g.M, g.N, g.K, g.alpha,
+                                                                               g.beta, c->d_flag);
+        else
+            k_gemm_tcp<4, 1><<<grid, TC_THREADS, tcp_smem(4, 1), c->stream>>>(ma, mb, md, g.M, g.N, g.K, g.alpha,
+                                                                               g.beta, c->d_flag);
+        kp_end(c, kp, MIDAS_KC_GEMM_TC, 2.0 * g.M * g.N * g.K, gemm_bytes(g));
+        MIDAS_CUDA(c, cudaGetLastError());
+        return MIDAS_OK;
+    }
     dim3 grd((g.N + TC_BN - 1) / TC_BN, (g.M + TC_BM - 1) / TC_BM);
     ++c->launches;
     int kp = kp_begin(c);
