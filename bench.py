@@ -32,48 +32,7 @@ METRIC = "orientation-avg solves/s vs plain FP64 MoM on same GB300 at 1e-6 rel f
 PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
 
-# ---------------------------------------------------------------------------
-# workloads
-# ---------------------------------------------------------------------------
-def workload_mom_c1():
-    """Plain MoM, homogeneous sphere x = 2, m = 1.5 + 0.01i, a/d = 10 (4,224 cells,
-    12,672 unknowns), +z incidence (MIDAS angles theta = phi = 90 deg), V + H."""
-    from midas_gb300 import geometry as G
-    a, x, m = 1.0, 2.0, 1.5 + 0.01j
-    k0 = x / a
-    sc = a / 10.0
-    xyz = G.sphere_cells(2 * a, sc)
-    return {"name": "mom_c1_sphere_x2_m1.5+0.01i_4224cells", "xyz": xyz, "sc": sc,
-            "eps": np.full(len(xyz), m * m), "k0": k0, "th": np.array([90.0]), "ph": np.array([90.0]),
-            "method": "mom"}
-
-
-def workload_cbfm_c2():
-    """CBFM-E on a seeded Gaussian random sphere: x = 6, m = 1.55 + 0.005i, log-radius
-    std 0.15, correlation angle 20 deg, voxel a/21.1 (~41k cells, ~123k unknowns),
-    3x3x3 bounding-box blocks with a 15 % (of the block edge) extension, CBF
-    excitations from the reference's Niws table ('un'), 24 seeded incident
-    directions x 2 polarisations."""
-    from midas_gb300 import geometry as G
-    a, x, m = 1.0, 6.0, 1.55 + 0.005j
-    k0 = x / a
-    sc = a / 21.1
-    xyz = G.gaussian_sphere(a, 0.15, 20.0, sc, seed=2026)
-    perm, offs = G.box_partition(xyz, 3, 3, 3)
-    xyz = np.ascontiguousarray(xyz[perm])
-    box, sph = G.block_contours(xyz, offs)
-    edge = float((box[:, 1] - box[:, 0]).max(axis=1).mean())
-    ext = G.extend_blocks(xyz, offs, 0.15 * edge, sc)
-    lam = 2 * math.pi / k0
-    niws = G.init_nipws(float(sph[:, 3].max()) / (lam / abs(m)))
-    cth, cph = G.transmitters_un(niws)
-    th, ph = G.random_directions(24, seed=7)
-    return {"name": "cbfm_c2_gaussian_sphere_x6_m1.55+0.005i", "xyz": xyz, "sc": sc,
-            "eps": np.full(len(xyz), m * m), "k0": k0, "th": th, "ph": ph, "method": "cbfm",
-            "offs": offs, "ext": ext, "cth": cth, "cph": cph, "homog": 1, "niws": niws}
-
-
-WORKLOADS = {"mom_c1": workload_mom_c1, "cbfm_c2": workload_cbfm_c2}
+from midas_gb300.workloads import WORKLOADS, mom_c1 as workload_mom_c1  # noqa: E402
 
 
 # ---------------------------------------------------------------------------
@@ -297,9 +256,8 @@ def run_ours(args, wl, world, rank, local, pg):
     cbfm = wl["method"] == "cbfm"
     if cbfm:
         from midas_gb300 import _lib as LB
-        bo = np.ascontiguousarray(wl["offs"], np.int32)
-        eo = np.ascontiguousarray(np.concatenate([[0], np.cumsum([len(e) for e in wl["ext"]])]), np.int32)
-        ei = np.ascontiguousarray(np.concatenate(wl["ext"]), np.int32)
+        from midas_gb300.workloads import cbfm_args
+        bo, eo, ei = cbfm_args(wl)
         cth, cph = np.ascontiguousarray(wl["cth"]), np.ascontiguousarray(wl["cph"])
         flags = LB.CBFM_SR | (LB.CBFM_HOMOG if wl.get("homog") else 0) | (LB.CBFM_ACA if wl.get("aca") else 0)
         Kb = np.zeros(len(bo) - 1, np.int32)

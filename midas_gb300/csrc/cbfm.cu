@@ -22,9 +22,11 @@
 //   3. Vc = C^T Einc [829-849], reduced solve (mixed LU + FP64 refinement) [873-943],
 //      E = C alpha [990-1006].
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <thread>
 
 #include "common.cuh"
 #include "kernels.cuh"
@@ -53,7 +55,7 @@ __global__ void k_pad_diag32(float2 *Z, long long ld, int n0, int np)
 // X64 += d32 ; Xh = fp32(X64) ; Xl = fp32(X64 - Xh)   (n x m column-major, ld n);
 // with rm = 1, Xh and Xl are written row-major (n x m) for the CSR residual
 __global__ void k_ir_update(long long tot, int n, int m, double2 *X64, const float2 *d32, float2 *Xh, float2 *Xl,
-                            int first, int rm)
+                            float2 *Drm, int first, int rm)
 {
     long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i >= tot) return;
@@ -63,6 +65,7 @@ __global__ void k_ir_update(long long tot, int n, int m, double2 *X64, const flo
     long long o = rm ? (i % n) * m + i / n : i;
     Xh[o] = h;
     Xl[o] = make_float2((float)(x.x - h.x), (float)(x.y - h.y));
+    if (Drm) Drm[o] = d32[i];   // the correction, for the FP32 residual update
 }
 
 // d32 = fp32(r); per-column max |r| and max |x| into red (bit patterns of >= 0 doubles)
@@ -133,6 +136,247 @@ struct Buf {
     }
 };
 
+// Read-only description of the CBF generation shared by the lanes.
+struct CbfShared {
+    const int *bo, *xo;            // host: block / extended-block offsets
+    const int *d_xall;             // device: cell indices of every extended block
+    const double *d_cth, *d_cph;   // device: CBF excitation directions
+    int ncbf, m;
+    bool sr, homog;
+    double res_sr, cbf_tol;
+    double2 *Xall;                 // device: FP64 block solutions (output)
+    const size_t *xoff;
+    double2 *Gall;                 // device: Gram matrices (output)
+    size_t mm;
+    int *srefine;                  // host: refinement steps per block (output)
+};
+
+static int cbf_block(midas_gpu_ctx *c, const CbfShared &S, int b)
+{
+    const int *bo = S.bo, *xo = S.xo, m = S.m, ncbf = S.ncbf;
+    const bool sr = S.sr, homog = S.homog;
+    const double res_sr = S.res_sr, cbf_tol = S.cbf_tol;
+    const int *d_xall = S.d_xall;
+    const double *d_cth = S.d_cth, *d_cph = S.d_cph;
+    {
+        const int s = xo[b + 1] - xo[b];
+        const int N3 = 3 * s, sp = pad64(N3);
+        const int *idx = d_xall + xo[b];
+        double2 *X64 = S.Xall + S.xoff[b];
+        // work buffers of this lane (grow-only; the lane takes its blocks largest first)
+        const size_t nrm = (size_t)sp * m;
+        void *p1, *p2 = nullptr, *p3, *pred;
+        MIDAS_TRY(ensure(c, S_CBF1, sizeof(float2) * (size_t)sp * sp, &p1));
+        if (!sr) MIDAS_TRY(ensure(c, S_CBF2, sizeof(float2) * (size_t)sp * sp, &p2));
+        MIDAS_TRY(ensure(c, S_CBF3, (sizeof(float2) * 5 + sizeof(double2)) * nrm + 8 * 256, &p3));
+        MIDAS_TRY(ensure(c, S_RED2, sizeof(unsigned long long) * 2 * m + 64, &pred));
+        float2 *Zlu = (float2 *)p1, *Zsr = (float2 *)p2;
+        Buf b3{c, 0, (char *)p3};
+        float2 *Bm = b3.take<float2>(nrm), *Xh = b3.take<float2>(nrm), *Xl = b3.take<float2>(nrm),
+               *d32 = b3.take<float2>(nrm), *Drm = b3.take<float2>(nrm);
+        double2 *R64 = b3.take<double2>(nrm);
+        unsigned long long *red = (unsigned long long *)pred;
+        std::vector<unsigned long long> hred(2 * m);
+        double thr_sr = 0.0;
+        if (sr) {
+            double fsr;
+            long long nnz;
+            MIDAS_TRY(sr_ladder(c, s, idx, bo[b], homog, res_sr, &fsr, &nnz, 0, nullptr, nullptr, nullptr));
+            double2 zn;
+            MIDAS_CUDA(c, cudaMemcpyAsync(&zn, c->znnpp + bo[b], sizeof(double2), cudaMemcpyDeviceToHost, c->stream));
+            MIDAS_CUDA(c, cudaStreamSynchronize(c->stream));
+            thr_sr = hypot(1 - zn.x, -zn.y) / fsr;
+            if (c->opts.verbose >= 2) fprintf(stderr, "[midas] cbf block %d: fSR=%g nnz=%lld thr=%.17g\n", b, fsr, nnz, thr_sr);
+        }
+        // the thresholded block goes straight into the LU buffer; with SR its CSR
+        // form (about a sixth of the entries) serves the refinement residuals,
+        // without SR a dense copy does
+        MIDAS_CUDA(c, cudaMemsetAsync(Zlu, 0, sizeof(float2) * (size_t)sp * sp, c->stream));
+        MIDAS_TRY(launch_block_fill4<float2>(c, s, idx, s, idx, sr ? 1 : 0, thr_sr, homog, Zlu, (size_t)sp, 1));
+        if (sp > N3) {
+            ++c->launches;
+            k_pad_diag32<<<1, 64, 0, c->stream>>>(Zlu, sp, N3, sp);
+        }
+        Csr zcsr;
+        if (sr)
+            MIDAS_TRY(csr_from_dense(c, sp, Zlu, sp, S_CSR, &zcsr));
+        else
+            MIDAS_CUDA(c, cudaMemcpyAsync(Zsr, Zlu, sizeof(float2) * (size_t)sp * sp, cudaMemcpyDeviceToDevice,
+                                          c->stream));
+        MIDAS_CUDA(c, cudaMemsetAsync(Bm, 0, sizeof(float2) * (size_t)sp * m, c->stream));
+        MIDAS_TRY(launch_incident4<float2>(c, s, idx, ncbf, d_cth, d_cph, Bm, 1, (size_t)sp));
+        DenseLU lu;
+        lu.n = sp;
+        lu.A = Zlu;
+        lu.lda = sp;
+        MIDAS_TRY(lu_factor_nopiv(c, lu));
+        // x0 = LU^-1 B, then refinement with the double-float residual
+        MIDAS_CUDA(c, cudaMemcpyAsync(d32, Bm, sizeof(float2) * (size_t)sp * m, cudaMemcpyDeviceToDevice, c->stream));
+        MIDAS_TRY(lu_solve(c, lu, d32, m));
+        long long tot = (long long)sp * m;
+        ++c->launches;
+        k_ir_update<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(tot, sp, m, X64, d32, Xh, Xl, nullptr, 1,
+                                                                          sr);
+        // Residuals: double-float B - Z x while the corrections are large; once the
+        // relative residual is below 1e-7 the next correction d is ~1e-7 |x| or
+        // smaller, and r - Z d in FP32 (error ~1e-6 |Z||d|) is as accurate as the
+        // double-float residual of x + d.
+        int it;
+        bool upd = false;
+        for (it = 0; it < 12; ++it) {
+            if (sr && upd)
+                MIDAS_TRY(residual_csr_update_f32(c, zcsr, m, Drm, R64));
+            else if (sr)
+                MIDAS_TRY(residual_csr_df32(c, zcsr, m, Xh, Xl, Bm, R64));
+            else
+                MIDAS_TRY(residual_df32(c, sp, m, Zsr, sp, Xh, Xl, Bm, R64));
+            MIDAS_CUDA(c, cudaMemsetAsync(red, 0, sizeof(unsigned long long) * 2 * m, c->stream));
+            ++c->launches;
+            k_r_to32<<<dim3(32, m), 256, 0, c->stream>>>(sp, m, R64, d32, X64, red);
+            MIDAS_CUDA(c, cudaMemcpyAsync(hred.data(), red, sizeof(unsigned long long) * 2 * m,
+                                          cudaMemcpyDeviceToHost, c->stream));
+            MIDAS_CUDA(c, cudaStreamSynchronize(c->stream));
+            MIDAS_TRY(check_flag(c, "cbf block solve"));
+            double worst = 0;
+            for (int k = 0; k < m; ++k) {
+                double rn, xn;
+                memcpy(&rn, &hred[k], 8);
+                memcpy(&xn, &hred[m + k], 8);
+                worst = std::max(worst, xn > 0 ? rn / xn : rn);
+            }
+            if (!(worst == worst)) return c->err.set(MIDAS_ERR_NOT_CONVERGED, "cbf block solve: NaN");
+            if (worst <= cbf_tol) break;
+            upd = sr && worst <= 1e-7;
+            MIDAS_TRY(lu_solve(c, lu, d32, m));
+            ++c->launches;
+            k_ir_update<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(tot, sp, m, X64, d32, Xh, Xl,
+                                                                              upd ? Drm : nullptr, 0, sr);
+        }
+        if (it == 12) return c->err.set(MIDAS_ERR_NOT_CONVERGED, "cbf block solve: refinement did not converge");
+        // Gram G = X^H X over the 3s rows of the extended block (FP64)
+        MIDAS_TRY(zgemm64(c, m, m, N3, X64, sp, 1, 1, X64, 1, sp, S.Gall + S.mm * b, m, 1, make_double2(1, 0),
+                          make_double2(0, 0)));
+        S.srefine[b] = it;
+    }
+    return MIDAS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Lanes: the extended blocks are independent, so CBF generation runs NLANES
+// blocks at once, each lane a host thread driving its own stream and scratch
+// pool (the cells and lattice tables are shared read-only).  The latency-bound
+// parts of one block (diagonal LUs, small GEMMs, host checks of the
+// refinement) then overlap the bandwidth-bound parts of another.  The lanes
+// live as long as the context.
+// ---------------------------------------------------------------------------
+constexpr int CBF_LANES = 4;
+
+static void lane_sync_cells(midas_gpu_ctx *L, const midas_gpu_ctx *c)
+{
+    L->opts = c->opts;
+    L->device = c->device;
+    L->pi = c->pi;
+    L->n = c->n; L->k0 = c->k0;
+    L->x = c->x; L->y = c->y; L->z = c->z; L->sc = c->sc; L->an = c->an; L->kappa = c->kappa;
+    L->eps = c->eps; L->che = c->che; L->znnpp = c->znnpp; L->fk4 = c->fk4; L->fk8 = c->fk8;
+    L->lattice = c->lattice; L->lat_d = c->lat_d;
+    for (int i = 0; i < 3; ++i) {
+        L->lat_o[i] = c->lat_o[i]; L->lat_lo[i] = c->lat_lo[i]; L->lat_hi[i] = c->lat_hi[i];
+        L->lat_dim[i] = c->lat_dim[i];
+    }
+    L->lat_ijk = c->lat_ijk; L->lat_tab4 = c->lat_tab4; L->lat_tab8 = c->lat_tab8;
+    L->kprof.on = c->kprof.on;
+    L->err = Err();
+}
+
+static int get_lanes(midas_gpu_ctx *c, int nl)
+{
+    while ((int)c->lanes.size() < nl) {
+        midas_gpu_ctx *L = new midas_gpu_ctx;
+        L->device = c->device;
+        L->pool.resize(S_NSLOTS);
+        c->lanes.push_back(L);
+        MIDAS_CUDA(c, cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking));
+        MIDAS_CUDA(c, cudaMalloc(&L->d_flag, sizeof(int)));
+        MIDAS_CUDA(c, cudaMemset(L->d_flag, 0, sizeof(int)));
+    }
+    return MIDAS_OK;
+}
+
+void free_lanes(midas_gpu_ctx *c)
+{
+    for (midas_gpu_ctx *L : c->lanes) {
+        if (L->stream) cudaStreamSynchronize(L->stream);
+        for (auto &d : L->pool)
+            if (d.p) cudaFree(d.p);
+        if (L->d_flag) cudaFree(L->d_flag);
+        for (cudaEvent_t e : L->kprof.ev) cudaEventDestroy(e);
+        if (L->stream) cudaStreamDestroy(L->stream);
+        delete L;   // the cell arrays belong to the parent context
+    }
+    c->lanes.clear();
+}
+
+static int cbf_generate(midas_gpu_ctx *c, int nb, const CbfShared &S)
+{
+    // with kernel-class profiling on, one lane: each launch's event interval then
+    // covers that kernel alone
+    const int nl = c->kprof.on ? 1 : std::min(nb, CBF_LANES);
+    MIDAS_TRY(get_lanes(c, nl));
+    MIDAS_CUDA(c, cudaStreamSynchronize(c->stream));   // the shared inputs are on the device
+    // largest blocks first, each to the least-loaded lane (cost ~ s^3)
+    std::vector<int> order(nb);
+    for (int b = 0; b < nb; ++b) order[b] = b;
+    auto sz = [&](int b) { return (double)(S.xo[b + 1] - S.xo[b]); };
+    std::sort(order.begin(), order.end(), [&](int a, int b2) { return sz(a) > sz(b2); });
+    std::vector<std::vector<int>> plan(nl);
+    std::vector<double> load(nl, 0.0);
+    for (int b : order) {
+        int l = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        plan[l].push_back(b);
+        load[l] += sz(b) * sz(b) * sz(b);
+    }
+    std::vector<long long> l0(nl);
+    for (int l = 0; l < nl; ++l) {
+        lane_sync_cells(c->lanes[l], c);
+        l0[l] = c->lanes[l]->launches;
+    }
+    std::atomic<int> fail{0};
+    std::vector<int> status(nl, MIDAS_OK);
+    auto work = [&](int l) {
+        midas_gpu_ctx *L = c->lanes[l];
+        cudaSetDevice(L->device);
+        for (int b : plan[l]) {
+            if (fail.load()) break;
+            int st = cbf_block(L, S, b);
+            if (st != MIDAS_OK) { status[l] = st; fail = 1; break; }
+        }
+        if (cudaStreamSynchronize(L->stream) != cudaSuccess && status[l] == MIDAS_OK) {
+            status[l] = L->err.set(MIDAS_ERR_CUDA, "cbf lane: stream failed");
+            fail = 1;
+        }
+    };
+    std::vector<std::thread> th;
+    for (int l = 1; l < nl; ++l) th.emplace_back(work, l);
+    work(0);
+    for (auto &t : th) t.join();
+    for (int l = 0; l < nl; ++l) {
+        midas_gpu_ctx *L = c->lanes[l];
+        c->launches += L->launches - l0[l];
+        if (L->kprof.on) {
+            kp_flush(L);
+            for (int k = 0; k < MIDAS_KC_COUNT; ++k) {
+                c->kprof.ms[k] += L->kprof.ms[k]; c->kprof.flops[k] += L->kprof.flops[k];
+                c->kprof.bytes[k] += L->kprof.bytes[k]; c->kprof.n[k] += L->kprof.n[k];
+                L->kprof.ms[k] = L->kprof.flops[k] = L->kprof.bytes[k] = 0; L->kprof.n[k] = 0;
+            }
+        }
+    }
+    for (int l = 0; l < nl; ++l)
+        if (status[l] != MIDAS_OK) return c->err.set(status[l], c->lanes[l]->err.msg);
+    return MIDAS_OK;
+}
+
 int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_offsets, const int *ext_idx, int ncbf,
              const double *cbf_theta, const double *cbf_phi, double thr_cbf, double res_sr, int flags, double eps_aca,
              int aca_itmax, int ntr, const double *theta, const double *phi, double2 *E_user, int *K_user,
@@ -190,7 +434,6 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
         smax = std::max(smax, xo[b + 1] - xo[b]);
         nbmax = std::max(nbmax, bo[b + 1] - bo[b]);
     }
-    const int spmax = pad64(3 * smax);
     // ---- persistent buffers ------------------------------------------------
     void *p0;
     size_t need0 = sizeof(int) * (xall.size() + n + 64) + sizeof(double) * 4 * (ncbf + ntr + 64) + 4096;
@@ -213,111 +456,29 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
     double2 *Call = (double2 *)pC;
     std::vector<size_t> coff(nb + 1, 0);
     std::vector<int> Kb(nb, 0);
-    // per-block work buffers (sized for the largest extended block)
-    void *p1, *p2 = nullptr, *p3, *p4;
-    MIDAS_TRY(ensure(c, S_CBF1, sizeof(float2) * (size_t)spmax * spmax, &p1));
-    if (!sr) MIDAS_TRY(ensure(c, S_CBF2, sizeof(float2) * (size_t)spmax * spmax, &p2));
-    size_t nrm = (size_t)spmax * m;
     // FP64 block solutions of every block are kept for the batched eigen-solve
+    void *p3, *p4;
     std::vector<size_t> xoff(nb + 1, 0);
     for (int b = 0; b < nb; ++b) xoff[b + 1] = xoff[b] + (size_t)pad64(3 * (xo[b + 1] - xo[b])) * m;
-    MIDAS_TRY(ensure(c, S_CBF3, sizeof(float2) * 4 * nrm + sizeof(double2) * (nrm + xoff[nb]) + 4096, &p3));
+    MIDAS_TRY(ensure(c, S_CBF3, sizeof(double2) * xoff[nb] + 4096, &p3));
     MIDAS_TRY(ensure(c, S_CBF4, (sizeof(double2) * (size_t)3 * m * m + sizeof(double) * m) * nb + 4096, &p4));
-    float2 *Zlu = (float2 *)p1, *Zsr = (float2 *)p2;
-    Buf b3{c, 0, (char *)p3};
-    float2 *Bm = b3.take<float2>(nrm), *Xh = b3.take<float2>(nrm), *Xl = b3.take<float2>(nrm),
-           *d32 = b3.take<float2>(nrm);
-    double2 *Xall = b3.take<double2>(xoff[nb]), *R64 = b3.take<double2>(nrm);
+    double2 *Xall = (double2 *)p3;
     Buf b4{c, 0, (char *)p4};
     const size_t mm = (size_t)m * m;
     double2 *Gall = b4.take<double2>(mm * nb), *Vall = b4.take<double2>(mm * nb), *Hall = b4.take<double2>(mm * nb);
     double *Wall = b4.take<double>((size_t)m * nb);
-    void *pred;
-    MIDAS_TRY(ensure(c, S_RED2, sizeof(unsigned long long) * 2 * m + 64, &pred));
-    unsigned long long *red = (unsigned long long *)pred;
-    std::vector<unsigned long long> hred(2 * m);
     std::vector<int> srefine(nb, 0);
     const double cbf_tol = (flags & MIDAS_CBFM_FAST_CBF) ? 1e-7 : 1e-11;
     cudaEvent_t e0, e1, e2, e3;
     cudaEventCreate(&e0); cudaEventCreate(&e1); cudaEventCreate(&e2); cudaEventCreate(&e3);
     cudaEventRecord(e0, c->stream);
     int ir_max = 0;
-    // ---- 1. CBF generation ---------------------------------------------------
-    for (int b = 0; b < nb; ++b) {
-        const int s = xo[b + 1] - xo[b], nbc = bo[b + 1] - bo[b];
-        const int N3 = 3 * s, sp = pad64(N3);
-        const int *idx = d_xall + xo[b];
-        double2 *X64 = Xall + xoff[b];
-        double thr_sr = 0.0;
-        if (sr) {
-            double fsr;
-            long long nnz;
-            MIDAS_TRY(sr_ladder(c, s, idx, bo[b], homog, res_sr, &fsr, &nnz, 0, nullptr, nullptr, nullptr));
-            double2 zn;
-            MIDAS_CUDA(c, cudaMemcpy(&zn, c->znnpp + bo[b], sizeof(double2), cudaMemcpyDeviceToHost));
-            thr_sr = hypot(1 - zn.x, -zn.y) / fsr;
-            if (c->opts.verbose >= 2) fprintf(stderr, "[midas] cbf block %d: fSR=%g nnz=%lld thr=%.17g\n", b, fsr, nnz, thr_sr);
-        }
-        // the thresholded block goes straight into the LU buffer; with SR its CSR
-        // form (about a sixth of the entries) serves the refinement residuals,
-        // without SR a dense copy does
-        MIDAS_CUDA(c, cudaMemsetAsync(Zlu, 0, sizeof(float2) * (size_t)sp * sp, c->stream));
-        MIDAS_TRY(launch_block_fill4<float2>(c, s, idx, s, idx, sr ? 1 : 0, thr_sr, homog, Zlu, (size_t)sp, 1));
-        if (sp > N3) {
-            ++c->launches;
-            k_pad_diag32<<<1, 64, 0, c->stream>>>(Zlu, sp, N3, sp);
-        }
-        Csr zcsr;
-        if (sr)
-            MIDAS_TRY(csr_from_dense(c, sp, Zlu, sp, S_CSR, &zcsr));
-        else
-            MIDAS_CUDA(c, cudaMemcpyAsync(Zsr, Zlu, sizeof(float2) * (size_t)sp * sp, cudaMemcpyDeviceToDevice,
-                                          c->stream));
-        MIDAS_CUDA(c, cudaMemsetAsync(Bm, 0, sizeof(float2) * (size_t)sp * m, c->stream));
-        MIDAS_TRY(launch_incident4<float2>(c, s, idx, ncbf, d_cth, d_cph, Bm, 1, (size_t)sp));
-        DenseLU lu;
-        lu.n = sp;
-        lu.A = Zlu;
-        lu.lda = sp;
-        MIDAS_TRY(lu_factor_nopiv(c, lu));
-        // x0 = LU^-1 B, then refinement with the double-float residual
-        MIDAS_CUDA(c, cudaMemcpyAsync(d32, Bm, sizeof(float2) * (size_t)sp * m, cudaMemcpyDeviceToDevice, c->stream));
-        MIDAS_TRY(lu_solve(c, lu, d32, m));
-        long long tot = (long long)sp * m;
-        ++c->launches;
-        k_ir_update<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(tot, sp, m, X64, d32, Xh, Xl, 1, sr);
-        int it;
-        for (it = 0; it < 12; ++it) {
-            if (sr)
-                MIDAS_TRY(residual_csr_df32(c, zcsr, m, Xh, Xl, Bm, R64));
-            else
-                MIDAS_TRY(residual_df32(c, sp, m, Zsr, sp, Xh, Xl, Bm, R64));
-            MIDAS_CUDA(c, cudaMemsetAsync(red, 0, sizeof(unsigned long long) * 2 * m, c->stream));
-            ++c->launches;
-            k_r_to32<<<dim3(32, m), 256, 0, c->stream>>>(sp, m, R64, d32, X64, red);
-            MIDAS_CUDA(c, cudaMemcpyAsync(hred.data(), red, sizeof(unsigned long long) * 2 * m,
-                                          cudaMemcpyDeviceToHost, c->stream));
-            MIDAS_CUDA(c, cudaStreamSynchronize(c->stream));
-            MIDAS_TRY(check_flag(c, "cbf block solve"));
-            double worst = 0;
-            for (int k = 0; k < m; ++k) {
-                double rn, xn;
-                memcpy(&rn, &hred[k], 8);
-                memcpy(&xn, &hred[m + k], 8);
-                worst = std::max(worst, xn > 0 ? rn / xn : rn);
-            }
-            if (!(worst == worst)) return c->err.set(MIDAS_ERR_NOT_CONVERGED, "cbf block solve: NaN");
-            if (worst <= cbf_tol) break;
-            MIDAS_TRY(lu_solve(c, lu, d32, m));
-            ++c->launches;
-            k_ir_update<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(tot, sp, m, X64, d32, Xh, Xl, 0, sr);
-        }
-        if (it == 12) return c->err.set(MIDAS_ERR_NOT_CONVERGED, "cbf block solve: refinement did not converge");
-        ir_max = std::max(ir_max, it);
-        // Gram G = X^H X over the 3s rows of the extended block (FP64)
-        MIDAS_TRY(zgemm64(c, m, m, N3, X64, sp, 1, 1, X64, 1, sp, Gall + mm * b, m, 1, make_double2(1, 0),
-                          make_double2(0, 0)));
-        srefine[b] = it;
+    // ---- 1. CBF generation: blocks run concurrently on the lanes ----------------
+    {
+        CbfShared S{bo.data(), xo.data(), d_xall, d_cth, d_cph, ncbf, m, sr, homog, res_sr, cbf_tol, Xall,
+                    xoff.data(), Gall, mm, srefine.data()};
+        MIDAS_TRY(cbf_generate(c, nb, S));
+        for (int b = 0; b < nb; ++b) ir_max = std::max(ir_max, srefine[b]);
     }
     // eigen-decomposition of every block's Gram matrix in one launch (one CTA per block)
     MIDAS_TRY(heev_dev(c, nb, m, Gall, m, (long long)mm, Hall, Vall, (long long)mm, Wall));

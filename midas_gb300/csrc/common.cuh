@@ -94,6 +94,9 @@ struct midas_gpu_ctx {
     int *d_flag = nullptr;   // device error flag
     long long launches = 0;  // kernels launched on this context
     midas::KProf kprof;
+    // lanes: child contexts (own stream and scratch pool, the cells aliased)
+    // that run independent CBFM blocks concurrently
+    std::vector<midas_gpu_ctx *> lanes;
     void *cusolver = nullptr;
     void *cublas = nullptr;
 };

@@ -128,7 +128,7 @@ int lu_factor_nopiv(midas_gpu_ctx *c, DenseLU &lu)
     lu.Uinv = lu.Linv + (size_t)lu.nblk * nb * nb;
     MIDAS_TRY(ensure(c, S_BEXP, sizeof(float) * (size_t)(2 * nb) * (2 * nb), &p));
     float *uexp = (float *)p;
-    MIDAS_TRY(ensure(c, S_BEXP2, sizeof(float) * (size_t)2 * n * 2 * nb, &p));
+    MIDAS_TRY(ensure(c, S_BEXP2, sizeof(float) * (size_t)2 * n * 2 * LU_NB2, &p));
     float *bexp = (float *)p;
     const size_t smem = sizeof(float2) * 3 * nb * nb;
     static bool attr = false;
@@ -138,36 +138,57 @@ int lu_factor_nopiv(midas_gpu_ctx *c, DenseLU &lu)
     }
     const long long lda = lu.lda;
     float *Af = (float *)lu.A;
-    for (int k = 0; k < lu.nblk; ++k) {
-        const int j0 = k * nb, rem = n - j0 - nb;
-        float2 *A11 = lu.A + (long long)j0 * lda + j0;
-        ++c->launches;
-        int kp = kp_begin(c);
-        k_diag_lu<LU_NB><<<1, 512, smem, c->stream>>>(A11, lda, lu.Linv + (size_t)k * nb * nb,
-                                                      lu.Uinv + (size_t)k * nb * nb, uexp, 1e-30f, c->d_flag);
-        kp_end(c, kp, MIDAS_KC_DIAG_LU, 8.0 * nb * nb * nb, 8.0 * nb * nb * 4);
-        MIDAS_CUDA(c, cudaGetLastError());
-        if (rem == 0) break;
-        // L21 = A21 U11^-1 (in place: each output row tile reads only its own rows)
-        {
-            GemmArgs g{rem, 2 * nb, 2 * nb, Af + 2 * ((long long)(j0 + nb) * lda + j0), 2 * lda, uexp, 2 * nb,
-                       Af + 2 * ((long long)(j0 + nb) * lda + j0), 2 * lda, 1.f, 0.f};
-            MIDAS_TRY(gemm_tf32(c, g));
+    auto gemm = [&](int M, int N, int K, const float *A, long long la, const float *B, long long lb, float *D,
+                    long long ld, float alpha, float beta) {
+        GemmArgs g{M, N, K, A, la, B, lb, D, ld, alpha, beta};
+        return gemm_tf32(c, g);
+    };
+    // Two levels: panels of LU_NB2 columns are factored with LU_NB-wide steps that
+    // update only the panel; the rows of U to the right of the panel follow by a
+    // blocked forward substitution, and the trailing matrix takes one update with
+    // K = LU_NB2 -- a quarter of the trailing-matrix traffic of LU_NB-wide updates.
+    for (int J0 = 0; J0 < n; J0 += LU_NB2) {
+        const int J1 = std::min(n, J0 + LU_NB2);
+        for (int j0 = J0; j0 < J1; j0 += nb) {
+            const int k = j0 / nb, rem = n - j0 - nb, wp = J1 - j0 - nb;
+            float2 *A11 = lu.A + (long long)j0 * lda + j0;
+            ++c->launches;
+            int kp = kp_begin(c);
+            k_diag_lu<LU_NB><<<1, 512, smem, c->stream>>>(A11, lda, lu.Linv + (size_t)k * nb * nb,
+                                                          lu.Uinv + (size_t)k * nb * nb, uexp, 1e-30f, c->d_flag);
+            kp_end(c, kp, MIDAS_KC_DIAG_LU, 8.0 * nb * nb * nb, 8.0 * nb * nb * 4);
+            MIDAS_CUDA(c, cudaGetLastError());
+            if (rem == 0) break;
+            // L21 = A21 U11^-1 (in place: each output row tile reads only its own rows)
+            MIDAS_TRY(gemm(rem, 2 * nb, 2 * nb, Af + 2 * ((long long)(j0 + nb) * lda + j0), 2 * lda, uexp, 2 * nb,
+                           Af + 2 * ((long long)(j0 + nb) * lda + j0), 2 * lda, 1.f, 0.f));
+            if (wp == 0) continue;
+            // panel columns right of the step: U12 = L11^-1 A12, then A22(panel) -= L21 U12
+            MIDAS_TRY(expand_b(c, nb, wp, lu.A + (long long)j0 * lda + j0 + nb, lda, 1, bexp, 2 * nb));
+            MIDAS_TRY(gemm(nb, 2 * wp, 2 * nb, (const float *)(lu.Linv + (size_t)k * nb * nb), 2 * nb, bexp, 2 * nb,
+                           Af + 2 * ((long long)j0 * lda + j0 + nb), 2 * lda, 1.f, 0.f));
+            MIDAS_TRY(expand_b(c, nb, wp, lu.A + (long long)j0 * lda + j0 + nb, lda, 1, bexp, 2 * nb));
+            MIDAS_TRY(gemm(rem, 2 * wp, 2 * nb, Af + 2 * ((long long)(j0 + nb) * lda + j0), 2 * lda, bexp, 2 * nb,
+                           Af + 2 * ((long long)(j0 + nb) * lda + j0 + nb), 2 * lda, -1.f, 1.f));
         }
-        // U12 = L11^-1 A12 : Bt = expand(A12) (copy), then write U12 in place
-        MIDAS_TRY(expand_b(c, nb, rem, lu.A + (long long)j0 * lda + j0 + nb, lda, 1, bexp, 2 * nb));
-        {
-            GemmArgs g{nb, 2 * rem, 2 * nb, (const float *)(lu.Linv + (size_t)k * nb * nb), 2 * nb, bexp, 2 * nb,
-                       Af + 2 * ((long long)j0 * lda + j0 + nb), 2 * lda, 1.f, 0.f};
-            MIDAS_TRY(gemm_tf32(c, g));
+        const int rt = n - J1;
+        if (rt == 0) break;
+        // U(J0:J1, J1:n) = L(J0:J1, J0:J1)^-1 A(J0:J1, J1:n), LU_NB rows at a time
+        for (int j0 = J0; j0 < J1; j0 += nb) {
+            const int k = j0 / nb, below = J1 - j0 - nb;
+            MIDAS_TRY(expand_b(c, nb, rt, lu.A + (long long)j0 * lda + J1, lda, 1, bexp, 2 * nb));
+            MIDAS_TRY(gemm(nb, 2 * rt, 2 * nb, (const float *)(lu.Linv + (size_t)k * nb * nb), 2 * nb, bexp, 2 * nb,
+                           Af + 2 * ((long long)j0 * lda + J1), 2 * lda, 1.f, 0.f));
+            if (below == 0) continue;
+            MIDAS_TRY(expand_b(c, nb, rt, lu.A + (long long)j0 * lda + J1, lda, 1, bexp, 2 * nb));
+            MIDAS_TRY(gemm(below, 2 * rt, 2 * nb, Af + 2 * ((long long)(j0 + nb) * lda + j0), 2 * lda, bexp, 2 * nb,
+                           Af + 2 * ((long long)(j0 + nb) * lda + J1), 2 * lda, -1.f, 1.f));
         }
-        // A22 -= L21 U12
-        MIDAS_TRY(expand_b(c, nb, rem, lu.A + (long long)j0 * lda + j0 + nb, lda, 1, bexp, 2 * nb));
-        {
-            GemmArgs g{rem, 2 * rem, 2 * nb, Af + 2 * ((long long)(j0 + nb) * lda + j0), 2 * lda, bexp, 2 * nb,
-                       Af + 2 * ((long long)(j0 + nb) * lda + j0 + nb), 2 * lda, -1.f, 1.f};
-            MIDAS_TRY(gemm_tf32(c, g));
-        }
+        // trailing matrix: A(J1:n, J1:n) -= L(J1:n, J0:J1) U(J0:J1, J1:n), K = J1 - J0
+        const int kw = J1 - J0;
+        MIDAS_TRY(expand_b(c, kw, rt, lu.A + (long long)J0 * lda + J1, lda, 1, bexp, 2 * kw));
+        MIDAS_TRY(gemm(rt, 2 * rt, 2 * kw, Af + 2 * ((long long)J1 * lda + J0), 2 * lda, bexp, 2 * kw,
+                       Af + 2 * ((long long)J1 * lda + J1), 2 * lda, -1.f, 1.f));
     }
     return MIDAS_OK;
 }

@@ -33,6 +33,8 @@ int aca_batch(midas_gpu_ctx *c, int npairs, const AcaPair *d_pairs, double eps, 
 int aca_uw(midas_gpu_ctx *c, int nrows, int k, int ncol, const double2 *U, const double2 *W, float2 *T, long long ldt);
 int aca_run(midas_gpu_ctx *c, int row0, int nrows, int col0, int ncols, double eps, int itmax, double2 *U,
             double2 *V, int *rank);
+// cbfm.cu: release the CBFM lanes of a context
+void free_lanes(midas_gpu_ctx *c);
 
 // sparse.cu: CSR matrix (0-based, columns ascending within a row)
 struct Csr {
@@ -43,6 +45,7 @@ struct Csr {
 int csr_from_dense(midas_gpu_ctx *c, int n, const float2 *Z, long long ldz, int slot, Csr *out);
 int residual_csr_df32(midas_gpu_ctx *c, const Csr &Z, int m, const float2 *Xh_rm, const float2 *Xl_rm,
                       const float2 *B, double2 *R);
+int residual_csr_update_f32(midas_gpu_ctx *c, const Csr &Z, int m, const float2 *D_rm, double2 *R);
 
 // fill.cu
 int launch_set_cells(midas_gpu_ctx *c);
@@ -91,6 +94,7 @@ struct DenseLU {
 };
 int lu_factor_nopiv(midas_gpu_ctx *c, DenseLU &lu);
 // solve LU X = R in place; R is n x nrhs column-major complex64 (ld = n)
+constexpr int LU_NB2 = 256;   // panel width of the two-level factorisation (slot S_BEXP2 holds 2n x 2 LU_NB2 floats)
 int lu_solve(midas_gpu_ctx *c, const DenseLU &lu, float2 *R, int nrhs);
 size_t lu_solve_scratch_bytes(int n, int nrhs);   // device scratch lu_solve takes from slot S_SOLVE
 // mixed-precision solve of Z x = b: Z64 row-major FP64 (for residuals), lu factored;

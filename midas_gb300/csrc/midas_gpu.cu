@@ -291,6 +291,7 @@ int midas_gpu_free(midas_gpu_ctx *c)
         if (b.p) cudaFree(b.p);
     if (c->d_flag) cudaFree(c->d_flag);
     if (c->cusolver) destroy_cusolver(c->cusolver);
+    free_lanes(c);
     for (cudaEvent_t e : c->kprof.ev) cudaEventDestroy(e);
     cudaStreamDestroy(c->stream);
     delete c;

@@ -129,7 +129,7 @@ extern "C" int midas_gpu_dense_solve_noalloc(int device, void *stream, int n, in
     slot(S_Z32, sizeof(float2) * (size_t)np * np);
     slot(S_LINV, sizeof(float2) * (size_t)nblk * nb * nb * 2);
     slot(S_BEXP, sizeof(float) * (size_t)(2 * nb) * (2 * nb));
-    slot(S_BEXP2, sizeof(float) * (size_t)2 * np * 2 * nb);
+    slot(S_BEXP2, sizeof(float) * (size_t)2 * np * 2 * LU_NB2);
     slot(S_RHS64, sizeof(double2) * nn);
     slot(S_X64, sizeof(double2) * nn);
     slot(S_R64, sizeof(double2) * nn);

@@ -208,4 +208,64 @@ int residual_csr_df32(midas_gpu_ctx *c, const Csr &Z, int m, const float2 *Xh_rm
     return MIDAS_OK;
 }
 
+// ---------------------------------------------------------------------------
+// r -= Z d (FP32): the residual of x + d from the residual of x, once the
+// correction d is small -- its FP32 product error is then below the double-float
+// accuracy the refinement needs.  d row-major (n x m), r column-major FP64.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_csr_sub_f32(int n, int m, const int *rowptr, const int *col,
+                                                      const float2 *val, const float2 *D, double2 *R)
+{
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (i >= n) return;
+    const int c0 = blockIdx.y * RESID_COLS;
+    float ar[RESID_T], ai[RESID_T];
+#pragma unroll
+    for (int t = 0; t < RESID_T; ++t) { ar[t] = 0.f; ai[t] = 0.f; }
+    const int p1 = rowptr[i + 1];
+    for (int p0 = rowptr[i]; p0 < p1; p0 += 32) {
+        const int cnt = min(32, p1 - p0);
+        int mk = 0;
+        float2 mz = make_float2(0.f, 0.f);
+        if (lane < cnt) { mk = col[p0 + lane]; mz = val[p0 + lane]; }
+#pragma unroll 4
+        for (int q = 0; q < cnt; ++q) {
+            const int k = __shfl_sync(0xffffffffu, mk, q);
+            float2 z;
+            z.x = __shfl_sync(0xffffffffu, mz.x, q);
+            z.y = __shfl_sync(0xffffffffu, mz.y, q);
+            const float2 *dr = D + (long long)k * m;
+#pragma unroll
+            for (int t = 0; t < RESID_T; ++t) {
+                const int cc = c0 + lane + 32 * t;
+                if (cc < m) {
+                    float2 d = dr[cc];
+                    ar[t] = fmaf(z.x, d.x, fmaf(-z.y, d.y, ar[t]));
+                    ai[t] = fmaf(z.x, d.y, fmaf(z.y, d.x, ai[t]));
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int t = 0; t < RESID_T; ++t) {
+        const int cc = c0 + lane + 32 * t;
+        if (cc < m) {
+            double2 *r = R + (long long)cc * n + i;
+            *r = make_double2(r->x - (double)ar[t], r->y - (double)ai[t]);
+        }
+    }
+}
+
+int residual_csr_update_f32(midas_gpu_ctx *c, const Csr &Z, int m, const float2 *D_rm, double2 *R)
+{
+    const int n = Z.n;
+    dim3 grd((unsigned)(((long long)n * 32 + 255) / 256), (m + RESID_COLS - 1) / RESID_COLS);
+    ++c->launches;
+    int kp = kp_begin(c);
+    k_csr_sub_f32<<<grd, 256, 0, c->stream>>>(n, m, Z.rowptr, Z.col, Z.val, D_rm, R);
+    kp_end(c, kp, MIDAS_KC_RESID, 8.0 * Z.nnz * m, 12.0 * Z.nnz + 8.0 * (double)n * m + 32.0 * (double)n * m);
+    MIDAS_CUDA(c, cudaGetLastError());
+    return MIDAS_OK;
+}
+
 }  // namespace midas

@@ -1,0 +1,107 @@
+"""Benchmark scenes of the MIDAS hot path, and a runner that solves them
+through the library without PyTorch (the command the profiler runs).
+
+    python -m midas_gb300.workloads cbfm_c2_small --steps 1
+
+Each scene is seeded synthetic input with the shapes of the reference's
+configurations: the reference sphere voxeliser (src/Discretization.f90:246-310)
+for the homogeneous sphere, a voxelised Gaussian random sphere for the CBFM
+scene, a 3x3x3 bounding-box partition extended by 15 % of the block edge
+(Extend_blocks, src/Extend_blocks.f90:46-151) and the 'un' CBF excitations
+(getTransmitters_CBFM, src/getParameters_CBFM.f90:34-75).
+"""
+from __future__ import annotations
+
+import argparse
+import math
+import time
+
+import numpy as np
+
+
+def mom_c1():
+    """Plain MoM, homogeneous sphere x = 2, m = 1.5 + 0.01i, a/d = 10 (4,224 cells,
+    12,672 unknowns), +z incidence (MIDAS angles theta = phi = 90 deg), V + H."""
+    from . import geometry as G
+    a, x, m = 1.0, 2.0, 1.5 + 0.01j
+    k0 = x / a
+    sc = a / 10.0
+    xyz = G.sphere_cells(2 * a, sc)
+    return {"name": "mom_c1_sphere_x2_m1.5+0.01i_4224cells", "xyz": xyz, "sc": sc,
+            "eps": np.full(len(xyz), m * m), "k0": k0, "th": np.array([90.0]), "ph": np.array([90.0]),
+            "method": "mom"}
+
+
+def _gaussian_sphere_cbfm(name, x, a_over_d, ndir, nbox=3, seed=2026):
+    from . import geometry as G
+    a, m = 1.0, 1.55 + 0.005j
+    k0 = x / a
+    sc = a / a_over_d
+    xyz = G.gaussian_sphere(a, 0.15, 20.0, sc, seed=seed)
+    perm, offs = G.box_partition(xyz, nbox, nbox, nbox)
+    xyz = np.ascontiguousarray(xyz[perm])
+    box, sph = G.block_contours(xyz, offs)
+    edge = float((box[:, 1] - box[:, 0]).max(axis=1).mean())
+    ext = G.extend_blocks(xyz, offs, 0.15 * edge, sc)
+    lam = 2 * math.pi / k0
+    niws = G.init_nipws(float(sph[:, 3].max()) / (lam / abs(m)))
+    cth, cph = G.transmitters_un(niws)
+    th, ph = G.random_directions(ndir, seed=7)
+    return {"name": name, "xyz": xyz, "sc": sc, "eps": np.full(len(xyz), m * m), "k0": k0, "th": th, "ph": ph,
+            "method": "cbfm", "offs": offs, "ext": ext, "cth": cth, "cph": cph, "homog": 1, "niws": niws}
+
+
+def cbfm_c2():
+    """CBFM-E on a seeded Gaussian random sphere: x = 6, m = 1.55 + 0.005i, log-radius
+    std 0.15, correlation angle 20 deg, voxel a/21.1 (~41k cells, ~123k unknowns),
+    3x3x3 bounding-box blocks with a 15 % (of the block edge) extension, CBF
+    excitations from the reference's Niws table ('un'), 24 seeded incident
+    directions x 2 polarisations."""
+    return _gaussian_sphere_cbfm("cbfm_c2_gaussian_sphere_x6_m1.55+0.005i", 6.0, 21.1, 24)
+
+
+def cbfm_c2_small():
+    """The same scene at a/d = 12 (~7.6k cells) in 2x2x2 blocks: the kernels of
+    the full scene with a launch count a profiler lists in minutes.  (A 3x3x3
+    split at this resolution leaves corner blocks of a few cells, fewer unknowns
+    than CBFs, and a singular reduced system.)"""
+    return _gaussian_sphere_cbfm("cbfm_c2_small_gaussian_sphere_x6_ad12_2x2x2", 6.0, 12.0, 24, nbox=2)
+
+
+WORKLOADS = {"mom_c1": mom_c1, "cbfm_c2": cbfm_c2, "cbfm_c2_small": cbfm_c2_small}
+
+
+def cbfm_args(wl):
+    """Partition arrays of a CBFM scene in the C-ABI layout."""
+    bo = np.ascontiguousarray(wl["offs"], np.int32)
+    eo = np.ascontiguousarray(np.concatenate([[0], np.cumsum([len(e) for e in wl["ext"]])]), np.int32)
+    ei = np.ascontiguousarray(np.concatenate(wl["ext"]), np.int32)
+    return bo, eo, ei
+
+
+def main(argv=None):
+    from . import _lib
+    from .solver import Context
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("workload", choices=sorted(WORKLOADS))
+    ap.add_argument("--steps", type=int, default=1)
+    ap.add_argument("--fill", default="fast", choices=["fast", "faithful"])
+    args = ap.parse_args(argv)
+    wl = WORKLOADS[args.workload]()
+    ctx = Context(device=0, fill_mode=_lib.FILL_FAST if args.fill == "fast" else _lib.FILL_FAITHFUL)
+    ctx.set_cells(wl["xyz"], wl["sc"], wl["eps"], wl["k0"])
+    for step in range(args.steps):
+        t0 = time.perf_counter()
+        if wl["method"] == "cbfm":
+            flags = _lib.CBFM_SR | (_lib.CBFM_HOMOG if wl.get("homog") else 0)
+            E, K = ctx.cbfm_solve(wl["offs"], wl["ext"], wl["cth"], wl["cph"], wl["th"], wl["ph"], flags=flags)
+        else:
+            E = ctx.mom_solve(wl["th"], wl["ph"])
+        dt = time.perf_counter() - t0
+        print(f"{wl['name']}: step {step} {dt:.3f} s, {ctx.launch_count()} launches so far", flush=True)
+    ctx.close()
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())
