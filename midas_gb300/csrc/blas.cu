@@ -23,12 +23,6 @@
 
 namespace midas {
 
-__device__ __forceinline__ float tf32_rna(float x)
-{
-    uint32_t u;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(u) : "f"(x));
-    return __uint_as_float(u);
-}
 
 template <typename T>
 __device__ __forceinline__ double2 ld2(const T *p, long long i);

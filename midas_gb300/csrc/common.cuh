@@ -40,6 +40,16 @@ struct Err {
 // Device error flags (written by kernels that hit a bounded wait or a bad pivot).
 enum DevErr : int { DEV_OK = 0, DEV_TIMEOUT = 1, DEV_ZERO_PIVOT = 2, DEV_BAD_ARG = 4 };
 
+// FP32 -> TF32 with round-to-nearest (ties away): the tensor cores read only the
+// top 19 bits of an FP32 operand (truncation, a one-sided error), so values that
+// feed them repeatedly are stored pre-rounded to keep the errors unbiased.
+__device__ __forceinline__ float tf32_rna(float x)
+{
+    uint32_t u;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(u) : "f"(x));
+    return __uint_as_float(u);
+}
+
 // Reference Pi = Acos(-1.) evaluated in single precision (src/Initialization.f90:39).
 inline double ref_pi_host() { return (double)acosf(-1.0f); }
 

@@ -97,16 +97,17 @@ __global__ void __launch_bounds__(512) k_diag_lu(float2 *A11, long long lda, flo
         }
     }
     __syncthreads();
+    // the inverses are GEMM operands: stored rounded to TF32 (nearest)
     for (int i = tid; i < NB * NB; i += nt) {
         A11[(long long)(i / NB) * lda + (i % NB)] = a[i];
-        Linv[i] = li[i];
-        Uinv[i] = ui[i];
+        Linv[i] = make_float2(tf32_rna(li[i].x), tf32_rna(li[i].y));
+        Uinv[i] = make_float2(tf32_rna(ui[i].x), tf32_rna(ui[i].y));
     }
     // expanded U^-1 as the Bt operand (rows = output columns j, along p):
     // Bt[2j][2p] = Ur(p,j), Bt[2j][2p+1] = -Ui(p,j), Bt[2j+1][2p] = Ui, Bt[2j+1][2p+1] = Ur
     for (int t = tid; t < NB * NB; t += nt) {
         int p = t / NB, j = t % NB;
-        float2 u = ui[p * NB + j];
+        float2 u = make_float2(tf32_rna(ui[p * NB + j].x), tf32_rna(ui[p * NB + j].y));
         float *r0 = UinvExp + (long long)(2 * j) * (2 * NB) + 2 * p;
         float *r1 = r0 + 2 * NB;
         r0[0] = u.x; r0[1] = -u.y;
@@ -138,9 +139,11 @@ int lu_factor_nopiv(midas_gpu_ctx *c, DenseLU &lu)
     }
     const long long lda = lu.lda;
     float *Af = (float *)lu.A;
+    // rnd = 1 for the GEMMs that produce final L or U entries: those are stored
+    // rounded to TF32 (round to nearest), as every later use reads them in TF32
     auto gemm = [&](int M, int N, int K, const float *A, long long la, const float *B, long long lb, float *D,
-                    long long ld, float alpha, float beta) {
-        GemmArgs g{M, N, K, A, la, B, lb, D, ld, alpha, beta};
+                    long long ld, float alpha, float beta, int rnd) {
+        GemmArgs g{M, N, K, A, la, B, lb, D, ld, alpha, beta, rnd};
         return gemm_tf32(c, g);
     };
     // Two levels: panels of LU_NB2 columns are factored with LU_NB-wide steps that
@@ -161,15 +164,15 @@ int lu_factor_nopiv(midas_gpu_ctx *c, DenseLU &lu)
             if (rem == 0) break;
             // L21 = A21 U11^-1 (in place: each output row tile reads only its own rows)
             MIDAS_TRY(gemm(rem, 2 * nb, 2 * nb, Af + 2 * ((long long)(j0 + nb) * lda + j0), 2 * lda, uexp, 2 * nb,
-                           Af + 2 * ((long long)(j0 + nb) * lda + j0), 2 * lda, 1.f, 0.f));
+                           Af + 2 * ((long long)(j0 + nb) * lda + j0), 2 * lda, 1.f, 0.f, 1));
             if (wp == 0) continue;
             // panel columns right of the step: U12 = L11^-1 A12, then A22(panel) -= L21 U12
             MIDAS_TRY(expand_b(c, nb, wp, lu.A + (long long)j0 * lda + j0 + nb, lda, 1, bexp, 2 * nb));
             MIDAS_TRY(gemm(nb, 2 * wp, 2 * nb, (const float *)(lu.Linv + (size_t)k * nb * nb), 2 * nb, bexp, 2 * nb,
-                           Af + 2 * ((long long)j0 * lda + j0 + nb), 2 * lda, 1.f, 0.f));
+                           Af + 2 * ((long long)j0 * lda + j0 + nb), 2 * lda, 1.f, 0.f, 1));
             MIDAS_TRY(expand_b(c, nb, wp, lu.A + (long long)j0 * lda + j0 + nb, lda, 1, bexp, 2 * nb));
             MIDAS_TRY(gemm(rem, 2 * wp, 2 * nb, Af + 2 * ((long long)(j0 + nb) * lda + j0), 2 * lda, bexp, 2 * nb,
-                           Af + 2 * ((long long)(j0 + nb) * lda + j0 + nb), 2 * lda, -1.f, 1.f));
+                           Af + 2 * ((long long)(j0 + nb) * lda + j0 + nb), 2 * lda, -1.f, 1.f, 0));
         }
         const int rt = n - J1;
         if (rt == 0) break;
@@ -178,17 +181,17 @@ int lu_factor_nopiv(midas_gpu_ctx *c, DenseLU &lu)
             const int k = j0 / nb, below = J1 - j0 - nb;
             MIDAS_TRY(expand_b(c, nb, rt, lu.A + (long long)j0 * lda + J1, lda, 1, bexp, 2 * nb));
             MIDAS_TRY(gemm(nb, 2 * rt, 2 * nb, (const float *)(lu.Linv + (size_t)k * nb * nb), 2 * nb, bexp, 2 * nb,
-                           Af + 2 * ((long long)j0 * lda + J1), 2 * lda, 1.f, 0.f));
+                           Af + 2 * ((long long)j0 * lda + J1), 2 * lda, 1.f, 0.f, 1));
             if (below == 0) continue;
             MIDAS_TRY(expand_b(c, nb, rt, lu.A + (long long)j0 * lda + J1, lda, 1, bexp, 2 * nb));
             MIDAS_TRY(gemm(below, 2 * rt, 2 * nb, Af + 2 * ((long long)(j0 + nb) * lda + j0), 2 * lda, bexp, 2 * nb,
-                           Af + 2 * ((long long)(j0 + nb) * lda + J1), 2 * lda, -1.f, 1.f));
+                           Af + 2 * ((long long)(j0 + nb) * lda + J1), 2 * lda, -1.f, 1.f, 0));
         }
         // trailing matrix: A(J1:n, J1:n) -= L(J1:n, J0:J1) U(J0:J1, J1:n), K = J1 - J0
         const int kw = J1 - J0;
         MIDAS_TRY(expand_b(c, kw, rt, lu.A + (long long)J0 * lda + J1, lda, 1, bexp, 2 * kw));
         MIDAS_TRY(gemm(rt, 2 * rt, 2 * kw, Af + 2 * ((long long)J1 * lda + J0), 2 * lda, bexp, 2 * kw,
-                       Af + 2 * ((long long)J1 * lda + J1), 2 * lda, -1.f, 1.f));
+                       Af + 2 * ((long long)J1 * lda + J1), 2 * lda, -1.f, 1.f, 0));
     }
     return MIDAS_OK;
 }
@@ -230,8 +233,9 @@ __global__ void k_apply_inv_rm(const float2 *Minv, float2 *Rt, int nrhs, int r0,
     }
     x[(long long)i * nrhs] = s;
     float *b0 = Bt + (long long)(2 * j) * ldb + col0 + 2 * i, *b1 = b0 + ldb;
-    b0[0] = s.x; b0[1] = -s.y;
-    b1[0] = s.y; b1[1] = s.x;
+    const float yr = tf32_rna(s.x), yi = tf32_rna(s.y);   // GEMM operand: unbiased TF32
+    b0[0] = yr; b0[1] = -yi;
+    b1[0] = yi; b1[1] = yr;
 }
 
 // column-major R (n x nrhs, ld n) -> row-major Rt (n x nrhs), 32 x 32 tiles

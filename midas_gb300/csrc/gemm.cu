@@ -195,7 +195,7 @@ constexpr int TC_PROMOTE_KB = 2;
 template <bool PROMOTE, int TC_STAGES>
 __global__ void __launch_bounds__(TC_THREADS, TC_STAGES == 2 ? 2 : 1)
     k_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int M, int N, int K,
-              float *D, long long ldd, float alpha, float beta, int *gflag)
+              float *D, long long ldd, float alpha, float beta, int rnd, int *gflag)
 {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -342,12 +342,16 @@ __global__ void __launch_bounds__(TC_THREADS, TC_STAGES == 2 ? 2 : 1)
                             } else {
                                 o = make_float4(alpha * a.x, alpha * a.y, alpha * a.z, alpha * a.w);
                             }
+                            if (rnd) o = make_float4(tf32_rna(o.x), tf32_rna(o.y), tf32_rna(o.z), tf32_rna(o.w));
                             *(float4 *)d = o;
                         } else {
                             const float av[4] = {a.x, a.y, a.z, a.w};
 #pragma unroll
                             for (int e = 0; e < 4; ++e)
-                                if (col + e < N) d[e] = alpha * av[e] + (beta != 0.f ? beta * d[e] : 0.f);
+                                if (col + e < N) {
+                                    float o = alpha * av[e] + (beta != 0.f ? beta * d[e] : 0.f);
+                                    d[e] = rnd ? tf32_rna(o) : o;
+                                }
                         }
                     }
                     __syncwarp();
@@ -415,7 +419,8 @@ __device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, const void 
 template <int STAGES, int DBUF>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_gemm_tcp(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-               const __grid_constant__ CUtensorMap tmD, int M, int N, int K, float alpha, float beta, int *gflag)
+               const __grid_constant__ CUtensorMap tmD, int M, int N, int K, float alpha, float beta, int rnd,
+               int *gflag)
 {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -544,6 +549,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                         o = make_float4(alpha * v[4 * u], alpha * v[4 * u + 1], alpha * v[4 * u + 2],
                                         alpha * v[4 * u + 3]);
                     }
+                    if (rnd) o = make_float4(tf32_rna(o.x), tf32_rna(o.y), tf32_rna(o.z), tf32_rna(o.w));
                     *p = o;
                 }
             }
@@ -672,10 +678,10 @@ static int gemm_tc(midas_gpu_ctx *c, const GemmArgs &g, bool precise)
         int kp = kp_begin(c);
         if (g.K <= 256)
             k_gemm_tcp<2, 2><<<grid, TC_THREADS, tcp_smem(2, 2), c->stream>>>(ma, mb, md, g.M, g.N, g.K, g.alpha,
-                                                                               g.beta, c->d_flag);
+                                                                               g.beta, g.round_tf32, c->d_flag);
         else
             k_gemm_tcp<4, 1><<<grid, TC_THREADS, tcp_smem(4, 1), c->stream>>>(ma, mb, md, g.M, g.N, g.K, g.alpha,
-                                                                               g.beta, c->d_flag);
+                                                                               g.beta, g.round_tf32, c->d_flag);
         kp_end(c, kp, MIDAS_KC_GEMM_TC, 2.0 * g.M * g.N * g.K, gemm_bytes(g));
         MIDAS_CUDA(c, cudaGetLastError());
         return MIDAS_OK;
@@ -685,13 +691,13 @@ static int gemm_tc(midas_gpu_ctx *c, const GemmArgs &g, bool precise)
     int kp = kp_begin(c);
     if (precise)
         k_gemm_tc<true, 4><<<grd, TC_THREADS, tc_smem(4), c->stream>>>(ma, mb, g.M, g.N, g.K, g.D, g.ldd, g.alpha,
-                                                                       g.beta, c->d_flag);
+                                                                       g.beta, 0, c->d_flag);
     else if (g.K <= 256)
         k_gemm_tc<false, 2><<<grd, TC_THREADS, tc_smem(2), c->stream>>>(ma, mb, g.M, g.N, g.K, g.D, g.ldd, g.alpha,
-                                                                        g.beta, c->d_flag);
+                                                                        g.beta, g.round_tf32, c->d_flag);
     else
         k_gemm_tc<false, 4><<<grd, TC_THREADS, tc_smem(4), c->stream>>>(ma, mb, g.M, g.N, g.K, g.D, g.ldd, g.alpha,
-                                                                        g.beta, c->d_flag);
+                                                                        g.beta, g.round_tf32, c->d_flag);
     kp_end(c, kp, MIDAS_KC_GEMM_TC, 2.0 * g.M * g.N * g.K, gemm_bytes(g));
     MIDAS_CUDA(c, cudaGetLastError());
     return MIDAS_OK;
@@ -713,6 +719,7 @@ __global__ void k_expand_b(int k, int n, const float2 *B, long long rsb, long lo
     if (p >= k) return;
     for (int j = blockIdx.y; j < n; j += gridDim.y) {   // columns beyond the 65535 grid limit loop
         float2 b = B[(long long)p * rsb + (long long)j * csb];
+        b = make_float2(tf32_rna(b.x), tf32_rna(b.y));   // B operand: unbiased TF32
         float *r0 = Bt + (long long)(2 * j) * ldt + 2 * p;
         float *r1 = r0 + ldt;
         r0[0] = b.x; r0[1] = -b.y;

@@ -72,6 +72,7 @@ struct GemmArgs {
     const float *Bt; long long ldb;
     float *D; long long ldd;
     float alpha, beta;
+    int round_tf32 = 0;   // store D rounded to TF32 (final L / U factor entries)
 };
 // precise = periodic promotion of the tensor-core partial sums to FP32 registers
 int gemm_tf32(midas_gpu_ctx *c, const GemmArgs &g, bool precise = false);
