@@ -218,9 +218,9 @@ static int cbf_block(midas_gpu_ctx *c, const CbfShared &S, int b)
         k_ir_update<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(tot, sp, m, X64, d32, Xh, Xl, nullptr, 1,
                                                                           sr);
         // Residuals: double-float B - Z x while the corrections are large; once the
-        // relative residual is below 1e-7 the next correction d is ~1e-7 |x| or
-        // smaller, and r - Z d in FP32 (error ~1e-6 |Z||d|) is as accurate as the
-        // double-float residual of x + d.
+        // relative residual is below 1e-5 every later correction d is ~1e-5 |x| or
+        // smaller, and r - Z d in FP32 (error ~1e-6 |Z||d| over a row's ~3k
+        // nonzeros) keeps the computed residual within ~1e-11 |x| of the true one.
         int it;
         bool upd = false;
         for (it = 0; it < 12; ++it) {
@@ -246,7 +246,7 @@ static int cbf_block(midas_gpu_ctx *c, const CbfShared &S, int b)
             }
             if (!(worst == worst)) return c->err.set(MIDAS_ERR_NOT_CONVERGED, "cbf block solve: NaN");
             if (worst <= cbf_tol) break;
-            upd = sr && worst <= 1e-7;
+            upd = sr && worst <= 1e-5;
             MIDAS_TRY(lu_solve(c, lu, d32, m));
             ++c->launches;
             k_ir_update<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(tot, sp, m, X64, d32, Xh, Xl,
