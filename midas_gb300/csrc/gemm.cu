@@ -385,7 +385,8 @@ __host__ __device__ constexpr int tcp_smem(int stages, int dbuf)
 {
     return stages * TC_STAGE_BYTES + dbuf * TCP_D_BYTES + 1024 /*align*/ + 512 /*barriers*/;
 }
-static_assert(tcp_smem(3, 2) <= 227 * 1024, "persistent GEMM exceeds the shared memory of one CTA");
+static_assert(tcp_smem(4, 1) <= 227 * 1024 && tcp_smem(2, 2) <= 227 * 1024,
+              "persistent GEMM exceeds the shared memory of one CTA");
 
 __device__ __forceinline__ void tcp_tile(int t, int mt, int nt, int &m0, int &n0)
 {
@@ -667,8 +668,8 @@ static int gemm_tc(midas_gpu_ctx *c, const GemmArgs &g, bool precise)
         if (!pattr) {
             MIDAS_CUDA(c, cudaFuncSetAttribute(k_gemm_tcp<2, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               tcp_smem(2, 2)));
-            MIDAS_CUDA(c, cudaFuncSetAttribute(k_gemm_tcp<3, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              tcp_smem(3, 2)));
+            MIDAS_CUDA(c, cudaFuncSetAttribute(k_gemm_tcp<4, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              tcp_smem(4, 1)));
             pattr = true;
         }
         CUtensorMap md;
@@ -680,8 +681,8 @@ static int gemm_tc(midas_gpu_ctx *c, const GemmArgs &g, bool precise)
         if (g.K <= 256)
             k_gemm_tcp<2, 2><<<grid, TC_THREADS, tcp_smem(2, 2), c->stream>>>(ma, mb, md, g.M, g.N, g.K, g.alpha,
                                                                                g.beta, g.round_tf32, c->d_flag);
-        else   // 3 stages and two D buffers: 225.5 KB of shared memory
-            k_gemm_tcp<3, 2><<<grid, TC_THREADS, tcp_smem(3, 2), c->stream>>>(ma, mb, md, g.M, g.N, g.K, g.alpha,
+        else   // long K: 4 stages, one D buffer (requested after the tile's k-blocks)
+            k_gemm_tcp<4, 1><<<grid, TC_THREADS, tcp_smem(4, 1), c->stream>>>(ma, mb, md, g.M, g.N, g.K, g.alpha,
                                                                                g.beta, g.round_tf32, c->d_flag);
         kp_end(c, kp, MIDAS_KC_GEMM_TC, 2.0 * g.M * g.N * g.K, gemm_bytes(g));
         MIDAS_CUDA(c, cudaGetLastError());
