@@ -25,6 +25,7 @@
 #include <atomic>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <thread>
 
@@ -269,7 +270,14 @@ static int cbf_block(midas_gpu_ctx *c, const CbfShared &S, int b)
 // refinement) then overlap the bandwidth-bound parts of another.  The lanes
 // live as long as the context.
 // ---------------------------------------------------------------------------
-constexpr int CBF_LANES = 4;
+constexpr int CBF_LANES = 6;   // default (measured best of 1-8 on GB300); MIDAS_CBFM_LANES (1..16) overrides
+
+static int cbf_lanes()
+{
+    const char *e = getenv("MIDAS_CBFM_LANES");
+    int v = e ? atoi(e) : CBF_LANES;
+    return v < 1 ? 1 : (v > 16 ? 16 : v);
+}
 
 static void lane_sync_cells(midas_gpu_ctx *L, const midas_gpu_ctx *c)
 {
@@ -321,7 +329,7 @@ static int cbf_generate(midas_gpu_ctx *c, int nb, const CbfShared &S)
 {
     // with kernel-class profiling on, one lane: each launch's event interval then
     // covers that kernel alone
-    const int nl = c->kprof.on ? 1 : std::min(nb, CBF_LANES);
+    const int nl = c->kprof.on ? 1 : std::min(nb, cbf_lanes());
     MIDAS_TRY(get_lanes(c, nl));
     MIDAS_CUDA(c, cudaStreamSynchronize(c->stream));   // the shared inputs are on the device
     // largest blocks first, each to the least-loaded lane (cost ~ s^3)

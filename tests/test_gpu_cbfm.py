@@ -64,3 +64,30 @@ def test_cbfm_rejects_bad_partition(gpulib, oracle):
         ctx.cbfm_solve(bad, ext, cth, cph, [90.0], [90.0])
     assert e.value.status == 1
     ctx.close()
+
+
+def test_cbfm_lanes_bit_identical(gpulib, oracle, monkeypatch):
+    """The extended blocks run on concurrent lanes; every block is computed the same
+    way whatever lane takes it, so E is bit-identical for any lane count, and with
+    kernel-class profiling on (one lane)."""
+    from midas_gb300 import _lib, geometry as G
+    from midas_gb300.solver import Context
+    xyz, sc, eps, k0, offs, ext = _case(oracle, (2, 2, 1), True)
+    th, ph = np.array([90.0, 35.0]), np.array([90.0, 120.0])
+    cth, cph = G.transmitters_un(91)
+    ctx = Context(fill_mode=_lib.FILL_FAST).set_cells(xyz, sc, eps, k0)
+    runs = []
+    for lanes in ("1", "3", "6"):
+        monkeypatch.setenv("MIDAS_CBFM_LANES", lanes)
+        runs.append(ctx.cbfm_solve(offs, ext, cth, cph, th, ph, flags=_lib.CBFM_SR))
+    ctx.profile(True)
+    runs.append(ctx.cbfm_solve(offs, ext, cth, cph, th, ph, flags=_lib.CBFM_SR))
+    prof = ctx.profile_query()
+    ctx.profile(False)
+    for E, K in runs[1:]:
+        assert np.array_equal(E, runs[0][0]) and np.array_equal(K, runs[0][1])
+    # the profiler saw the solve's kernels
+    assert prof["gemm_tc"]["launches"] > 0 and prof["gemm_tc"]["ms"] > 0
+    assert prof["resid"]["launches"] > 0 and prof["diag_lu"]["launches"] > 0
+    assert prof["gemm_tc"]["flops"] > 0 and prof["fill"]["bytes"] > 0
+    ctx.close()

@@ -1,0 +1,25 @@
+"""Benchmark scenes: sizes and partition arrays in the C-ABI layout (CPU only)."""
+import numpy as np
+
+
+def test_mom_scene_size():
+    from midas_gb300.workloads import mom_c1
+    wl = mom_c1()
+    assert len(wl["xyz"]) == 4224 and wl["method"] == "mom"
+
+
+def test_small_cbfm_scene_partition():
+    from midas_gb300.workloads import cbfm_args, cbfm_c2_small
+    wl = cbfm_c2_small()
+    n = len(wl["xyz"])
+    bo, eo, ei = cbfm_args(wl)
+    assert bo[0] == 0 and bo[-1] == n and np.all(np.diff(bo) > 0)
+    assert len(bo) == 9                     # 2 x 2 x 2 blocks, none empty
+    assert eo[0] == 0 and eo[-1] == len(ei) and np.all(np.diff(eo) >= 0)
+    for b in range(len(bo) - 1):
+        e = ei[eo[b]:eo[b + 1]]
+        # extension cells lie outside the block and are distinct
+        assert np.all((e < bo[b]) | (e >= bo[b + 1])) and len(np.unique(e)) == len(e)
+    # every block has more unknowns than CBF excitations (a well-posed reduced system)
+    assert np.min(3 * np.diff(bo)) > 2 * len(wl["cth"])
+    assert wl["niws"] in (91, 190, 231) and len(wl["th"]) == 24   # initializeNipws table
