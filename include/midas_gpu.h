@@ -217,7 +217,7 @@ long long midas_gpu_launch_count(const midas_gpu_ctx *ctx);
 void *midas_gpu_stream(const midas_gpu_ctx *ctx);
 
 /* Kernel classes timed by the profiler below. */
-#define MIDAS_KC_GEMM_TC   0   /* tcgen05 GEMM (LU panels and trailing updates, CBFM products) */
+#define MIDAS_KC_GEMM_TC   0   /* tcgen05 GEMM: LU trailing-matrix updates (and untagged GEMMs) */
 #define MIDAS_KC_GEMM_SIMT 1   /* CUDA-core FP32 GEMM (fallback engine) */
 #define MIDAS_KC_FILL      2   /* impedance fills (MoM element, CBFM block, SR threshold) */
 #define MIDAS_KC_SR_SCAN   3   /* setfSR ladder scan */
@@ -226,8 +226,11 @@ void *midas_gpu_stream(const midas_gpu_ctx *ctx);
 #define MIDAS_KC_RESID     6   /* refinement residuals (FP64 / double-float) */
 #define MIDAS_KC_ZGEMM64   7   /* FP64 complex GEMMs (Gram, CBF projections, Vc, E) */
 #define MIDAS_KC_EIG       8   /* Hermitian eigensolver */
-#define MIDAS_KC_OTHER     9   /* everything else that is instrumented */
-#define MIDAS_KC_COUNT     10
+#define MIDAS_KC_OTHER     9   /* everything else that is instrumented (ACA) */
+#define MIDAS_KC_GEMM_PANEL 10  /* tcgen05 GEMM: LU panel and U-row (forward substitution) steps */
+#define MIDAS_KC_GEMM_SOLVE 11  /* tcgen05 GEMM: triangular-solve updates */
+#define MIDAS_KC_GEMM_PROD  12  /* tcgen05 GEMM: split-TF32 products (reduced matrix, FP32-grade ZGEMM) */
+#define MIDAS_KC_COUNT     13
 /* enable = 1 clears the per-class totals and starts timing every instrumented
  * launch with CUDA events on the context stream; 0 stops.  Timing adds one event
  * record before and after each instrumented launch. */

@@ -102,7 +102,7 @@ int zgemm_x3(midas_gpu_ctx *c, int M, int N, int K, const TA *A, long long ars, 
     k_split_expand_b<TB><<<dim3((K + 127) / 128, std::min(N, 65535)), 128, 0, c->stream>>>(K, N, B, brs, bcs, B3,
                                                                                             K6);
     MIDAS_CUDA(c, cudaGetLastError());
-    GemmArgs g{M, 2 * N, (int)K6, A3, K6, B3, K6, D, ldd, alpha, beta};
+    GemmArgs g{M, 2 * N, (int)K6, A3, K6, B3, K6, D, ldd, alpha, beta, 0, MIDAS_KC_GEMM_PROD};
     return gemm_tf32(c, g, true);
 }
 template int zgemm_x3<float2, double2>(midas_gpu_ctx *, int, int, int, const float2 *, long long, long long, int,

@@ -142,8 +142,8 @@ int lu_factor_nopiv(midas_gpu_ctx *c, DenseLU &lu)
     // rnd = 1 for the GEMMs that produce final L or U entries: those are stored
     // rounded to TF32 (round to nearest), as every later use reads them in TF32
     auto gemm = [&](int M, int N, int K, const float *A, long long la, const float *B, long long lb, float *D,
-                    long long ld, float alpha, float beta, int rnd) {
-        GemmArgs g{M, N, K, A, la, B, lb, D, ld, alpha, beta, rnd};
+                    long long ld, float alpha, float beta, int rnd, int kc = MIDAS_KC_GEMM_PANEL) {
+        GemmArgs g{M, N, K, A, la, B, lb, D, ld, alpha, beta, rnd, kc};
         return gemm_tf32(c, g);
     };
     // Two levels: panels of LU_NB2 columns are factored with LU_NB-wide steps that
@@ -191,7 +191,7 @@ int lu_factor_nopiv(midas_gpu_ctx *c, DenseLU &lu)
         const int kw = J1 - J0;
         MIDAS_TRY(expand_b(c, kw, rt, lu.A + (long long)J0 * lda + J1, lda, 1, bexp, 2 * kw));
         MIDAS_TRY(gemm(rt, 2 * rt, 2 * kw, Af + 2 * ((long long)J1 * lda + J0), 2 * lda, bexp, 2 * kw,
-                       Af + 2 * ((long long)J1 * lda + J1), 2 * lda, -1.f, 1.f, 0));
+                       Af + 2 * ((long long)J1 * lda + J1), 2 * lda, -1.f, 1.f, 0, MIDAS_KC_GEMM_TC));
     }
     return MIDAS_OK;
 }
@@ -297,13 +297,13 @@ int lu_solve(midas_gpu_ctx *c, const DenseLU &lu, float2 *R, int nrhs)
             const int rows = K1 - (r0 + nb);
             if (rows > 0) {
                 GemmArgs g{rows, 2 * nrhs, 2 * nb, Af + 2 * ((r0 + nb) * lda + r0), 2 * lda, Bt + 2 * (r0 - K0), ldb,
-                           Rtf + 2LL * (r0 + nb) * nrhs, 2LL * nrhs, -1.f, 1.f};
+                           Rtf + 2LL * (r0 + nb) * nrhs, 2LL * nrhs, -1.f, 1.f, 0, MIDAS_KC_GEMM_SOLVE};
                 MIDAS_TRY(gemm_tf32(c, g));
             }
         }
         if (K1 < n) {
             GemmArgs g{n - K1, 2 * nrhs, ldb, Af + 2 * (K1 * lda + K0), 2 * lda, Bt, ldb, Rtf + 2LL * K1 * nrhs,
-                       2LL * nrhs, -1.f, 1.f};
+                       2LL * nrhs, -1.f, 1.f, 0, MIDAS_KC_GEMM_SOLVE};
             MIDAS_TRY(gemm_tf32(c, g));
         }
     }
@@ -315,12 +315,13 @@ int lu_solve(midas_gpu_ctx *c, const DenseLU &lu, float2 *R, int nrhs)
             const int rows = r0 - K0;
             if (rows > 0) {
                 GemmArgs g{rows, 2 * nrhs, 2 * nb, Af + 2 * (K0 * lda + r0), 2 * lda, Bt + 2 * (r0 - K0), ldb,
-                           Rtf + 2LL * K0 * nrhs, 2LL * nrhs, -1.f, 1.f};
+                           Rtf + 2LL * K0 * nrhs, 2LL * nrhs, -1.f, 1.f, 0, MIDAS_KC_GEMM_SOLVE};
                 MIDAS_TRY(gemm_tf32(c, g));
             }
         }
         if (K0 > 0) {
-            GemmArgs g{K0, 2 * nrhs, ldb, Af + 2 * K0, 2 * lda, Bt, ldb, Rtf, 2LL * nrhs, -1.f, 1.f};
+            GemmArgs g{K0, 2 * nrhs, ldb, Af + 2 * K0, 2 * lda, Bt, ldb, Rtf, 2LL * nrhs, -1.f, 1.f, 0,
+                       MIDAS_KC_GEMM_SOLVE};
             MIDAS_TRY(gemm_tf32(c, g));
         }
     }

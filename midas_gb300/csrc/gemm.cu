@@ -684,7 +684,7 @@ static int gemm_tc(midas_gpu_ctx *c, const GemmArgs &g, bool precise)
         else   // long K: 4 stages, one D buffer (requested after the tile's k-blocks)
             k_gemm_tcp<4, 1><<<grid, TC_THREADS, tcp_smem(4, 1), c->stream>>>(ma, mb, md, g.M, g.N, g.K, g.alpha,
                                                                                g.beta, g.round_tf32, c->d_flag);
-        kp_end(c, kp, MIDAS_KC_GEMM_TC, 2.0 * g.M * g.N * g.K, gemm_bytes(g));
+        kp_end(c, kp, g.kclass, 2.0 * g.M * g.N * g.K, gemm_bytes(g));
         MIDAS_CUDA(c, cudaGetLastError());
         return MIDAS_OK;
     }
@@ -700,7 +700,7 @@ static int gemm_tc(midas_gpu_ctx *c, const GemmArgs &g, bool precise)
     else
         k_gemm_tc<false, 4><<<grd, TC_THREADS, tc_smem(4), c->stream>>>(ma, mb, g.M, g.N, g.K, g.D, g.ldd, g.alpha,
                                                                         g.beta, g.round_tf32, c->d_flag);
-    kp_end(c, kp, MIDAS_KC_GEMM_TC, 2.0 * g.M * g.N * g.K, gemm_bytes(g));
+    kp_end(c, kp, g.kclass, 2.0 * g.M * g.N * g.K, gemm_bytes(g));
     MIDAS_CUDA(c, cudaGetLastError());
     return MIDAS_OK;
 }

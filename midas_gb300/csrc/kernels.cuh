@@ -73,6 +73,7 @@ struct GemmArgs {
     float *D; long long ldd;
     float alpha, beta;
     int round_tf32 = 0;   // store D rounded to TF32 (final L / U factor entries)
+    int kclass = MIDAS_KC_GEMM_TC;   // kernel class for the profiler
 };
 // precise = periodic promotion of the tensor-core partial sums to FP32 registers
 int gemm_tf32(midas_gpu_ctx *c, const GemmArgs &g, bool precise = false);
