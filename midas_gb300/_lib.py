@@ -22,7 +22,7 @@ FILL_FAITHFUL, FILL_FAST = 0, 1
 CBFM_SR, CBFM_HOMOG, CBFM_ACA, CBFM_FAST_CBF = 1, 2, 4, 8
 # kernel classes of midas_gpu_profile_query (MIDAS_KC_* in the header)
 KCLASSES = ["gemm_trail", "gemm_simt", "fill", "sr_scan", "diag_lu", "trsv", "resid", "zgemm64", "eig", "other",
-            "gemm_panel", "gemm_solve", "gemm_prod"]
+            "gemm_panel", "gemm_solve", "gemm_prod", "split"]
 
 # every symbol the header declares (checked by the CPU tests)
 EXPORTS = [

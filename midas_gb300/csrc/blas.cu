@@ -60,6 +60,8 @@ __global__ void k_split_a(int M, int K, const T *src, long long rs, long long cs
         row[2 * k] = hr; row[2 * k + 1] = hi_;
         row[2 * K + 2 * k] = hr; row[2 * K + 2 * k + 1] = hi_;
         row[4 * K + 2 * k] = lr; row[4 * K + 2 * k + 1] = li;
+        if (k == K - 1)   // the padding columns of the row
+            for (long long p = 6LL * K; p < lda3; ++p) row[p] = 0.f;
     }
 }
 
@@ -79,6 +81,8 @@ __global__ void k_split_expand_b(int K, int N, const T *src, long long rs, long 
         r0[2 * k] = hr; r0[2 * k + 1] = -hi_; r1[2 * k] = hi_; r1[2 * k + 1] = hr;
         r0[2 * K + 2 * k] = lr; r0[2 * K + 2 * k + 1] = -li; r1[2 * K + 2 * k] = li; r1[2 * K + 2 * k + 1] = lr;
         r0[4 * K + 2 * k] = hr; r0[4 * K + 2 * k + 1] = -hi_; r1[4 * K + 2 * k] = hi_; r1[4 * K + 2 * k + 1] = hr;
+        if (k == K - 1)
+            for (long long p = 6LL * K; p < ldb3; ++p) { r0[p] = 0.f; r1[p] = 0.f; }
     }
 }
 
@@ -92,19 +96,42 @@ int zgemm_x3(midas_gpu_ctx *c, int M, int N, int K, const TA *A, long long ars, 
     MIDAS_TRY(ensure(c, S_CBF8, sizeof(float) * (size_t)M * K6, &pa));
     MIDAS_TRY(ensure(c, S_CBF9, sizeof(float) * (size_t)2 * N * K6, &pb));
     float *A3 = (float *)pa, *B3 = (float *)pb;
-    if (K6 != 6LL * K) {   // keep the padding columns zero
-        MIDAS_CUDA(c, cudaMemsetAsync(A3, 0, sizeof(float) * (size_t)M * K6, c->stream));
-        MIDAS_CUDA(c, cudaMemsetAsync(B3, 0, sizeof(float) * (size_t)2 * N * K6, c->stream));
-    }
     ++c->launches;
+    int kp = kp_begin(c);
     k_split_a<TA><<<dim3((K + 127) / 128, std::min(M, 65535)), 128, 0, c->stream>>>(M, K, A, ars, acs, conjA, A3, K6);
+    kp_end(c, kp, MIDAS_KC_SPLIT, 0.0, (double)M * K * sizeof(TA) + 4.0 * M * K6);
     ++c->launches;
+    kp = kp_begin(c);
     k_split_expand_b<TB><<<dim3((K + 127) / 128, std::min(N, 65535)), 128, 0, c->stream>>>(K, N, B, brs, bcs, B3,
                                                                                             K6);
+    kp_end(c, kp, MIDAS_KC_SPLIT, 0.0, (double)N * K * sizeof(TB) + 8.0 * N * K6);
     MIDAS_CUDA(c, cudaGetLastError());
     GemmArgs g{M, 2 * N, (int)K6, A3, K6, B3, K6, D, ldd, alpha, beta, 0, MIDAS_KC_GEMM_PROD};
     return gemm_tf32(c, g, true);
 }
+// the same product with A already split (hi | hi | lo rows of K6 floats, e.g.
+// written by launch_block_fill4_a3)
+template <typename TB>
+int zgemm_x3_a3(midas_gpu_ctx *c, int M, int N, int K, const float *A3, long long K6, const TB *B, long long brs,
+                long long bcs, float *D, long long ldd, float alpha, float beta)
+{
+    if (M <= 0 || N <= 0 || K <= 0) return MIDAS_OK;
+    if (K6 != (6LL * K + 3) / 4 * 4) return c->err.set(MIDAS_ERR_ARG, "zgemm_x3_a3: bad A3 stride");
+    void *pb;
+    MIDAS_TRY(ensure(c, S_CBF9, sizeof(float) * (size_t)2 * N * K6, &pb));
+    float *B3 = (float *)pb;
+    ++c->launches;
+    int kp = kp_begin(c);
+    k_split_expand_b<TB><<<dim3((K + 127) / 128, std::min(N, 65535)), 128, 0, c->stream>>>(K, N, B, brs, bcs, B3,
+                                                                                            K6);
+    kp_end(c, kp, MIDAS_KC_SPLIT, 0.0, (double)N * K * sizeof(TB) + 8.0 * N * K6);
+    MIDAS_CUDA(c, cudaGetLastError());
+    GemmArgs g{M, 2 * N, (int)K6, A3, K6, B3, K6, D, ldd, alpha, beta, 0, MIDAS_KC_GEMM_PROD};
+    return gemm_tf32(c, g, true);
+}
+template int zgemm_x3_a3<double2>(midas_gpu_ctx *, int, int, int, const float *, long long, const double2 *,
+                                  long long, long long, float *, long long, float, float);
+
 template int zgemm_x3<float2, double2>(midas_gpu_ctx *, int, int, int, const float2 *, long long, long long, int,
                                        const double2 *, long long, long long, float *, long long, float, float);
 template int zgemm_x3<double2, float2>(midas_gpu_ctx *, int, int, int, const double2 *, long long, long long, int,

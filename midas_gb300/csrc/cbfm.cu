@@ -40,6 +40,9 @@ int zgemm64(midas_gpu_ctx *c, int M, int N, int K, const double2 *A, long long a
 template <typename TA, typename TB>
 int zgemm_x3(midas_gpu_ctx *c, int M, int N, int K, const TA *A, long long ars, long long acs, int conjA,
              const TB *B, long long brs, long long bcs, float *D, long long ldd, float alpha, float beta);
+template <typename TB>
+int zgemm_x3_a3(midas_gpu_ctx *c, int M, int N, int K, const float *A3, long long K6, const TB *B, long long brs,
+                long long bcs, float *D, long long ldd, float alpha, float beta);
 int residual_df32(midas_gpu_ctx *c, int n, int nrhs, const float2 *Z, long long ldz, const float2 *Xh,
                   const float2 *Xl, const float2 *B, double2 *R);
 int heev_dev(midas_gpu_ctx *c, int batch, int m, double2 *A, long long lda, long long sa, double2 *H, double2 *V,
@@ -566,10 +569,8 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
         if (c->opts.verbose >= 1) fprintf(stderr, "[midas] aca: %d of %d pairs low-rank\n", n_far, npairs);
     }
     auto dense = [&](int i, int j) { return i == j || !use_aca || std::min(rank[pidx(i, j)], aca_itmax) >= aca_itmax; };
-    void *pz, *pt;
-    MIDAS_TRY(ensure(c, S_CBF6, sizeof(float2) * (size_t)3 * n * 3 * nbmax, &pz));
+    void *pt;
     MIDAS_TRY(ensure(c, S_CBF7, sizeof(float) * (size_t)3 * n * ldT + sizeof(float) * (size_t)Kt * ldT, &pt));
-    float2 *Zcol = (float2 *)pz;
     float *T = (float *)pt, *Zcf = T + (size_t)3 * n * ldT;
     for (int j = 0; j < nb; ++j) {
         const int nj = bo[j + 1] - bo[j];
@@ -581,10 +582,13 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
             int i1 = i;
             while (i1 < nb && dense(i1, j)) ++i1;
             const int r0 = bo[i], nr = bo[i1] - bo[i];
-            MIDAS_TRY(launch_block_fill4<float2>(c, nr, d_all + r0, nj, d_all + bo[j], 0, 0.0, 0, Zcol,
-                                                 (size_t)3 * nj, 1));
-            MIDAS_TRY(zgemm_x3<float2, double2>(c, 3 * nr, Kb[j], 3 * nj, Zcol, 3 * nj, 1, 0, Cj, 1, 3 * nj,
-                                                T + (size_t)3 * r0 * ldT + 2LL * koff[j], ldT, 1.f, 0.f));
+            // the fill writes the split-TF32 A operand (hi | hi | lo) directly
+            const long long K6 = (6LL * 3 * nj + 3) / 4 * 4;
+            void *pa;
+            MIDAS_TRY(ensure(c, S_CBF8, sizeof(float) * (size_t)3 * nr * K6, &pa));
+            MIDAS_TRY(launch_block_fill4_a3(c, nr, d_all + r0, nj, d_all + bo[j], (float *)pa, K6));
+            MIDAS_TRY(zgemm_x3_a3<double2>(c, 3 * nr, Kb[j], 3 * nj, (const float *)pa, K6, Cj, 1, 3LL * nj,
+                                           T + (size_t)3 * r0 * ldT + 2LL * koff[j], ldT, 1.f, 0.f));
             i = i1;
         }
         // low-rank pairs: T(rows of i, cols of j) = U (V C_j), FP64 products

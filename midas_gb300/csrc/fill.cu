@@ -265,6 +265,84 @@ __global__ void k_block_fill4(int n1, const int *idx1, int n2, const int *idx2, 
 }
 
 // ---------------------------------------------------------------------------
+// a4 fill straight into the split-TF32 A operand of the reduced-matrix product:
+// row r of A3 holds (hi | hi | lo) of the complex(4) entries Z(r, 0..K), hi =
+// TF32(z), lo = TF32(z - hi) (the layout zgemm_x3 builds), so the complex(4)
+// block is never stored on its own.  Entries are those of mode 0 of
+// k_block_fill4; the padding columns 6K..lda3 of each row are zeroed.
+// ---------------------------------------------------------------------------
+template <bool LAT>
+__global__ void k_block_fill4_a3(int n1, const int *idx1, int n2, const int *idx2, const double *x, const double *y,
+                                 const double *z, const double2 *znnpp, const float2 *fk4, double k0, double Pi,
+                                 Lat lat, const float2 *tab4, float *A3, long long lda3)
+{
+    int js = blockIdx.x * blockDim.x + threadIdx.x;
+    int io = blockIdx.y * blockDim.y + threadIdx.y;
+    const long long K = 3LL * n2;
+    float2 V[9];
+    const bool live = js < n2 && io < n1;   // every thread reaches the staging barrier
+    const int o = live ? idx1[io] : 0, s = live ? idx2[js] : 0;
+    if (!live) {
+#pragma unroll
+        for (int e = 0; e < 9; ++e) V[e] = make_float2(0.f, 0.f);
+    } else if (o == s) {
+        float2 dg = make_float2((float)(1 - znnpp[s].x), (float)(-znnpp[s].y));
+#pragma unroll
+        for (int p = 0; p < 3; ++p)
+#pragma unroll
+            for (int q = 0; q < 3; ++q) V[p * 3 + q] = (p == q) ? dg : make_float2(0.f, 0.f);
+    } else {
+        float2 F[6];
+        if (LAT) {
+            size_t sl = lat.slot(o, s);
+#pragma unroll
+            for (int cc = 0; cc < 6; ++cc) F[cc] = tab4[6 * sl + cc];
+        } else {
+            dyadF4(x[o] - x[s], y[o] - y[s], z[o] - z[s], k0, Pi, F);
+        }
+        const float2 fk = fk4[s];
+#pragma unroll
+        for (int p = 0; p < 3; ++p)
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                float2 g = zmul4_rn(F[comp6(p, q)], fk);
+                V[p * 3 + q] = make_float2(-g.x, -g.y);
+            }
+    }
+    // stage the CTA's 6 rows x (64 cells x 3) complex entries (hi and lo) in shared
+    // memory, then write each row segment as one contiguous run
+    __shared__ float2 sh[6][192], sl[6][192];
+    const int tr = threadIdx.y, tc = threadIdx.x;
+#pragma unroll
+    for (int p = 0; p < 3; ++p)
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const float2 v = V[p * 3 + q];
+            const float hr = tf32_rna(v.x), hi = tf32_rna(v.y);
+            sh[3 * tr + p][3 * tc + q] = make_float2(hr, hi);
+            sl[3 * tr + p][3 * tc + q] = make_float2(tf32_rna(v.x - hr), tf32_rna(v.y - hi));
+        }
+    __syncthreads();
+    const int js0 = blockIdx.x * blockDim.x, io0 = blockIdx.y * blockDim.y;
+    const int ncol = 3 * min(64, n2 - js0);                       // complex columns of this CTA
+    const int nrow = 3 * min((int)blockDim.y, n1 - io0);
+    const long long kc0 = 3LL * js0;
+    for (int t = threadIdx.y * blockDim.x + threadIdx.x; t < nrow * ncol; t += blockDim.x * blockDim.y) {
+        const int rr = t / ncol, cc = t % ncol;
+        float2 *row = (float2 *)(A3 + (3LL * io0 + rr) * lda3);
+        const float2 h = sh[rr][cc];
+        row[kc0 + cc] = h;
+        row[K + kc0 + cc] = h;
+        row[2 * K + kc0 + cc] = sl[rr][cc];
+    }
+    if (js0 + 64 >= n2)   // the CTA holding the last columns zeroes the row padding
+        for (int t = threadIdx.y * blockDim.x + threadIdx.x; t < nrow; t += blockDim.x * blockDim.y) {
+            float *row = A3 + (3LL * io0 + t) * lda3;
+            for (long long pad = 6 * K; pad < lda3; ++pad) row[pad] = 0.f;
+        }
+}
+
+// ---------------------------------------------------------------------------
 // setfSR scan: one pass over the extended block computes
 //   fnz   -- Green_s_tr_partial_FN (src/Green_functions.f90:176-287), and
 //   for each fSR of the ladder j: nnz_j and sum |g|^2 of SR_Green_s_tr_partial_FN
@@ -435,6 +513,24 @@ int launch_block_fill4(midas_gpu_ctx *c, int n1, const int *idx1, int n2, const 
         k_block_fill4<false, T><<<grd, blk, 0, c->stream>>>(n1, idx1, n2, idx2, c->x, c->y, c->z, c->znnpp, c->fk4,
                                                             c->k0, c->pi, l, nullptr, mode, thr, homog, out, rs, cs);
     kp_end(c, kp, MIDAS_KC_FILL, 0.0, 9.0 * n1 * n2 * sizeof(T));
+    MIDAS_CUDA(c, cudaGetLastError());
+    return MIDAS_OK;
+}
+int launch_block_fill4_a3(midas_gpu_ctx *c, int n1, const int *idx1, int n2, const int *idx2, float *A3,
+                          long long lda3)
+{
+    dim3 blk(64, 2);
+    dim3 grd((n2 + 63) / 64, (n1 + 1) / 2);
+    Lat l = make_lat(c);
+    ++c->launches;
+    int kp = kp_begin(c);
+    if (c->opts.fill_mode == MIDAS_FILL_FAST && use_lat(c))
+        k_block_fill4_a3<true><<<grd, blk, 0, c->stream>>>(n1, idx1, n2, idx2, c->x, c->y, c->z, c->znnpp, c->fk4,
+                                                           c->k0, c->pi, l, c->lat_tab4, A3, lda3);
+    else
+        k_block_fill4_a3<false><<<grd, blk, 0, c->stream>>>(n1, idx1, n2, idx2, c->x, c->y, c->z, c->znnpp, c->fk4,
+                                                            c->k0, c->pi, l, nullptr, A3, lda3);
+    kp_end(c, kp, MIDAS_KC_FILL, 0.0, 4.0 * 3 * n1 * (double)lda3);
     MIDAS_CUDA(c, cudaGetLastError());
     return MIDAS_OK;
 }

@@ -60,6 +60,9 @@ int launch_incident4(midas_gpu_ctx *c, int ncell, const int *idx, int ntr, const
 template <typename T>
 int launch_block_fill4(midas_gpu_ctx *c, int n1, const int *idx1, int n2, const int *idx2, int mode, double thr,
                        int homog, T *out, size_t rs, size_t cs);
+// Z(idx1 rows, idx2 cols) (mode 0) written as the split-TF32 A operand (hi | hi | lo)
+int launch_block_fill4_a3(midas_gpu_ctx *c, int n1, const int *idx1, int n2, const int *idx2, float *A3,
+                          long long lda3);
 int sr_ladder(midas_gpu_ctx *c, int s_n, const int *d_idx, int first_cell, int homog, double res_sr, double *fsr_out,
               long long *nnz_out, int want_all, double *all_nnz, double *all_fn, double *fnz_out);
 
