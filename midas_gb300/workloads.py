@@ -32,6 +32,17 @@ def mom_c1():
             "method": "mom"}
 
 
+def mom_tiny():
+    """The reference's literal sphere case: x = 2, m = 1.5 + 0.01i, a/d = 4.775
+    (447 cells), +z incidence, V + H -- small enough for CPU tests."""
+    from . import geometry as G
+    a, x, m = 1.0, 2.0, 1.5 + 0.01j
+    sc = a / 4.775
+    xyz = G.sphere_cells(2 * a, sc)
+    return {"name": "mom_tiny_sphere_x2_ad4.775", "xyz": xyz, "sc": sc, "eps": np.full(len(xyz), m * m),
+            "k0": x / a, "th": np.array([90.0]), "ph": np.array([90.0]), "method": "mom"}
+
+
 def _gaussian_sphere_cbfm(name, x, a_over_d, ndir, nbox=3, seed=2026):
     from . import geometry as G
     a, m = 1.0, 1.55 + 0.005j
@@ -68,7 +79,7 @@ def cbfm_c2_small():
     return _gaussian_sphere_cbfm("cbfm_c2_small_gaussian_sphere_x6_ad12_2x2x2", 6.0, 12.0, 24, nbox=2)
 
 
-WORKLOADS = {"mom_c1": mom_c1, "cbfm_c2": cbfm_c2, "cbfm_c2_small": cbfm_c2_small}
+WORKLOADS = {"mom_c1": mom_c1, "mom_tiny": mom_tiny, "cbfm_c2": cbfm_c2, "cbfm_c2_small": cbfm_c2_small}
 
 
 def cbfm_args(wl):
