@@ -72,6 +72,13 @@ __global__ void k_ir_update(long long tot, int n, int m, double2 *X64, const flo
     if (Drm) Drm[o] = d32[i];   // the correction, for the FP32 residual update
 }
 
+// R = B (FP64 copy of the FP32 right-hand sides)
+__global__ void k_b_to_r64(long long tot, const float2 *B, double2 *R)
+{
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < tot) R[i] = make_double2(B[i].x, B[i].y);
+}
+
 // d32 = fp32(r); per-column max |r| and max |x| into red (bit patterns of >= 0 doubles)
 __global__ void k_r_to32(int n, int m, const double2 *r, float2 *d32, const double2 *X64,
                          unsigned long long *red)
@@ -219,16 +226,22 @@ static int cbf_block(midas_gpu_ctx *c, const CbfShared &S, int b)
         MIDAS_TRY(lu_solve(c, lu, d32, m));
         long long tot = (long long)sp * m;
         ++c->launches;
-        k_ir_update<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(tot, sp, m, X64, d32, Xh, Xl, nullptr, 1,
-                                                                          sr);
-        // Residuals: double-float B - Z x while the corrections are large; once the
+        k_ir_update<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(tot, sp, m, X64, d32, Xh, Xl,
+                                                                          sr ? Drm : nullptr, 1, sr);
+        // Residuals.  The first, B - Z x0, is needed only to ~1e-3 of itself (x0 from
+        // the TF32 factors is ~1e-3.5 off), so it is formed in FP32 on the CSR matrix.
+        // Then double-float B - Z x while the corrections are large; once the
         // relative residual is below 1e-5 every later correction d is ~1e-5 |x| or
         // smaller, and r - Z d in FP32 (error ~1e-6 |Z||d| over a row's ~3k
         // nonzeros) keeps the computed residual within ~1e-11 |x| of the true one.
         int it;
         bool upd = false;
         for (it = 0; it < 12; ++it) {
-            if (sr && upd)
+            if (sr && it == 0) {
+                ++c->launches;
+                k_b_to_r64<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(tot, Bm, R64);
+                MIDAS_TRY(residual_csr_update_f32(c, zcsr, m, Drm, R64));
+            } else if (sr && upd)
                 MIDAS_TRY(residual_csr_update_f32(c, zcsr, m, Drm, R64));
             else if (sr)
                 MIDAS_TRY(residual_csr_df32(c, zcsr, m, Xh, Xl, Bm, R64));
@@ -249,8 +262,8 @@ static int cbf_block(midas_gpu_ctx *c, const CbfShared &S, int b)
                 worst = std::max(worst, xn > 0 ? rn / xn : rn);
             }
             if (!(worst == worst)) return c->err.set(MIDAS_ERR_NOT_CONVERGED, "cbf block solve: NaN");
-            if (worst <= cbf_tol) break;
-            upd = sr && worst <= 1e-5;
+            if (worst <= cbf_tol && !(sr && it == 0)) break;   // the FP32 first residual never ends it
+            upd = sr && it > 0 && worst <= 1e-5;
             MIDAS_TRY(lu_solve(c, lu, d32, m));
             ++c->launches;
             k_ir_update<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(tot, sp, m, X64, d32, Xh, Xl,
