@@ -367,6 +367,8 @@ static int cbf_generate(midas_gpu_ctx *c, int nb, const CbfShared &S)
     }
     std::atomic<int> fail{0};
     std::vector<int> status(nl, MIDAS_OK);
+    const auto t0 = std::chrono::steady_clock::now();
+    std::vector<double> lane_ms(nl, 0.0);
     auto work = [&](int l) {
         midas_gpu_ctx *L = c->lanes[l];
         cudaSetDevice(L->device);
@@ -379,6 +381,7 @@ static int cbf_generate(midas_gpu_ctx *c, int nb, const CbfShared &S)
             status[l] = L->err.set(MIDAS_ERR_CUDA, "cbf lane: stream failed");
             fail = 1;
         }
+        lane_ms[l] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     };
     std::vector<std::thread> th;
     for (int l = 1; l < nl; ++l) th.emplace_back(work, l);
@@ -395,6 +398,11 @@ static int cbf_generate(midas_gpu_ctx *c, int nb, const CbfShared &S)
                 L->kprof.ms[k] = L->kprof.flops[k] = L->kprof.bytes[k] = 0; L->kprof.n[k] = 0;
             }
         }
+    }
+    if (c->opts.verbose >= 1) {
+        fprintf(stderr, "[midas] cbf lanes (finish ms / blocks):");
+        for (int l = 0; l < nl; ++l) fprintf(stderr, " %.0f/%zu", lane_ms[l], plan[l].size());
+        fprintf(stderr, "\n");
     }
     for (int l = 0; l < nl; ++l)
         if (status[l] != MIDAS_OK) return c->err.set(status[l], c->lanes[l]->err.msg);
