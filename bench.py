@@ -195,6 +195,28 @@ def cbfm_cpu_sample(wl):
     return T, desc
 
 
+def mom_cpu_sample(wl, cells_sample=3000):
+    """Bounded CPU sample of a large MoM solve: the oracle's FP64 fill and LAPACK solve
+    on the first `cells_sample` cells, scaled to the full size by order (fill N^2,
+    solve N^3).  Returns (seconds per step, description)."""
+    from oracle import oracle as O
+    import scipy.linalg as sla
+    O.build()
+    ns = min(cells_sample, len(wl["xyz"]))
+    cells = O.Cells(wl["xyz"][:ns], wl["sc"], wl["eps"][:ns], wl["k0"])
+    t0 = time.perf_counter()
+    Z = O.mom_fill(cells)
+    V = O.mom_rhs(cells, wl["th"], wl["ph"])
+    t1 = time.perf_counter()
+    sla.solve(Z, V, check_finite=False)
+    t2 = time.perf_counter()
+    r = len(wl["xyz"]) / ns
+    T = (t1 - t0) * r ** 2 + (t2 - t1) * r ** 3
+    desc = (f"oracle FP64 fill + LAPACK zgesv on the first {ns} cells ({3 * ns} unknowns): {t2 - t0:.1f} s measured, "
+            f"fill x{r ** 2:.0f} (N^2) and solve x{r ** 3:.0f} (N^3) to {len(wl['xyz'])} cells")
+    return T, desc
+
+
 def run_reference(args, wl, world, rank, pg):
     if rank != 0:
         return 0
@@ -205,7 +227,9 @@ def run_reference(args, wl, world, rank, pg):
     desc = None
     for it in range(args.warmup + args.steps):
         t0 = time.perf_counter()
-        if wl["method"] == "mom":
+        if wl["method"] == "mom" and 3 * len(wl["xyz"]) > 20000:
+            dt, desc = mom_cpu_sample(wl)
+        elif wl["method"] == "mom":
             O.mom_solve(cells, wl["th"], wl["ph"])
             dt = time.perf_counter() - t0
         else:
@@ -383,7 +407,7 @@ def run_ours(args, wl, world, rank, local, pg):
     # the plain FP64 MoM on the same GPU (cuSOLVER zgetrf), the metric's denominator
     fp64 = None
     if rank == 0 and not args.no_fp64:
-        if cbfm:
+        if cbfm or N > 20000:   # a full-size FP64 LU would take minutes to hours
             fp64 = fp64_mom_extrapolated(local, wl, value)
         else:
             c64 = Context(device=local, solve_mode=_lib.SOLVE_FP64)
@@ -402,6 +426,9 @@ def run_ours(args, wl, world, rank, local, pg):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         if cbfm:
             tc, desc = cbfm_cpu_sample(wl)
+            cpu = {"value": ntr / tc, "unit": "solves/s", "cores": os.cpu_count(), "kind": "port", "sample": desc}
+        elif N > 20000:
+            tc, desc = mom_cpu_sample(wl)
             cpu = {"value": ntr / tc, "unit": "solves/s", "cores": os.cpu_count(), "kind": "port", "sample": desc}
         else:
             from oracle import oracle as O

@@ -230,7 +230,8 @@ void *midas_gpu_stream(const midas_gpu_ctx *ctx);
 #define MIDAS_KC_GEMM_PANEL 10  /* tcgen05 GEMM: LU panel and U-row (forward substitution) steps */
 #define MIDAS_KC_GEMM_SOLVE 11  /* tcgen05 GEMM: triangular-solve updates */
 #define MIDAS_KC_GEMM_PROD  12  /* tcgen05 GEMM: split-TF32 products (reduced matrix, FP32-grade ZGEMM) */
-#define MIDAS_KC_COUNT     13
+#define MIDAS_KC_SPLIT      13  /* split-TF32 operand preparation (hi / lo pieces) */
+#define MIDAS_KC_COUNT     14
 /* enable = 1 clears the per-class totals and starts timing every instrumented
  * launch with CUDA events on the context stream; 0 stops.  Timing adds one event
  * record before and after each instrumented launch. */

@@ -32,6 +32,23 @@ def mom_c1():
             "method": "mom"}
 
 
+def mom_c3(n_cells=20000, ndir=32, seed=5):
+    """Mixed-precision dense solve on an inhomogeneous cube of side 2 lambda: a
+    28^3 lattice truncated to n_cells voxels (20,000: 60k unknowns), per-voxel
+    eps' ~ U[1.5, 3.5], eps'' ~ U[0, 0.2] (seeded), ndir seeded plane-wave
+    directions x 2 polarisations (64 right-hand sides)."""
+    from . import geometry as G
+    side = 28
+    d = 1.0 / side                      # cube side 1 = 2 lambda  ->  lambda = 0.5
+    k0 = 2 * math.pi / 0.5
+    rng = np.random.default_rng(seed)
+    xyz = G.cube_cells(side, d, n_cells)
+    eps = rng.uniform(1.5, 3.5, len(xyz)) + 1j * rng.uniform(0.0, 0.2, len(xyz))
+    th, ph = G.random_directions(ndir, seed=seed + 1)
+    return {"name": f"mom_c3_cube_2lambda_{len(xyz)}cells_{2 * ndir}rhs", "xyz": xyz, "sc": d, "eps": eps, "k0": k0,
+            "th": th, "ph": ph, "method": "mom"}
+
+
 def mom_tiny():
     """The reference's literal sphere case: x = 2, m = 1.5 + 0.01i, a/d = 4.775
     (447 cells), +z incidence, V + H -- small enough for CPU tests."""
@@ -79,7 +96,8 @@ def cbfm_c2_small():
     return _gaussian_sphere_cbfm("cbfm_c2_small_gaussian_sphere_x6_ad12_2x2x2", 6.0, 12.0, 24, nbox=2)
 
 
-WORKLOADS = {"mom_c1": mom_c1, "mom_tiny": mom_tiny, "cbfm_c2": cbfm_c2, "cbfm_c2_small": cbfm_c2_small}
+WORKLOADS = {"mom_c1": mom_c1, "mom_c3": mom_c3, "mom_tiny": mom_tiny, "cbfm_c2": cbfm_c2,
+             "cbfm_c2_small": cbfm_c2_small}
 
 
 def cbfm_args(wl):

@@ -81,6 +81,25 @@ def test_mom_solve_inhomogeneous_fast_fill(gpulib, oracle):
     c.close()
 
 
+def test_dense_c3_like_mixed_vs_fp64(gpulib, oracle):
+    """The inhomogeneous-cube dense solve (eps' ~ U[1.5,3.5], eps'' ~ U[0,0.2], 64 plane-wave
+    right-hand sides) at 1,600 voxels: the mixed TF32 LU + FP64 refinement reaches a backward
+    error <= 1e-8 (it goes to ~1e-14) and matches the FP64 LU and the oracle's LAPACK solve."""
+    from midas_gb300 import _lib, workloads as W
+    from midas_gb300.solver import Context
+    wl = W.mom_c3(n_cells=1600, ndir=32)
+    cm = Context(fill_mode=_lib.FILL_FAST).set_cells(wl["xyz"], wl["sc"], wl["eps"], wl["k0"])
+    Em = cm.mom_solve(wl["th"], wl["ph"])
+    assert Em.shape[1] == 64 and cm.info.backward_error <= 1e-8
+    cd = Context(solve_mode=_lib.SOLVE_FP64).set_cells(wl["xyz"], wl["sc"], wl["eps"], wl["k0"])
+    Ed = cd.mom_solve(wl["th"], wl["ph"])
+    assert np.linalg.norm(Em - Ed) / np.linalg.norm(Ed) < 1e-10
+    ref = oracle.mom_solve(oracle.Cells(wl["xyz"], wl["sc"], wl["eps"], wl["k0"]), wl["th"], wl["ph"])
+    assert np.linalg.norm(Em - ref["E"]) / np.linalg.norm(ref["E"]) < 1e-10
+    cm.close()
+    cd.close()
+
+
 def test_errors_are_reported(gpulib):
     from midas_gb300._lib import MidasError
     from midas_gb300.solver import Context
