@@ -200,26 +200,6 @@ int zgemm64(midas_gpu_ctx *c, int M, int N, int K, const double2 *A, long long a
 // (fp32 pairs, column-major ld = n), B fp32 column-major (ld n).  r is FP64.
 // Tile: 32 rows x 32 rhs per CTA (256 threads, 4 outputs each).
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
-{
-    s = a + b;
-    float bb = s - a;
-    e = (a - (s - bb)) + (b - bb);
-}
-
-struct DF {
-    float hi, lo;
-};
-__device__ __forceinline__ void df_add_prod(DF &acc, float a, float b)
-{
-    float p = a * b;
-    float pe = fmaf(a, b, -p);   // exact product = p + pe
-    float s, e;
-    two_sum(acc.hi, p, s, e);
-    acc.hi = s;
-    acc.lo += e + pe;
-}
-
 __global__ void __launch_bounds__(256) k_residual_df32(int n, int nrhs, const float2 *Z, long long ldz,
                                                         const float2 *Xh, const float2 *Xl, const float2 *B,
                                                         double2 *R)
@@ -230,9 +210,9 @@ __global__ void __launch_bounds__(256) k_residual_df32(int n, int nrhs, const fl
     int r0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
     int lr = tid / 8;          // row within tile (0..31)
     int lc = (tid % 8) * 4;    // 4 rhs columns per thread
-    DF accr[4], acci[4];
+    float arh[4], arl[4], aih[4], ail[4];
     float cr[4] = {0, 0, 0, 0}, ci[4] = {0, 0, 0, 0};   // lo-part products (plain fp32)
-    for (int q = 0; q < 4; ++q) { accr[q] = {0.f, 0.f}; acci[q] = {0.f, 0.f}; }
+    for (int q = 0; q < 4; ++q) arh[q] = arl[q] = aih[q] = ail[q] = 0.f;
     for (int k0 = 0; k0 < n; k0 += 32) {
         for (int t = tid; t < 32 * 32; t += 256) {
             int a = t / 32, b = t % 32;
@@ -250,10 +230,10 @@ __global__ void __launch_bounds__(256) k_residual_df32(int n, int nrhs, const fl
             for (int q = 0; q < 4; ++q) {
                 float2 xh = Xhs[k][lc + q], xl = Xls[k][lc + q];
                 // real: z.x*xh.x - z.y*xh.y ; imag: z.x*xh.y + z.y*xh.x (exact products)
-                df_add_prod(accr[q], z.x, xh.x);
-                df_add_prod(accr[q], -z.y, xh.y);
-                df_add_prod(acci[q], z.x, xh.y);
-                df_add_prod(acci[q], z.y, xh.x);
+                df_fma(arh[q], arl[q], z.x, xh.x);
+                df_fma(arh[q], arl[q], -z.y, xh.y);
+                df_fma(aih[q], ail[q], z.x, xh.y);
+                df_fma(aih[q], ail[q], z.y, xh.x);
                 cr[q] += z.x * xl.x - z.y * xl.y;
                 ci[q] += z.x * xl.y + z.y * xl.x;
             }
@@ -266,8 +246,8 @@ __global__ void __launch_bounds__(256) k_residual_df32(int n, int nrhs, const fl
     for (int q = 0; q < 4; ++q) {
         int col = c0 + lc + q;
         if (col >= nrhs) continue;
-        double zr = (double)accr[q].hi + (double)accr[q].lo + (double)cr[q];
-        double zi = (double)acci[q].hi + (double)acci[q].lo + (double)ci[q];
+        double zr = (double)arh[q] + (double)arl[q] + (double)cr[q];
+        double zi = (double)aih[q] + (double)ail[q] + (double)ci[q];
         float2 b = B[(long long)col * n + row];
         R[(long long)col * n + row] = make_double2((double)b.x - zr, (double)b.y - zi);
     }

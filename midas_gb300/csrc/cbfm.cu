@@ -656,7 +656,7 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
     }
     midas_gpu_info sinfo;
     memset(&sinfo, 0, sizeof(sinfo));
-    MIDAS_TRY(mixed_solve(c, npd, (float2 *)p32, (const double2 *)p64, Vc, (double2 *)px, nr, &sinfo));
+    MIDAS_TRY(mixed_solve(c, npd, (float2 *)p32, (double2 *)p64, Vc, (double2 *)px, nr, &sinfo));
     // E = C alpha per block
     double2 *Eout = E_user;
     void *peo = nullptr;

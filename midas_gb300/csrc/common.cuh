@@ -50,6 +50,31 @@ __device__ __forceinline__ float tf32_rna(float x)
     return __uint_as_float(u);
 }
 
+// Error-free transformations in FP32 for double-float (hi + lo) accumulation:
+// Knuth's TwoSum and the FMA TwoProduct.  The _rn intrinsics are never
+// contracted, so a product cannot be fused into the following sum (which would
+// make s differ from hi + p and break the exactness the pair relies on).
+__device__ __forceinline__ void ef_two_sum(float a, float b, float &s, float &e)
+{
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// (hi, lo) += (ah + al)(bh + bl): ah*bh exactly (TwoProduct), the cross terms
+// in FP32 (they are 2^-24 of the product), al*bl dropped (2^-48).
+__device__ __forceinline__ void df_fma(float &hi, float &lo, float ah, float bh, float al = 0.f, float bl = 0.f)
+{
+    const float p = __fmul_rn(ah, bh);
+    float pe = fmaf(ah, bh, -p);
+    pe = fmaf(ah, bl, pe);
+    pe = fmaf(al, bh, pe);
+    float s, e;
+    ef_two_sum(hi, p, s, e);
+    hi = s;
+    lo += e + pe;
+}
+
 // Reference Pi = Acos(-1.) evaluated in single precision (src/Initialization.f90:39).
 inline double ref_pi_host() { return (double)acosf(-1.0f); }
 
@@ -139,7 +164,7 @@ enum Slot : int {
     S_IN0 = 0, S_IN1, S_IN2, S_IN3, S_IN4, S_IN5, S_OUT0, S_OUT1,
     S_Z32, S_Z64, S_LINV, S_UINV, S_BEXP, S_BEXP2, S_RHS64, S_X64, S_R64, S_T32, S_T32B, S_RED,
     S_CBF0, S_CBF1, S_CBF2, S_CBF3, S_CBF4, S_CBF5, S_CBF6, S_CBF7, S_CBF8, S_CBF9, S_RED2, S_EINC,
-    S_ACA, S_SOLVE, S_CSR, S_NSLOTS
+    S_ACA, S_SOLVE, S_CSR, S_RPART, S_NSLOTS
 };
 
 }  // namespace midas

@@ -102,16 +102,27 @@ int lu_factor_nopiv(midas_gpu_ctx *c, DenseLU &lu);
 constexpr int LU_NB2 = 256;   // panel width of the two-level factorisation (slot S_BEXP2 holds 2n x 2 LU_NB2 floats)
 int lu_solve(midas_gpu_ctx *c, const DenseLU &lu, float2 *R, int nrhs);
 size_t lu_solve_scratch_bytes(int n, int nrhs);   // device scratch lu_solve takes from slot S_SOLVE
-// mixed-precision solve of Z x = b: Z64 row-major FP64 (for residuals), lu factored;
-// b/x are n x nrhs column-major FP64.
-int ir_solve(midas_gpu_ctx *c, const DenseLU &lu, const double2 *Z64, long long ldz, const double2 *b, double2 *x,
+// mixed-precision solve of Z x = b: Z64 row-major FP64 (n % 64 == 0), lu factored;
+// b/x are n x nrhs column-major FP64.  Z64 is overwritten with its double-float
+// split (float4 per element), which the refinement residuals read.
+int ir_solve(midas_gpu_ctx *c, const DenseLU &lu, double2 *Z64, long long ldz, const double2 *b, double2 *x,
              int nrhs, midas_gpu_info *info);
 int zgesv_fp64(midas_gpu_ctx *c, int n, int nrhs, double2 *Acol, double2 *Bcol, midas_gpu_info *info);
 void destroy_cusolver(void *h);
 // Mixed solve of a system whose FP64 row-major matrix Z64 and complex64 copy Z32
 // (np x np, padded to 64) are filled; b/x are np x nrhs column-major (ld np).
-int mixed_solve(midas_gpu_ctx *c, int np, float2 *Z32, const double2 *Z64, const double2 *b, double2 *x, int nrhs,
+// Both matrices are consumed (Z32 holds the factors, Z64 the split).
+int mixed_solve(midas_gpu_ctx *c, int np, float2 *Z32, double2 *Z64, const double2 *b, double2 *x, int nrhs,
                 midas_gpu_info *info);
-int inf_norm_rows(midas_gpu_ctx *c, const double2 *Z, long long ldz, int n, double *out);
+
+// refinement residuals on the FP32 cores (resid.cu)
+size_t resid_scratch_bytes(int n, int nrhs);   // slot S_RPART
+// Z64 (row-major, ldz) -> float4 (hi.re, hi.im, lo.re, lo.im) in place; ||Z||_inf
+int z_split_inplace(midas_gpu_ctx *c, double2 *Z64, long long ldz, int n, double *znorm);
+// r = base - Z X for X = x (double-float, df) or X = d (complex64, FP32 product);
+// r32 = fl32(r); rmax[j] = max over column j of max(|Re r|, |Im r|) (atomicMax of
+// the FP64 bits, caller zeroes).  base may alias r.  n % 64 == 0.
+int resid_dense(midas_gpu_ctx *c, int n, int nrhs, const float4 *Zs, long long ldz, bool df, const double2 *x,
+                const float2 *d, const double2 *base, double2 *r, float2 *r32, unsigned long long *rmax);
 
 }  // namespace midas

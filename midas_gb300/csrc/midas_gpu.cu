@@ -621,7 +621,7 @@ int midas_gpu_dense_solve(midas_gpu_ctx *c, int n, int nrhs, const double *A, do
         k_copy_pad<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>((const double2 *)pbin, n, np, nrhs,
                                                                          (double2 *)pb);
         MIDAS_CUDA(c, cudaGetLastError());
-        st = mixed_solve(c, np, (float2 *)p32, (const double2 *)p64, (const double2 *)pb, (double2 *)px, nrhs,
+        st = mixed_solve(c, np, (float2 *)p32, (double2 *)p64, (const double2 *)pb, (double2 *)px, nrhs,
                                 info);
         if (st == MIDAS_OK) {
             void *pout;
@@ -689,7 +689,7 @@ int midas_gpu_mom_solve(midas_gpu_ctx *c, int ntr, const double *theta, const do
         MIDAS_TRY(launch_mom_rhs<double2>(c, ntr, (const double *)th, (const double *)ph, (double2 *)pb, 1, np));
         float tfill = tf.stop();
         if (info) info->t_fill_ms = tfill;
-        st = mixed_solve(c, np, (float2 *)p32, (const double2 *)p64, (const double2 *)pb, (double2 *)px, nrhs,
+        st = mixed_solve(c, np, (float2 *)p32, (double2 *)p64, (const double2 *)pb, (double2 *)px, nrhs,
                                 info);
         if (st == MIDAS_OK) {
             void *pout;

@@ -137,6 +137,7 @@ extern "C" int midas_gpu_dense_solve_noalloc(int device, void *stream, int n, in
     slot(S_T32, sizeof(float2) * nn);
     slot(S_RED, sizeof(unsigned long long) * 3 * (size_t)nrhs + 64);
     slot(S_SOLVE, lu_solve_scratch_bytes(np, nrhs));
+    slot(S_RPART, resid_scratch_bytes(np, nrhs));
     slot(S_IN3, sizeof(double2) * (size_t)n * n);      // staging of A when it is host memory
     slot(S_IN2, sizeof(double2) * (size_t)n * nrhs);   // staging of B / output
     if (!cv.ok) return MIDAS_ERR_ARG;

@@ -126,23 +126,6 @@ int csr_from_dense(midas_gpu_ctx *c, int n, const float2 *Z, long long ldz, int 
 constexpr int RESID_COLS = 96;
 constexpr int RESID_T = RESID_COLS / 32;
 
-__device__ __forceinline__ void two_sum_f(float a, float b, float &s, float &e)
-{
-    s = a + b;
-    float bb = s - a;
-    e = (a - (s - bb)) + (b - bb);
-}
-
-__device__ __forceinline__ void dfa(float &hi, float &lo, float a, float b)
-{
-    float p = a * b;
-    float pe = fmaf(a, b, -p);
-    float s, e;
-    two_sum_f(hi, p, s, e);
-    hi = s;
-    lo += e + pe;
-}
-
 __global__ void __launch_bounds__(256) k_resid_csr_df32(int n, int m, const int *rowptr, const int *col,
                                                          const float2 *val, const float2 *Xh, const float2 *Xl,
                                                          const float2 *B, double2 *R)
@@ -173,10 +156,10 @@ __global__ void __launch_bounds__(256) k_resid_csr_df32(int n, int m, const int 
                 const int cc = c0 + lane + 32 * t;
                 if (cc < m) {
                     float2 h = xh[cc], l = xl[cc];
-                    dfa(rh[t], rl[t], z.x, h.x);
-                    dfa(rh[t], rl[t], -z.y, h.y);
-                    dfa(ih[t], il[t], z.x, h.y);
-                    dfa(ih[t], il[t], z.y, h.x);
+                    df_fma(rh[t], rl[t], z.x, h.x);
+                    df_fma(rh[t], rl[t], -z.y, h.y);
+                    df_fma(ih[t], il[t], z.x, h.y);
+                    df_fma(ih[t], il[t], z.y, h.x);
                     cr[t] += z.x * l.x - z.y * l.y;
                     ci[t] += z.x * l.y + z.y * l.x;
                 }

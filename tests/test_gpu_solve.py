@@ -29,6 +29,35 @@ def test_dense_solve_mixed(ctx, n, nrhs):
     assert ctx.info.backward_error <= 1e-13 and ctx.info.ir_iters >= 1
 
 
+def _true_backward_error(A, X, B):
+    """max over columns of |B - A X|_inf / (|A|_inf |X|_inf + |B|_inf), FP64 on the host,
+    with the solver's vector norm max(|Re|, |Im|)."""
+    R = B - A @ X
+    vn = lambda V: np.maximum(np.abs(V.real), np.abs(V.imag)).max(axis=0)
+    an = np.abs(A).sum(axis=1).max()
+    return float(np.max(vn(R) / (an * vn(X) + vn(B))))
+
+
+@pytest.mark.parametrize("n,nrhs,d,c", [(1000, 5, 1.5 + 0.3j, 0.4), (1000, 20, 1.5 + 0.3j, 0.4),
+                                         (640, 70, 1.0, 0.9)])
+def test_dense_solve_true_backward_error(ctx, n, nrhs, d, c):
+    """The refinement's residuals (FP32 first residual, double-float full residuals, FP32
+    updates r -= Z d) track the true FP64 residual: the backward error of the returned x,
+    measured on the host in FP64, is within the 1e-13 tolerance.  Both residual tile
+    shapes (<= 16 and > 16 right-hand sides), and a system d I + c G / sqrt(n) with its
+    eigenvalues out to 0.1 of the origin (c = 0.9), where the TF32 factors gain about a
+    digit per step and several double-float residuals run before the FP32 updates."""
+    rng = np.random.default_rng(n + nrhs)
+    A = c * (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) / np.sqrt(2 * n) + d * np.eye(n)
+    B = rng.standard_normal((n, nrhs)) + 1j * rng.standard_normal((n, nrhs))
+    X = ctx.dense_solve(A, B)
+    be = _true_backward_error(A, X, B)
+    assert be <= 2e-13, (be, ctx.info.backward_error, ctx.info.ir_iters)
+    assert ctx.info.backward_error <= 1e-13
+    Xr = np.linalg.solve(A, B)
+    assert np.linalg.norm(X - Xr) / np.linalg.norm(Xr) < 1e-11
+
+
 def test_dense_solve_torch_reference(ctx):
     """The LU/IR result against a plain PyTorch reference solve of the same system."""
     torch = pytest.importorskip("torch")
