@@ -264,7 +264,7 @@ def run_ours(args, wl, world, rank, local, pg):
     ntr = len(wl["th"])
     N = 3 * n
     # FAST fill: dyads from the per-lattice-offset tables (voxel scatterers sit on one lattice)
-    ctx = Context(device=local, fill_mode=_lib.FILL_FAST)
+    ctx = Context(device=local, fill_mode=_lib.FILL_FAST, ir_tol=wl.get("ir_tol", 1e-13))
     stream = torch.cuda.ExternalStream(ctx.stream_handle(), device=dev)
     # device-resident inputs
     xyz_d = torch.from_numpy(np.ascontiguousarray(wl["xyz"].T)).to(dev)
@@ -442,7 +442,7 @@ def run_ours(args, wl, world, rank, local, pg):
 
     if rank == 0:
         cfg = {"workload": wl["name"], "cells": n, "unknowns": N, "directions": ntr, "polarisations": 2,
-               "parallelism": f"replicas x{world}"}
+               "parallelism": f"replicas x{world}", "ir_tol": wl.get("ir_tol", 1e-13)}
         if cbfm:
             cfg.update({"blocks": len(bo) - 1, "cbf_excitations": int(2 * len(cth)), "K_total": int(Kb.sum()),
                         "K_min_max": [int(Kb.min()), int(Kb.max())], "flags": flags,

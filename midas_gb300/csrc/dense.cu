@@ -16,6 +16,16 @@
 // contiguous), so the L21 panel is a K-major TMA operand in place; the inverses
 // of the nb x nb diagonal blocks (unit-lower L^-1, upper U^-1) are kept for the
 // blocked triangular solves.
+//
+// The trailing update (the dominant GEMM) reads FP16 copies of its L and U
+// panels: every final L / U entry is stored rounded to TF32 (11-bit
+// significand), which FP16 holds exactly once the panel is scaled by a power of
+// two that puts its largest entry in [2^14, 2^15).  kind::f16 MMAs then form
+// the same products as kind::tf32 at half the operand bytes and twice the rate;
+// the epilogue multiplies by the inverse scales.  Entries more than 2^28 below
+// the panel maximum fall into the FP16 subnormal range (absolute error below
+// 2^-40 of the maximum, far under the TF32 rounding of the large entries).
+#include <cuda_fp16.h>
 #include <cusolverDn.h>
 #include <cmath>
 
@@ -115,6 +125,83 @@ __global__ void __launch_bounds__(512) k_diag_lu(float2 *A11, long long lda, flo
     }
 }
 
+// ---------------------------------------------------------------------------
+// FP16 panels of the trailing update
+// ---------------------------------------------------------------------------
+// max over rows x cols complex entries of max(|re|, |im|), as FP32 bits (>= 0)
+__global__ void k_panel_absmax(int rows0, int cols0, const float2 *A0, int rows1, int cols1, const float2 *A1,
+                               long long lda, unsigned *out)
+{
+    const int which = blockIdx.y;
+    const int rows = which ? rows1 : rows0, cols = which ? cols1 : cols0;
+    const float2 *A = which ? A1 : A0;
+    const long long tot = (long long)rows * cols;
+    float m = 0.f;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tot;
+         e += (long long)gridDim.x * blockDim.x) {
+        const float2 v = A[(e / cols) * lda + e % cols];
+        m = fmaxf(m, fmaxf(fabsf(v.x), fabsf(v.y)));
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m > 0.f) atomicMax(out + which, __float_as_uint(m));
+}
+
+// power of two taking the panel maximum into [2^14, 2^15)
+__device__ __forceinline__ float h16_scale(unsigned bits)
+{
+    const float m = __uint_as_float(bits);
+    if (!(m > 0.f) || m > 3.0e38f) return 1.f;
+    int e;
+    frexpf(m, &e);   // m = f 2^e, f in [0.5, 1)
+    return ldexpf(1.f, 15 - e);
+}
+
+// L panel (rows x kc complex, row-major lda) -> A16 rows of 2 kc fp16 (re, im
+// interleaved), scaled; alpha = -1 / (sL sU) for the update D -= L U.
+__global__ void k_pack_a16(int rows, int kc, const float2 *A, long long lda, const unsigned *mx, __half2 *A16,
+                           float *alpha)
+{
+    const float sl = h16_scale(mx[0]);
+    if (blockIdx.x == 0 && threadIdx.x == 0) *alpha = -1.f / (sl * h16_scale(mx[1]));
+    const long long tot = (long long)rows * kc;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tot;
+         e += (long long)gridDim.x * blockDim.x) {
+        const float2 v = A[(e / kc) * lda + e % kc];
+        A16[e] = __floats2half2_rn(v.x * sl, v.y * sl);
+    }
+}
+
+// U panel (k x n complex, element (p, j) at B[p * ldb + j]) -> Bt16 (2n rows of
+// 2k fp16): row 2j = (Br, -Bi), row 2j+1 = (Bi, Br) along p, scaled.  32 x 32
+// tiles through shared memory: reads along j and writes along p both coalesce.
+__global__ void k_expand_b16(int k, int n, const float2 *B, long long ldb, const unsigned *mx, __half2 *Bt,
+                             long long ldt2)
+{
+    __shared__ float2 t[32][33];
+    const float su = h16_scale(mx[1]);
+    const int p0 = blockIdx.x * 32, tx = threadIdx.x, ty = threadIdx.y;
+    for (int j0 = blockIdx.y * 32; j0 < n; j0 += gridDim.y * 32) {
+#pragma unroll
+        for (int q = 0; q < 32; q += 8) {
+            const int p = p0 + ty + q, j = j0 + tx;
+            t[ty + q][tx] = (p < k && j < n) ? B[(long long)p * ldb + j] : make_float2(0.f, 0.f);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < 32; q += 8) {
+            const int j = j0 + ty + q, p = p0 + tx;
+            if (j < n && p < k) {
+                const float2 b = t[tx][ty + q];
+                Bt[(long long)(2 * j) * ldt2 + p] = __floats2half2_rn(b.x * su, -b.y * su);
+                Bt[(long long)(2 * j + 1) * ldt2 + p] = __floats2half2_rn(b.y * su, b.x * su);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+size_t lu_h16_scratch_bytes(int n) { return sizeof(__half) * (size_t)3 * n * 2 * lu_panel_width(n) + 256; }
+
 constexpr int LU_NB = 64;
 
 int lu_factor_nopiv(midas_gpu_ctx *c, DenseLU &lu)
@@ -129,8 +216,21 @@ int lu_factor_nopiv(midas_gpu_ctx *c, DenseLU &lu)
     lu.Uinv = lu.Linv + (size_t)lu.nblk * nb * nb;
     MIDAS_TRY(ensure(c, S_BEXP, sizeof(float) * (size_t)(2 * nb) * (2 * nb), &p));
     float *uexp = (float *)p;
-    MIDAS_TRY(ensure(c, S_BEXP2, sizeof(float) * (size_t)2 * n * 2 * LU_NB2, &p));
+    const int nb2 = lu_panel_width(n);
+    MIDAS_TRY(ensure(c, S_BEXP2, lu_bexp2_bytes(n), &p));
     float *bexp = (float *)p;
+    // FP16 trailing-update panels (tcgen05 engine): A16 (n x 2 nb2), B16 (2n x 2 nb2), maxima, alpha
+    const bool h16 = gemm_tc_engine();
+    __half *a16 = nullptr, *b16 = nullptr;
+    unsigned *hmax = nullptr;
+    float *halpha = nullptr;
+    if (h16) {
+        MIDAS_TRY(ensure(c, S_H16, lu_h16_scratch_bytes(n), &p));
+        a16 = (__half *)p;
+        b16 = a16 + (size_t)n * 2 * nb2;
+        hmax = (unsigned *)(b16 + (size_t)2 * n * 2 * nb2);
+        halpha = (float *)(hmax + 2);
+    }
     const size_t smem = sizeof(float2) * 3 * nb * nb;
     static bool attr = false;
     if (!attr) {
@@ -146,12 +246,12 @@ int lu_factor_nopiv(midas_gpu_ctx *c, DenseLU &lu)
         GemmArgs g{M, N, K, A, la, B, lb, D, ld, alpha, beta, rnd, kc};
         return gemm_tf32(c, g);
     };
-    // Two levels: panels of LU_NB2 columns are factored with LU_NB-wide steps that
+    // Two levels: panels of nb2 columns are factored with LU_NB-wide steps that
     // update only the panel; the rows of U to the right of the panel follow by a
     // blocked forward substitution, and the trailing matrix takes one update with
-    // K = LU_NB2 -- a quarter of the trailing-matrix traffic of LU_NB-wide updates.
-    for (int J0 = 0; J0 < n; J0 += LU_NB2) {
-        const int J1 = std::min(n, J0 + LU_NB2);
+    // K = nb2 -- 1/4 (1/8) of the trailing-matrix traffic of LU_NB-wide updates.
+    for (int J0 = 0; J0 < n; J0 += nb2) {
+        const int J1 = std::min(n, J0 + nb2);
         for (int j0 = J0; j0 < J1; j0 += nb) {
             const int k = j0 / nb, rem = n - j0 - nb, wp = J1 - j0 - nb;
             float2 *A11 = lu.A + (long long)j0 * lda + j0;
@@ -189,6 +289,24 @@ int lu_factor_nopiv(midas_gpu_ctx *c, DenseLU &lu)
         }
         // trailing matrix: A(J1:n, J1:n) -= L(J1:n, J0:J1) U(J0:J1, J1:n), K = J1 - J0
         const int kw = J1 - J0;
+        if (h16) {
+            const float2 *Lp = lu.A + (long long)J1 * lda + J0, *Up = lu.A + (long long)J0 * lda + J1;
+            MIDAS_CUDA(c, cudaMemsetAsync(hmax, 0, 2 * sizeof(unsigned), c->stream));
+            const long long big = (long long)rt * kw;
+            const unsigned gx = (unsigned)std::min<long long>((big + 255) / 256, 4LL * 152);
+            c->launches += 3;
+            k_panel_absmax<<<dim3(gx, 2), 256, 0, c->stream>>>(rt, kw, Lp, kw, rt, Up, lda, hmax);
+            k_pack_a16<<<gx, 256, 0, c->stream>>>(rt, kw, Lp, lda, hmax, (__half2 *)a16, halpha);
+            k_expand_b16<<<dim3((kw + 31) / 32, (unsigned)std::min(65535, (rt + 31) / 32)), dim3(32, 8), 0,
+                           c->stream>>>(kw, rt, Up, lda, hmax, (__half2 *)b16, kw);
+            MIDAS_CUDA(c, cudaGetLastError());
+            GemmArgs g{rt, 2 * rt, 2 * kw, (const float *)a16, 2 * kw, (const float *)b16, 2 * kw,
+                       Af + 2 * ((long long)J1 * lda + J1), 2 * lda, -1.f, 1.f, 0, MIDAS_KC_GEMM_TC};
+            g.h16 = 1;
+            g.alpha_dev = halpha;
+            MIDAS_TRY(gemm_tf32(c, g));
+            continue;
+        }
         MIDAS_TRY(expand_b(c, kw, rt, lu.A + (long long)J0 * lda + J1, lda, 1, bexp, 2 * kw));
         MIDAS_TRY(gemm(rt, 2 * rt, 2 * kw, Af + 2 * ((long long)J1 * lda + J0), 2 * lda, bexp, 2 * kw,
                        Af + 2 * ((long long)J1 * lda + J1), 2 * lda, -1.f, 1.f, 0, MIDAS_KC_GEMM_TC));
@@ -347,10 +465,19 @@ __global__ void k_colmax(const double2 *v, int n, int nrhs, unsigned long long *
     if ((threadIdx.x & 31) == 0) atomicMax(out + k, __double_as_longlong(m));
 }
 
-__global__ void k_add_corr(double2 *x, const float2 *d, long long n)
+// x += d; dmax[j] = max over column j (ld n, n % 32 == 0) of max(|Re d|, |Im d|)
+__global__ void k_add_corr(double2 *x, const float2 *d, long long nn, int n, unsigned long long *dmax)
 {
-    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i < n) { x[i].x += d[i].x; x[i].y += d[i].y; }
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    double m = 0;
+    if (i < nn) {
+        const float2 v = d[i];
+        x[i].x += v.x;
+        x[i].y += v.y;
+        m = fmax(fabs((double)v.x), fabs((double)v.y));
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && i < nn) atomicMax(dmax + i / n, (unsigned long long)__double_as_longlong(m));
 }
 
 __global__ void k_to32(const double2 *v, long long n, float2 *out)
@@ -364,12 +491,15 @@ __global__ void k_to32(const double2 *v, long long n, float2 *out)
 // off, and each step gains ~3 decimal digits.  Residuals on the FP32 cores:
 //   step 0   r = b - Zh x0 in FP32: x0 is only ~1e-4 accurate, the ~1e-7
 //            error of the product does not limit the next correction;
-//   step 1   r = b - Z x in double-float (FP64 grade);
-//   later    r -= Zh d in FP32 once max|r| / (|Z| |x| + |b|) <= 1e-5: d is then
-//            below 1e-5 |x|, so the FP32 product adds < 1e-12 |Z| |x| per step,
-//            and the recursively updated r stays within ~1e-14 of the true one;
-//            otherwise another double-float residual.
-// The FP32 step-0 residual never ends the iteration.
+//   then     r = b - Z x in double-float (FP64 grade), or the update
+//            r -= Zh d in FP32 (d the correction just added to x).
+// An update moves r away from the true residual b - Z x by at most
+// g |Z|_inf |d|_inf (g = resid_update_error_factor: the FP32 partial sums of
+// the product).  That drift bound D is carried (reset by a double-float
+// residual, set to g after the FP32 step 0), an update is taken only while
+// D + g |d| / |x| stays within tol / 4, and convergence is accepted when
+// berr + D <= tol -- so the backward error of b - Z x in FP64 grade is within
+// the tolerance, whichever residual ended the iteration.
 int ir_solve(midas_gpu_ctx *c, const DenseLU &lu, double2 *Z64, long long ldz, const double2 *b, double2 *x,
              int nrhs, midas_gpu_info *info)
 {
@@ -385,62 +515,81 @@ int ir_solve(midas_gpu_ctx *c, const DenseLU &lu, double2 *Z64, long long ldz, c
     float2 *r32 = (float2 *)p;
     MIDAS_TRY(ensure(c, S_T32, sizeof(float2) * nn, &p));
     float2 *d32 = (float2 *)p;
-    MIDAS_TRY(ensure(c, S_RED, sizeof(unsigned long long) * 3 * nrhs + 64, &p));
+    MIDAS_TRY(ensure(c, S_RED, sizeof(unsigned long long) * 4 * nrhs + 64, &p));
+    // red: [0, nrhs) max|r|, [nrhs, 2 nrhs) max|x|, [2 nrhs, 3 nrhs) max|b|, [3 nrhs, 4 nrhs) max|d|
     unsigned long long *red = (unsigned long long *)p;
-    std::vector<unsigned long long> h(3 * nrhs);
-    // |b| per column; x = 0; r32 = fl32(b)
-    MIDAS_CUDA(c, cudaMemsetAsync(red, 0, sizeof(unsigned long long) * 3 * nrhs, c->stream));
+    std::vector<unsigned long long> h(4 * nrhs);
+    auto colmax = [&](int k, int slot) {
+        double v;
+        memcpy(&v, &h[(size_t)slot * nrhs + k], 8);
+        return v;
+    };
+    MIDAS_CUDA(c, cudaMemsetAsync(red, 0, sizeof(unsigned long long) * 4 * nrhs, c->stream));
     ++c->launches;
     k_colmax<<<dim3(64, nrhs), 256, 0, c->stream>>>(b, n, nrhs, red + 2 * nrhs);
     MIDAS_CUDA(c, cudaMemsetAsync(x, 0, sizeof(double2) * nn, c->stream));
     ++c->launches;
     k_to32<<<(unsigned)std::min<size_t>((nn + 255) / 256, 65535), 256, 0, c->stream>>>(b, (long long)nn, r32);
     MIDAS_CUDA(c, cudaGetLastError());
-    int it = 0;
-    double berr = 1e300;
     const double tol = c->opts.ir_tol > 0 ? c->opts.ir_tol : 1e-13;
     const int itmax = c->opts.ir_max_iter > 0 ? c->opts.ir_max_iter : 30;
-    bool upd = false;
-    for (it = 0; it < itmax; ++it) {
+    const double g = resid_update_error_factor(c, n, nrhs);
+    double berr = 1e300, drift = 1e300;
+    int it;
+    bool done = false;
+    for (it = 0; it < itmax && !done; ++it) {
         MIDAS_CUDA(c, cudaMemcpyAsync(d32, r32, sizeof(float2) * nn, cudaMemcpyDeviceToDevice, c->stream));
         MIDAS_TRY(lu_solve(c, lu, d32, nrhs));
-        ++c->launches;
-        k_add_corr<<<(unsigned)((nn + 255) / 256), 256, 0, c->stream>>>(x, d32, (long long)nn);
         MIDAS_CUDA(c, cudaMemsetAsync(red, 0, sizeof(unsigned long long) * 2 * nrhs, c->stream));
-        if (it == 0)   // x = d exactly
-            MIDAS_TRY(resid_dense(c, n, nrhs, Zs, ldz, false, nullptr, d32, b, r, r32, red));
-        else if (upd)
-            MIDAS_TRY(resid_dense(c, n, nrhs, Zs, ldz, false, nullptr, d32, r, r, r32, red));
-        else
-            MIDAS_TRY(resid_dense(c, n, nrhs, Zs, ldz, true, x, nullptr, b, r, r32, red));
+        MIDAS_CUDA(c, cudaMemsetAsync(red + 3 * nrhs, 0, sizeof(unsigned long long) * nrhs, c->stream));
+        ++c->launches;
+        k_add_corr<<<(unsigned)((nn + 255) / 256), 256, 0, c->stream>>>(x, d32, (long long)nn, n, red + 3 * nrhs);
         ++c->launches;
         k_colmax<<<dim3(64, nrhs), 256, 0, c->stream>>>(x, n, nrhs, red + nrhs);
         MIDAS_CUDA(c, cudaGetLastError());
-        MIDAS_CUDA(c, cudaMemcpyAsync(h.data(), red, sizeof(unsigned long long) * 3 * nrhs, cudaMemcpyDeviceToHost,
+        // |d| / |x| of this correction decides between an update and a double-float residual
+        double dn = 0;
+        if (it > 0) {
+            MIDAS_CUDA(c, cudaMemcpyAsync(h.data(), red, sizeof(unsigned long long) * 4 * nrhs,
+                                          cudaMemcpyDeviceToHost, c->stream));
+            MIDAS_CUDA(c, cudaStreamSynchronize(c->stream));
+            for (int k = 0; k < nrhs; ++k) {
+                const double xn = colmax(k, 1), dk = colmax(k, 3);
+                dn = std::max(dn, xn > 0 ? dk / xn : (dk > 0 ? 1e300 : 0.0));
+            }
+        }
+        const int mode = it == 0 ? 0 : (drift + g * dn <= 0.25 * tol ? 1 : 2);   // 0 fp32, 1 update, 2 double-float
+        if (mode == 0)   // x = d exactly
+            MIDAS_TRY(resid_dense(c, n, nrhs, Zs, ldz, false, nullptr, d32, b, r, r32, red));
+        else if (mode == 1)
+            MIDAS_TRY(resid_dense(c, n, nrhs, Zs, ldz, false, nullptr, d32, r, r, r32, red));
+        else
+            MIDAS_TRY(resid_dense(c, n, nrhs, Zs, ldz, true, x, nullptr, b, r, r32, red));
+        drift = mode == 0 ? g : mode == 1 ? drift + g * dn : 0.0;
+        MIDAS_CUDA(c, cudaMemcpyAsync(h.data(), red, sizeof(unsigned long long) * 4 * nrhs, cudaMemcpyDeviceToHost,
                                       c->stream));
         MIDAS_CUDA(c, cudaStreamSynchronize(c->stream));
         MIDAS_TRY(check_flag(c, "ir_solve"));
         berr = 0;
         for (int k = 0; k < nrhs; ++k) {
-            double rn, xn, bn;
-            memcpy(&rn, &h[k], 8);
-            memcpy(&xn, &h[nrhs + k], 8);
-            memcpy(&bn, &h[2 * nrhs + k], 8);
-            double den = znorm * xn + bn;
+            const double den = znorm * colmax(k, 1) + colmax(k, 2);
+            const double rn = colmax(k, 0);
             berr = fmax(berr, den > 0 ? rn / den : rn);
         }
         if (!(berr == berr)) return c->err.set(MIDAS_ERR_NOT_CONVERGED, "ir_solve: NaN residual");
-        if (berr <= tol && it > 0) { ++it; break; }
-        upd = it > 0 && berr <= 1e-5;
+        if (c->opts.verbose)
+            fprintf(stderr, "[midas] ir step %d (%s residual): backward error %.3e, drift bound %.1e\n", it,
+                    mode == 0 ? "fp32" : mode == 1 ? "fp32 update" : "double-float", berr, drift);
+        done = berr + drift <= tol;
     }
     if (info) {
         info->ir_iters = it;
-        info->backward_error = berr;
+        info->backward_error = berr + drift;
         info->anorm = znorm;
     }
-    if (berr > tol) {
+    if (!done) {
         char m[160];
-        snprintf(m, sizeof m, "iterative refinement stalled at backward error %.3e after %d steps", berr, it);
+        snprintf(m, sizeof m, "iterative refinement stalled at backward error %.3e after %d steps", berr + drift, it);
         return c->err.set(MIDAS_ERR_NOT_CONVERGED, m);
     }
     return MIDAS_OK;

@@ -15,6 +15,7 @@
 // Engine "simt": a register-tiled CUDA-core kernel used to validate the tensor
 // path on the device (gemm_selftest) and selectable with MIDAS_GEMM=simt.
 #include <cuda.h>
+#include <cuda_fp16.h>
 #include <cstdlib>
 #include <cstring>
 
@@ -158,6 +159,22 @@ __device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64
     asm volatile(
         "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
         "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+
+// kind::f16 with A/B fp16 (type 0), D f32: the same 11-bit operand significands
+// as TF32, half the bytes, twice the rate
+__host__ __device__ constexpr uint32_t idesc_f16(int M, int N)
+{
+    return (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                        uint32_t accumulate)
+{
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
         "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
 }
 
@@ -418,12 +435,14 @@ __device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, const void 
                  : "memory");
 }
 
-template <int STAGES, int DBUF>
+template <int STAGES, int DBUF, bool H16 = false>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_gemm_tcp(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                const __grid_constant__ CUtensorMap tmD, int M, int N, int K, float alpha, float beta, int rnd,
-               int *gflag)
+               const float *alpha_dev, int *gflag)
 {
+    // one k-block = one 128-byte swizzle row of each operand row: 32 fp32 or 64 fp16
+    constexpr int BKE = H16 ? 2 * TC_BK : TC_BK;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t *dsm = smem + STAGES * TC_STAGE_BYTES;                 // DBUF x 64 KB, 1024-aligned
@@ -438,7 +457,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
     const int mt = (M + TC_BM - 1) / TC_BM, nt = (N + TC_BN - 1) / TC_BN, ntiles = mt * nt;
-    const int nk = (K + TC_BK - 1) / TC_BK;
+    const int nk = (K + BKE - 1) / BKE;
     const bool use_d = beta != 0.f;
 
     if (threadIdx.x == 0) {
@@ -489,15 +508,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     if (!mbar_wait(&empty[s], (int)((kg / STAGES) + 1) & 1, abort_flag, gflag)) { ok = false; break; }
                     uint8_t *sa = smem + s * TC_STAGE_BYTES;
                     mbar_arrive_tx(&full[s], TC_STAGE_BYTES);
-                    tma_load_2d(sa, &tmA, &full[s], kb * TC_BK, m0);
-                    tma_load_2d(sa + TC_A_BYTES, &tmB, &full[s], kb * TC_BK, n0);
+                    tma_load_2d(sa, &tmA, &full[s], kb * BKE, m0);
+                    tma_load_2d(sa + TC_A_BYTES, &tmB, &full[s], kb * BKE, n0);
                 }
                 if (ok && use_d && DBUF == 1 && !load_d(li, m0, n0)) break;
             }
         }
     } else if (warp == 1) {
         if (lane == 0) {
-            const uint32_t idesc = idesc_tf32(TC_BM, TC_BN);
+            const uint32_t idesc = H16 ? idesc_f16(TC_BM, TC_BN) : idesc_tf32(TC_BM, TC_BN);
             long long kg = 0;
             int li = 0;
             bool ok = true;
@@ -512,15 +531,21 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                     const uint32_t sa = smem_u32(smem + s * TC_STAGE_BYTES), sb = sa + TC_A_BYTES;
 #pragma unroll
-                    for (int k4 = 0; k4 < TC_BK / 8; ++k4)
-                        mma_tf32(dst, smem_desc_sw128(sa + k4 * 32), smem_desc_sw128(sb + k4 * 32), idesc,
-                                 (kb > 0 || k4 > 0) ? 1u : 0u);
+                    for (int k4 = 0; k4 < 4; ++k4) {   // 32 bytes of K per MMA: 8 tf32 or 16 fp16
+                        const uint64_t ad = smem_desc_sw128(sa + k4 * 32), bd = smem_desc_sw128(sb + k4 * 32);
+                        const uint32_t acc = (kb > 0 || k4 > 0) ? 1u : 0u;
+                        if constexpr (H16)
+                            mma_f16(dst, ad, bd, idesc, acc);
+                        else
+                            mma_tf32(dst, ad, bd, idesc, acc);
+                    }
                     mma_commit(&empty[s]);
                 }
                 if (ok) mma_commit(&tfull[buf]);
             }
         }
     } else {
+        if (alpha_dev) alpha = *alpha_dev;               // set by an earlier kernel on the stream
         const int lg = warp % 4, et = threadIdx.x - 64;   // epilogue thread 0..127
         const int r = lg * 32 + lane;                     // tile row of this thread
         const uint32_t lane_base = (uint32_t)(lg * 32) << 16;
@@ -599,13 +624,17 @@ static int get_encode(midas_gpu_ctx *c)
     return MIDAS_OK;
 }
 
-static int make_map(midas_gpu_ctx *c, CUtensorMap *m, const float *base, int rows, int K, long long ld, int box_rows)
+// rows x K operand (ld elements per row) in 128-byte boxes along K: fp32, or fp16 when h16
+static int make_map(midas_gpu_ctx *c, CUtensorMap *m, const void *base, int rows, int K, long long ld, int box_rows,
+                    bool h16 = false)
 {
+    const int es_bytes = h16 ? 2 : 4;
     cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
-    cuuint64_t strides[1] = {(cuuint64_t)ld * 4};
-    cuuint32_t box[2] = {(cuuint32_t)TC_BK, (cuuint32_t)box_rows};
+    cuuint64_t strides[1] = {(cuuint64_t)ld * es_bytes};
+    cuuint32_t box[2] = {(cuuint32_t)(128 / es_bytes), (cuuint32_t)box_rows};
     cuuint32_t es[2] = {1, 1};
-    CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)base, dims, strides, box, es,
+    CUresult r = g_encode(m, h16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+                          (void *)base, dims, strides, box, es,
                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return c->err.set(MIDAS_ERR_CUDA, "cuTensorMapEncodeTiled failed");
@@ -625,6 +654,8 @@ static int pick_engine()
     return g_engine;
 }
 
+bool gemm_tc_engine() { return pick_engine() == 1; }
+
 // algorithmic bytes of one real GEMM: A and Bt once, D written (and read when beta != 0)
 static double gemm_bytes(const GemmArgs &g)
 {
@@ -642,11 +673,48 @@ static int gemm_simt(midas_gpu_ctx *c, const GemmArgs &g)
     return MIDAS_OK;
 }
 
+// FP16-operand persistent GEMM (A, Bt fp16 with ld in fp16 elements; D fp32)
+static int gemm_tcp_h16(midas_gpu_ctx *c, const GemmArgs &g)
+{
+    if ((((uintptr_t)g.D) & 15) || ((g.ldd * 4) & 15))
+        return c->err.set(MIDAS_ERR_ARG, "gemm fp16: D must be a 16-byte aligned TMA operand");
+    static int nsm = 0;
+    static bool pattr = false;
+    if (!nsm) MIDAS_CUDA(c, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
+    if (!pattr) {
+        MIDAS_CUDA(c, cudaFuncSetAttribute(k_gemm_tcp<2, 2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          tcp_smem(2, 2)));
+        MIDAS_CUDA(c, cudaFuncSetAttribute(k_gemm_tcp<4, 1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          tcp_smem(4, 1)));
+        pattr = true;
+    }
+    CUtensorMap ma, mb, md;
+    MIDAS_TRY(make_map(c, &ma, g.A, g.M, g.K, g.lda, TC_BM, true));
+    MIDAS_TRY(make_map(c, &mb, g.Bt, g.N, g.K, g.ldb, TC_BN, true));
+    MIDAS_TRY(make_map(c, &md, g.D, g.M, g.N, g.ldd, TC_BM));
+    const long long ntiles = (long long)((g.M + TC_BM - 1) / TC_BM) * ((g.N + TC_BN - 1) / TC_BN);
+    const int grid = (int)std::min<long long>(ntiles, nsm);
+    ++c->launches;
+    int kp = kp_begin(c);
+    if (g.K <= 512)   // the k-block count of the fp32 K <= 256 case
+        k_gemm_tcp<2, 2, true><<<grid, TC_THREADS, tcp_smem(2, 2), c->stream>>>(
+            ma, mb, md, g.M, g.N, g.K, g.alpha, g.beta, g.round_tf32, g.alpha_dev, c->d_flag);
+    else
+        k_gemm_tcp<4, 1, true><<<grid, TC_THREADS, tcp_smem(4, 1), c->stream>>>(
+            ma, mb, md, g.M, g.N, g.K, g.alpha, g.beta, g.round_tf32, g.alpha_dev, c->d_flag);
+    kp_end(c, kp, g.kclass, 2.0 * g.M * g.N * g.K,
+           2.0 * ((double)g.M * g.K + (double)g.N * g.K) + 4.0 * (double)g.M * g.N * (g.beta != 0.f ? 2 : 1));
+    MIDAS_CUDA(c, cudaGetLastError());
+    return MIDAS_OK;
+}
+
 static int gemm_tc(midas_gpu_ctx *c, const GemmArgs &g, bool precise)
 {
     MIDAS_TRY(get_encode(c));
-    if ((((uintptr_t)g.A) & 15) || (((uintptr_t)g.Bt) & 15) || (g.lda & 3) || (g.ldb & 3))
-        return c->err.set(MIDAS_ERR_ARG, "gemm_tf32: operands must be 16-byte aligned with ld % 4 == 0");
+    const int ldm = g.h16 ? 7 : 3;
+    if ((((uintptr_t)g.A) & 15) || (((uintptr_t)g.Bt) & 15) || (g.lda & ldm) || (g.ldb & ldm))
+        return c->err.set(MIDAS_ERR_ARG, "gemm_tf32: operands must be 16-byte aligned with 16-byte row strides");
+    if (g.h16) return gemm_tcp_h16(c, g);
     static bool attr = false;
     if (!attr) {
         MIDAS_CUDA(c, cudaFuncSetAttribute(k_gemm_tc<false, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -679,11 +747,11 @@ static int gemm_tc(midas_gpu_ctx *c, const GemmArgs &g, bool precise)
         ++c->launches;
         int kp = kp_begin(c);
         if (g.K <= 256)
-            k_gemm_tcp<2, 2><<<grid, TC_THREADS, tcp_smem(2, 2), c->stream>>>(ma, mb, md, g.M, g.N, g.K, g.alpha,
-                                                                               g.beta, g.round_tf32, c->d_flag);
+            k_gemm_tcp<2, 2><<<grid, TC_THREADS, tcp_smem(2, 2), c->stream>>>(
+                ma, mb, md, g.M, g.N, g.K, g.alpha, g.beta, g.round_tf32, g.alpha_dev, c->d_flag);
         else   // long K: 4 stages, one D buffer (requested after the tile's k-blocks)
-            k_gemm_tcp<4, 1><<<grid, TC_THREADS, tcp_smem(4, 1), c->stream>>>(ma, mb, md, g.M, g.N, g.K, g.alpha,
-                                                                               g.beta, g.round_tf32, c->d_flag);
+            k_gemm_tcp<4, 1><<<grid, TC_THREADS, tcp_smem(4, 1), c->stream>>>(
+                ma, mb, md, g.M, g.N, g.K, g.alpha, g.beta, g.round_tf32, g.alpha_dev, c->d_flag);
         kp_end(c, kp, g.kclass, 2.0 * g.M * g.N * g.K, gemm_bytes(g));
         MIDAS_CUDA(c, cudaGetLastError());
         return MIDAS_OK;
@@ -709,6 +777,7 @@ int gemm_tf32(midas_gpu_ctx *c, const GemmArgs &g, bool precise)
 {
     if (g.M <= 0 || g.N <= 0) return MIDAS_OK;
     if (g.K <= 0) return c->err.set(MIDAS_ERR_ARG, "gemm_tf32: K must be positive");
+    if (g.h16 && !pick_engine()) return c->err.set(MIDAS_ERR_ARG, "gemm_tf32: fp16 operands need the tcgen05 engine");
     return pick_engine() ? gemm_tc(c, g, precise) : gemm_simt(c, g);
 }
 
@@ -751,36 +820,67 @@ __global__ void k_fill_pattern(float *p, long long n, uint32_t seed)
     p[i] = ((h & 0xFFFF) / 32768.0f) - 1.0f;
 }
 
+__global__ void k_to_h16(float *p, __half *h, long long n, float *alpha)
+{
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i == 0) *alpha = -1.f;
+    if (i >= n) return;
+    const __half v = __float2half_rn(p[i]);
+    h[i] = v;
+    p[i] = __half2float(v);
+}
+
 int gemm_selftest(midas_gpu_ctx *c)
 {
     const int M = 300, N = 200, K = 136;   // ragged in every dimension
     size_t na = (size_t)M * K, nb = (size_t)N * K, nd = (size_t)M * N;
     void *buf;
-    MIDAS_TRY(ensure(c, S_T32, sizeof(float) * (na + nb + 2 * nd), &buf));
-    float *A = (float *)buf, *B = A + na, *D0 = B + nb, *D1 = D0 + nd;
+    MIDAS_TRY(ensure(c, S_T32, sizeof(float) * (na + nb + 3 * nd + 64) + sizeof(__half) * (na + nb), &buf));
+    float *A = (float *)buf, *B = A + na, *D0 = B + nb, *D1 = D0 + nd, *Di = D1 + nd, *dal = Di + nd;
+    __half *A16 = (__half *)(dal + 64), *B16 = A16 + na;
     ++c->launches;
     k_fill_pattern<<<(unsigned)((na + 255) / 256), 256, 0, c->stream>>>(A, (long long)na, 1u);
     ++c->launches;
     k_fill_pattern<<<(unsigned)((nb + 255) / 256), 256, 0, c->stream>>>(B, (long long)nb, 7u);
     ++c->launches;
-    k_fill_pattern<<<(unsigned)((nd + 255) / 256), 256, 0, c->stream>>>(D0, (long long)nd, 11u);
-    MIDAS_CUDA(c, cudaMemcpyAsync(D1, D0, sizeof(float) * nd, cudaMemcpyDeviceToDevice, c->stream));
-    GemmArgs g{M, N, K, A, K, B, K, D0, N, -1.0f, 1.0f};
-    MIDAS_TRY(gemm_simt(c, g));
-    g.D = D1;
-    MIDAS_TRY(gemm_tc(c, g, false));
+    k_fill_pattern<<<(unsigned)((nd + 255) / 256), 256, 0, c->stream>>>(Di, (long long)nd, 11u);
     std::vector<float> h0(nd), h1(nd);
-    MIDAS_CUDA(c, cudaMemcpyAsync(h0.data(), D0, sizeof(float) * nd, cudaMemcpyDeviceToHost, c->stream));
-    MIDAS_CUDA(c, cudaMemcpyAsync(h1.data(), D1, sizeof(float) * nd, cudaMemcpyDeviceToHost, c->stream));
-    MIDAS_CUDA(c, cudaStreamSynchronize(c->stream));
-    MIDAS_TRY(check_flag(c, "gemm_selftest"));
-    double md = 0;
-    for (size_t i = 0; i < nd; ++i) md = fmax(md, fabs((double)h0[i] - (double)h1[i]));
-    // TF32 operands: |err| <= K * 2^-10 * max|a||b| ~ 0.13 worst case; typical << 0.05
-    if (!(md < 0.05)) {
-        char msg[128];
-        snprintf(msg, sizeof msg, "tcgen05 GEMM self-test mismatch: max |diff| = %g", md);
-        return c->err.set(MIDAS_ERR_CUDA, msg);
+    // leg 0: fp32 operands (tf32 MMAs) against the SIMT engine; leg 1: the same
+    // operands rounded to fp16, kind::f16 MMAs with alpha read from device memory
+    for (int leg = 0; leg < 2; ++leg) {
+        if (leg == 1) {
+            c->launches += 2;
+            k_to_h16<<<(unsigned)((na + 255) / 256), 256, 0, c->stream>>>(A, A16, (long long)na, dal);
+            k_to_h16<<<(unsigned)((nb + 255) / 256), 256, 0, c->stream>>>(B, B16, (long long)nb, dal);
+        }
+        MIDAS_CUDA(c, cudaMemcpyAsync(D0, Di, sizeof(float) * nd, cudaMemcpyDeviceToDevice, c->stream));
+        MIDAS_CUDA(c, cudaMemcpyAsync(D1, Di, sizeof(float) * nd, cudaMemcpyDeviceToDevice, c->stream));
+        GemmArgs g{M, N, K, A, K, B, K, D0, N, -1.0f, 1.0f};
+        MIDAS_TRY(gemm_simt(c, g));
+        g.D = D1;
+        if (leg == 1) {
+            g.A = (const float *)A16;
+            g.Bt = (const float *)B16;
+            g.h16 = 1;
+            g.alpha = 0.f;   // must come from dal
+            g.alpha_dev = dal;
+        }
+        MIDAS_TRY(gemm_tc(c, g, false));
+        MIDAS_CUDA(c, cudaMemcpyAsync(h0.data(), D0, sizeof(float) * nd, cudaMemcpyDeviceToHost, c->stream));
+        MIDAS_CUDA(c, cudaMemcpyAsync(h1.data(), D1, sizeof(float) * nd, cudaMemcpyDeviceToHost, c->stream));
+        MIDAS_CUDA(c, cudaStreamSynchronize(c->stream));
+        MIDAS_TRY(check_flag(c, "gemm_selftest"));
+        double md = 0;
+        for (size_t i = 0; i < nd; ++i) md = fmax(md, fabs((double)h0[i] - (double)h1[i]));
+        // leg 0, TF32 operands: |err| <= K * 2^-10 * max|a||b| ~ 0.13 worst case, typical << 0.05;
+        // leg 1, exact fp16 operands: products exact, only the fp32 summation order differs
+        const double tol = leg == 0 ? 0.05 : 1e-3;
+        if (!(md < tol)) {
+            char msg[128];
+            snprintf(msg, sizeof msg, "tcgen05 GEMM self-test mismatch (%s operands): max |diff| = %g",
+                     leg == 0 ? "tf32" : "fp16", md);
+            return c->err.set(MIDAS_ERR_CUDA, msg);
+        }
     }
     return MIDAS_OK;
 }

@@ -77,7 +77,10 @@ struct GemmArgs {
     float alpha, beta;
     int round_tf32 = 0;   // store D rounded to TF32 (final L / U factor entries)
     int kclass = MIDAS_KC_GEMM_TC;   // kernel class for the profiler
+    int h16 = 0;                     // A, Bt are fp16 (__half*, ld in fp16 elements): kind::f16 MMAs
+    const float *alpha_dev = nullptr;   // when set, alpha is read from device memory at launch
 };
+bool gemm_tc_engine();   // the tcgen05 engine is selected (required for h16 operands)
 // precise = periodic promotion of the tensor-core partial sums to FP32 registers
 int gemm_tf32(midas_gpu_ctx *c, const GemmArgs &g, bool precise = false);
 // expand a complex k x n operand B (element (p,j) at B[p*rsb + j*csb], complex64) into
@@ -99,9 +102,14 @@ struct DenseLU {
 };
 int lu_factor_nopiv(midas_gpu_ctx *c, DenseLU &lu);
 // solve LU X = R in place; R is n x nrhs column-major complex64 (ld = n)
-constexpr int LU_NB2 = 256;   // panel width of the two-level factorisation (slot S_BEXP2 holds 2n x 2 LU_NB2 floats)
+// Panel width of the two-level factorisation: the trailing update reads and
+// writes the whole trailing matrix once per panel, so wide panels cut that
+// traffic; narrow ones keep the sequential in-panel work short on small systems.
+inline int lu_panel_width(int n) { return n >= 16384 ? 512 : 256; }
+inline size_t lu_bexp2_bytes(int n) { return sizeof(float) * (size_t)2 * n * 2 * lu_panel_width(n); }   // slot S_BEXP2
 int lu_solve(midas_gpu_ctx *c, const DenseLU &lu, float2 *R, int nrhs);
 size_t lu_solve_scratch_bytes(int n, int nrhs);   // device scratch lu_solve takes from slot S_SOLVE
+size_t lu_h16_scratch_bytes(int n);               // FP16 trailing-update panels, slot S_H16
 // mixed-precision solve of Z x = b: Z64 row-major FP64 (n % 64 == 0), lu factored;
 // b/x are n x nrhs column-major FP64.  Z64 is overwritten with its double-float
 // split (float4 per element), which the refinement residuals read.
@@ -117,6 +125,8 @@ int mixed_solve(midas_gpu_ctx *c, int np, float2 *Z32, double2 *Z64, const doubl
 
 // refinement residuals on the FP32 cores (resid.cu)
 size_t resid_scratch_bytes(int n, int nrhs);   // slot S_RPART
+// bound on |fl(Zh d) - Z d| / (|Z|_inf |d|_inf) of the FP32 product of resid_dense
+double resid_update_error_factor(midas_gpu_ctx *c, int n, int nrhs);
 // Z64 (row-major, ldz) -> float4 (hi.re, hi.im, lo.re, lo.im) in place; ||Z||_inf
 int z_split_inplace(midas_gpu_ctx *c, double2 *Z64, long long ldz, int n, double *znorm);
 // r = base - Z X for X = x (double-float, df) or X = d (complex64, FP32 product);

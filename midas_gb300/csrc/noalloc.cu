@@ -129,15 +129,16 @@ extern "C" int midas_gpu_dense_solve_noalloc(int device, void *stream, int n, in
     slot(S_Z32, sizeof(float2) * (size_t)np * np);
     slot(S_LINV, sizeof(float2) * (size_t)nblk * nb * nb * 2);
     slot(S_BEXP, sizeof(float) * (size_t)(2 * nb) * (2 * nb));
-    slot(S_BEXP2, sizeof(float) * (size_t)2 * np * 2 * LU_NB2);
+    slot(S_BEXP2, lu_bexp2_bytes(np));
     slot(S_RHS64, sizeof(double2) * nn);
     slot(S_X64, sizeof(double2) * nn);
     slot(S_R64, sizeof(double2) * nn);
     slot(S_T32B, sizeof(float2) * nn);
     slot(S_T32, sizeof(float2) * nn);
-    slot(S_RED, sizeof(unsigned long long) * 3 * (size_t)nrhs + 64);
+    slot(S_RED, sizeof(unsigned long long) * 4 * (size_t)nrhs + 64);
     slot(S_SOLVE, lu_solve_scratch_bytes(np, nrhs));
     slot(S_RPART, resid_scratch_bytes(np, nrhs));
+    slot(S_H16, lu_h16_scratch_bytes(np));
     slot(S_IN3, sizeof(double2) * (size_t)n * n);      // staging of A when it is host memory
     slot(S_IN2, sizeof(double2) * (size_t)n * nrhs);   // staging of B / output
     if (!cv.ok) return MIDAS_ERR_ARG;

@@ -134,7 +134,10 @@ __global__ void __launch_bounds__(RD_THREADS, 2)
         rd_commit();
         const V *zs = Zs + (size_t)(t % RD_STAGES) * TK * ZLD;
         const V *xs = Xs + (size_t)(t % RD_STAGES) * TK * TN;
-#pragma unroll
+        // the 4 x 4 micro-tile is unrolled; the k loop is not (fully unrolled, the
+        // double-float body is ~12k instructions and the kernel stalls on
+        // instruction fetch)
+#pragma unroll(DF ? 1 : 4)
         for (int kk = 0; kk < TK; ++kk) {
             V z[4], x[4];
 #pragma unroll
@@ -309,6 +312,14 @@ int launch_resid(midas_gpu_ctx *c, int n, int nrhs, const float4 *Z, long long l
 }
 
 }  // namespace
+
+double resid_update_error_factor(midas_gpu_ctx *c, int n, int nrhs)
+{
+    const int nsplit = rd_splits(c, n, nrhs);
+    const int kchunk = ((n + nsplit - 1) / nsplit + 63) / 64 * 64;
+    // sequential FP32 sums of kchunk products (gamma_k <= k u), the dropped Zl d (u), rounding of the product (u)
+    return (kchunk + 2) * 0x1p-24;
+}
 
 size_t resid_scratch_bytes(int n, int nrhs)
 {

@@ -36,7 +36,8 @@ def mom_c3(n_cells=20000, ndir=32, seed=5):
     """Mixed-precision dense solve on an inhomogeneous cube of side 2 lambda: a
     28^3 lattice truncated to n_cells voxels (20,000: 60k unknowns), per-voxel
     eps' ~ U[1.5, 3.5], eps'' ~ U[0, 0.2] (seeded), ndir seeded plane-wave
-    directions x 2 polarisations (64 right-hand sides)."""
+    directions x 2 polarisations (64 right-hand sides), refined to a 1e-8
+    backward error."""
     from . import geometry as G
     side = 28
     d = 1.0 / side                      # cube side 1 = 2 lambda  ->  lambda = 0.5
@@ -46,7 +47,13 @@ def mom_c3(n_cells=20000, ndir=32, seed=5):
     eps = rng.uniform(1.5, 3.5, len(xyz)) + 1j * rng.uniform(0.0, 0.2, len(xyz))
     th, ph = G.random_directions(ndir, seed=seed + 1)
     return {"name": f"mom_c3_cube_2lambda_{len(xyz)}cells_{2 * ndir}rhs", "xyz": xyz, "sc": d, "eps": eps, "k0": k0,
-            "th": th, "ph": ph, "method": "mom"}
+            "th": th, "ph": ph, "method": "mom", "ir_tol": 1e-8}
+
+
+def mom_c3_small():
+    """The same cube truncated to 4,000 voxels (12k unknowns, 3.5 GB of matrices):
+    the dense-solve kernels at a size a profiler captures in minutes."""
+    return mom_c3(n_cells=4000)
 
 
 def mom_tiny():
@@ -96,8 +103,8 @@ def cbfm_c2_small():
     return _gaussian_sphere_cbfm("cbfm_c2_small_gaussian_sphere_x6_ad12_2x2x2", 6.0, 12.0, 24, nbox=2)
 
 
-WORKLOADS = {"mom_c1": mom_c1, "mom_c3": mom_c3, "mom_tiny": mom_tiny, "cbfm_c2": cbfm_c2,
-             "cbfm_c2_small": cbfm_c2_small}
+WORKLOADS = {"mom_c1": mom_c1, "mom_c3": mom_c3, "mom_c3_small": mom_c3_small, "mom_tiny": mom_tiny,
+             "cbfm_c2": cbfm_c2, "cbfm_c2_small": cbfm_c2_small}
 
 
 def cbfm_args(wl):
@@ -115,9 +122,11 @@ def main(argv=None):
     ap.add_argument("workload", choices=sorted(WORKLOADS))
     ap.add_argument("--steps", type=int, default=1)
     ap.add_argument("--fill", default="fast", choices=["fast", "faithful"])
+    ap.add_argument("--verbose", action="store_true", help="library trace (refinement steps, CBFM lanes)")
     args = ap.parse_args(argv)
     wl = WORKLOADS[args.workload]()
-    ctx = Context(device=0, fill_mode=_lib.FILL_FAST if args.fill == "fast" else _lib.FILL_FAITHFUL)
+    ctx = Context(device=0, fill_mode=_lib.FILL_FAST if args.fill == "fast" else _lib.FILL_FAITHFUL,
+                  ir_tol=wl.get("ir_tol", 1e-13), verbose=int(args.verbose))
     ctx.set_cells(wl["xyz"], wl["sc"], wl["eps"], wl["k0"])
     for step in range(args.steps):
         t0 = time.perf_counter()

@@ -23,3 +23,12 @@ def test_small_cbfm_scene_partition():
     # every block has more unknowns than CBF excitations (a well-posed reduced system)
     assert np.min(3 * np.diff(bo)) > 2 * len(wl["cth"])
     assert wl["niws"] in (91, 190, 231) and len(wl["th"]) == 24   # initializeNipws table
+
+
+def test_dense_cube_scenes():
+    from midas_gb300.workloads import mom_c3, mom_c3_small
+    wl = mom_c3()
+    assert len(wl["xyz"]) == 20000 and len(wl["th"]) == 32 and wl["ir_tol"] == 1e-8
+    assert np.all((wl["eps"].real >= 1.5) & (wl["eps"].real <= 3.5))
+    assert np.all((wl["eps"].imag >= 0) & (wl["eps"].imag <= 0.2))
+    assert len(mom_c3_small()["xyz"]) == 4000
