@@ -61,9 +61,20 @@ __device__ __forceinline__ void ef_two_sum(float a, float b, float &s, float &e)
     e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 
-// (hi, lo) += (ah + al)(bh + bl): ah*bh exactly (TwoProduct), the cross terms
-// in FP32 (they are 2^-24 of the product), al*bl dropped (2^-48).
-__device__ __forceinline__ void df_fma(float &hi, float &lo, float ah, float bh, float al = 0.f, float bl = 0.f)
+// (hi, lo) += a * b exactly up to the FP32 rounding of lo (TwoProduct + TwoSum).
+__device__ __forceinline__ void df_fma(float &hi, float &lo, float a, float b)
+{
+    const float p = __fmul_rn(a, b);
+    const float pe = fmaf(a, b, -p);
+    float s, e;
+    ef_two_sum(hi, p, s, e);
+    hi = s;
+    lo += e + pe;
+}
+
+// (hi, lo) += (ah + al)(bh + bl): ah*bh exactly, the cross terms in FP32 (they
+// are 2^-24 of the product), al*bl dropped (2^-48).
+__device__ __forceinline__ void df_fma(float &hi, float &lo, float ah, float bh, float al, float bl)
 {
     const float p = __fmul_rn(ah, bh);
     float pe = fmaf(ah, bh, -p);

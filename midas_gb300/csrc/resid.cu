@@ -115,7 +115,9 @@ __global__ void __launch_bounds__(RD_THREADS, 2)
     };
 
     float ah[4][4], bh[4][4];
-    float al[4][4], bl[4][4];   // low parts (double-float only)
+    // double-float: the low parts; FP32: this k-tile's sums, added to (ah, bh) once
+    // per tile, so the rounding-error bound is ~(2 TK + K / TK) u instead of 2 K u
+    float al[4][4], bl[4][4];
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
@@ -134,6 +136,12 @@ __global__ void __launch_bounds__(RD_THREADS, 2)
         rd_commit();
         const V *zs = Zs + (size_t)(t % RD_STAGES) * TK * ZLD;
         const V *xs = Xs + (size_t)(t % RD_STAGES) * TK * TN;
+        if constexpr (!DF) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) al[i][j] = bl[i][j] = 0.f;
+        }
         // the 4 x 4 micro-tile is unrolled; the k loop is not (fully unrolled, the
         // double-float body is ~12k instructions and the kernel stalls on
         // instruction fetch)
@@ -155,9 +163,18 @@ __global__ void __launch_bounds__(RD_THREADS, 2)
                         df_fma(bh[i][j], bl[i][j], z[i].x, x[j].y, z[i].z, x[j].w);
                         df_fma(bh[i][j], bl[i][j], z[i].y, x[j].x, z[i].w, x[j].z);
                     } else {
-                        ah[i][j] = fmaf(z[i].x, x[j].x, fmaf(-z[i].y, x[j].y, ah[i][j]));
-                        bh[i][j] = fmaf(z[i].x, x[j].y, fmaf(z[i].y, x[j].x, bh[i][j]));
+                        al[i][j] = fmaf(z[i].x, x[j].x, fmaf(-z[i].y, x[j].y, al[i][j]));
+                        bl[i][j] = fmaf(z[i].x, x[j].y, fmaf(z[i].y, x[j].x, bl[i][j]));
                     }
+                }
+        }
+        if constexpr (!DF) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    ah[i][j] += al[i][j];
+                    bh[i][j] += bl[i][j];
                 }
         }
     }
@@ -317,8 +334,10 @@ double resid_update_error_factor(midas_gpu_ctx *c, int n, int nrhs)
 {
     const int nsplit = rd_splits(c, n, nrhs);
     const int kchunk = ((n + nsplit - 1) / nsplit + 63) / 64 * 64;
-    // sequential FP32 sums of kchunk products (gamma_k <= k u), the dropped Zl d (u), rounding of the product (u)
-    return (kchunk + 2) * 0x1p-24;
+    const int tk = nrhs <= 16 ? RdShape<16>::TK : RdShape<64>::TK;
+    // FMA chains of 2 TK real products per tile (re: zr xr - zi xi), the FP32 sum of
+    // the kchunk / TK tile sums, the dropped Zl d (u), the FP64 sum of the splits (< u)
+    return (2 * tk + kchunk / tk + 2) * 0x1p-24;
 }
 
 size_t resid_scratch_bytes(int n, int nrhs)
