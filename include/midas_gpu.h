@@ -211,6 +211,9 @@ int midas_gpu_zgemm_x3(midas_gpu_ctx *ctx, int M, int N, int K, const double *A,
 /* Average device time (CUDA events on the context stream) of `iters` launches of
  * the tensor-core GEMM D[M x N] -= A[M x K] Bt[N x K]^T on internal buffers (fp32). */
 int midas_gpu_bench_gemm(midas_gpu_ctx *ctx, int M, int N, int K, int iters, double *ms);
+/* The same with fp16 operands (the kind::f16 path of the LU trailing update) when
+ * f16 != 0; D stays fp32. */
+int midas_gpu_bench_gemm_ex(midas_gpu_ctx *ctx, int M, int N, int K, int iters, int f16, double *ms);
 /* Number of kernels this context has launched so far. */
 long long midas_gpu_launch_count(const midas_gpu_ctx *ctx);
 /* The context's CUDA stream (a cudaStream_t): every kernel of the context runs on it. */

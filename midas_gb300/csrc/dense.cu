@@ -51,22 +51,30 @@ __global__ void __launch_bounds__(512) k_diag_lu(float2 *A11, long long lda, flo
     const int tid = threadIdx.x, nt = blockDim.x;
     for (int i = tid; i < NB * NB; i += nt) a[i] = A11[(long long)(i / NB) * lda + (i % NB)];
     __syncthreads();
-    // right-looking elimination without pivoting
+    // right-looking elimination without pivoting; the update maps a thread to a
+    // column (tx) and every (nt / NB)-th row (ty), so no index division is needed
+    static_assert(NB == 64, "thread mapping assumes 64-wide blocks");
+    const int tx = tid % NB, ty = tid / NB, nty = nt / NB;
     for (int j = 0; j < NB; ++j) {
-        float2 piv = a[j * NB + j];
-        float pm = piv.x * piv.x + piv.y * piv.y;
-        if (tid == 0 && !(pm > tiny * tiny)) atomicOr(flag, DEV_ZERO_PIVOT);
-        float2 ip = make_float2(piv.x / pm, -piv.y / pm);
-        for (int i = j + 1 + tid; i < NB; i += nt) {
-            float2 v = a[i * NB + j];
+        if (tid < NB - j - 1) {
+            const float2 piv = a[j * NB + j];
+            const float pm = piv.x * piv.x + piv.y * piv.y;
+            const float2 ip = make_float2(piv.x / pm, -piv.y / pm);
+            const int i = j + 1 + tid;
+            const float2 v = a[i * NB + j];
             a[i * NB + j] = make_float2(v.x * ip.x - v.y * ip.y, v.x * ip.y + v.y * ip.x);
         }
+        if (tid == 0) {
+            const float2 piv = a[j * NB + j];
+            if (!(piv.x * piv.x + piv.y * piv.y > tiny * tiny)) atomicOr(flag, DEV_ZERO_PIVOT);
+        }
         __syncthreads();
-        int m = NB - j - 1;
-        for (int t = tid; t < m * m; t += nt) {
-            int i = j + 1 + t / m, cc = j + 1 + t % m;
-            float2 l = a[i * NB + j], u = a[j * NB + cc], d = a[i * NB + cc];
-            a[i * NB + cc] = make_float2(d.x - (l.x * u.x - l.y * u.y), d.y - (l.x * u.y + l.y * u.x));
+        if (tx > j) {
+            const float2 u = a[j * NB + tx];
+            for (int i = j + 1 + ty; i < NB; i += nty) {
+                const float2 l = a[i * NB + j], d = a[i * NB + tx];
+                a[i * NB + tx] = make_float2(d.x - (l.x * u.x - l.y * u.y), d.y - (l.x * u.y + l.y * u.x));
+            }
         }
         __syncthreads();
     }
@@ -249,7 +257,7 @@ int lu_factor_nopiv(midas_gpu_ctx *c, DenseLU &lu)
     // Two levels: panels of nb2 columns are factored with LU_NB-wide steps that
     // update only the panel; the rows of U to the right of the panel follow by a
     // blocked forward substitution, and the trailing matrix takes one update with
-    // K = nb2 -- 1/4 (1/8) of the trailing-matrix traffic of LU_NB-wide updates.
+    // K = nb2 -- 1/4 to 1/16 of the trailing-matrix traffic of LU_NB-wide updates.
     for (int J0 = 0; J0 < n; J0 += nb2) {
         const int J1 = std::min(n, J0 + nb2);
         for (int j0 = J0; j0 < J1; j0 += nb) {

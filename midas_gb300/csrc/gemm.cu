@@ -887,19 +887,30 @@ int gemm_selftest(midas_gpu_ctx *c)
 
 // Time `iters` launches of one M x N x K GEMM (D = D - A Bt^T) with CUDA events on
 // the context stream; returns the average device time per launch in *ms.
-int gemm_bench(midas_gpu_ctx *c, int M, int N, int K, int iters, double *ms)
+int gemm_bench(midas_gpu_ctx *c, int M, int N, int K, int iters, double *ms, bool f16)
 {
     if (M <= 0 || N <= 0 || K <= 0 || iters <= 0) return c->err.set(MIDAS_ERR_ARG, "bench_gemm: bad sizes");
+    if (f16 && (K % 8 || !gemm_tc_engine()))
+        return c->err.set(MIDAS_ERR_ARG, "bench_gemm: fp16 operands need K % 8 == 0 and the tcgen05 engine");
     size_t na = (size_t)M * K, nb = (size_t)N * K, nd = (size_t)M * N;
     void *buf;
-    MIDAS_TRY(ensure(c, S_T32, sizeof(float) * (na + nb + nd) + 256, &buf));
-    float *A = (float *)buf, *B = A + na, *D = B + nb;
+    MIDAS_TRY(ensure(c, S_T32, sizeof(float) * (na + nb + nd + 64) + sizeof(__half) * (na + nb) + 256, &buf));
+    float *A = (float *)buf, *B = A + na, *D = B + nb, *dal = D + nd;
+    __half *A16 = (__half *)(dal + 64), *B16 = A16 + na;
     ++c->launches;
     k_fill_pattern<<<(unsigned)((na + 255) / 256), 256, 0, c->stream>>>(A, (long long)na, 3u);
     ++c->launches;
     k_fill_pattern<<<(unsigned)((nb + 255) / 256), 256, 0, c->stream>>>(B, (long long)nb, 5u);
     MIDAS_CUDA(c, cudaMemsetAsync(D, 0, sizeof(float) * nd, c->stream));
     GemmArgs g{M, N, K, A, K, B, K, D, N, -1.0f, 1.0f};
+    if (f16) {
+        c->launches += 2;
+        k_to_h16<<<(unsigned)((na + 255) / 256), 256, 0, c->stream>>>(A, A16, (long long)na, dal);
+        k_to_h16<<<(unsigned)((nb + 255) / 256), 256, 0, c->stream>>>(B, B16, (long long)nb, dal);
+        g.A = (const float *)A16;
+        g.Bt = (const float *)B16;
+        g.h16 = 1;
+    }
     MIDAS_TRY(gemm_tf32(c, g));   // warm-up
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);

@@ -90,7 +90,7 @@ int expand_b(midas_gpu_ctx *c, int k, int n, const float2 *B, long long rsb, lon
 // which GEMM engine is active ("tcgen05" or "simt")
 const char *gemm_engine();
 int gemm_selftest(midas_gpu_ctx *c);
-int gemm_bench(midas_gpu_ctx *c, int M, int N, int K, int iters, double *ms);
+int gemm_bench(midas_gpu_ctx *c, int M, int N, int K, int iters, double *ms, bool f16 = false);
 
 // dense.cu
 struct DenseLU {
@@ -105,7 +105,7 @@ int lu_factor_nopiv(midas_gpu_ctx *c, DenseLU &lu);
 // Panel width of the two-level factorisation: the trailing update reads and
 // writes the whole trailing matrix once per panel, so wide panels cut that
 // traffic; narrow ones keep the sequential in-panel work short on small systems.
-inline int lu_panel_width(int n) { return n >= 16384 ? 512 : 256; }
+inline int lu_panel_width(int n) { return n >= 32768 ? 1024 : n >= 16384 ? 512 : 256; }
 inline size_t lu_bexp2_bytes(int n) { return sizeof(float) * (size_t)2 * n * 2 * lu_panel_width(n); }   // slot S_BEXP2
 int lu_solve(midas_gpu_ctx *c, const DenseLU &lu, float2 *R, int nrhs);
 size_t lu_solve_scratch_bytes(int n, int nrhs);   // device scratch lu_solve takes from slot S_SOLVE

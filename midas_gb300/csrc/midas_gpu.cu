@@ -818,6 +818,13 @@ int midas_gpu_bench_gemm(midas_gpu_ctx *c, int M, int N, int K, int iters, doubl
     return gemm_bench(c, M, N, K, iters, ms);
 }
 
+int midas_gpu_bench_gemm_ex(midas_gpu_ctx *c, int M, int N, int K, int iters, int f16, double *ms)
+{
+    if (!c || !ms) return MIDAS_ERR_ARG;
+    c->err = Err();
+    return gemm_bench(c, M, N, K, iters, ms, f16 != 0);
+}
+
 long long midas_gpu_launch_count(const midas_gpu_ctx *c) { return c ? c->launches : 0; }
 
 int midas_gpu_profile(midas_gpu_ctx *c, int enable)

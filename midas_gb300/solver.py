@@ -219,10 +219,11 @@ class Context:
         """cudaStream_t of the context (wrap with torch.cuda.ExternalStream to time on it)."""
         return int(self.L.midas_gpu_stream(self.h) or 0)
 
-    def bench_gemm(self, M, N, K, iters=20) -> float:
-        """Average ms per launch of one tensor-core GEMM (CUDA events on the context stream)."""
+    def bench_gemm(self, M, N, K, iters=20, f16=False) -> float:
+        """Average ms per launch of one tensor-core GEMM (CUDA events on the context stream);
+        fp16 operands (the LU trailing-update path) when f16."""
         ms = ctypes.c_double(0)
-        self._ck(self.L.midas_gpu_bench_gemm(self.h, M, N, K, iters, ctypes.byref(ms)))
+        self._ck(self.L.midas_gpu_bench_gemm_ex(self.h, M, N, K, iters, int(bool(f16)), ctypes.byref(ms)))
         return ms.value
 
     def heev(self, A):
