@@ -196,6 +196,129 @@ int zgemm64(midas_gpu_ctx *c, int M, int N, int K, const double2 *A, long long a
 }
 
 // ---------------------------------------------------------------------------
+// Gram matrix G = X^H X (m x m, row-major FP64) of a block's CBF solutions in
+// double float on the FP32 pipe (the FP64 pipe of GB300 runs at 1/64 of it).
+// X = Xh + Xl (the refinement's own hi/lo copies), element (k, j) at
+// X[k * rs + j * cs], k < K.  64 x 64 output tiles on the upper tile triangle,
+// K split S ways (the m <= ~200 Gram has only a handful of tiles); every CTA
+// writes its partial (hi, lo) pairs, and k_gram_reduce sums them in FP64 and
+// mirrors the upper triangle, so G is exactly Hermitian.  The products are exact
+// (FMA TwoProduct + cross terms) and the sums compensated: ~2^-48 relative, far
+// below the 1e-11 to which the refinement determines X.
+// ---------------------------------------------------------------------------
+constexpr int GR_TK = 8, GR_SMAX = 24;   // 2 stages x (A + B) x 8 x 64 float4 = 32 KB static shared memory
+
+__device__ __forceinline__ void gr_cp8(void *dst, const void *src, bool ok)
+{
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(sa), "l"(src), "r"(ok ? 8 : 0));
+}
+
+__global__ void __launch_bounds__(256) k_gram_df(int m, int K, const float2 *Xh, const float2 *Xl, long long rs,
+                                                  long long cs, int kchunk, float4 *P)
+{
+    __shared__ __align__(16) float4 As[2][GR_TK][64], Bs[2][GR_TK][64];
+    // tile pair (I, J), I <= J, from blockIdx.x; split from blockIdx.y
+    const int nt = (m + 63) / 64;
+    int t = blockIdx.x, I = 0;
+    while (t >= nt - I) { t -= nt - I; ++I; }
+    const int J = I + t, i0 = 64 * I, j0 = 64 * J, sp = blockIdx.y;
+    const int kb = sp * kchunk, ke = min(K, kb + kchunk);
+    const int nkt = ke > kb ? (ke - kb + GR_TK - 1) / GR_TK : 0;
+    const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
+    auto load = [&](int st, int k0) {
+        for (int e = tid; e < GR_TK * 64; e += 256) {
+            const int kk = e / 64, c = e % 64, k = k0 + kk;
+            const int ia = i0 + c, jb = j0 + c;
+            const bool oka = k < ke && ia < m, okb = k < ke && jb < m;
+            const long long oa = oka ? (long long)k * rs + (long long)ia * cs : 0;
+            const long long ob = okb ? (long long)k * rs + (long long)jb * cs : 0;
+            gr_cp8(&As[st][kk][c].x, Xh + oa, oka);
+            gr_cp8(&As[st][kk][c].z, Xl + oa, oka);
+            gr_cp8(&Bs[st][kk][c].x, Xh + ob, okb);
+            gr_cp8(&Bs[st][kk][c].z, Xl + ob, okb);
+        }
+        asm volatile("cp.async.commit_group;\n" ::);
+    };
+    float rh[4][4], rl[4][4], ih[4][4], il[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) rh[a][b] = rl[a][b] = ih[a][b] = il[a][b] = 0.f;
+    if (nkt > 0) load(0, kb);
+    for (int q = 0; q < nkt; ++q) {
+        if (q + 1 < nkt) {
+            load((q + 1) & 1, kb + (q + 1) * GR_TK);
+            asm volatile("cp.async.wait_group 1;\n" ::);
+        } else {
+            asm volatile("cp.async.wait_group 0;\n" ::);
+        }
+        __syncthreads();
+        const int st = q & 1;
+#pragma unroll 1
+        for (int kk = 0; kk < GR_TK; ++kk) {
+            float4 a[4], b[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) a[u] = As[st][kk][tx + 16 * u];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) b[u] = Bs[st][kk][ty + 16 * u];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int v = 0; v < 4; ++v) {
+                    // conj(a) b: re = ar br + ai bi, im = ar bi - ai br (hi = .x/.y, lo = .z/.w)
+                    df_fma(rh[u][v], rl[u][v], a[u].x, b[v].x, a[u].z, b[v].z);
+                    df_fma(rh[u][v], rl[u][v], a[u].y, b[v].y, a[u].w, b[v].w);
+                    df_fma(ih[u][v], il[u][v], a[u].x, b[v].y, a[u].z, b[v].w);
+                    df_fma(ih[u][v], il[u][v], -a[u].y, b[v].x, -a[u].w, b[v].z);
+                }
+        }
+        __syncthreads();   // stage st is refilled by the next iteration's prefetch
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const int i = i0 + tx + 16 * u, j = j0 + ty + 16 * v;
+            if (i < m && j < m) P[((long long)sp * m + i) * m + j] = make_float4(rh[u][v], ih[u][v], rl[u][v], il[u][v]);
+        }
+}
+
+__global__ void k_gram_reduce(int m, int nsplit, const float4 *P, double2 *G)
+{
+    const int i = blockIdx.y, j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= m || j < i) return;
+    double re = 0, im = 0;
+    for (int s = 0; s < nsplit; ++s) {
+        const float4 p = P[((long long)s * m + i) * m + j];
+        re += (double)p.x + (double)p.z;
+        im += (double)p.y + (double)p.w;
+    }
+    if (i == j) im = 0;   // conj(x) x is real; the exact products cancel to 0 already
+    G[(long long)i * m + j] = make_double2(re, im);
+    G[(long long)j * m + i] = make_double2(re, -im);
+}
+
+size_t gram_df_scratch_bytes(int m) { return sizeof(float4) * (size_t)GR_SMAX * m * m + 256; }
+
+int gram_df(midas_gpu_ctx *c, int m, int K, const float2 *Xh, const float2 *Xl, long long rs, long long cs,
+            double2 *G, float4 *P)
+{
+    if (m <= 0) return MIDAS_OK;
+    const int nt = (m + 63) / 64, npair = nt * (nt + 1) / 2;
+    const int nsplit = std::max(1, std::min(GR_SMAX, K / 512));
+    const int kchunk = (K + nsplit - 1) / nsplit;
+    ++c->launches;
+    int kp = kp_begin(c);
+    k_gram_df<<<dim3(npair, nsplit), 256, 0, c->stream>>>(m, K, Xh, Xl, rs, cs, kchunk, P);
+    kp_end(c, kp, MIDAS_KC_ZGEMM64, 8.0 * m * (double)m * K, 16.0 * (double)m * K + 16.0 * m * m);
+    ++c->launches;
+    k_gram_reduce<<<dim3((m + 127) / 128, m), 128, 0, c->stream>>>(m, nsplit, P, G);
+    MIDAS_CUDA(c, cudaGetLastError());
+    return MIDAS_OK;
+}
+
+// ---------------------------------------------------------------------------
 // double-float residual: r = B - Z X,  Z (n x n row-major fp32, ldz), X = Xh + Xl
 // (fp32 pairs, column-major ld = n), B fp32 column-major (ld n).  r is FP64.
 // Tile: 32 rows x 32 rhs per CTA (256 threads, 4 outputs each).

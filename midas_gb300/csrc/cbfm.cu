@@ -47,6 +47,9 @@ int residual_df32(midas_gpu_ctx *c, int n, int nrhs, const float2 *Z, long long 
                   const float2 *Xl, const float2 *B, double2 *R);
 int heev_dev(midas_gpu_ctx *c, int batch, int m, double2 *A, long long lda, long long sa, double2 *H, double2 *V,
              long long sv, double *W);
+size_t gram_df_scratch_bytes(int m);
+int gram_df(midas_gpu_ctx *c, int m, int K, const float2 *Xh, const float2 *Xl, long long rs, long long cs,
+            double2 *G, float4 *P);
 
 static inline int pad64(int x) { return (x + 63) / 64 * 64; }
 
@@ -270,9 +273,11 @@ static int cbf_block(midas_gpu_ctx *c, const CbfShared &S, int b)
                                                                               upd ? Drm : nullptr, 0, sr);
         }
         if (it == 12) return c->err.set(MIDAS_ERR_NOT_CONVERGED, "cbf block solve: refinement did not converge");
-        // Gram G = X^H X over the 3s rows of the extended block (FP64)
-        MIDAS_TRY(zgemm64(c, m, m, N3, X64, sp, 1, 1, X64, 1, sp, S.Gall + S.mm * b, m, 1, make_double2(1, 0),
-                          make_double2(0, 0)));
+        // Gram G = X^H X over the 3s rows of the extended block, in double float from
+        // the refinement's hi/lo copies of X (row-major with SR, column-major without)
+        void *pg;
+        MIDAS_TRY(ensure(c, S_CBF9, gram_df_scratch_bytes(m), &pg));
+        MIDAS_TRY(gram_df(c, m, N3, Xh, Xl, sr ? m : 1, sr ? 1 : sp, S.Gall + S.mm * b, (float4 *)pg));
         S.srefine[b] = it;
     }
     return MIDAS_OK;
@@ -319,8 +324,13 @@ static int get_lanes(midas_gpu_ctx *c, int nl)
         midas_gpu_ctx *L = new midas_gpu_ctx;
         L->device = c->device;
         L->pool.resize(S_NSLOTS);
+        const bool first = c->lanes.empty();
         c->lanes.push_back(L);
-        MIDAS_CUDA(c, cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking));
+        // lane 0 starts with the largest block, the critical path of the step: its
+        // stream has the highest priority, so its CTAs are scheduled first when SMs free up
+        int least = 0, greatest = 0;
+        MIDAS_CUDA(c, cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        MIDAS_CUDA(c, cudaStreamCreateWithPriority(&L->stream, cudaStreamNonBlocking, first ? greatest : least));
         MIDAS_CUDA(c, cudaMalloc(&L->d_flag, sizeof(int)));
         MIDAS_CUDA(c, cudaMemset(L->d_flag, 0, sizeof(int)));
     }
@@ -348,18 +358,15 @@ static int cbf_generate(midas_gpu_ctx *c, int nb, const CbfShared &S)
     const int nl = c->kprof.on ? 1 : std::min(nb, cbf_lanes());
     MIDAS_TRY(get_lanes(c, nl));
     MIDAS_CUDA(c, cudaStreamSynchronize(c->stream));   // the shared inputs are on the device
-    // largest blocks first, each to the least-loaded lane (cost ~ s^3)
+    // largest blocks first; lane 0 (highest-priority stream) takes the largest, and
+    // every lane then pulls the next block from a shared counter as it finishes one,
+    // so the lanes end within about one small block of each other
     std::vector<int> order(nb);
     for (int b = 0; b < nb; ++b) order[b] = b;
-    auto sz = [&](int b) { return (double)(S.xo[b + 1] - S.xo[b]); };
-    std::sort(order.begin(), order.end(), [&](int a, int b2) { return sz(a) > sz(b2); });
-    std::vector<std::vector<int>> plan(nl);
-    std::vector<double> load(nl, 0.0);
-    for (int b : order) {
-        int l = (int)(std::min_element(load.begin(), load.end()) - load.begin());
-        plan[l].push_back(b);
-        load[l] += sz(b) * sz(b) * sz(b);
-    }
+    auto sz = [&](int b) { return S.xo[b + 1] - S.xo[b]; };
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b2) { return sz(a) > sz(b2); });
+    std::atomic<int> next{nl > 1 ? 1 : 0};
+    std::vector<std::vector<int>> done_by(nl);
     std::vector<long long> l0(nl);
     for (int l = 0; l < nl; ++l) {
         lane_sync_cells(c->lanes[l], c);
@@ -372,10 +379,20 @@ static int cbf_generate(midas_gpu_ctx *c, int nb, const CbfShared &S)
     auto work = [&](int l) {
         midas_gpu_ctx *L = c->lanes[l];
         cudaSetDevice(L->device);
-        for (int b : plan[l]) {
+        for (int q = (l == 0 && nl > 1) ? 0 : next++; q < nb; q = next++) {
             if (fail.load()) break;
+            const int b = order[q];
+            done_by[l].push_back(b);
+            const auto tb = std::chrono::steady_clock::now();
             int st = cbf_block(L, S, b);
             if (st != MIDAS_OK) { status[l] = st; fail = 1; break; }
+            if (c->opts.verbose >= 2) {
+                cudaStreamSynchronize(L->stream);
+                const auto te = std::chrono::steady_clock::now();
+                fprintf(stderr, "[midas] cbf lane %d block %d (s=%d): %.0f -> %.0f ms\n", l, b, sz(b),
+                        std::chrono::duration<double, std::milli>(tb - t0).count(),
+                        std::chrono::duration<double, std::milli>(te - t0).count());
+            }
         }
         if (cudaStreamSynchronize(L->stream) != cudaSuccess && status[l] == MIDAS_OK) {
             status[l] = L->err.set(MIDAS_ERR_CUDA, "cbf lane: stream failed");
@@ -401,7 +418,7 @@ static int cbf_generate(midas_gpu_ctx *c, int nb, const CbfShared &S)
     }
     if (c->opts.verbose >= 1) {
         fprintf(stderr, "[midas] cbf lanes (finish ms / blocks):");
-        for (int l = 0; l < nl; ++l) fprintf(stderr, " %.0f/%zu", lane_ms[l], plan[l].size());
+        for (int l = 0; l < nl; ++l) fprintf(stderr, " %.0f/%zu", lane_ms[l], done_by[l].size());
         fprintf(stderr, "\n");
     }
     for (int l = 0; l < nl; ++l)

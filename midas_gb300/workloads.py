@@ -122,11 +122,12 @@ def main(argv=None):
     ap.add_argument("workload", choices=sorted(WORKLOADS))
     ap.add_argument("--steps", type=int, default=1)
     ap.add_argument("--fill", default="fast", choices=["fast", "faithful"])
-    ap.add_argument("--verbose", action="store_true", help="library trace (refinement steps, CBFM lanes)")
+    ap.add_argument("--verbose", "-v", action="count", default=0,
+                    help="library trace: -v refinement steps and CBFM lanes, -vv per-block detail")
     args = ap.parse_args(argv)
     wl = WORKLOADS[args.workload]()
     ctx = Context(device=0, fill_mode=_lib.FILL_FAST if args.fill == "fast" else _lib.FILL_FAITHFUL,
-                  ir_tol=wl.get("ir_tol", 1e-13), verbose=int(args.verbose))
+                  ir_tol=wl.get("ir_tol", 1e-13), verbose=args.verbose)
     ctx.set_cells(wl["xyz"], wl["sc"], wl["eps"], wl["k0"])
     for step in range(args.steps):
         t0 = time.perf_counter()
