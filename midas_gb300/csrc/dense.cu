@@ -210,6 +210,116 @@ __global__ void k_expand_b16(int k, int n, const float2 *B, long long ldb, const
 
 size_t lu_h16_scratch_bytes(int n) { return sizeof(__half) * (size_t)3 * n * 2 * lu_panel_width(n) + 256; }
 
+// ---------------------------------------------------------------------------
+// Inverses of the LU_MB x LU_MB (256) diagonal blocks of L and U, for the
+// triangular solves: one apply of a 256-row inverse replaces four applies of the
+// 64-row inverses and the three small GEMMs between them.  Built per panel
+// from the 64-block inverses D_i and the factor blocks inside the diagonal
+// block, by block substitution in FP32 on the CUDA cores (the operands are the
+// stored TF32-rounded factor entries):
+//   L: X_jj = D_j,  X_ij = -D_i sum_{k=j}^{i-1} L_ik X_kj        (i > j)
+//   U: X_jj = D_j,  X_ij = -D_i sum_{k=i+1}^{j} U_ik X_kj        (i < j)
+// One CTA per (diagonal block, block column j, L or U); X is stored transposed
+// (XT[c * LU_MB + r]) so that the apply reads it coalesced, zero outside the
+// triangle.
+// ---------------------------------------------------------------------------
+constexpr int MI_LD = 65;   // padded row stride of the 64 x 64 shared tiles
+
+// 64 x 64 block of a row-major complex matrix into a shared tile
+__device__ __forceinline__ void mi_load(float2 *t, const float2 *g, long long ld)
+{
+    for (int e = threadIdx.x; e < 64 * 64; e += blockDim.x) t[(e / 64) * MI_LD + (e % 64)] = g[(long long)(e / 64) * ld + (e % 64)];
+}
+
+// acc (this thread's 4 x 4 outputs, rows ty + 16a, cols tx + 16b) += A B
+__device__ __forceinline__ void mi_mma(const float2 *A, const float2 *B, float2 acc[4][4], int tx, int ty)
+{
+#pragma unroll 4
+    for (int k = 0; k < 64; ++k) {
+        float2 a[4], b[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) a[u] = A[(ty + 16 * u) * MI_LD + k];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) b[u] = B[k * MI_LD + tx + 16 * u];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int v = 0; v < 4; ++v) {
+                acc[u][v].x = fmaf(a[u].x, b[v].x, fmaf(-a[u].y, b[v].y, acc[u][v].x));
+                acc[u][v].y = fmaf(a[u].x, b[v].y, fmaf(a[u].y, b[v].x, acc[u][v].y));
+            }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_macro_inv(const float2 *A, long long lda, int n, int mac0,
+                                                    const float2 *Linv, const float2 *Uinv, float2 *MLinvT,
+                                                    float2 *MUinvT)
+{
+    extern __shared__ float2 mi_sm[];
+    float2 *As = mi_sm, *Bs = mi_sm + 64 * MI_LD;
+    const int mac = mac0 + blockIdx.x / 4, j = blockIdx.x % 4, upper = blockIdx.y;
+    const int I0 = mac * LU_MB, mb = min(LU_MB, n - I0), nbk = mb / 64;
+    if (j >= nbk) return;
+    const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
+    const float2 *D = upper ? Uinv : Linv;   // 64-block inverses, row-major
+    float2 *XT = (upper ? MUinvT : MLinvT) + (size_t)mac * LU_MB * LU_MB;
+    const float2 *Ab = A + (long long)I0 * lda + I0;
+    auto put = [&](int bi, const float2 acc[4][4], float sgn) {   // block (bi, j) of X from registers
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int v = 0; v < 4; ++v) {
+                const int r = 64 * bi + ty + 16 * u, cc = 64 * j + tx + 16 * v;
+                XT[(size_t)cc * LU_MB + r] = make_float2(sgn * acc[u][v].x, sgn * acc[u][v].y);
+            }
+    };
+    // zero blocks of column j outside the triangle, and the diagonal block D_j
+    for (int bi = 0; bi < LU_MB / 64; ++bi) {
+        const bool zero = bi >= nbk || (upper ? bi > j : bi < j);
+        if (!zero && bi != j) continue;
+        for (int e = tid; e < 64 * 64; e += blockDim.x) {
+            const int cc = e / 64, rr = e % 64;   // consecutive threads write consecutive rows
+            XT[(size_t)(64 * j + cc) * LU_MB + 64 * bi + rr] =
+                zero ? make_float2(0.f, 0.f) : D[(size_t)(I0 / 64 + j) * 4096 + rr * 64 + cc];
+        }
+    }
+    __syncthreads();
+    const int step = upper ? -1 : 1;
+    for (int i = j + step; upper ? i >= 0 : i < nbk; i += step) {
+        float2 acc[4][4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int v = 0; v < 4; ++v) acc[u][v] = make_float2(0.f, 0.f);
+        // T = sum over k between i and j of F_ik X_kj (F = L below, U above the diagonal)
+        const int k0 = upper ? i + 1 : j, k1 = upper ? j : i - 1;
+        for (int k = k0; k <= k1; ++k) {
+            mi_load(As, Ab + (long long)(64 * i) * lda + 64 * k, lda);
+            for (int e = tid; e < 64 * 64; e += blockDim.x) {   // X_kj from XT (written above)
+                const int cc = e / 64, rr = e % 64;
+                Bs[rr * MI_LD + cc] = XT[(size_t)(64 * j + cc) * LU_MB + 64 * k + rr];
+            }
+            __syncthreads();
+            mi_mma(As, Bs, acc, tx, ty);
+            __syncthreads();
+        }
+        // X_ij = -D_i T
+        mi_load(As, D + (size_t)(I0 / 64 + i) * 4096, 64);
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int v = 0; v < 4; ++v) Bs[(ty + 16 * u) * MI_LD + tx + 16 * v] = acc[u][v];
+        __syncthreads();
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int v = 0; v < 4; ++v) acc[u][v] = make_float2(0.f, 0.f);
+        mi_mma(As, Bs, acc, tx, ty);
+        put(i, acc, -1.f);
+        __syncthreads();   // X_ij is read back by the next i; the tiles are reloaded
+    }
+}
+
 constexpr int LU_NB = 64;
 
 int lu_factor_nopiv(midas_gpu_ctx *c, DenseLU &lu)
@@ -219,9 +329,12 @@ int lu_factor_nopiv(midas_gpu_ctx *c, DenseLU &lu)
     lu.nblk = (n + nb - 1) / nb;
     if (n % nb != 0) return c->err.set(MIDAS_ERR_ARG, "lu_factor_nopiv: n must be a multiple of 64 (pad)");
     void *p;
-    MIDAS_TRY(ensure(c, S_LINV, sizeof(float2) * (size_t)lu.nblk * nb * nb * 2, &p));
+    MIDAS_TRY(ensure(c, S_LINV, lu_inv_bytes(n), &p));
+    lu.nmac = (n + LU_MB - 1) / LU_MB;
     lu.Linv = (float2 *)p;
     lu.Uinv = lu.Linv + (size_t)lu.nblk * nb * nb;
+    lu.MLinvT = lu.Uinv + (size_t)lu.nblk * nb * nb;
+    lu.MUinvT = lu.MLinvT + (size_t)lu.nmac * LU_MB * LU_MB;
     MIDAS_TRY(ensure(c, S_BEXP, sizeof(float) * (size_t)(2 * nb) * (2 * nb), &p));
     float *uexp = (float *)p;
     const int nb2 = lu_panel_width(n);
@@ -239,10 +352,11 @@ int lu_factor_nopiv(midas_gpu_ctx *c, DenseLU &lu)
         hmax = (unsigned *)(b16 + (size_t)2 * n * 2 * nb2);
         halpha = (float *)(hmax + 2);
     }
-    const size_t smem = sizeof(float2) * 3 * nb * nb;
+    const size_t smem = sizeof(float2) * 3 * nb * nb, mi_smem = sizeof(float2) * 2 * 64 * MI_LD;
     static bool attr = false;
     if (!attr) {
         MIDAS_CUDA(c, cudaFuncSetAttribute(k_diag_lu<LU_NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        MIDAS_CUDA(c, cudaFuncSetAttribute(k_macro_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mi_smem));
         attr = true;
     }
     const long long lda = lu.lda;
@@ -281,6 +395,15 @@ int lu_factor_nopiv(midas_gpu_ctx *c, DenseLU &lu)
             MIDAS_TRY(expand_b(c, nb, wp, lu.A + (long long)j0 * lda + j0 + nb, lda, 1, bexp, 2 * nb));
             MIDAS_TRY(gemm(rem, 2 * wp, 2 * nb, Af + 2 * ((long long)(j0 + nb) * lda + j0), 2 * lda, bexp, 2 * nb,
                            Af + 2 * ((long long)(j0 + nb) * lda + j0 + nb), 2 * lda, -1.f, 1.f, 0));
+        }
+        {   // inverses of the solve's 256-row diagonal blocks inside this panel (final now)
+            const int m0 = J0 / LU_MB, m1 = (J1 + LU_MB - 1) / LU_MB;
+            ++c->launches;
+            int kp = kp_begin(c);
+            k_macro_inv<<<dim3(4 * (m1 - m0), 2), 256, mi_smem, c->stream>>>(lu.A, lda, n, m0, lu.Linv, lu.Uinv,
+                                                                             lu.MLinvT, lu.MUinvT);
+            kp_end(c, kp, MIDAS_KC_DIAG_LU, 8.0 * 64 * 64 * 64 * 16 * (m1 - m0), 0.0);
+            MIDAS_CUDA(c, cudaGetLastError());
         }
         const int rt = n - J1;
         if (rt == 0) break;
@@ -328,40 +451,18 @@ int lu_factor_nopiv(midas_gpu_ctx *c, DenseLU &lu)
 // whose A operand is the L or U panel read in place (row-major, no copy):
 //   Rt[rows below] -= L[rows below, block] * Y[block]      (forward)
 //   Rt[rows above] -= U[rows above, block] * X[block]      (backward)
-// Two levels: inside a super-block of SOLVE_SB rows the 64-row diagonal
+// Two levels: inside a super-block of SOLVE_SB rows the 256-row diagonal
 // blocks are applied one after the other (their inverses come from the
 // factorisation) and update only the rows of the super-block; one GEMM with
 // K = SOLVE_SB then updates every row outside it.  The right-hand-side
 // traffic per super-block is then O(n nrhs) instead of O(n nrhs) per 64 rows.
 // ---------------------------------------------------------------------------
 constexpr int SOLVE_SB = 512;
+static_assert(SOLVE_SB % LU_MB == 0, "super-blocks hold whole diagonal blocks");
 
 size_t lu_solve_scratch_bytes(int n, int nrhs)
 {
     return sizeof(float2) * (size_t)n * nrhs + sizeof(float) * 4 * (size_t)nrhs * SOLVE_SB + 512;
-}
-
-// Y = Minv * Rt[r0 .. r0+64) (in place, one CTA per right-hand side j), and the
-// expanded copy of Y for the next GEMM's B operand: rows 2j, 2j+1 of Bt hold
-// (Yr, -Yi) and (Yi, Yr) interleaved along the 64 rows, from column col0.
-__global__ void k_apply_inv_rm(const float2 *Minv, float2 *Rt, int nrhs, int r0, float *Bt, long long ldb, int col0)
-{
-    __shared__ float2 t[64];
-    const int j = blockIdx.x, i = threadIdx.x;
-    float2 *x = Rt + (long long)r0 * nrhs + j;
-    t[i] = x[(long long)i * nrhs];
-    __syncthreads();
-    float2 s = make_float2(0.f, 0.f);
-    for (int m = 0; m < 64; ++m) {
-        float2 a = Minv[i * 64 + m], v = t[m];
-        s.x += a.x * v.x - a.y * v.y;
-        s.y += a.x * v.y + a.y * v.x;
-    }
-    x[(long long)i * nrhs] = s;
-    float *b0 = Bt + (long long)(2 * j) * ldb + col0 + 2 * i, *b1 = b0 + ldb;
-    const float yr = tf32_rna(s.x), yi = tf32_rna(s.y);   // GEMM operand: unbiased TF32
-    b0[0] = yr; b0[1] = -yi;
-    b1[0] = yi; b1[1] = yr;
 }
 
 // column-major R (n x nrhs, ld n) -> row-major Rt (n x nrhs), 32 x 32 tiles
@@ -388,13 +489,58 @@ __global__ void k_rm_to_cm(const float2 *Rt, int n, int nrhs, float2 *R)
         if (r0 + tx < n && c0 + k < nrhs) R[(long long)(c0 + k) * n + r0 + tx] = tile[tx][k];
 }
 
-static int apply_inv(midas_gpu_ctx *c, const float2 *Minv, float2 *Rt, int nrhs, int r0, float *Bt, long long ldb,
-                     int col0)
+// Y = X * Rt[r0 .. r0+mb) for a 256-row diagonal-block inverse X (transposed,
+// XT[c * LU_MB + r]; block lower triangular for L, upper for U), in place, 4
+// right-hand sides per CTA, one row per thread.  The expanded copy of Y for the
+// next GEMM's B operand goes to Bt: rows 2j, 2j+1 hold (Yr, -Yi) and (Yi, Yr),
+// rounded to TF32, interleaved along the mb rows from column col0.
+constexpr int AM_RC = 4;
+__global__ void __launch_bounds__(LU_MB) k_apply_minv(const float2 *XT, int mb, int upper, float2 *Rt, int nrhs,
+                                                      int r0, float *Bt, long long ldb, int col0)
+{
+    __shared__ float2 t[LU_MB][AM_RC];
+    const int c0 = blockIdx.x * AM_RC, r = threadIdx.x;
+    for (int q = threadIdx.x; q < mb * AM_RC; q += blockDim.x) {
+        const int rr = q / AM_RC, j = q % AM_RC;
+        t[rr][j] = c0 + j < nrhs ? Rt[(long long)(r0 + rr) * nrhs + c0 + j] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    if (r >= mb) return;
+    // the nonzero 64-column blocks of row r (warp-uniform bounds)
+    const int cb = upper ? (r / 64) * 64 : 0, ce = upper ? mb : (r / 64 + 1) * 64;
+    float2 acc[AM_RC];
+#pragma unroll
+    for (int j = 0; j < AM_RC; ++j) acc[j] = make_float2(0.f, 0.f);
+#pragma unroll 4
+    for (int cc = cb; cc < ce; ++cc) {
+        const float2 x = XT[(size_t)cc * LU_MB + r];
+#pragma unroll
+        for (int j = 0; j < AM_RC; ++j) {
+            const float2 v = t[cc][j];
+            acc[j].x = fmaf(x.x, v.x, fmaf(-x.y, v.y, acc[j].x));
+            acc[j].y = fmaf(x.x, v.y, fmaf(x.y, v.x, acc[j].y));
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < AM_RC; ++j) {
+        const int col = c0 + j;
+        if (col >= nrhs) break;
+        Rt[(long long)(r0 + r) * nrhs + col] = acc[j];
+        float *b0 = Bt + (long long)(2 * col) * ldb + col0 + 2 * r, *b1 = b0 + ldb;
+        const float yr = tf32_rna(acc[j].x), yi = tf32_rna(acc[j].y);   // GEMM operand: unbiased TF32
+        b0[0] = yr; b0[1] = -yi;
+        b1[0] = yi; b1[1] = yr;
+    }
+}
+
+static int apply_minv(midas_gpu_ctx *c, const float2 *XT, int mb, int upper, float2 *Rt, int nrhs, int r0, float *Bt,
+                      long long ldb, int col0)
 {
     ++c->launches;
     int kp = kp_begin(c);
-    k_apply_inv_rm<<<nrhs, 64, 0, c->stream>>>(Minv, Rt, nrhs, r0, Bt, ldb, col0);
-    kp_end(c, kp, MIDAS_KC_TRSV, 8.0 * 64 * 64 * nrhs, 8.0 * 64 * 64 + 32.0 * 64 * nrhs);
+    k_apply_minv<<<(nrhs + AM_RC - 1) / AM_RC, LU_MB, 0, c->stream>>>(XT, mb, upper, Rt, nrhs, r0, Bt, ldb, col0);
+    kp_end(c, kp, MIDAS_KC_TRSV, 4.0 * mb * mb * nrhs, 8.0 * mb * mb / 2 * ((nrhs + AM_RC - 1) / AM_RC) +
+                                                         32.0 * mb * nrhs);
     MIDAS_CUDA(c, cudaGetLastError());
     return MIDAS_OK;
 }
@@ -418,12 +564,14 @@ int lu_solve(midas_gpu_ctx *c, const DenseLU &lu, float2 *R, int nrhs)
     // forward: L Y = B
     for (int S = 0; S < nsb; ++S) {
         const int K0 = S * SOLVE_SB, K1 = std::min(n, K0 + SOLVE_SB), ldb = 2 * (K1 - K0);
-        for (int r0 = K0; r0 < K1; r0 += nb) {
-            MIDAS_TRY(apply_inv(c, lu.Linv + (size_t)(r0 / nb) * nb * nb, Rt, nrhs, r0, Bt, ldb, 2 * (r0 - K0)));
-            const int rows = K1 - (r0 + nb);
+        for (int r0 = K0; r0 < K1; r0 += LU_MB) {
+            const int mb = std::min(LU_MB, K1 - r0);
+            MIDAS_TRY(apply_minv(c, lu.MLinvT + (size_t)(r0 / LU_MB) * LU_MB * LU_MB, mb, 0, Rt, nrhs, r0, Bt, ldb,
+                                 2 * (r0 - K0)));
+            const int rows = K1 - (r0 + mb);
             if (rows > 0) {
-                GemmArgs g{rows, 2 * nrhs, 2 * nb, Af + 2 * ((r0 + nb) * lda + r0), 2 * lda, Bt + 2 * (r0 - K0), ldb,
-                           Rtf + 2LL * (r0 + nb) * nrhs, 2LL * nrhs, -1.f, 1.f, 0, MIDAS_KC_GEMM_SOLVE};
+                GemmArgs g{rows, 2 * nrhs, 2 * mb, Af + 2 * ((r0 + mb) * lda + r0), 2 * lda, Bt + 2 * (r0 - K0), ldb,
+                           Rtf + 2LL * (r0 + mb) * nrhs, 2LL * nrhs, -1.f, 1.f, 0, MIDAS_KC_GEMM_SOLVE};
                 MIDAS_TRY(gemm_tf32(c, g));
             }
         }
@@ -436,11 +584,13 @@ int lu_solve(midas_gpu_ctx *c, const DenseLU &lu, float2 *R, int nrhs)
     // backward: U X = Y
     for (int S = nsb - 1; S >= 0; --S) {
         const int K0 = S * SOLVE_SB, K1 = std::min(n, K0 + SOLVE_SB), ldb = 2 * (K1 - K0);
-        for (int r0 = K1 - nb; r0 >= K0; r0 -= nb) {
-            MIDAS_TRY(apply_inv(c, lu.Uinv + (size_t)(r0 / nb) * nb * nb, Rt, nrhs, r0, Bt, ldb, 2 * (r0 - K0)));
+        for (int r0 = (K1 - 1) / LU_MB * LU_MB; r0 >= K0; r0 -= LU_MB) {
+            const int mb = std::min(LU_MB, K1 - r0);
+            MIDAS_TRY(apply_minv(c, lu.MUinvT + (size_t)(r0 / LU_MB) * LU_MB * LU_MB, mb, 1, Rt, nrhs, r0, Bt, ldb,
+                                 2 * (r0 - K0)));
             const int rows = r0 - K0;
             if (rows > 0) {
-                GemmArgs g{rows, 2 * nrhs, 2 * nb, Af + 2 * (K0 * lda + r0), 2 * lda, Bt + 2 * (r0 - K0), ldb,
+                GemmArgs g{rows, 2 * nrhs, 2 * mb, Af + 2 * (K0 * lda + r0), 2 * lda, Bt + 2 * (r0 - K0), ldb,
                            Rtf + 2LL * K0 * nrhs, 2LL * nrhs, -1.f, 1.f, 0, MIDAS_KC_GEMM_SOLVE};
                 MIDAS_TRY(gemm_tf32(c, g));
             }

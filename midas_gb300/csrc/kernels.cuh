@@ -93,13 +93,22 @@ int gemm_selftest(midas_gpu_ctx *c);
 int gemm_bench(midas_gpu_ctx *c, int M, int N, int K, int iters, double *ms, bool f16 = false);
 
 // dense.cu
+constexpr int LU_MB = 256;   // macro block of the triangular solves
 struct DenseLU {
-    int n = 0, nb = 64, nblk = 0;
+    int n = 0, nb = 64, nblk = 0, nmac = 0;
     float2 *A = nullptr;     // n x n row-major, overwritten by L\U
     long long lda = 0;
     float2 *Linv = nullptr;  // nblk blocks of nb x nb (row-major), unit-lower inverses
     float2 *Uinv = nullptr;  // nblk blocks of nb x nb, upper inverses
+    float2 *MLinvT = nullptr;   // nmac inverses of the LU_MB x LU_MB diagonal blocks of L, transposed
+    float2 *MUinvT = nullptr;   // the same for U
 };
+// bytes of the diagonal-block inverses (slot S_LINV)
+inline size_t lu_inv_bytes(int n)
+{
+    const size_t nblk = (size_t)(n + 63) / 64, nmac = (size_t)(n + LU_MB - 1) / LU_MB;
+    return sizeof(float2) * (nblk * 64 * 64 * 2 + nmac * LU_MB * LU_MB * 2);
+}
 int lu_factor_nopiv(midas_gpu_ctx *c, DenseLU &lu);
 // solve LU X = R in place; R is n x nrhs column-major complex64 (ld = n)
 // Panel width of the two-level factorisation: the trailing update reads and

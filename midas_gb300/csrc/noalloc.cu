@@ -117,7 +117,7 @@ extern "C" int midas_gpu_dense_solve_noalloc(int device, void *stream, int n, in
     c.stream = (cudaStream_t)stream;
     c.pi = ref_pi_host();
     c.pool.resize(S_NSLOTS);
-    const int np = (n + 63) / 64 * 64, nb = 64, nblk = np / 64;
+    const int np = (n + 63) / 64 * 64;
     Carver cv{(char *)g_noalloc_addr[device], 0, NOALLOC_BYTES};
     c.d_flag = (int *)cv.take(256);
     auto slot = [&](int s, size_t bytes) {
@@ -127,8 +127,8 @@ extern "C" int midas_gpu_dense_solve_noalloc(int device, void *stream, int n, in
     const size_t nn = (size_t)np * nrhs;
     slot(S_Z64, sizeof(double2) * (size_t)np * np);
     slot(S_Z32, sizeof(float2) * (size_t)np * np);
-    slot(S_LINV, sizeof(float2) * (size_t)nblk * nb * nb * 2);
-    slot(S_BEXP, sizeof(float) * (size_t)(2 * nb) * (2 * nb));
+    slot(S_LINV, lu_inv_bytes(np));
+    slot(S_BEXP, sizeof(float) * (size_t)128 * 128);   // expanded 64 x 64 U^-1
     slot(S_BEXP2, lu_bexp2_bytes(np));
     slot(S_RHS64, sizeof(double2) * nn);
     slot(S_X64, sizeof(double2) * nn);
