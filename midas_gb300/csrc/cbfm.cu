@@ -345,6 +345,7 @@ void free_lanes(midas_gpu_ctx *c)
             if (d.p) cudaFree(d.p);
         if (L->d_flag) cudaFree(L->d_flag);
         for (cudaEvent_t e : L->kprof.ev) cudaEventDestroy(e);
+        destroy_side(L);
         if (L->stream) cudaStreamDestroy(L->stream);
         delete L;   // the cell arrays belong to the parent context
     }

@@ -143,6 +143,11 @@ struct midas_gpu_ctx {
     // lanes: child contexts (own stream and scratch pool, the cells aliased)
     // that run independent CBFM blocks concurrently
     std::vector<midas_gpu_ctx *> lanes;
+    // side stream (created on first use, same priority as `stream`) for work that
+    // only joins later, e.g. the solve's diagonal-block inverses during the LU
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    bool allow_side = true;   // false for the allocation-free entry point
     void *cusolver = nullptr;
     void *cublas = nullptr;
 };
@@ -158,6 +163,10 @@ int ensure(midas_gpu_ctx *ctx, int slot, size_t bytes, void **out);
 int kp_begin(midas_gpu_ctx *ctx);
 void kp_end(midas_gpu_ctx *ctx, int e0, int cls, double flops, double bytes);
 int kp_flush(midas_gpu_ctx *ctx);
+
+// The context's side stream and fork/join events (created on first use).
+int side_stream(midas_gpu_ctx *ctx, cudaStream_t *out);
+void destroy_side(midas_gpu_ctx *ctx);
 
 // Is p a device (or managed) pointer?
 bool is_device_ptr(const void *p);

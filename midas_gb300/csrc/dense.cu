@@ -361,6 +361,21 @@ int lu_factor_nopiv(midas_gpu_ctx *c, DenseLU &lu)
     }
     const long long lda = lu.lda;
     float *Af = (float *)lu.A;
+    // the 256-row diagonal-block inverses only feed the later solves: off the
+    // critical path on the side stream (joined when the factorisation returns;
+    // on the main stream while per-kernel profiling is on)
+    cudaStream_t mi_stream = c->stream;
+    if (c->allow_side && !c->kprof.on) MIDAS_TRY(side_stream(c, &mi_stream));
+    struct Join {
+        midas_gpu_ctx *c;
+        bool on;
+        ~Join() {
+            if (on) {
+                cudaEventRecord(c->ev_join, c->side);
+                cudaStreamWaitEvent(c->stream, c->ev_join, 0);
+            }
+        }
+    } join{c, mi_stream != c->stream};
     // rnd = 1 for the GEMMs that produce final L or U entries: those are stored
     // rounded to TF32 (round to nearest), as every later use reads them in TF32
     auto gemm = [&](int M, int N, int K, const float *A, long long la, const float *B, long long lb, float *D,
@@ -396,12 +411,17 @@ int lu_factor_nopiv(midas_gpu_ctx *c, DenseLU &lu)
             MIDAS_TRY(gemm(rem, 2 * wp, 2 * nb, Af + 2 * ((long long)(j0 + nb) * lda + j0), 2 * lda, bexp, 2 * nb,
                            Af + 2 * ((long long)(j0 + nb) * lda + j0 + nb), 2 * lda, -1.f, 1.f, 0));
         }
-        {   // inverses of the solve's 256-row diagonal blocks inside this panel (final now)
+        {   // inverses of the solve's 256-row diagonal blocks inside this panel (final now;
+            // nothing later in the factorisation writes the panel's diagonal region)
             const int m0 = J0 / LU_MB, m1 = (J1 + LU_MB - 1) / LU_MB;
+            if (join.on) {
+                MIDAS_CUDA(c, cudaEventRecord(c->ev_fork, c->stream));
+                MIDAS_CUDA(c, cudaStreamWaitEvent(mi_stream, c->ev_fork, 0));
+            }
             ++c->launches;
-            int kp = kp_begin(c);
-            k_macro_inv<<<dim3(4 * (m1 - m0), 2), 256, mi_smem, c->stream>>>(lu.A, lda, n, m0, lu.Linv, lu.Uinv,
-                                                                             lu.MLinvT, lu.MUinvT);
+            int kp = join.on ? -1 : kp_begin(c);
+            k_macro_inv<<<dim3(4 * (m1 - m0), 2), 256, mi_smem, mi_stream>>>(lu.A, lda, n, m0, lu.Linv, lu.Uinv,
+                                                                            lu.MLinvT, lu.MUinvT);
             kp_end(c, kp, MIDAS_KC_DIAG_LU, 8.0 * 64 * 64 * 64 * 16 * (m1 - m0), 0.0);
             MIDAS_CUDA(c, cudaGetLastError());
         }
@@ -511,7 +531,7 @@ __global__ void __launch_bounds__(LU_MB) k_apply_minv(const float2 *XT, int mb, 
     float2 acc[AM_RC];
 #pragma unroll
     for (int j = 0; j < AM_RC; ++j) acc[j] = make_float2(0.f, 0.f);
-#pragma unroll 4
+#pragma unroll 16   // 16 independent loads of the inverse in flight per thread
     for (int cc = cb; cc < ce; ++cc) {
         const float2 x = XT[(size_t)cc * LU_MB + r];
 #pragma unroll

@@ -63,6 +63,31 @@ int to_device(midas_gpu_ctx *ctx, const void *p, size_t bytes, int slot, const v
     return MIDAS_OK;
 }
 
+int side_stream(midas_gpu_ctx *c, cudaStream_t *out)
+{
+    if (!c->side) {
+        int prio = 0;
+        MIDAS_CUDA(c, cudaStreamGetPriority(c->stream, &prio));
+        MIDAS_CUDA(c, cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, prio));
+        MIDAS_CUDA(c, cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+        MIDAS_CUDA(c, cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
+    }
+    *out = c->side;
+    return MIDAS_OK;
+}
+
+void destroy_side(midas_gpu_ctx *c)
+{
+    if (c->side) {
+        cudaStreamSynchronize(c->side);
+        cudaStreamDestroy(c->side);
+    }
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
+    c->side = nullptr;
+    c->ev_fork = c->ev_join = nullptr;
+}
+
 int kp_begin(midas_gpu_ctx *c)
 {
     KProf &k = c->kprof;
@@ -292,6 +317,7 @@ int midas_gpu_free(midas_gpu_ctx *c)
     if (c->d_flag) cudaFree(c->d_flag);
     if (c->cusolver) destroy_cusolver(c->cusolver);
     free_lanes(c);
+    destroy_side(c);
     for (cudaEvent_t e : c->kprof.ev) cudaEventDestroy(e);
     cudaStreamDestroy(c->stream);
     delete c;

@@ -115,6 +115,7 @@ extern "C" int midas_gpu_dense_solve_noalloc(int device, void *stream, int n, in
     c.opts.device = device;
     c.device = device;
     c.stream = (cudaStream_t)stream;
+    c.allow_side = false;   // no stream or event creation on this path
     c.pi = ref_pi_host();
     c.pool.resize(S_NSLOTS);
     const int np = (n + 63) / 64 * 64;
