@@ -511,36 +511,54 @@ __global__ void k_rm_to_cm(const float2 *Rt, int n, int nrhs, float2 *R)
 
 // Y = X * Rt[r0 .. r0+mb) for a 256-row diagonal-block inverse X (transposed,
 // XT[c * LU_MB + r]; block lower triangular for L, upper for U), in place, 4
-// right-hand sides per CTA, one row per thread.  The expanded copy of Y for the
+// right-hand sides per CTA.  Each row's columns are split over AM_CS threads
+// (thread (s, r) takes columns s, s + AM_CS, ...; a warp is 32 rows of one s,
+// so the reads of XT coalesce), which keeps the chain of L2 loads per thread
+// short; the partial sums meet in shared memory.  The expanded copy of Y for the
 // next GEMM's B operand goes to Bt: rows 2j, 2j+1 hold (Yr, -Yi) and (Yi, Yr),
 // rounded to TF32, interleaved along the mb rows from column col0.
-constexpr int AM_RC = 4;
-__global__ void __launch_bounds__(LU_MB) k_apply_minv(const float2 *XT, int mb, int upper, float2 *Rt, int nrhs,
-                                                      int r0, float *Bt, long long ldb, int col0)
+constexpr int AM_RC = 4, AM_CS = 4;
+__global__ void __launch_bounds__(LU_MB * AM_CS) k_apply_minv(const float2 *XT, int mb, int upper, float2 *Rt,
+                                                              int nrhs, int r0, float *Bt, long long ldb, int col0)
 {
     __shared__ float2 t[LU_MB][AM_RC];
-    const int c0 = blockIdx.x * AM_RC, r = threadIdx.x;
+    __shared__ float2 part[AM_CS - 1][LU_MB][AM_RC];
+    const int c0 = blockIdx.x * AM_RC, r = threadIdx.x % LU_MB, sp = threadIdx.x / LU_MB;
     for (int q = threadIdx.x; q < mb * AM_RC; q += blockDim.x) {
         const int rr = q / AM_RC, j = q % AM_RC;
         t[rr][j] = c0 + j < nrhs ? Rt[(long long)(r0 + rr) * nrhs + c0 + j] : make_float2(0.f, 0.f);
     }
     __syncthreads();
-    if (r >= mb) return;
-    // the nonzero 64-column blocks of row r (warp-uniform bounds)
-    const int cb = upper ? (r / 64) * 64 : 0, ce = upper ? mb : (r / 64 + 1) * 64;
     float2 acc[AM_RC];
 #pragma unroll
     for (int j = 0; j < AM_RC; ++j) acc[j] = make_float2(0.f, 0.f);
-#pragma unroll 16   // 16 independent loads of the inverse in flight per thread
-    for (int cc = cb; cc < ce; ++cc) {
-        const float2 x = XT[(size_t)cc * LU_MB + r];
+    if (r < mb) {
+        // the nonzero 64-column blocks of row r (warp-uniform bounds)
+        const int cb = upper ? (r / 64) * 64 : 0, ce = upper ? mb : (r / 64 + 1) * 64;
+#pragma unroll 8
+        for (int cc = cb + sp; cc < ce; cc += AM_CS) {
+            const float2 x = XT[(size_t)cc * LU_MB + r];
 #pragma unroll
-        for (int j = 0; j < AM_RC; ++j) {
-            const float2 v = t[cc][j];
-            acc[j].x = fmaf(x.x, v.x, fmaf(-x.y, v.y, acc[j].x));
-            acc[j].y = fmaf(x.x, v.y, fmaf(x.y, v.x, acc[j].y));
+            for (int j = 0; j < AM_RC; ++j) {
+                const float2 v = t[cc][j];
+                acc[j].x = fmaf(x.x, v.x, fmaf(-x.y, v.y, acc[j].x));
+                acc[j].y = fmaf(x.x, v.y, fmaf(x.y, v.x, acc[j].y));
+            }
         }
     }
+    if (sp > 0) {
+#pragma unroll
+        for (int j = 0; j < AM_RC; ++j) part[sp - 1][r][j] = acc[j];
+    }
+    __syncthreads();
+    if (sp > 0 || r >= mb) return;
+#pragma unroll
+    for (int s2 = 0; s2 < AM_CS - 1; ++s2)
+#pragma unroll
+        for (int j = 0; j < AM_RC; ++j) {
+            acc[j].x += part[s2][r][j].x;
+            acc[j].y += part[s2][r][j].y;
+        }
 #pragma unroll
     for (int j = 0; j < AM_RC; ++j) {
         const int col = c0 + j;
@@ -558,7 +576,8 @@ static int apply_minv(midas_gpu_ctx *c, const float2 *XT, int mb, int upper, flo
 {
     ++c->launches;
     int kp = kp_begin(c);
-    k_apply_minv<<<(nrhs + AM_RC - 1) / AM_RC, LU_MB, 0, c->stream>>>(XT, mb, upper, Rt, nrhs, r0, Bt, ldb, col0);
+    k_apply_minv<<<(nrhs + AM_RC - 1) / AM_RC, LU_MB * AM_CS, 0, c->stream>>>(XT, mb, upper, Rt, nrhs, r0, Bt, ldb,
+                                                                                col0);
     kp_end(c, kp, MIDAS_KC_TRSV, 4.0 * mb * mb * nrhs, 8.0 * mb * mb / 2 * ((nrhs + AM_RC - 1) / AM_RC) +
                                                          32.0 * mb * nrhs);
     MIDAS_CUDA(c, cudaGetLastError());
