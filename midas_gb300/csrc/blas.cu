@@ -462,16 +462,20 @@ __global__ void __launch_bounds__(256) k_heev_tridiag(int m, double2 *Ab, long l
         if (tid == 0) tau[k] = t;
         __syncthreads();
         if (t.x != 0 || t.y != 0) {
-            // x = tau * A22 v
-            for (int i = tid; i < L; i += nt) {
+            // x = tau * A22 v, a warp per row (the lanes read the row coalesced)
+            for (int i = tid / 32; i < L; i += nt / 32) {
                 const double2 *row = A + (long long)(k + 1 + i) * lda + (k + 1);
                 double sx = 0, sy = 0;
-                for (int j = 0; j < L; ++j) {
+                for (int j = tid % 32; j < L; j += 32) {
                     double2 a = row[j], vj = v[j];
                     sx += a.x * vj.x - a.y * vj.y;
                     sy += a.x * vj.y + a.y * vj.x;
                 }
-                x[i] = make_double2(t.x * sx - t.y * sy, t.x * sy + t.y * sx);
+                for (int o = 16; o > 0; o >>= 1) {
+                    sx += __shfl_down_sync(0xffffffffu, sx, o);
+                    sy += __shfl_down_sync(0xffffffffu, sy, o);
+                }
+                if (tid % 32 == 0) x[i] = make_double2(t.x * sx - t.y * sy, t.x * sy + t.y * sx);
             }
             __syncthreads();
             // dot = x^H v ; alpha = -1/2 tau dot ; w = x + alpha v  (w stored in x)
@@ -542,17 +546,21 @@ __global__ void __launch_bounds__(256) k_heev_tridiag(int m, double2 *Ab, long l
                 break;
             }
             if (tid == 0) {
+                // one thread runs the sweep on the FP64 pipe; sqrt(f^2 + g^2) and one
+                // reciprocal per rotation (|g| <= ~1/eps after the deflation test and f,
+                // g are bounded by ||T||, so the squares cannot overflow)
                 double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
-                double r = hypot(g, 1.0);
+                double r = sqrt(g * g + 1.0);
                 g = d[mm] - d[l] + e[l] / (g + copysign(r, g));
                 double s = 1, c = 1, p = 0;
                 int cnt = 0, broke = 0;
                 for (int i = mm - 1; i >= l; --i) {
                     double f = s * e[i], b = c * e[i];
-                    r = hypot(f, g);
+                    r = sqrt(f * f + g * g);
                     e[i + 1] = r;
                     if (r == 0.0) { d[i + 1] -= p; e[mm] = 0.0; broke = 1; break; }
-                    s = f / r; c = g / r;
+                    const double ir = 1.0 / r;
+                    s = f * ir; c = g * ir;
                     g = d[i + 1] - p;
                     r = (d[i] - g) * s + 2.0 * c * b;
                     p = s * r;
@@ -565,16 +573,21 @@ __global__ void __launch_bounds__(256) k_heev_tridiag(int m, double2 *Ab, long l
                 nrot = cnt;
             }
             __syncthreads();
-            // apply the rotations (in generation order) to every row of Z
+            // apply the rotations (in generation order) to every row of Z; rotation q
+            // mixes z[i] and z[i+1] (i = mm-1-q), and its new z[i] is the next
+            // rotation's z[i+1]: that value stays in a register, so each step loads
+            // one element that no earlier step wrote
             for (int row = tid; row < m; row += nt) {
                 double2 *z = V + (long long)row * m;
+                if (nrot == 0) continue;
+                double f = z[mm].x;
                 for (int q = 0; q < nrot; ++q) {
-                    int i = mm - 1 - q;
-                    double s = rs[q], c = rc[q];
-                    double f = z[i + 1].x;
-                    z[i + 1].x = s * z[i].x + c * f;
-                    z[i].x = c * z[i].x - s * f;
+                    const int i = mm - 1 - q;
+                    const double s = rs[q], c = rc[q], zi = z[i].x;
+                    z[i + 1].x = s * zi + c * f;
+                    f = c * zi - s * f;
                 }
+                z[mm - nrot].x = f;
             }
             __syncthreads();
         }

@@ -54,6 +54,10 @@ __global__ void __launch_bounds__(512) k_diag_lu(float2 *A11, long long lda, flo
     // right-looking elimination without pivoting; the update maps a thread to a
     // column (tx) and every (nt / NB)-th row (ty), so no index division is needed
     static_assert(NB == 64, "thread mapping assumes 64-wide blocks");
+    if (nt != 8 * NB) {   // the update below gives each thread NB / 8 rows
+        if (tid == 0) atomicOr(flag, DEV_BAD_ARG);
+        return;
+    }
     const int tx = tid % NB, ty = tid / NB, nty = nt / NB;
     for (int j = 0; j < NB; ++j) {
         if (tid < NB - j - 1) {
@@ -70,48 +74,80 @@ __global__ void __launch_bounds__(512) k_diag_lu(float2 *A11, long long lda, flo
         }
         __syncthreads();
         if (tx > j) {
+            // all loads first, then the updates: 16 independent shared loads in flight
+            constexpr int RPT = NB / 8;   // rows per thread (nty == 8)
             const float2 u = a[j * NB + tx];
-            for (int i = j + 1 + ty; i < NB; i += nty) {
-                const float2 l = a[i * NB + j], d = a[i * NB + tx];
-                a[i * NB + tx] = make_float2(d.x - (l.x * u.x - l.y * u.y), d.y - (l.x * u.y + l.y * u.x));
+            float2 l[RPT], d[RPT];
+#pragma unroll
+            for (int k = 0; k < RPT; ++k) {
+                const int i = j + 1 + ty + nty * k;
+                if (i < NB) { l[k] = a[i * NB + j]; d[k] = a[i * NB + tx]; }
+            }
+#pragma unroll
+            for (int k = 0; k < RPT; ++k) {
+                const int i = j + 1 + ty + nty * k;
+                if (i < NB)
+                    a[i * NB + tx] = make_float2(d[k].x - (l[k].x * u.x - l[k].y * u.y),
+                                                 d[k].y - (l[k].x * u.y + l[k].y * u.x));
             }
         }
         __syncthreads();
     }
-    // Triangular inverses, one column per thread (no barriers inside): threads
-    // 0..NB-1 build column c of L^-1 (unit lower) top-down,
+    // Triangular inverses, a column per group of 4 lanes: threads 0..255 build
+    // L^-1 (unit lower) column c = t / 4 top-down,
     //   X[c][c] = 1,  X[i][c] = -sum_{m=c}^{i-1} L[i][m] X[m][c];
-    // threads NB..2NB-1 build column c of U^-1 bottom-up,
+    // threads 256..511 build U^-1 column c bottom-up,
     //   X[c][c] = 1/U[c][c],  X[i][c] = -(sum_{m=i+1}^{c} U[i][m] X[m][c]) / U[i][i].
-    // L[i][m] / U[i][m] is the same word for the whole warp (broadcast); X[m][c]
-    // is consecutive across the warp.
+    // The 4 lanes split the sum over m and meet by shuffles; the i loop runs over
+    // the warp's whole column range (8 columns) so every lane reaches the shuffles.
+    __shared__ float2 rdiag[NB];
     for (int t = tid; t < NB * NB; t += nt) { li[t] = make_float2(0.f, 0.f); ui[t] = make_float2(0.f, 0.f); }
-    __syncthreads();
     if (tid < NB) {
-        const int cc = tid;
-        li[cc * NB + cc] = make_float2(1.f, 0.f);
-        for (int i = cc + 1; i < NB; ++i) {
-            float2 s = make_float2(0.f, 0.f);
-            for (int m = cc; m < i; ++m) {
-                float2 l = a[i * NB + m], x = li[m * NB + cc];
-                s.x += l.x * x.x - l.y * x.y;
-                s.y += l.x * x.y + l.y * x.x;
+        const float2 d = a[tid * NB + tid];
+        const float dm = d.x * d.x + d.y * d.y;
+        rdiag[tid] = make_float2(d.x / dm, -d.y / dm);
+    }
+    __syncthreads();
+    {
+        const int q = tid % 256, cc = q / 4, l4 = q % 4;
+        const int cw0 = (q / 32) * 8, cw1 = cw0 + 7;   // the warp's columns
+        if (tid < 256) {
+            if (l4 == 0) li[cc * NB + cc] = make_float2(1.f, 0.f);
+            __syncwarp();
+            for (int i = cw0 + 1; i < NB; ++i) {
+                float2 s = make_float2(0.f, 0.f);
+                if (i > cc)
+                    for (int m = cc + l4; m < i; m += 4) {
+                        const float2 l = a[i * NB + m], x = li[m * NB + cc];
+                        s.x += l.x * x.x - l.y * x.y;
+                        s.y += l.x * x.y + l.y * x.x;
+                    }
+                s.x += __shfl_xor_sync(0xffffffffu, s.x, 1);
+                s.y += __shfl_xor_sync(0xffffffffu, s.y, 1);
+                s.x += __shfl_xor_sync(0xffffffffu, s.x, 2);
+                s.y += __shfl_xor_sync(0xffffffffu, s.y, 2);
+                if (i > cc && l4 == 0) li[i * NB + cc] = make_float2(-s.x, -s.y);
+                __syncwarp();
             }
-            li[i * NB + cc] = make_float2(-s.x, -s.y);
-        }
-    } else if (tid < 2 * NB) {
-        const int cc = tid - NB;
-        for (int i = cc; i >= 0; --i) {
-            float2 s = make_float2(i == cc ? 1.f : 0.f, 0.f);
-            for (int m = i + 1; m <= cc; ++m) {
-                float2 u = a[i * NB + m], x = ui[m * NB + cc];
-                s.x -= u.x * x.x - u.y * x.y;
-                s.y -= u.x * x.y + u.y * x.x;
+        } else {
+            for (int i = cw1; i >= 0; --i) {
+                float2 s = make_float2(0.f, 0.f);
+                if (i <= cc)
+                    for (int m = i + 1 + l4; m <= cc; m += 4) {
+                        const float2 u = a[i * NB + m], x = ui[m * NB + cc];
+                        s.x += u.x * x.x - u.y * x.y;
+                        s.y += u.x * x.y + u.y * x.x;
+                    }
+                s.x += __shfl_xor_sync(0xffffffffu, s.x, 1);
+                s.y += __shfl_xor_sync(0xffffffffu, s.y, 1);
+                s.x += __shfl_xor_sync(0xffffffffu, s.x, 2);
+                s.y += __shfl_xor_sync(0xffffffffu, s.y, 2);
+                if (i <= cc && l4 == 0) {
+                    const float2 v = make_float2((i == cc ? 1.f : 0.f) - s.x, -s.y), id = rdiag[i];
+                    ui[i * NB + cc] = make_float2(v.x * id.x - v.y * id.y, v.x * id.y + v.y * id.x);
+                }
+                __syncwarp();
             }
-            float2 d = a[i * NB + i];
-            float dm = d.x * d.x + d.y * d.y;
-            float2 id = make_float2(d.x / dm, -d.y / dm);
-            ui[i * NB + cc] = make_float2(s.x * id.x - s.y * id.y, s.x * id.y + s.y * id.x);
         }
     }
     __syncthreads();
@@ -123,8 +159,9 @@ __global__ void __launch_bounds__(512) k_diag_lu(float2 *A11, long long lda, flo
     }
     // expanded U^-1 as the Bt operand (rows = output columns j, along p):
     // Bt[2j][2p] = Ur(p,j), Bt[2j][2p+1] = -Ui(p,j), Bt[2j+1][2p] = Ui, Bt[2j+1][2p+1] = Ur
+    // (consecutive threads take consecutive p: the global writes coalesce)
     for (int t = tid; t < NB * NB; t += nt) {
-        int p = t / NB, j = t % NB;
+        int j = t / NB, p = t % NB;
         float2 u = make_float2(tf32_rna(ui[p * NB + j].x), tf32_rna(ui[p * NB + j].y));
         float *r0 = UinvExp + (long long)(2 * j) * (2 * NB) + 2 * p;
         float *r1 = r0 + 2 * NB;

@@ -155,8 +155,10 @@ def test_heev_jacobi(ctx, m):
     ref = np.sort(np.linalg.eigvalsh(A))[::-1]
     assert np.all(np.diff(W) <= 0)
     assert np.max(np.abs(W - ref)) <= 1e-13 * ref[0]
-    sel = ref > 1e-8 * ref[0]       # the range the CBF threshold (sigma ratio >= 1e-4) uses
-    assert np.max(np.abs(W[sel] - ref[sel]) / ref[sel]) < 1e-8
+    # the range the CBF threshold (sigma ratio >= 1e-4) uses: a backward-stable solver
+    # gets these to eps ||A|| / lambda, i.e. 2.2e-8 relative at lambda = 1e-8 ||A||
+    sel = ref > 1e-8 * ref[0]
+    assert np.max(np.abs(W[sel] - ref[sel]) / ref[sel]) < 4e-8
     assert np.max(np.abs(V.conj().T @ A @ V - np.diag(W))) <= 1e-12 * ref[0]
 
 
