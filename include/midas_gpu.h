@@ -185,7 +185,7 @@ int midas_gpu_smatrix(midas_gpu_ctx *ctx, int nrx, const double *rx_theta, const
  * B n x nrhs, column-major complex, host or device memory; B is overwritten by X)
  * with the same mixed-precision LU + FP64 refinement as midas_gpu_dense_solve,
  * on `stream` (a cudaStream_t; NULL = the legacy default stream) of `device`.
- * No context is needed.  All scratch comes from one static 16 MiB device array
+ * No context is needed.  All scratch comes from one static 24 MiB device array
  * inside the library, which every GPU that loads the library holds until exit.
  * Limits: n <= 512, nrhs <= 32 (larger sizes return MIDAS_ERR_ARG).  All calls
  * share the array: calls that overlap on the GPU race, so serialise them.  The

@@ -8,7 +8,7 @@
 // LU + FP64 refinement as midas_gpu_dense_solve(), taking every byte of device
 // scratch from one file-scope static __device__ array of NOALLOC_BYTES.  That
 // array is part of the loaded library: every GPU that loads it holds the
-// 16 MiB until the process exits, and all calls share it.
+// 24 MiB until the process exits, and all calls share it.
 //
 // Limits: n <= NOALLOC_NMAX (512) unknowns and nrhs <= NOALLOC_RMAX (32)
 // right-hand sides; larger requests return MIDAS_ERR_ARG before any device work.
@@ -27,7 +27,7 @@ namespace midas {
 
 constexpr int NOALLOC_NMAX = 512;
 constexpr int NOALLOC_RMAX = 32;
-constexpr size_t NOALLOC_BYTES = (size_t)16 << 20;
+constexpr size_t NOALLOC_BYTES = (size_t)24 << 20;   // n = 512, nrhs = 32 needs 19.2 MiB
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
 

@@ -343,7 +343,8 @@ double resid_update_error_factor(midas_gpu_ctx *c, int n, int nrhs)
 size_t resid_scratch_bytes(int n, int nrhs)
 {
     const size_t ldx = (size_t)rd_ldx(nrhs);
-    return sizeof(float4) * ldx * n * (1 + RD_SMAX) + 256;
+    const size_t smax = (size_t)std::max(1, std::min(RD_SMAX, n / 256));   // rd_splits never exceeds this
+    return sizeof(float4) * ldx * n * (1 + smax) + 256;
 }
 
 int z_split_inplace(midas_gpu_ctx *c, double2 *Z64, long long ldz, int n, double *znorm)

@@ -33,8 +33,9 @@ def _noalloc(L, A, B):
 def test_noalloc_matches_dense_solve_twice(gpulib):
     from midas_gb300.solver import Context
     ctx = Context()
-    # two calls in a row with different sizes and data: the second must not see the first's leftovers
-    for n, nrhs, seed in [(300, 3, 1), (131, 5, 2)]:
+    # calls in a row with different sizes and data: each must not see the previous one's
+    # leftovers; (512, 32) is the documented maximum and must fit the static scratch
+    for n, nrhs, seed in [(300, 3, 1), (131, 5, 2), (512, 32, 5)]:
         A, B = _system(n, nrhs, seed)
         st, X, berr = _noalloc(gpulib, A, B)
         assert st == 0
