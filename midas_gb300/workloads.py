@@ -103,8 +103,15 @@ def cbfm_c2_small():
     return _gaussian_sphere_cbfm("cbfm_c2_small_gaussian_sphere_x6_ad12_2x2x2", 6.0, 12.0, 24, nbox=2)
 
 
+def cbfm_c2_mid():
+    """The same scene at a/d = 16 (~18k cells) in 2x2x2 blocks: extended blocks of
+    ~15k unknowns with tens of millions of CSR nonzeros, the regime of the full
+    scene's large blocks, in a few GB (for full profiler captures)."""
+    return _gaussian_sphere_cbfm("cbfm_c2_mid_gaussian_sphere_x6_ad16_2x2x2", 6.0, 16.0, 24, nbox=2)
+
+
 WORKLOADS = {"mom_c1": mom_c1, "mom_c3": mom_c3, "mom_c3_small": mom_c3_small, "mom_tiny": mom_tiny,
-             "cbfm_c2": cbfm_c2, "cbfm_c2_small": cbfm_c2_small}
+             "cbfm_c2": cbfm_c2, "cbfm_c2_small": cbfm_c2_small, "cbfm_c2_mid": cbfm_c2_mid}
 
 
 def cbfm_args(wl):
