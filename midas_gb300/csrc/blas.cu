@@ -389,15 +389,21 @@ int residual_df32(midas_gpu_ctx *c, int n, int nrhs, const float2 *Z, long long 
 }
 
 // ---------------------------------------------------------------------------
-// Hermitian eigen-decomposition (FP64), one CTA per matrix: Householder
-// tridiagonalisation (the zhetd2 recurrence: H = I - tau v v^H, x = tau A v,
-// w = x - tau/2 (x^H v) v, A <- A - v w^H - w v^H), implicit-shift QL on the real
-// tridiagonal (one thread generates the Givens rotations of an iteration, all
-// threads apply them to their rows of Z), back-transformation V = H_0 .. H_{m-2} Z,
-// eigenpairs sorted by decreasing eigenvalue.  Backward stable: absolute errors
-// ~ eps ||A||, so the CBF threshold subspace is resolved to eps ||A|| / gap.
-// A (m x m row-major, lda) is destroyed; Hv (m x m) holds the reflectors; Z is the
-// output V (row-major m x m).  Shared memory: d, e, tau, v, x, rotation buffers.
+// Hermitian eigen-decomposition (FP64) in three kernels:
+//  * k_heev_tridiag, one CTA per matrix: Householder tridiagonalisation (the
+//    zhetd2 recurrence: H = I - tau v v^H, x = tau A v, w = x - tau/2 (x^H v) v,
+//    A <- A - v w^H - w v^H) and the implicit-shift QL sweeps on the real
+//    tridiagonal; one thread generates the Givens rotations of each sweep and
+//    logs them, eigenvalues sorted by decreasing value;
+//  * k_heev_rot: Z = (the logged rotations applied in order to I), rows of Z
+//    split over CTAs (each row takes every rotation; rows are independent);
+//  * k_heev_back: V = H_0 .. H_{m-2} Z, columns split over CTAs, written in the
+//    sorted order.
+// The FP64 pipe of GB300 is the limit (60 % busy in the single-CTA form), so
+// the two O(m^3) phases that parallelise go to many SMs.  Backward stable:
+// absolute errors ~ eps ||A||, so the CBF threshold subspace is resolved to
+// eps ||A|| / gap.  A (m x m row-major, lda) is destroyed; H (m x m) holds the
+// reflectors (tau_k on its diagonal); V (row-major m x m) the eigenvectors.
 // ---------------------------------------------------------------------------
 __device__ double block_sum_d(double v, double *red)
 {
@@ -411,18 +417,20 @@ __device__ double block_sum_d(double v, double *red)
 }
 
 __global__ void __launch_bounds__(256) k_heev_tridiag(int m, double2 *Ab, long long lda, long long sa, double2 *Hb,
-                                                      double2 *Vb, long long sv, double *Wb, int *flag)
+                                                      long long sv, double *Wb, int *posb, double2 *logb,
+                                                      long long logcap, long long *logn, int *flag)
 {
     extern __shared__ double shm[];
     double *d = shm, *e = d + m, *rc = e + m, *rs = rc + m, *red = rs + m;   // red: 32 doubles
     double2 *tau = (double2 *)(red + 32), *v = tau + m, *x = v + m;
-    __shared__ int nrot;
     __shared__ double2 s_tau, s_scale;
     __shared__ double s_beta;
     double2 *A = Ab + blockIdx.x * sa;
     double2 *H = Hb + blockIdx.x * sv;
-    double2 *V = Vb + blockIdx.x * sv;
     double *W = Wb + (long long)blockIdx.x * m;
+    int *pos = posb + (long long)blockIdx.x * m;
+    double2 *lg = logb + blockIdx.x * logcap;   // per sweep: (mm, nrot), then nrot (s, c)
+    long long lp = 0;                            // log length (thread 0)
     const int tid = threadIdx.x, nt = blockDim.x;
     // ---- tridiagonalisation --------------------------------------------------
     for (int k = 0; k < m - 1; ++k) {
@@ -459,7 +467,7 @@ __global__ void __launch_bounds__(256) k_heev_tridiag(int m, double2 *Ab, long l
             v[i] = vi;
             H[(long long)(k + 1 + i) * m + k] = vi;
         }
-        if (tid == 0) tau[k] = t;
+        if (tid == 0) { tau[k] = t; H[(long long)k * m + k] = t; }
         __syncthreads();
         if (t.x != 0 || t.y != 0) {
             // x = tau * A22 v, a warp per row (the lanes read the row coalesced)
@@ -510,8 +518,7 @@ __global__ void __launch_bounds__(256) k_heev_tridiag(int m, double2 *Ab, long l
         __syncthreads();
     }
     if (tid == 0) { d[m - 1] = A[(long long)(m - 1) * lda + (m - 1)].x; e[m - 1] = 0; }
-    // Z = I (real, kept in V.x; V.y = 0)
-    for (int q = tid; q < m * m; q += nt) V[q] = make_double2((q / m == q % m) ? 1.0 : 0.0, 0.0);
+    if (tid == 0) H[(long long)(m - 1) * m + (m - 1)] = make_double2(0, 0);   // no reflector k = m - 1
     __syncthreads();
     // ---- implicit QL on (d, e) ------------------------------------------------
     // deflation: |e| <= eps (|d_i| + |d_i+1|), or |e| <= eps ||T|| -- eigenvalues at the
@@ -570,50 +577,20 @@ __global__ void __launch_bounds__(256) k_heev_tridiag(int m, double2 *Ab, long l
                     ++cnt;
                 }
                 if (!broke) { d[l] -= p; e[l] = g; e[mm] = 0.0; }
-                nrot = cnt;
-            }
-            __syncthreads();
-            // apply the rotations (in generation order) to every row of Z; rotation q
-            // mixes z[i] and z[i+1] (i = mm-1-q), and its new z[i] is the next
-            // rotation's z[i+1]: that value stays in a register, so each step loads
-            // one element that no earlier step wrote
-            for (int row = tid; row < m; row += nt) {
-                double2 *z = V + (long long)row * m;
-                if (nrot == 0) continue;
-                double f = z[mm].x;
-                for (int q = 0; q < nrot; ++q) {
-                    const int i = mm - 1 - q;
-                    const double s = rs[q], c = rc[q], zi = z[i].x;
-                    z[i + 1].x = s * zi + c * f;
-                    f = c * zi - s * f;
+                if (cnt > 0) {
+                    if (lp + 1 + cnt > logcap) {
+                        atomicOr(flag, DEV_BAD_ARG);   // rotation log full (not expected: ~1.5 m^2 rotations)
+                    } else {
+                        lg[lp] = make_double2((double)mm, (double)cnt);
+                        for (int q = 0; q < cnt; ++q) lg[lp + 1 + q] = make_double2(rs[q], rc[q]);
+                        lp += 1 + cnt;
+                    }
                 }
-                z[mm - nrot].x = f;
             }
             __syncthreads();
         }
     }
-    // ---- back-transformation V = H_0 H_1 ... H_{m-2} Z --------------------------
-    for (int k = m - 2; k >= 0; --k) {
-        double2 t = tau[k];
-        if (t.x == 0 && t.y == 0) continue;
-        const int L = m - k - 1;
-        for (int j = tid; j < m; j += nt) {
-            double wr = 0, wi = 0;   // w_j = sum_r conj(v_r) V[r][j]
-            for (int r = 0; r < L; ++r) {
-                double2 vr = H[(long long)(k + 1 + r) * m + k], z = V[(long long)(k + 1 + r) * m + j];
-                wr += vr.x * z.x + vr.y * z.y;
-                wi += vr.x * z.y - vr.y * z.x;
-            }
-            double2 tw = make_double2(t.x * wr - t.y * wi, t.x * wi + t.y * wr);
-            for (int r = 0; r < L; ++r) {
-                double2 vr = H[(long long)(k + 1 + r) * m + k];
-                double2 *z = V + (long long)(k + 1 + r) * m + j;
-                z->x -= vr.x * tw.x - vr.y * tw.y;
-                z->y -= vr.x * tw.y + vr.y * tw.x;
-            }
-        }
-        __syncthreads();
-    }
+    if (tid == 0) logn[blockIdx.x] = lp;
     // ---- sort (descending) ------------------------------------------------------
     __shared__ int ord[1024];
     if (tid == 0) {
@@ -626,21 +603,125 @@ __global__ void __launch_bounds__(256) k_heev_tridiag(int m, double2 *Ab, long l
         }
     }
     __syncthreads();
-    for (int i = tid; i < m; i += nt) W[i] = d[ord[i]];
-    // permute the columns of V through A (scratch)
-    for (int q = tid; q < m * m; q += nt) A[(long long)(q / m) * lda + q % m] = V[(long long)(q / m) * m + ord[q % m]];
+    for (int i = tid; i < m; i += nt) {
+        W[i] = d[ord[i]];
+        pos[ord[i]] = i;   // eigenvector i goes to column pos[i]
+    }
+}
+
+// Z = R_N ... R_1 I for the logged rotations, rows of Z split over CTAs (thread
+// per row).  Z is real, column-major (m x m per matrix in its own buffer), so
+// the threads' accesses to one column coalesce.  Within a sweep, rotation q
+// mixes z[i] and z[i+1] (i = mm-1-q) and its new z[i] is the next rotation's
+// z[i+1]: it stays in a register.
+__global__ void k_heev_rot(int m, double *Zb, const double2 *logb, long long logcap, const long long *logn)
+{
+    const int r = blockIdx.y * blockDim.x + threadIdx.x;
+    if (r >= m) return;
+    double *Z = Zb + (long long)blockIdx.x * m * m;
+    const double2 *lg = logb + blockIdx.x * logcap;
+    for (int col = 0; col < m; ++col) Z[(long long)col * m + r] = col == r ? 1.0 : 0.0;
+    const long long n = logn[blockIdx.x];
+    for (long long lp = 0; lp < n;) {
+        const double2 h = lg[lp];
+        const int mm = (int)h.x, nrot = (int)h.y;
+        double f = Z[(long long)mm * m + r];
+        for (int q = 0; q < nrot; ++q) {
+            const int i = mm - 1 - q;
+            const double2 sc = lg[lp + 1 + q];
+            const double zi = Z[(long long)i * m + r];
+            Z[(long long)(i + 1) * m + r] = sc.x * zi + sc.y * f;
+            f = sc.y * zi - sc.x * f;
+        }
+        Z[(long long)(mm - nrot) * m + r] = f;
+        lp += 1 + nrot;
+    }
+}
+
+// V = H_0 H_1 ... H_{m-2} Z: a CTA takes CB columns of Z into shared memory
+// (complex), applies the reflectors from k = m-2 down to 0 -- column j gets
+// w = tau (v^H z_j), z_j -= v w, each column's sum split over P = 256 / CB
+// threads and met by shuffles -- and writes the columns to their sorted places.
+__global__ void __launch_bounds__(256) k_heev_back(int m, int cb, const double2 *Hb, const double *Zb, double2 *Vb,
+                                                   long long sv, const int *posb)
+{
+    extern __shared__ double2 hb_sm[];
+    double2 *Zs = hb_sm;                        // [m][cb]
+    double2 *vk = hb_sm + (size_t)m * cb;       // [m] current reflector
+    const double2 *H = Hb + blockIdx.x * sv;
+    double2 *V = Vb + blockIdx.x * sv;
+    const double *Z = Zb + (long long)blockIdx.x * m * m;   // column-major real, from k_heev_rot
+    const int *pos = posb + (long long)blockIdx.x * m;
+    const int j0 = blockIdx.y * cb, ncol = min(cb, m - j0);
+    const int P = blockDim.x / cb, tid = threadIdx.x, jj = tid / P, part = tid % P;
+    for (int q = tid; q < m * cb; q += blockDim.x) {
+        const int jc = q / m, r = q % m;        // consecutive threads: consecutive rows of one column
+        Zs[(size_t)r * cb + jc] = make_double2(jc < ncol ? Z[(long long)(j0 + jc) * m + r] : 0.0, 0.0);
+    }
     __syncthreads();
-    for (int q = tid; q < m * m; q += nt) V[q] = A[(long long)(q / m) * lda + q % m];
+    for (int k = m - 2; k >= 0; --k) {
+        const double2 t = H[(long long)k * m + k];
+        if (t.x == 0 && t.y == 0) continue;
+        const int L = m - k - 1;
+        for (int r = tid; r < L; r += blockDim.x) vk[r] = H[(long long)(k + 1 + r) * m + k];
+        __syncthreads();
+        double wr = 0, wi = 0;   // w_j = sum_r conj(v_r) Z[k+1+r][j]
+        for (int r = part; r < L; r += P) {
+            const double2 vr = vk[r], z = Zs[(size_t)(k + 1 + r) * cb + jj];
+            wr += vr.x * z.x + vr.y * z.y;
+            wi += vr.x * z.y - vr.y * z.x;
+        }
+        for (int o = P / 2; o > 0; o >>= 1) {
+            wr += __shfl_xor_sync(0xffffffffu, wr, o);
+            wi += __shfl_xor_sync(0xffffffffu, wi, o);
+        }
+        const double2 tw = make_double2(t.x * wr - t.y * wi, t.x * wi + t.y * wr);
+        for (int r = part; r < L; r += P) {
+            const double2 vr = vk[r];
+            double2 *z = Zs + (size_t)(k + 1 + r) * cb + jj;
+            z->x -= vr.x * tw.x - vr.y * tw.y;
+            z->y -= vr.x * tw.y + vr.y * tw.x;
+        }
+        __syncthreads();   // vk is reloaded for the next reflector
+    }
+    for (int q = tid; q < m * cb; q += blockDim.x) {
+        const int r = q / cb, jc = q % cb;
+        if (jc < ncol) V[(long long)r * m + pos[j0 + jc]] = Zs[(size_t)r * cb + jc];
+    }
 }
 
 int heev_dev(midas_gpu_ctx *c, int batch, int m, double2 *A, long long lda, long long sa, double2 *H, double2 *V,
              long long sv, double *W)
 {
     if (m > 1024) return c->err.set(MIDAS_ERR_ARG, "heev: m > 1024");
+    // scratch: rotation log (16 m^2 + m entries per matrix; QL takes ~1.5 m^2),
+    // log lengths, sort positions, Z (m x m real per matrix)
+    const long long logcap = 16LL * m * m + m;
+    const size_t need = sizeof(double2) * (size_t)batch * logcap + sizeof(long long) * batch +
+                        sizeof(int) * (size_t)batch * m + sizeof(double) * (size_t)batch * m * m + 4 * 256;
+    void *p;
+    MIDAS_TRY(ensure(c, S_HEEV, need, &p));
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        off = (off + 255) & ~(size_t)255;
+        char *q = (char *)p + off;
+        off += bytes;
+        return q;
+    };
+    double2 *lg = (double2 *)take(sizeof(double2) * (size_t)batch * logcap);
+    long long *logn = (long long *)take(sizeof(long long) * batch);
+    int *pos = (int *)take(sizeof(int) * (size_t)batch * m);
+    double *Z = (double *)take(sizeof(double) * (size_t)batch * m * m);
     size_t sm = sizeof(double) * (4 * (size_t)m + 32) + sizeof(double2) * 3 * (size_t)m;
-    ++c->launches;
+    int cb = 32;   // columns per back-transformation CTA: Z columns [m][cb] + the reflector [m]
+    while (cb > 8 && sizeof(double2) * (size_t)m * (cb + 1) > 200 * 1024) cb /= 2;
+    const size_t smb = sizeof(double2) * (size_t)m * (cb + 1);
+    MIDAS_CUDA(c, cudaFuncSetAttribute(k_heev_back, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smb));
+    c->launches += 3;
     int kp = kp_begin(c);
-    k_heev_tridiag<<<batch, 256, sm, c->stream>>>(m, A, lda, sa, H, V, sv, W, c->d_flag);
+    k_heev_tridiag<<<batch, 256, sm, c->stream>>>(m, A, lda, sa, H, sv, W, pos, lg, logcap, logn, c->d_flag);
+    k_heev_rot<<<dim3(batch, (m + 31) / 32), 32, 0, c->stream>>>(m, Z, lg, logcap, logn);   // a warp per CTA: more SMs
+    k_heev_back<<<dim3(batch, (m + cb - 1) / cb), 256, smb, c->stream>>>(m, cb, H, Z, V, sv, pos);
     kp_end(c, kp, MIDAS_KC_EIG, 0.0, 0.0);
     MIDAS_CUDA(c, cudaGetLastError());
     return MIDAS_OK;
