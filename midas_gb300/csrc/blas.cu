@@ -196,6 +196,132 @@ int zgemm64(midas_gpu_ctx *c, int M, int N, int K, const double2 *A, long long a
 }
 
 // ---------------------------------------------------------------------------
+// C = A B, complex, FP64 in and out (strided: A(i,k) at A[i*ars + k*acs], B(k,j)
+// at B[k*brs + j*bcs], C(i,j) at C[i*crs + j*ccs]), computed in double float on
+// the FP32 pipe: operands split into hi = fl32(x), lo = fl32(x - hi) as they are
+// staged, products exact (FMA TwoProduct + cross terms), sums compensated
+// (TwoSum) -- ~2^-48 relative, on a pipe 64x faster than GB300's FP64.  For the
+// CBF construction C_b = X V Sigma^-1, Vc = C^T Einc and E = C alpha.  64 x 64
+// output tiles, 4 x 4 per thread; the K range is split S ways when the tiles are
+// too few to fill the GPU, the S partial (hi, lo) pairs summed in FP64.
+// ---------------------------------------------------------------------------
+constexpr int ZD_TK = 16, ZD_SMAX = 32;
+
+__device__ __forceinline__ float4 zd_split(double2 v)
+{
+    float4 r;
+    r.x = (float)v.x;
+    r.y = (float)v.y;
+    r.z = (float)(v.x - (double)r.x);
+    r.w = (float)(v.y - (double)r.y);
+    return r;
+}
+
+__global__ void __launch_bounds__(256) k_zgemm_df(int M, int N, int K, const double2 *__restrict__ A, long long ars,
+                                                   long long acs, const double2 *__restrict__ B, long long brs,
+                                                   long long bcs, double2 *C, long long crs, long long ccs,
+                                                   int kchunk, float4 *P)
+{
+    __shared__ float4 As[ZD_TK][64], Bs[ZD_TK][64];
+    const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
+    const int i0 = blockIdx.y * 64, j0 = blockIdx.x * 64, sp = blockIdx.z;
+    const int kb = sp * kchunk, ke = min(K, kb + kchunk);
+    float rh[4][4], rl[4][4], ih[4][4], il[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) rh[a][b] = rl[a][b] = ih[a][b] = il[a][b] = 0.f;
+    for (int k0 = kb; k0 < ke; k0 += ZD_TK) {
+        for (int e = tid; e < ZD_TK * 64; e += 256) {
+            const int kk = e / 64, c = e % 64, k = k0 + kk;
+            const int i = i0 + c, j = j0 + c;
+            As[kk][c] = (k < ke && i < M) ? zd_split(A[(long long)i * ars + (long long)k * acs])
+                                          : make_float4(0.f, 0.f, 0.f, 0.f);
+            Bs[kk][c] = (k < ke && j < N) ? zd_split(B[(long long)k * brs + (long long)j * bcs])
+                                          : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        __syncthreads();
+#pragma unroll 1
+        for (int kk = 0; kk < ZD_TK; ++kk) {
+            float4 a[4], b[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) a[u] = As[kk][ty + 16 * u];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) b[u] = Bs[kk][tx + 16 * u];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int v = 0; v < 4; ++v) {
+                    // re += ar br - ai bi, im += ar bi + ai br (hi = .x/.y, lo = .z/.w)
+                    df_fma(rh[u][v], rl[u][v], a[u].x, b[v].x, a[u].z, b[v].z);
+                    df_fma(rh[u][v], rl[u][v], -a[u].y, b[v].y, -a[u].w, b[v].w);
+                    df_fma(ih[u][v], il[u][v], a[u].x, b[v].y, a[u].z, b[v].w);
+                    df_fma(ih[u][v], il[u][v], a[u].y, b[v].x, a[u].w, b[v].z);
+                }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const int i = i0 + ty + 16 * u, j = j0 + tx + 16 * v;
+            if (i >= M || j >= N) continue;
+            if (P)
+                P[((long long)sp * M + i) * N + j] = make_float4(rh[u][v], ih[u][v], rl[u][v], il[u][v]);
+            else
+                C[(long long)i * crs + (long long)j * ccs] =
+                    make_double2((double)rh[u][v] + (double)rl[u][v], (double)ih[u][v] + (double)il[u][v]);
+        }
+}
+
+__global__ void k_zgemm_df_reduce(int M, int N, int nsplit, const float4 *P, double2 *C, long long crs, long long ccs)
+{
+    const long long tot = (long long)M * N;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tot;
+         e += (long long)gridDim.x * blockDim.x) {
+        double re = 0, im = 0;
+        for (int s = 0; s < nsplit; ++s) {
+            const float4 p = P[(long long)s * tot + e];
+            re += (double)p.x + (double)p.z;
+            im += (double)p.y + (double)p.w;
+        }
+        const int i = (int)(e / N), j = (int)(e % N);
+        C[(long long)i * crs + (long long)j * ccs] = make_double2(re, im);
+    }
+}
+
+int zgemm_df(midas_gpu_ctx *c, int M, int N, int K, const double2 *A, long long ars, long long acs,
+             const double2 *B, long long brs, long long bcs, double2 *C, long long crs, long long ccs)
+{
+    if (M <= 0 || N <= 0) return MIDAS_OK;
+    if (K <= 0) return c->err.set(MIDAS_ERR_ARG, "zgemm_df: K must be positive");
+    const long long tiles = (long long)((M + 63) / 64) * ((N + 63) / 64);
+    int nsplit = (int)std::min<long long>(ZD_SMAX, std::max<long long>(1, 300 / tiles));
+    nsplit = std::max(1, std::min(nsplit, K / 64));
+    const int kchunk = ((K + nsplit - 1) / nsplit + ZD_TK - 1) / ZD_TK * ZD_TK;
+    float4 *P = nullptr;
+    if (nsplit > 1) {
+        void *p;
+        MIDAS_TRY(ensure(c, S_ZDF, sizeof(float4) * (size_t)nsplit * M * N + 256, &p));
+        P = (float4 *)p;
+    }
+    ++c->launches;
+    int kp = kp_begin(c);
+    k_zgemm_df<<<dim3((N + 63) / 64, (M + 63) / 64, nsplit), 256, 0, c->stream>>>(M, N, K, A, ars, acs, B, brs, bcs,
+                                                                                  C, crs, ccs, kchunk, P);
+    if (nsplit > 1) {
+        ++c->launches;
+        const long long tot = (long long)M * N;
+        k_zgemm_df_reduce<<<(unsigned)std::min<long long>((tot + 255) / 256, 4096), 256, 0, c->stream>>>(
+            M, N, nsplit, P, C, crs, ccs);
+    }
+    kp_end(c, kp, MIDAS_KC_ZGEMM64, 8.0 * M * (double)N * K, 16.0 * ((double)M * K + (double)K * N + (double)M * N));
+    MIDAS_CUDA(c, cudaGetLastError());
+    return MIDAS_OK;
+}
+
+// ---------------------------------------------------------------------------
 // Gram matrix G = X^H X (m x m, row-major FP64) of a block's CBF solutions in
 // double float on the FP32 pipe (the FP64 pipe of GB300 runs at 1/64 of it).
 // X = Xh + Xl (the refinement's own hi/lo copies), element (k, j) at

@@ -48,6 +48,8 @@ int residual_df32(midas_gpu_ctx *c, int n, int nrhs, const float2 *Z, long long 
 int heev_dev(midas_gpu_ctx *c, int batch, int m, double2 *A, long long lda, long long sa, double2 *H, double2 *V,
              long long sv, double *W);
 size_t gram_df_scratch_bytes(int m);
+int zgemm_df(midas_gpu_ctx *c, int M, int N, int K, const double2 *A, long long ars, long long acs,
+             const double2 *B, long long brs, long long bcs, double2 *C, long long crs, long long ccs);
 int gram_df(midas_gpu_ctx *c, int m, int K, const float2 *Xh, const float2 *Xl, long long rs, long long cs,
             double2 *G, float4 *P);
 
@@ -561,8 +563,7 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
         k_scale_cols<<<(m * K + 255) / 256, 256, 0, c->stream>>>(m, K, Vv, W);
         // C_b = X[0:3 n_b, :] V_K Sigma_K^-1  (column-major 3 n_b x K)
         double2 *Cb = Call + coff[b];
-        MIDAS_TRY(zgemm64(c, 3 * nbc, K, m, X64, 1, sp, 0, Vv, m, 1, Cb, 1, 3 * nbc, make_double2(1, 0),
-                          make_double2(0, 0)));
+        MIDAS_TRY(zgemm_df(c, 3 * nbc, K, m, X64, 1, sp, Vv, m, 1, Cb, 1, 3 * nbc));
         coff[b + 1] = coff[b] + (size_t)3 * nbc * K;
     }
     cudaEventRecord(e1, c->stream);
@@ -669,8 +670,7 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
         const int nbc = bo[b + 1] - bo[b];
         MIDAS_TRY(launch_incident4<double2>(c, nbc, d_all + bo[b], ntr, d_th, d_ph, Einc, 1, (size_t)3 * nbc));
         // Vc[koff_b .., :] = C_b^T Einc_b  (plain transpose)
-        MIDAS_TRY(zgemm64(c, Kb[b], nr, 3 * nbc, Call + coff[b], 3 * nbc, 1, 0, Einc, 1, 3 * nbc, Vc + koff[b], 1, npd,
-                          make_double2(1, 0), make_double2(0, 0)));
+        MIDAS_TRY(zgemm_df(c, Kb[b], nr, 3 * nbc, Call + coff[b], 3 * nbc, 1, Einc, 1, 3 * nbc, Vc + koff[b], 1, npd));
     }
     midas_gpu_info sinfo;
     memset(&sinfo, 0, sizeof(sinfo));
@@ -685,8 +685,8 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
     }
     for (int b = 0; b < nb; ++b) {
         const int nbc = bo[b + 1] - bo[b];
-        MIDAS_TRY(zgemm64(c, 3 * nbc, nr, Kb[b], Call + coff[b], 1, 3 * nbc, 0, (const double2 *)px + koff[b], 1, npd,
-                          Eout + 3 * (size_t)bo[b], 1, 3LL * n, make_double2(1, 0), make_double2(0, 0)));
+        MIDAS_TRY(zgemm_df(c, 3 * nbc, nr, Kb[b], Call + coff[b], 1, 3 * nbc, (const double2 *)px + koff[b], 1, npd,
+                           Eout + 3 * (size_t)bo[b], 1, 3LL * n));
     }
     cudaEventRecord(e3, c->stream);
     MIDAS_CUDA(c, cudaStreamSynchronize(c->stream));
