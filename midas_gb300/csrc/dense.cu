@@ -35,138 +35,145 @@
 namespace midas {
 
 // ---------------------------------------------------------------------------
-// diagonal block: unblocked LU of A11 (nb x nb, row-major, lda) in shared
-// memory, then L11^-1 and U11^-1 by substitution.  One CTA, 512 threads.
-// Writes L\U back to A11, Linv/Uinv to their slots, and the expanded U11^-1
-// (the Bt operand of L21 = A21 U11^-1) to UinvExp (2nb x 2nb floats).
+// diagonal block: unblocked LU of A11 (nb x nb, row-major, lda) without pivoting,
+// with L11^-1 built alongside (Gauss-Jordan on [A | I]) and U11^-1 by a backward
+// Gauss-Jordan sweep.  One CTA of 512 threads; the block, L^-1 and U^-1 stay in
+// registers (thread (tx, ty): column tx, rows ty + 8k), only the pivot row, the
+// multiplier column and the reciprocal diagonal go through shared memory.
+// Writes L\U back to A11, Linv/Uinv (rounded to TF32: GEMM operands), and the
+// expanded U11^-1 (the Bt operand of L21 = A21 U11^-1) to UinvExp (2nb x 2nb floats).
 // ---------------------------------------------------------------------------
 template <int NB>
 __global__ void __launch_bounds__(512) k_diag_lu(float2 *A11, long long lda, float2 *Linv, float2 *Uinv,
                                                   float *UinvExp, float tiny, int *flag)
 {
-    extern __shared__ float2 sm[];
-    float2 *a = sm;                 // NB x NB
-    float2 *li = sm + NB * NB;      // NB x NB
-    float2 *ui = li + NB * NB;      // NB x NB
-    const int tid = threadIdx.x, nt = blockDim.x;
-    for (int i = tid; i < NB * NB; i += nt) a[i] = A11[(long long)(i / NB) * lda + (i % NB)];
-    __syncthreads();
-    // right-looking elimination without pivoting; the update maps a thread to a
-    // column (tx) and every (nt / NB)-th row (ty), so no index division is needed
+    // register-resident: thread (tx, ty) holds column tx, rows ty + 8k (k < 8), of
+    // the block (ra), of L^-1 (rx) and of U^-1 (ry); only the pivot row, the
+    // multiplier column and the reciprocal diagonal go through shared memory.
     static_assert(NB == 64, "thread mapping assumes 64-wide blocks");
-    if (nt != 8 * NB) {   // the update below gives each thread NB / 8 rows
+    constexpr int R = NB / 8;
+    __shared__ float2 prow[2][NB], xrow[2][NB], lcol[NB], rdiag[NB];
+    __shared__ float2 stage[NB][NB + 1];
+    const int tid = threadIdx.x;
+    if (blockDim.x != 8 * NB) {
         if (tid == 0) atomicOr(flag, DEV_BAD_ARG);
         return;
     }
-    const int tx = tid % NB, ty = tid / NB, nty = nt / NB;
+    const int tx = tid % NB, ty = tid / NB;
+    float2 ra[R], rx[R], ry[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int i = ty + 8 * k;
+        ra[k] = A11[(long long)i * lda + tx];
+        rx[k] = make_float2(i == tx ? 1.f : 0.f, 0.f);
+        ry[k] = rx[k];
+    }
+    if (ty == 0) { prow[0][tx] = ra[0]; xrow[0][tx] = rx[0]; }
+    __syncthreads();
+    // ---- elimination with L^-1 by Gauss-Jordan on [A | I] ----------------------
     for (int j = 0; j < NB; ++j) {
-        if (tid < NB - j - 1) {
-            const float2 piv = a[j * NB + j];
-            const float pm = piv.x * piv.x + piv.y * piv.y;
-            const float2 ip = make_float2(piv.x / pm, -piv.y / pm);
-            const int i = j + 1 + tid;
-            const float2 v = a[i * NB + j];
-            a[i * NB + j] = make_float2(v.x * ip.x - v.y * ip.y, v.x * ip.y + v.y * ip.x);
-        }
-        if (tid == 0) {
-            const float2 piv = a[j * NB + j];
-            if (!(piv.x * piv.x + piv.y * piv.y > tiny * tiny)) atomicOr(flag, DEV_ZERO_PIVOT);
-        }
-        __syncthreads();
-        if (tx > j) {
-            // all loads first, then the updates: 16 independent shared loads in flight
-            constexpr int RPT = NB / 8;   // rows per thread (nty == 8)
-            const float2 u = a[j * NB + tx];
-            float2 l[RPT], d[RPT];
+        const int b = j & 1;
+        const float2 piv = prow[b][j];
+        const float pm = piv.x * piv.x + piv.y * piv.y;
+        if (tid == 0 && !(pm > tiny * tiny)) atomicOr(flag, DEV_ZERO_PIVOT);
+        if (tx == j) {   // multipliers of column j (kept as the L entries)
+            const float rp = __frcp_rn(pm);
+            const float2 ip = make_float2(piv.x * rp, -piv.y * rp);
 #pragma unroll
-            for (int k = 0; k < RPT; ++k) {
-                const int i = j + 1 + ty + nty * k;
-                if (i < NB) { l[k] = a[i * NB + j]; d[k] = a[i * NB + tx]; }
-            }
-#pragma unroll
-            for (int k = 0; k < RPT; ++k) {
-                const int i = j + 1 + ty + nty * k;
-                if (i < NB)
-                    a[i * NB + tx] = make_float2(d[k].x - (l[k].x * u.x - l[k].y * u.y),
-                                                 d[k].y - (l[k].x * u.y + l[k].y * u.x));
-            }
-        }
-        __syncthreads();
-    }
-    // Triangular inverses, a column per group of 4 lanes: threads 0..255 build
-    // L^-1 (unit lower) column c = t / 4 top-down,
-    //   X[c][c] = 1,  X[i][c] = -sum_{m=c}^{i-1} L[i][m] X[m][c];
-    // threads 256..511 build U^-1 column c bottom-up,
-    //   X[c][c] = 1/U[c][c],  X[i][c] = -(sum_{m=i+1}^{c} U[i][m] X[m][c]) / U[i][i].
-    // The 4 lanes split the sum over m and meet by shuffles; the i loop runs over
-    // the warp's whole column range (8 columns) so every lane reaches the shuffles.
-    __shared__ float2 rdiag[NB];
-    for (int t = tid; t < NB * NB; t += nt) { li[t] = make_float2(0.f, 0.f); ui[t] = make_float2(0.f, 0.f); }
-    if (tid < NB) {
-        const float2 d = a[tid * NB + tid];
-        const float dm = d.x * d.x + d.y * d.y;
-        rdiag[tid] = make_float2(d.x / dm, -d.y / dm);
-    }
-    __syncthreads();
-    {
-        const int q = tid % 256, cc = q / 4, l4 = q % 4;
-        const int cw0 = (q / 32) * 8, cw1 = cw0 + 7;   // the warp's columns
-        if (tid < 256) {
-            if (l4 == 0) li[cc * NB + cc] = make_float2(1.f, 0.f);
-            __syncwarp();
-            for (int i = cw0 + 1; i < NB; ++i) {
-                float2 s = make_float2(0.f, 0.f);
-                if (i > cc)
-                    for (int m = cc + l4; m < i; m += 4) {
-                        const float2 l = a[i * NB + m], x = li[m * NB + cc];
-                        s.x += l.x * x.x - l.y * x.y;
-                        s.y += l.x * x.y + l.y * x.x;
-                    }
-                s.x += __shfl_xor_sync(0xffffffffu, s.x, 1);
-                s.y += __shfl_xor_sync(0xffffffffu, s.y, 1);
-                s.x += __shfl_xor_sync(0xffffffffu, s.x, 2);
-                s.y += __shfl_xor_sync(0xffffffffu, s.y, 2);
-                if (i > cc && l4 == 0) li[i * NB + cc] = make_float2(-s.x, -s.y);
-                __syncwarp();
-            }
-        } else {
-            for (int i = cw1; i >= 0; --i) {
-                float2 s = make_float2(0.f, 0.f);
-                if (i <= cc)
-                    for (int m = i + 1 + l4; m <= cc; m += 4) {
-                        const float2 u = a[i * NB + m], x = ui[m * NB + cc];
-                        s.x += u.x * x.x - u.y * x.y;
-                        s.y += u.x * x.y + u.y * x.x;
-                    }
-                s.x += __shfl_xor_sync(0xffffffffu, s.x, 1);
-                s.y += __shfl_xor_sync(0xffffffffu, s.y, 1);
-                s.x += __shfl_xor_sync(0xffffffffu, s.x, 2);
-                s.y += __shfl_xor_sync(0xffffffffu, s.y, 2);
-                if (i <= cc && l4 == 0) {
-                    const float2 v = make_float2((i == cc ? 1.f : 0.f) - s.x, -s.y), id = rdiag[i];
-                    ui[i * NB + cc] = make_float2(v.x * id.x - v.y * id.y, v.x * id.y + v.y * id.x);
+            for (int k = 0; k < R; ++k) {
+                const int i = ty + 8 * k;
+                if (i > j) {
+                    const float2 v = ra[k];
+                    ra[k] = make_float2(v.x * ip.x - v.y * ip.y, v.x * ip.y + v.y * ip.x);
+                    lcol[i] = ra[k];
                 }
-                __syncwarp();
             }
         }
+        __syncthreads();
+        const float2 u = prow[b][tx], xv = xrow[b][tx];
+#pragma unroll
+        for (int k = 0; k < R; ++k) {
+            const int i = ty + 8 * k;
+            if (i > j) {
+                const float2 l = lcol[i];
+                if (tx > j) ra[k] = make_float2(ra[k].x - (l.x * u.x - l.y * u.y), ra[k].y - (l.x * u.y + l.y * u.x));
+                else rx[k] = make_float2(rx[k].x - (l.x * xv.x - l.y * xv.y), rx[k].y - (l.x * xv.y + l.y * xv.x));
+            }
+        }
+        if (j + 1 < NB && ty == (j + 1) % 8) {   // row j + 1 is final now: publish it
+            const int ks = (j + 1) / 8;
+            float2 sa = ra[0], sx = rx[0];   // select chains, not an indexed access: the arrays stay in registers
+#pragma unroll
+            for (int k = 1; k < R; ++k) {
+                sa = ks == k ? ra[k] : sa;
+                sx = ks == k ? rx[k] : sx;
+            }
+            prow[b ^ 1][tx] = sa;
+            xrow[b ^ 1][tx] = sx;
+        }
+        __syncthreads();
+    }
+    // ---- U^-1 by backward Gauss-Jordan on [U | I] ------------------------------
+#pragma unroll
+    for (int k = 0; k < R; ++k)
+        if (ty + 8 * k == tx) {
+            const float2 d = ra[k];
+            const float rp = __frcp_rn(d.x * d.x + d.y * d.y);
+            rdiag[tx] = make_float2(d.x * rp, -d.y * rp);
+        }
+    __syncthreads();
+    for (int j = NB - 1; j >= 0; --j) {
+        const int b = j & 1;
+        if (ty == j % 8) {   // row j of Y scaled by 1 / U[j][j]
+            const float2 r = rdiag[j];
+            const int ks = j / 8;
+#pragma unroll
+            for (int k = 0; k < R; ++k) {
+                const float2 sc = make_float2(ry[k].x * r.x - ry[k].y * r.y, ry[k].x * r.y + ry[k].y * r.x);
+                ry[k] = ks == k ? sc : ry[k];
+            }
+            float2 sy = ry[0];
+#pragma unroll
+            for (int k = 1; k < R; ++k) sy = ks == k ? ry[k] : sy;
+            xrow[b][tx] = sy;
+        }
+        if (tx == j) {   // column j of U above the diagonal
+#pragma unroll
+            for (int k = 0; k < R; ++k)
+                if (ty + 8 * k < j) lcol[ty + 8 * k] = ra[k];
+        }
+        __syncthreads();
+        const float2 yv = xrow[b][tx];
+#pragma unroll
+        for (int k = 0; k < R; ++k) {
+            const int i = ty + 8 * k;
+            if (i < j) {
+                const float2 uu = lcol[i];
+                ry[k] = make_float2(ry[k].x - (uu.x * yv.x - uu.y * yv.y), ry[k].y - (uu.x * yv.y + uu.y * yv.x));
+            }
+        }
+        __syncthreads();
+    }
+    // ---- write-back: L\U, the inverses rounded to TF32 (GEMM operands), and the
+    // expanded U^-1 as the Bt operand of L21 = A21 U11^-1:
+    // Bt[2j][2p] = Ur(p,j), Bt[2j][2p+1] = -Ui(p,j), Bt[2j+1][2p] = Ui, Bt[2j+1][2p+1] = Ur
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int i = ty + 8 * k;
+        A11[(long long)i * lda + tx] = ra[k];
+        Linv[i * NB + tx] = make_float2(tf32_rna(rx[k].x), tf32_rna(rx[k].y));
+        const float2 uq = make_float2(tf32_rna(ry[k].x), tf32_rna(ry[k].y));
+        Uinv[i * NB + tx] = uq;
+        stage[i][tx] = uq;
     }
     __syncthreads();
-    // the inverses are GEMM operands: stored rounded to TF32 (nearest)
-    for (int i = tid; i < NB * NB; i += nt) {
-        A11[(long long)(i / NB) * lda + (i % NB)] = a[i];
-        Linv[i] = make_float2(tf32_rna(li[i].x), tf32_rna(li[i].y));
-        Uinv[i] = make_float2(tf32_rna(ui[i].x), tf32_rna(ui[i].y));
-    }
-    // expanded U^-1 as the Bt operand (rows = output columns j, along p):
-    // Bt[2j][2p] = Ur(p,j), Bt[2j][2p+1] = -Ui(p,j), Bt[2j+1][2p] = Ui, Bt[2j+1][2p+1] = Ur
-    // (consecutive threads take consecutive p: the global writes coalesce)
-    for (int t = tid; t < NB * NB; t += nt) {
-        int j = t / NB, p = t % NB;
-        float2 u = make_float2(tf32_rna(ui[p * NB + j].x), tf32_rna(ui[p * NB + j].y));
-        float *r0 = UinvExp + (long long)(2 * j) * (2 * NB) + 2 * p;
+    for (int t = tid; t < NB * NB; t += blockDim.x) {
+        const int jo = t / NB, p = t % NB;   // consecutive threads: consecutive p, coalesced writes
+        const float2 uq = stage[p][jo];
+        float *r0 = UinvExp + (long long)(2 * jo) * (2 * NB) + 2 * p;
         float *r1 = r0 + 2 * NB;
-        r0[0] = u.x; r0[1] = -u.y;
-        r1[0] = u.y; r1[1] = u.x;
+        r0[0] = uq.x; r0[1] = -uq.y;
+        r1[0] = uq.y; r1[1] = uq.x;
     }
 }
 
@@ -389,10 +396,9 @@ int lu_factor_nopiv(midas_gpu_ctx *c, DenseLU &lu)
         hmax = (unsigned *)(b16 + (size_t)2 * n * 2 * nb2);
         halpha = (float *)(hmax + 2);
     }
-    const size_t smem = sizeof(float2) * 3 * nb * nb, mi_smem = sizeof(float2) * 2 * 64 * MI_LD;
+    const size_t mi_smem = sizeof(float2) * 2 * 64 * MI_LD;
     static bool attr = false;
     if (!attr) {
-        MIDAS_CUDA(c, cudaFuncSetAttribute(k_diag_lu<LU_NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         MIDAS_CUDA(c, cudaFuncSetAttribute(k_macro_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mi_smem));
         attr = true;
     }
@@ -431,7 +437,7 @@ int lu_factor_nopiv(midas_gpu_ctx *c, DenseLU &lu)
             float2 *A11 = lu.A + (long long)j0 * lda + j0;
             ++c->launches;
             int kp = kp_begin(c);
-            k_diag_lu<LU_NB><<<1, 512, smem, c->stream>>>(A11, lda, lu.Linv + (size_t)k * nb * nb,
+            k_diag_lu<LU_NB><<<1, 512, 0, c->stream>>>(A11, lda, lu.Linv + (size_t)k * nb * nb,
                                                           lu.Uinv + (size_t)k * nb * nb, uexp, 1e-30f, c->d_flag);
             kp_end(c, kp, MIDAS_KC_DIAG_LU, 8.0 * nb * nb * nb, 8.0 * nb * nb * 4);
             MIDAS_CUDA(c, cudaGetLastError());
