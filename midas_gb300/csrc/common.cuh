@@ -1,6 +1,7 @@
 // common.cuh -- shared definitions of the GB300 MIDAS library (internal).
 #pragma once
 #include <cuda_runtime.h>
+#include <atomic>
 #include <cstdint>
 #include <cstdio>
 #include <string>
@@ -153,6 +154,25 @@ struct midas_gpu_ctx {
 };
 
 namespace midas {
+
+// One-time per-device setup (kernel attributes) that several host threads -- the
+// CBFM lanes -- may reach at once: f runs until it succeeds once on a device; a
+// race only repeats the idempotent call.
+struct PerDeviceOnce {
+    std::atomic<unsigned long long> mask{0};
+    template <typename F>
+    cudaError_t run(int device, F f)
+    {
+        const unsigned long long bit = 1ull << (device & 63);
+        if (mask.load(std::memory_order_acquire) & bit) return cudaSuccess;
+        const cudaError_t e = f();
+        if (e == cudaSuccess) mask.fetch_or(bit, std::memory_order_acq_rel);
+        return e;
+    }
+};
+
+// Number of SMs of a device (cached per device, thread-safe).
+int device_sms(midas_gpu_ctx *ctx);
 
 // Scratch allocation helpers (pool slot i grows as needed).
 int ensure(midas_gpu_ctx *ctx, int slot, size_t bytes, void **out);

@@ -397,11 +397,10 @@ int lu_factor_nopiv(midas_gpu_ctx *c, DenseLU &lu)
         halpha = (float *)(hmax + 2);
     }
     const size_t mi_smem = sizeof(float2) * 2 * 64 * MI_LD;
-    static bool attr = false;
-    if (!attr) {
-        MIDAS_CUDA(c, cudaFuncSetAttribute(k_macro_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mi_smem));
-        attr = true;
-    }
+    static PerDeviceOnce once;
+    MIDAS_CUDA(c, once.run(c->device, [mi_smem] {
+        return cudaFuncSetAttribute(k_macro_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mi_smem);
+    }));
     const long long lda = lu.lda;
     float *Af = (float *)lu.A;
     // the 256-row diagonal-block inverses only feed the later solves: off the

@@ -16,6 +16,7 @@
 // path on the device (gemm_selftest) and selectable with MIDAS_GEMM=simt.
 #include <cuda.h>
 #include <cuda_fp16.h>
+#include <atomic>
 #include <cstdlib>
 #include <cstring>
 
@@ -610,17 +611,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 typedef CUresult (*PFN_encodeTiled)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
                                     const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
                                     CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-static PFN_encodeTiled g_encode = nullptr;
+static std::atomic<PFN_encodeTiled> g_encode{nullptr};
 
 static int get_encode(midas_gpu_ctx *c)
 {
-    if (g_encode) return MIDAS_OK;
+    if (g_encode.load(std::memory_order_acquire)) return MIDAS_OK;
     cudaDriverEntryPointQueryResult q;
     void *fn = nullptr;
     cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
     if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn)
         return c->err.set(MIDAS_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled entry point unavailable");
-    g_encode = (PFN_encodeTiled)fn;
+    g_encode.store((PFN_encodeTiled)fn, std::memory_order_release);
     return MIDAS_OK;
 }
 
@@ -633,7 +634,8 @@ static int make_map(midas_gpu_ctx *c, CUtensorMap *m, const void *base, int rows
     cuuint64_t strides[1] = {(cuuint64_t)ld * es_bytes};
     cuuint32_t box[2] = {(cuuint32_t)(128 / es_bytes), (cuuint32_t)box_rows};
     cuuint32_t es[2] = {1, 1};
-    CUresult r = g_encode(m, h16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+    CUresult r = g_encode.load(std::memory_order_acquire)(
+                          m, h16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
                           (void *)base, dims, strides, box, es,
                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
@@ -641,18 +643,18 @@ static int make_map(midas_gpu_ctx *c, CUtensorMap *m, const void *base, int rows
     return MIDAS_OK;
 }
 
-static int g_engine = -1;   // 0 simt, 1 tcgen05
-
-const char *gemm_engine() { return g_engine == 0 ? "simt" : "tcgen05"; }
-
+// 0 simt, 1 tcgen05 (MIDAS_GEMM=simt selects the CUDA-core engine); read once,
+// thread-safe (function-local static initialisation)
 static int pick_engine()
 {
-    if (g_engine < 0) {
+    static const int engine = [] {
         const char *e = getenv("MIDAS_GEMM");
-        g_engine = (e && strcmp(e, "simt") == 0) ? 0 : 1;
-    }
-    return g_engine;
+        return (e && strcmp(e, "simt") == 0) ? 0 : 1;
+    }();
+    return engine;
 }
+
+const char *gemm_engine() { return pick_engine() == 0 ? "simt" : "tcgen05"; }
 
 bool gemm_tc_engine() { return pick_engine() == 1; }
 
@@ -678,16 +680,16 @@ static int gemm_tcp_h16(midas_gpu_ctx *c, const GemmArgs &g)
 {
     if ((((uintptr_t)g.D) & 15) || ((g.ldd * 4) & 15))
         return c->err.set(MIDAS_ERR_ARG, "gemm fp16: D must be a 16-byte aligned TMA operand");
-    static int nsm = 0;
-    static bool pattr = false;
-    if (!nsm) MIDAS_CUDA(c, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
-    if (!pattr) {
-        MIDAS_CUDA(c, cudaFuncSetAttribute(k_gemm_tcp<2, 2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          tcp_smem(2, 2)));
-        MIDAS_CUDA(c, cudaFuncSetAttribute(k_gemm_tcp<4, 1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          tcp_smem(4, 1)));
-        pattr = true;
-    }
+    const int nsm = device_sms(c);
+    static PerDeviceOnce once;
+    MIDAS_CUDA(c, once.run(c->device, [] {
+        cudaError_t e = cudaFuncSetAttribute(k_gemm_tcp<2, 2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             tcp_smem(2, 2));
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_gemm_tcp<4, 1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     tcp_smem(4, 1));
+        return e;
+    }));
     CUtensorMap ma, mb, md;
     MIDAS_TRY(make_map(c, &ma, g.A, g.M, g.K, g.lda, TC_BM, true));
     MIDAS_TRY(make_map(c, &mb, g.Bt, g.N, g.K, g.ldb, TC_BN, true));
@@ -715,31 +717,31 @@ static int gemm_tc(midas_gpu_ctx *c, const GemmArgs &g, bool precise)
     if ((((uintptr_t)g.A) & 15) || (((uintptr_t)g.Bt) & 15) || (g.lda & ldm) || (g.ldb & ldm))
         return c->err.set(MIDAS_ERR_ARG, "gemm_tf32: operands must be 16-byte aligned with 16-byte row strides");
     if (g.h16) return gemm_tcp_h16(c, g);
-    static bool attr = false;
-    if (!attr) {
-        MIDAS_CUDA(c, cudaFuncSetAttribute(k_gemm_tc<false, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          tc_smem(4)));
-        MIDAS_CUDA(c, cudaFuncSetAttribute(k_gemm_tc<false, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          tc_smem(2)));
-        MIDAS_CUDA(c, cudaFuncSetAttribute(k_gemm_tc<true, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          tc_smem(4)));
-        attr = true;
-    }
+    static PerDeviceOnce once_tc;
+    MIDAS_CUDA(c, once_tc.run(c->device, [] {
+        cudaError_t e = cudaFuncSetAttribute(k_gemm_tc<false, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             tc_smem(4));
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_gemm_tc<false, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc_smem(2));
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_gemm_tc<true, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc_smem(4));
+        return e;
+    }));
     CUtensorMap ma, mb;
     MIDAS_TRY(make_map(c, &ma, g.A, g.M, g.K, g.lda, TC_BM));
     MIDAS_TRY(make_map(c, &mb, g.Bt, g.N, g.K, g.ldb, TC_BN));
     // persistent kernel whenever D can be a TMA operand
     if (!precise && !(((uintptr_t)g.D) & 15) && !((g.ldd * 4) & 15)) {
-        static int nsm = 0;
-        static bool pattr = false;
-        if (!nsm) MIDAS_CUDA(c, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
-        if (!pattr) {
-            MIDAS_CUDA(c, cudaFuncSetAttribute(k_gemm_tcp<2, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              tcp_smem(2, 2)));
-            MIDAS_CUDA(c, cudaFuncSetAttribute(k_gemm_tcp<4, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              tcp_smem(4, 1)));
-            pattr = true;
-        }
+        const int nsm = device_sms(c);
+        static PerDeviceOnce once_tcp;
+        MIDAS_CUDA(c, once_tcp.run(c->device, [] {
+            cudaError_t e = cudaFuncSetAttribute(k_gemm_tcp<2, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 tcp_smem(2, 2));
+            if (e == cudaSuccess)
+                e = cudaFuncSetAttribute(k_gemm_tcp<4, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         tcp_smem(4, 1));
+            return e;
+        }));
         CUtensorMap md;
         MIDAS_TRY(make_map(c, &md, g.D, g.M, g.N, g.ldd, TC_BM));
         const long long ntiles = (long long)((g.M + TC_BM - 1) / TC_BM) * ((g.N + TC_BN - 1) / TC_BN);

@@ -63,6 +63,20 @@ int to_device(midas_gpu_ctx *ctx, const void *p, size_t bytes, int slot, const v
     return MIDAS_OK;
 }
 
+int device_sms(midas_gpu_ctx *c)
+{
+    static std::atomic<int> cache[64];
+    std::atomic<int> &slot = cache[c->device & 63];
+    int v = slot.load(std::memory_order_relaxed);
+    if (v > 0) return v;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess || v <= 0) {
+        cudaGetLastError();
+        return 152;
+    }
+    slot.store(v, std::memory_order_relaxed);
+    return v;
+}
+
 int side_stream(midas_gpu_ctx *c, cudaStream_t *out)
 {
     if (!c->side) {

@@ -289,15 +289,7 @@ __global__ void __launch_bounds__(256) k_z_split(int n, long long ldz, double2 *
     }
 }
 
-int sm_count(midas_gpu_ctx *c)
-{
-    int v = 0;
-    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess || v <= 0) {
-        cudaGetLastError();
-        v = 152;
-    }
-    return v;
-}
+int sm_count(midas_gpu_ctx *c) { return device_sms(c); }
 
 int rd_ldx(int nrhs) { return nrhs <= 16 ? 16 : (nrhs + 63) / 64 * 64; }
 
