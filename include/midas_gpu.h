@@ -178,6 +178,44 @@ int midas_gpu_cext_cabs(midas_gpu_ctx *ctx, int ntr, const double *theta, const 
 int midas_gpu_smatrix(midas_gpu_ctx *ctx, int nrx, const double *rx_theta, const double *rx_phi, int ntr,
                       const double *E, double *S);
 
+/* Integration rules of the incident (transmitter) and scattering (receiver)
+ * direction sets: NumIntType_t / NumIntType_r (src/InOut_ReadWrite_Functions.f90:319). */
+enum midas_quad {
+    MIDAS_QUAD_UN = 0,   /* uniform theta x phi grid, adaptive quadrature ('un') */
+    MIDAS_QUAD_TR = 1,   /* uniform grid, trapezoid cubature ('tr') */
+    MIDAS_QUAD_GL = 2,   /* Gauss-Legendre grid, caller's weights ('gl') */
+    MIDAS_QUAD_SD = 3,   /* spherical design list, equal weights ('sd') */
+    MIDAS_QUAD_LB = 4,   /* Lebedev list, caller's weights ('lb') */
+    MIDAS_QUAD_RF = 5    /* directions read from a file, equal weights ('rf') */
+};
+
+/* Efficiencies per incident direction and their orientation averages:
+ * Compute_Scattering_Quantities_1 (grid transmitters 'un' / 'tr' / 'gl') and
+ * Compute_Scattering_Quantities_2 (transmitter lists 'sd' / 'rf' / 'lb'),
+ * src/Compute_Scattering_Quantities.f90:1-1012, with the reference's grid-sampled
+ * QUADPACK QAG (src/quadpack.f90, src/Numerical_Integration.f90:213-305).
+ *   Transmitters: ntr_theta x ntr_phi directions (degrees, theta fastest; a list
+ *   has ntr_phi = 1).  Receivers: nrx_theta x nrx_phi directions (a list: nrx_phi
+ *   = 1) followed by extra receivers up to nrx_tot (the forward and backward
+ *   directions, get_trans_Receiv, src/get_trans_Receiv.f90:506-600).
+ *   S: nrx_tot x 4ntr complex, column-major, Vv, Vh, Hv, Hh per transmitter (the
+ *   layout of midas_gpu_smatrix); cext / cabs: per transmitter
+ *   (midas_gpu_cext_cabs).  dm: the scatterer's diameter (X = k0 dm / 2).
+ *   cext_intfields: CextIntFields (1 = Q_ext from the internal field).
+ *   w_tr / w_rx: 'gl' theta weights then phi weights, 'lb' one per direction,
+ *   else NULL.
+ *   q_dir (5 x ntr): Q_ext, Q_abs, Q_sca, Q_bks, g per transmitter (the Qidtable
+ *   columns); q_avg (5): the same averaged over the transmitters (the qtable).
+ * Every array may live in host or device memory.  A forward or backward
+ * direction missing from the receivers, or an 'un' grid whose samples fall
+ * outside it (the reference's index map needs theta and phi ranges that start
+ * at 0), returns MIDAS_ERR_ARG. */
+int midas_gpu_scattering_quantities(midas_gpu_ctx *ctx, int quad_tr, int quad_rx, int ntr_theta, int ntr_phi,
+                                    const double *tr_theta, const double *tr_phi, int nrx_theta, int nrx_phi,
+                                    int nrx_tot, const double *rx_theta, const double *rx_phi, const double *S,
+                                    const double *cext, const double *cabs, double dm, double k0, int cext_intfields,
+                                    const double *w_tr, const double *w_rx, double *q_dir, double *q_avg);
+
 /* Dense complex solve that allocates no device memory (no counterpart in the
  * reference).  For callers that cannot call cudaMalloc -- code running while a
  * stream is captured into a CUDA graph, plug-ins whose host application owns and

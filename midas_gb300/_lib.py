@@ -20,6 +20,8 @@ STATUS = {0: "MIDAS_OK", 1: "MIDAS_ERR_ARG", 2: "MIDAS_ERR_CUDA", 3: "MIDAS_ERR_
 SOLVE_MIXED, SOLVE_FP64 = 0, 1
 FILL_FAITHFUL, FILL_FAST = 0, 1
 CBFM_SR, CBFM_HOMOG, CBFM_ACA, CBFM_FAST_CBF = 1, 2, 4, 8
+# integration rules NumIntType_t / NumIntType_r (MIDAS_QUAD_* in the header)
+QUAD = {"un": 0, "tr": 1, "gl": 2, "sd": 3, "lb": 4, "rf": 5}
 # kernel classes of midas_gpu_profile_query (MIDAS_KC_* in the header)
 KCLASSES = ["gemm_trail", "gemm_simt", "fill", "sr_scan", "diag_lu", "trsv", "resid", "zgemm64", "eig", "other",
             "gemm_panel", "gemm_solve", "gemm_prod", "split"]
@@ -30,6 +32,7 @@ EXPORTS = [
     "midas_gpu_get_cell_params", "midas_gpu_mom_fill", "midas_gpu_mom_rhs", "midas_gpu_incident_field",
     "midas_gpu_block_fill", "midas_gpu_sr_fill", "midas_gpu_set_fsr", "midas_gpu_aca", "midas_gpu_dense_solve",
     "midas_gpu_mom_solve", "midas_gpu_cbfm_solve", "midas_gpu_dense_solve_noalloc", "midas_gpu_cext_cabs", "midas_gpu_smatrix",
+    "midas_gpu_scattering_quantities",
     "midas_gpu_gemm_selftest", "midas_gpu_gemm_engine", "midas_gpu_launch_count", "midas_gpu_stream",
     "midas_gpu_bench_gemm", "midas_gpu_bench_gemm_ex", "midas_gpu_heev", "midas_gpu_zgemm_x3", "midas_gpu_profile", "midas_gpu_profile_query",
 ]
@@ -92,6 +95,7 @@ def load(path: str = LIB_PATH):
         "midas_gpu_cbfm_solve": (i, [vp, i, P, P, P, i, P, P, d, d, i, d, i, i, P, P, P, P, ctypes.POINTER(Info)]),
         "midas_gpu_cext_cabs": (i, [vp, i, P, P, P, P, P]),
         "midas_gpu_smatrix": (i, [vp, i, P, P, i, P, P]),
+        "midas_gpu_scattering_quantities": (i, [vp, i, i, i, i, P, P, i, i, i, P, P, P, P, P, d, d, i, P, P, P, P]),
         "midas_gpu_gemm_selftest": (i, [vp]),
         "midas_gpu_gemm_engine": (ctypes.c_char_p, []),
         "midas_gpu_launch_count": (ctypes.c_longlong, [vp]),

@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libmidas_gpu.so")
 OBJDIR = os.path.join(HERE, "_build")
-SOURCES = ["midas_gpu.cu", "fill.cu", "gemm.cu", "dense.cu", "post.cu", "cbfm.cu", "blas.cu", "noalloc.cu", "aca.cu", "sparse.cu", "resid.cu"]
+SOURCES = ["midas_gpu.cu", "fill.cu", "gemm.cu", "dense.cu", "post.cu", "cbfm.cu", "blas.cu", "noalloc.cu", "aca.cu", "sparse.cu", "resid.cu", "scatq.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 
@@ -27,7 +27,7 @@ def _nvcc() -> str:
 
 def _flags():
     return ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
-                   "-Xcompiler", "-Wno-unused-function", "--expt-relaxed-constexpr"]
+                   "-Xcompiler", "-Wno-unused-function", "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr"]
 
 
 def _stale(obj: str, src: str) -> bool:
@@ -36,6 +36,7 @@ def _stale(obj: str, src: str) -> bool:
     t = os.path.getmtime(obj)
     deps = [src] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith(".cuh")]
     deps.append(os.path.join(HERE, "..", "include", "midas_gpu.h"))
+    deps.append(os.path.abspath(__file__))   # compiler flags
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
 
 

@@ -13,6 +13,11 @@ int launch_cext_cabs(midas_gpu_ctx *c, int ntr, const double *th, const double *
                      double *cabs);
 int launch_smatrix(midas_gpu_ctx *c, int nrx, const double *rth, const double *rph, int ntr, const double2 *E,
                    double2 *S);
+int scattering_quantities(midas_gpu_ctx *c, int quad_tr, int quad_rx, int ntr_theta, int ntr_phi,
+                          const double *tr_theta, const double *tr_phi, int nrx_theta, int nrx_phi, int nrx_tot,
+                          const double *rx_theta, const double *rx_phi, const double *S, const double *cext,
+                          const double *cabs, double dm, double k0, int cext_intfields, const double *w_tr,
+                          const double *w_rx, double *q_dir, double *q_avg);
 template <typename TA, typename TB>
 int zgemm_x3(midas_gpu_ctx *c, int M, int N, int K, const TA *A, long long ars, long long acs, int conjA,
              const TB *B, long long brs, long long bcs, float *D, long long ldd, float alpha, float beta);
@@ -804,6 +809,19 @@ int midas_gpu_smatrix(midas_gpu_ctx *c, int nrx, const double *rx_theta, const d
     }
     MIDAS_TRY(launch_smatrix(c, nrx, (const double *)th, (const double *)ph, ntr, (const double2 *)dE, out));
     return copy_out(c, S, out, bytes);
+}
+
+int midas_gpu_scattering_quantities(midas_gpu_ctx *c, int quad_tr, int quad_rx, int ntr_theta, int ntr_phi,
+                                    const double *tr_theta, const double *tr_phi, int nrx_theta, int nrx_phi,
+                                    int nrx_tot, const double *rx_theta, const double *rx_phi, const double *S,
+                                    const double *cext, const double *cabs, double dm, double k0, int cext_intfields,
+                                    const double *w_tr, const double *w_rx, double *q_dir, double *q_avg)
+{
+    if (!c) return MIDAS_ERR_ARG;
+    c->err = Err();
+    return scattering_quantities(c, quad_tr, quad_rx, ntr_theta, ntr_phi, tr_theta, tr_phi, nrx_theta, nrx_phi,
+                                 nrx_tot, rx_theta, rx_phi, S, cext, cabs, dm, k0, cext_intfields, w_tr, w_rx,
+                                 q_dir, q_avg);
 }
 
 // internal hooks used by the tests

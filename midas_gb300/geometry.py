@@ -226,3 +226,48 @@ def random_directions(n: int, seed: int):
     u = rng.uniform(-1.0, 1.0, n)
     phi = rng.uniform(0.0, 360.0, n)
     return np.degrees(np.arccos(u)), phi
+
+
+def uniform_directions(th0: float, th1: float, nth: int, ph0: float, ph1: float, nph: int):
+    """Uniform-step direction grid in degrees, theta fastest (get_trans_Receiv,
+    src/get_trans_Receiv.f90:249-270 for transmitters, :509-524 for receivers)."""
+    sth = 0.0 if nth == 1 else (th1 - th0) / (nth - 1)
+    sph = 0.0 if nph == 1 else (ph1 - ph0) / (nph - 1)
+    th = th0 + np.arange(nth) * sth
+    ph = ph0 + np.arange(nph) * sph
+    return np.tile(th, nph), np.repeat(ph, nth)
+
+
+def receivers_with_extras(rx_th, rx_ph, tr_th, tr_ph):
+    """Append, for each transmitter, its forward and backward scattering
+    direction when the receiver grid lacks it (src/get_trans_Receiv.f90:571-590:
+    getTxRxIndex over the grid only, tolerance 1e-2 degree)."""
+    rx_th, rx_ph = np.asarray(rx_th, np.float64), np.asarray(rx_ph, np.float64)
+    eps = float(np.float32(1e-2))
+    extra_th, extra_ph = [], []
+
+    def on_grid(t, p):
+        return bool(np.any((np.abs(rx_th - t) <= eps) & (np.abs(rx_ph - p) <= eps)))
+
+    for t, p in zip(np.asarray(tr_th, np.float64), np.asarray(tr_ph, np.float64)):
+        for a, b in ((t, p), (180.0 - t, math.fmod(p + 180.0, 360.0))):
+            if not on_grid(a, b):
+                extra_th.append(a)
+                extra_ph.append(b)
+    return np.concatenate([rx_th, extra_th]), np.concatenate([rx_ph, extra_ph])
+
+
+def gauss_legendre_directions(th0: float, th1: float, nth: int, ph0: float, ph1: float, nph: int):
+    """Gauss-Legendre direction grid in degrees (theta fastest) and its weights
+    for the 'gl' rule: theta weights then phi weights on the radian intervals
+    (the phi weight is 1 for a single phi, src/Compute_Scattering_Quantities.f90:279-283)."""
+    def rule(n, a, b):
+        x, w = np.polynomial.legendre.leggauss(n)
+        return (a + b) / 2 + (b - a) / 2 * x, (b - a) / 2 * w
+    xt, wt = rule(nth, math.radians(th0), math.radians(th1))
+    if nph > 1:
+        xp, wp = rule(nph, math.radians(ph0), math.radians(ph1))
+    else:
+        xp, wp = np.array([math.radians(ph0)]), np.array([1.0])
+    th, ph = np.degrees(xt), np.degrees(xp)
+    return np.tile(th, nph), np.repeat(ph, nth), np.concatenate([wt, wp])

@@ -197,6 +197,29 @@ class Context:
         self._ck(self.L.midas_gpu_smatrix(self.h, len(rth), addr(rth), addr(rph), ntr, addr(Ef), addr(S)))
         return S.T
 
+    def scattering_quantities(self, quad_tr, quad_rx, tr_grid, rx_grid, tr_th, tr_ph, rx_th, rx_ph, S, cext, cabs,
+                              dm, k0, cext_intfields=0, w_tr=None, w_rx=None):
+        """Compute_Scattering_Quantities_1/_2 (src/Compute_Scattering_Quantities.f90:1-1012).
+
+        quad_tr / quad_rx: 'un', 'tr', 'gl', 'sd', 'lb' or 'rf'; tr_grid / rx_grid:
+        (n_theta, n_phi) of the transmitter and receiver sets (a list: (n, 1)); S
+        (nrx_tot, 4 ntr) from smatrix over the receivers followed by the extra
+        forward / backward ones; cext / cabs from cext_cabs; dm the scatterer's
+        diameter.  Returns (q_dir (ntr, 5), q_avg (5)) with columns Q_ext, Q_abs,
+        Q_sca, Q_bks, g."""
+        S = np.asfortranarray(S, dtype=np.complex128)
+        ntr = tr_grid[0] * tr_grid[1]
+        arrs = [_c(a, np.float64) for a in (tr_th, tr_ph, rx_th, rx_ph, cext, cabs)]
+        wt = _c(w_tr, np.float64) if w_tr is not None else None
+        wr = _c(w_rx, np.float64) if w_rx is not None else None
+        qd, qa = np.zeros((ntr, 5)), np.zeros(5)
+        self._ck(self.L.midas_gpu_scattering_quantities(
+            self.h, _lib.QUAD[quad_tr], _lib.QUAD[quad_rx], tr_grid[0], tr_grid[1], addr(arrs[0]), addr(arrs[1]),
+            rx_grid[0], rx_grid[1], S.shape[0], addr(arrs[2]), addr(arrs[3]), addr(S), addr(arrs[4]),
+            addr(arrs[5]), float(dm), float(k0), int(cext_intfields), addr(wt) if wt is not None else None,
+            addr(wr) if wr is not None else None, addr(qd), addr(qa)))
+        return qd, qa
+
     def launch_count(self) -> int:
         return int(self.L.midas_gpu_launch_count(self.h))
 

@@ -110,8 +110,44 @@ def cbfm_c2_mid():
     return _gaussian_sphere_cbfm("cbfm_c2_mid_gaussian_sphere_x6_ad16_2x2x2", 6.0, 16.0, 24, nbox=2)
 
 
+def _post_scene(name, tr_grid, rx_grid, seed=3):
+    """Orientation-averaging input: 'un' transmitter and receiver grids over theta
+    0..180, phi 0..360 (the extra forward / backward receivers appended as
+    get_trans_Receiv does), a seeded S matrix peaked in each forward direction,
+    and cross sections -- the shapes of a scattering run, with synthetic values."""
+    from . import geometry as G
+    rng = np.random.default_rng(seed)
+    tth, tph = G.uniform_directions(0.0, 180.0, tr_grid[0], 0.0, 360.0, tr_grid[1])
+    rth, rph = G.uniform_directions(0.0, 180.0, rx_grid[0], 0.0, 360.0, rx_grid[1])
+    rth, rph = G.receivers_with_extras(rth, rph, tth, tph)
+    ntr = len(tth)
+    r = np.radians
+    cosang = (np.cos(r(rth))[:, None] * np.cos(r(tth))[None, :]
+              + (np.sin(r(rth))[:, None] * np.sin(r(tth))[None, :]) * np.cos(r(rph[:, None] - tph[None, :])))
+    amp = 0.3 + 2.0 * np.exp(2.0 * (cosang - 1.0))
+    S = np.empty((len(rth), 4 * ntr), np.complex128)
+    for k, scale in enumerate((1.0, 0.1, 0.1, 1.0)):
+        S[:, k::4] = scale * amp * np.exp(2j * np.pi * rng.random(amp.shape))
+    return {"name": name, "method": "post", "tr_grid": tr_grid, "rx_grid": rx_grid, "tr_th": tth, "tr_ph": tph,
+            "rx_th": rth, "rx_ph": rph, "S": S, "cext": rng.uniform(5, 7, ntr), "cabs": rng.uniform(0.2, 0.4, ntr),
+            "dm": 2.0, "k0": 2.0}
+
+
+def post_sphere():
+    """Efficiencies of one incident direction over 181 x 25 receivers ('un'/'un'):
+    the receiver layout of the reference's sphere example."""
+    return _post_scene("post_un_1tr_181x25rx", (1, 1), (181, 25))
+
+
+def post_avg():
+    """Orientation average over a 19 x 37 'un' transmitter grid (703 incident
+    directions) with 181 x 25 'un' receivers: 35k adaptive quadratures."""
+    return _post_scene("post_un_19x37tr_181x25rx", (19, 37), (181, 25))
+
+
 WORKLOADS = {"mom_c1": mom_c1, "mom_c3": mom_c3, "mom_c3_small": mom_c3_small, "mom_tiny": mom_tiny,
-             "cbfm_c2": cbfm_c2, "cbfm_c2_small": cbfm_c2_small, "cbfm_c2_mid": cbfm_c2_mid}
+             "cbfm_c2": cbfm_c2, "cbfm_c2_small": cbfm_c2_small, "cbfm_c2_mid": cbfm_c2_mid,
+             "post_sphere": post_sphere, "post_avg": post_avg}
 
 
 def cbfm_args(wl):
@@ -135,6 +171,20 @@ def main(argv=None):
     wl = WORKLOADS[args.workload]()
     ctx = Context(device=0, fill_mode=_lib.FILL_FAST if args.fill == "fast" else _lib.FILL_FAITHFUL,
                   ir_tol=wl.get("ir_tol", 1e-13), verbose=args.verbose)
+    if wl["method"] == "post":
+        for step in range(args.steps):
+            ctx.profile(True)
+            t0 = time.perf_counter()
+            qd, qa = ctx.scattering_quantities("un", "un", wl["tr_grid"], wl["rx_grid"], wl["tr_th"], wl["tr_ph"],
+                                               wl["rx_th"], wl["rx_ph"], wl["S"], wl["cext"], wl["cabs"], wl["dm"],
+                                               wl["k0"])
+            dt = time.perf_counter() - t0
+            dev = ctx.profile_query().get("other", {}).get("ms", float("nan"))
+            ctx.profile(False)
+            print(f"{wl['name']}: step {step} {dt * 1e3:.2f} ms (kernels {dev:.2f} ms), "
+                  f"<Q_ext, Q_abs, Q_sca, Q_bks, g> = {np.array2string(qa, precision=5)}", flush=True)
+        ctx.close()
+        return 0
     ctx.set_cells(wl["xyz"], wl["sc"], wl["eps"], wl["k0"])
     for step in range(args.steps):
         t0 = time.perf_counter()

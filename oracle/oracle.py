@@ -5,7 +5,8 @@ CPU-baseline leg of ``bench.py`` import this module, and only as the checker.
 The GPU product (``midas_gb300``) never imports it.
 
 The element-level arithmetic (fills, incident fields, ACA, far field, cross
-sections) lives in ``midas_oracle.c`` (a C restatement of the reference
+sections) lives in ``midas_oracle.c`` and the orientation averaging in
+``midas_oracle_q.c`` (C restatements of the reference
 Fortran, each routine citing its source).  This module binds it with ctypes and
 restates the dense algebra of the reference drivers with LAPACK (numpy/scipy):
 
@@ -41,8 +42,8 @@ _ip = ctypes.POINTER(ctypes.c_int)
 
 def build() -> str:
     """Compile the C restatement (idempotent)."""
-    src = os.path.join(_HERE, "midas_oracle.c")
-    if (not os.path.exists(_LIB_PATH)) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(src):
+    srcs = [os.path.join(_HERE, f) for f in ("midas_oracle.c", "midas_oracle_q.c", "Makefile")]
+    if (not os.path.exists(_LIB_PATH)) or os.path.getmtime(_LIB_PATH) < max(map(os.path.getmtime, srcs)):
         subprocess.run(["make", "-s", "-C", _HERE], check=True)
     return _LIB_PATH
 
@@ -72,6 +73,9 @@ def lib():
             "or_cext_cabs": (None, [i, _dp, _dp, _dp, _dp, _dp, d, i, _dp, _dp, _dp, _dp, _dp]),
             "or_sphere_cells": (i, [d, d, _dp, i]),
             "or_num_threads": (i, []),
+            "or_qag_grid": (d, [_dp, i, d, d, _ip, _ip, _ip]),
+            "or_scattering_quantities": (i, [i, i, i, i, i, i, i, d, d, i, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
+                                             _dp, _dp, _dp, _dp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -274,6 +278,37 @@ def cext_cabs(c: Cells, th, ph, E: np.ndarray):
     lib().or_cext_cabs(c.n, *c.geo(), _d(c.sc), _d(c.che.view(np.float64)), c.k0, len(th), _d(th),
                        _d(ph), _d(Ef.T.view(np.float64).reshape(-1)), _d(cext), _d(cabs))
     return cext, cabs
+
+
+# Integration rules NumIntType_t / NumIntType_r (src/InOut_ReadWrite_Functions.f90:319).
+QUAD = {"un": 0, "tr": 1, "gl": 2, "sd": 3, "lb": 4, "rf": 5}
+
+
+def qag_grid(f, a0: float, b0: float):
+    """getAdaptiveQuadPts2 on one sampled column: (result, neval, ier, bad_index)."""
+    f = _f64(f)
+    ne, ier, bad = (np.zeros(1, np.int32) for _ in range(3))
+    r = lib().or_qag_grid(_d(f), len(f), a0, b0, _i(ne), _i(ier), _i(bad))
+    return r, int(ne[0]), int(ier[0]), int(bad[0])
+
+
+def scattering_quantities(quad_tr, quad_rx, tr_grid, rx_grid, tr_th, tr_ph, rx_th, rx_ph, S, cext, cabs,
+                          dm, k0, cext_intfields=0, w_tr=None, w_rx=None):
+    """Compute_Scattering_Quantities_1/_2: (status, q_dir (ntr, 5), q_avg (5)), columns
+    Q_ext, Q_abs, Q_sca, Q_bks, g.  tr_grid / rx_grid = (n_theta, n_phi); S is
+    (nrx_tot, 4 ntr) with the extra forward/backward receivers after the grid."""
+    S = np.asfortranarray(S, dtype=np.complex128)
+    ntr = tr_grid[0] * tr_grid[1]
+    qd = np.zeros((ntr, 5))
+    qa = np.zeros(5)
+    wt = _f64(w_tr) if w_tr is not None else None
+    wr = _f64(w_rx) if w_rx is not None else None
+    st = lib().or_scattering_quantities(
+        QUAD[quad_tr], QUAD[quad_rx], tr_grid[0], tr_grid[1], rx_grid[0], rx_grid[1], S.shape[0], dm, k0,
+        cext_intfields, _d(_f64(tr_th)), _d(_f64(tr_ph)), _d(_f64(rx_th)), _d(_f64(rx_ph)),
+        _d(S.T.view(np.float64).reshape(-1)), _d(_f64(cext)), _d(_f64(cabs)),
+        _d(wt) if wt is not None else None, _d(wr) if wr is not None else None, _d(qd), _d(qa))
+    return st, qd, qa
 
 
 def sphere_cells(dm: float, sc: float) -> np.ndarray:

@@ -1,0 +1,144 @@
+"""Oracle of the orientation-averaging step (Compute_Scattering_Quantities_1/_2,
+QUADPACK QAG on sampled grids): rule tables, quadrature behaviour, physics of a
+solved sphere, the averaging rules and the reference's error cases."""
+import math
+import os
+import re
+
+import numpy as np
+import pytest
+
+import scatq_cases as C
+from mie import mie_q
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _tables(path):
+    src = open(path).read()
+    out = {}
+    for name in ("X", "WK", "WG"):
+        m = re.search(r"(?:GK61_|c_gk_)" + name.lower() + r"\[\d+\]\s*=\s*\{([^}]*)\}", src, re.I)
+        out[name] = np.array([float(v.strip().rstrip("f")) for v in m.group(1).split(",") if v.strip()])
+    return out
+
+
+def test_gauss_kronrod_tables():
+    """The 61-point rule of the oracle and of the kernels are the same table, and it
+    is the Gauss-Kronrod pair: the 30 Gauss nodes match numpy's, the Gauss part
+    integrates polynomials of degree <= 59 and the Kronrod rule those of degree
+    <= 91 exactly (in FP64 on the 16-digit constants)."""
+    a = _tables(os.path.join(ROOT, "oracle", "midas_oracle_q.c"))
+    b = _tables(os.path.join(ROOT, "midas_gb300", "csrc", "scatq.cu"))
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+    x, wk, wg = a["X"], a["WK"], a["WG"]
+    assert x.shape == (31,) and wk.shape == (31,) and wg.shape == (15,)
+    xg = np.sort(np.concatenate([x[1::2], -x[1::2]]))
+    ref, _ = np.polynomial.legendre.leggauss(30)
+    assert np.max(np.abs(xg - ref)) < 1e-15
+    for deg in range(0, 92, 2):
+        exact = 2.0 / (deg + 1)
+        kr = wk[30] * (1.0 if deg == 0 else 0.0) + np.sum(wk[:30] * 2 * x[:30] ** deg)
+        assert abs(kr - exact) < 2e-15, (deg, kr - exact)
+        if deg <= 58:
+            ga = np.sum(wg * 2 * x[1::2] ** deg)
+            assert abs(ga - exact) < 2e-15, (deg, ga - exact)
+
+
+def test_qag_on_sampled_columns(oracle):
+    pi = oracle.ref_pi()
+    r, ne, ier, bad = oracle.qag_grid(np.full(181, 3.0), 0.0, pi)
+    assert r == float(np.float32(3.0) * np.float32(pi)) and ne == 61 and ier == 0 and not bad
+    # a smooth integrand read at the nearest of 181 samples: within the rule's 1e-3
+    r, ne, ier, bad = oracle.qag_grid(np.sin(np.linspace(0.0, pi, 181)), 0.0, pi)
+    assert abs(r - 2.0) < 2e-3 and not bad
+    # the index map x (n-1) / (b0 - a0) assumes a0 = 0: a range that starts elsewhere
+    # runs past the column (the reference reads out of bounds), which is reported
+    *_, bad = oracle.qag_grid(np.ones(50), 0.5, 2.0)
+    assert bad
+
+
+def test_sphere_energy_balance_and_mie(oracle):
+    """The reference's sphere example layout (one incident direction, theta 0..180,
+    phi 0..360 receivers) on a solved 447-cell sphere: optical theorem vs internal
+    field, Q_sca vs Q_ext - Q_abs, adaptive vs trapezoid, and Mie."""
+    from midas_gb300 import geometry as G
+    m, a, k0 = 1.5 + 0.01j, 1.0, 2.0
+    sc = a / 4.775
+    cells = oracle.Cells(oracle.sphere_cells(2 * a, sc), sc, m * m, k0)
+    th, ph = np.array([0.0]), np.array([0.0])
+    rth, rph = G.uniform_directions(0, 180, 37, 0, 360, 13)
+    rth, rph = G.receivers_with_extras(rth, rph, th, ph)
+    assert len(rth) == 37 * 13   # forward (0, 0) and backward (180, 180) lie on the grid
+    res = oracle.mom_solve(cells, th, ph, rth, rph)
+    st, qd, qa = oracle.scattering_quantities("un", "un", (1, 1), (37, 13), th, ph, rth, rph, res["S"],
+                                              res["cext"], res["cabs"], 2 * a, k0)
+    assert st == 0 and np.array_equal(qd[0], qa)
+    q_ext_ff, q_abs, q_sca, q_bks, g = qa
+    q_ext_int = res["cext"][0] / (oracle.ref_pi() * a * a)
+    assert abs(q_ext_ff - q_ext_int) / q_ext_int < 0.03
+    assert abs(q_sca - (q_ext_int - q_abs)) / q_sca < 0.03
+    assert 0.3 < g < 0.9 and q_bks > 0
+    st, qd_i, _ = oracle.scattering_quantities("un", "un", (1, 1), (37, 13), th, ph, rth, rph, res["S"],
+                                               res["cext"], res["cabs"], 2 * a, k0, cext_intfields=1)
+    assert st == 0 and qd_i[0, 0] == q_ext_int and np.array_equal(qd_i[0, 1:], qd[0, 1:])
+    st, qd_t, _ = oracle.scattering_quantities("un", "tr", (1, 1), (37, 13), th, ph, rth, rph, res["S"],
+                                               res["cext"], res["cabs"], 2 * a, k0)
+    assert st == 0 and abs(qd_t[0, 2] - q_sca) / q_sca < 1e-3
+    aeq = (3 * cells.n * sc ** 3 / (4 * np.pi)) ** (1 / 3)
+    qe_mie, qs_mie = mie_q(m, k0 * aeq)
+    assert abs(q_ext_int * a * a / aeq ** 2 - qe_mie) / qe_mie < 0.03
+    assert abs(q_sca * a * a / aeq ** 2 - qs_mie) / qs_mie < 0.05
+
+
+@pytest.mark.parametrize("tr,rx", [("un", "un"), ("tr", "tr"), ("gl", "gl"), ("un", "sd"), ("un", "lb"),
+                                   ("sd", "sd"), ("lb", "lb"), ("rf", "rf"), ("gl", "un")])
+def test_rules_run_and_conventions(oracle, tr, rx):
+    c = C.case(tr, rx)
+    st, qd, qa = C.oracle_call(oracle, c)
+    assert st == 0 and np.all(np.isfinite(qd)) and np.all(np.isfinite(qa))
+    pi = oracle.ref_pi()
+    ap = c["dm"] / 2
+    assert np.allclose(qd[:, 1], c["cabs"] / (pi * ap * ap), rtol=0, atol=0)   # Q_abs from the internal field
+    st, qdi, qai = C.oracle_call(oracle, c, cext_intfields=1)
+    assert np.array_equal(qdi[:, 0], c["cext"] / (pi * (ap * ap)))
+    if tr == "tr":
+        assert np.all(qa == 0.0)   # the reference passes TrPh_min as both phi limits: hy = 0
+    if tr in ("sd", "rf"):
+        assert np.allclose(qai, qdi.mean(axis=0), rtol=1e-14)
+    if tr == "lb":
+        assert np.allclose(qai, c["w_tr"] @ qdi, rtol=1e-14)
+
+
+def test_gl_average_of_a_constant(oracle):
+    """Gauss-Legendre transmitter weights average a direction-independent Q_ext
+    exactly: (1/4pi) sum w_th w_ph sin(theta) c = c."""
+    c = C.case("gl", "gl", tr=(8, 6))
+    c["cext"] = np.full(len(c["cext"]), 6.0)
+    st, qd, qa = C.oracle_call(oracle, c, cext_intfields=1)
+    # Sn uses the first and last grid angles, not 0 and 180: the average is exact
+    # for that patch of the sphere (to the 3e-8 of the single-precision Pi that
+    # converts the degrees)
+    th = np.radians(c["tr_th"][[0, c["tr_grid"][0] - 1]])
+    ph = np.radians(c["tr_ph"][[0, -1]])
+    patch = max(ph[1] - ph[0], 1.0) * (math.cos(th[0]) - math.cos(th[1]))
+    full = (2 * math.pi) * 2.0
+    assert st == 0 and abs(qa[0] * patch / full - qd[0, 0]) / qd[0, 0] < 3e-7
+
+
+def test_reference_error_cases(oracle):
+    c = C.case("un", "un")
+    # forward direction missing from the receivers (the reference stops)
+    fwd = np.where((np.abs(c["rx_th"] - c["tr_th"][1]) < 1e-9) & (np.abs(c["rx_ph"] - c["tr_ph"][1]) < 1e-9))[0]
+    assert len(fwd)
+    c2 = dict(c)
+    c2["rx_th"] = c["rx_th"].copy()
+    c2["rx_th"][fwd] += 1.0
+    st, _, _ = C.oracle_call(oracle, c2)
+    assert st in (1, 2)
+    # an 'un' receiver grid that does not start at theta = 0
+    c3 = C.case("un", "un")
+    c3["rx_th"] = np.where(c3["rx_th"] < 180.0 - 1e-9, c3["rx_th"] * 0.5 + 40.0, c3["rx_th"])
+    st, _, _ = C.oracle_call(oracle, c3)
+    assert st != 0
