@@ -42,8 +42,18 @@ namespace {
 constexpr int QAG_LIMIT = 500;
 // QAG work lists per running quadrature: alist, blist, rlist, elist (float) and iord (int).
 constexpr size_t QAG_WS = (size_t)QAG_LIMIT * 5 * 4;
-constexpr int QAG_TPB = 128;                   // threads per block of the quadrature kernels
-constexpr int QAG_WORKERS = 152 * QAG_TPB;     // concurrent quadratures at most (one block per SM)
+// Where the receiver quadratures keep their work lists.  Every bisection reads
+// and rewrites them through dependent loads: from shared memory that is ~30
+// cycles a step, from global memory (10 KB per quadrature, beyond L1 for a
+// block) an L2 round trip.  Shared memory holds 20 lists per SM, registers
+// allow 256 quadratures per SM: a call with few quadratures (one incident
+// direction: tens) runs them from shared memory, a call with many (an
+// orientation average: tens of thousands) from global memory at 6x the
+// concurrency.  Measured on GB300: 50 quadratures 14.2 -> 6.8 ms in shared
+// memory; 35k quadratures 56 ms in global memory, 84 ms in shared memory.
+constexpr int QAG_SM_TPB = 20;                         // quadratures per block (one block per SM)
+constexpr int QAG_SMEM = QAG_SM_TPB * (int)QAG_WS;     // 200,000 bytes of dynamic shared memory
+constexpr int Q_TPB = 128;                             // threads per block otherwise
 
 // Gauss-Kronrod 30/61 rule on [-1, 1] (QUADPACK qk61): Kronrod abscissae in
 // decreasing order (odd indices are the 30-point Gauss abscissae), their
@@ -93,32 +103,31 @@ __device__ __forceinline__ double abs2(double2 z)
 enum { QST_FWD = 0, QST_BKW = 1, QST_INDEX = 2, QST_N = 4 };
 
 // f(nint(x*(n-1)/(b0-a0))+1) of a sampled column (src/quadpack.f90:621-627);
-// an index outside the column is recorded and read at the nearest end.
-__device__ __forceinline__ float q_sample(const double *f, int n, float span, float x, int *st)
+// an index outside the column is flagged in `bad` and read at the nearest end.
+// Branch-free, so the 61 loads of a rule evaluation issue back to back.
+__device__ __forceinline__ float q_sample(const double *f, int n, float span, float x, bool &bad)
 {
     const float t = fdv(fm(x, (float)(n - 1)), span);
-    int i;
-    if (!(t > -1e9f && t < 1e9f)) { atomicOr(st + QST_INDEX, 1); i = 1; }
-    else i = (int)roundf(t) + 1;
-    if (i < 1) { atomicOr(st + QST_INDEX, 1); i = 1; }
-    if (i > n) { atomicOr(st + QST_INDEX, 1); i = n; }
-    return __double2float_rn(f[i - 1]);
+    const bool finite = t > -1e9f && t < 1e9f;
+    const int i = finite ? (int)roundf(t) + 1 : 1;
+    bad |= !finite || i < 1 || i > n;
+    return __double2float_rn(f[min(max(i, 1), n) - 1]);
 }
 
 // qk61 (src/quadpack.f90:486-728) over a sampled column spanning [a0, b0].
 __device__ void q_qk61(const double *f, int n, float span, float a, float b, float &result, float &abserr,
-                       float &resabs, float &resasc, int *st)
+                       float &resabs, float &resasc, bool &bad)
 {
     const float centr = fm(0.5f, fa(b, a)), hlgth = fm(0.5f, fs(b, a)), dhlgth = fabsf(hlgth);
     float fv1[30], fv2[30];
-    const float fc = q_sample(f, n, span, centr, st);
+    const float fc = q_sample(f, n, span, centr, bad);
     float resg = 0.0f, resk = fm(c_gk_wk[30], fc), ra = fabsf(resk);
 #pragma unroll
     for (int j = 1; j <= 15; ++j) {   // Gauss abscissae
         const int k = 2 * j - 1;
         const float absc = fm(hlgth, c_gk_x[k]);
-        const float f1 = q_sample(f, n, span, fs(centr, absc), st);
-        const float f2 = q_sample(f, n, span, fa(centr, absc), st);
+        const float f1 = q_sample(f, n, span, fs(centr, absc), bad);
+        const float f2 = q_sample(f, n, span, fa(centr, absc), bad);
         fv1[k] = f1;
         fv2[k] = f2;
         const float fsum = fa(f1, f2);
@@ -130,8 +139,8 @@ __device__ void q_qk61(const double *f, int n, float span, float a, float b, flo
     for (int j = 1; j <= 15; ++j) {   // Kronrod-only abscissae
         const int k = 2 * j - 2;
         const float absc = fm(hlgth, c_gk_x[k]);
-        const float f1 = q_sample(f, n, span, fs(centr, absc), st);
-        const float f2 = q_sample(f, n, span, fa(centr, absc), st);
+        const float f1 = q_sample(f, n, span, fs(centr, absc), bad);
+        const float f2 = q_sample(f, n, span, fa(centr, absc), bad);
         fv1[k] = f1;
         fv2[k] = f2;
         const float fsum = fa(f1, f2);
@@ -162,6 +171,12 @@ __device__ void q_qk61(const double *f, int n, float span, float a, float b, flo
 
 // QUADPACK qpsrt (src/quadpack.f90:730-890): keeps iord (1-based interval
 // numbers) in decreasing order of elist and picks the next interval to bisect.
+// The reference scans iord[ibeg..jbnd] linearly, twice; that segment is kept
+// non-increasing in elist, so the first entry <= errmax and the last entry >
+// errmin are found here by binary search and the entries in between moved as a
+// block: the same iord, maxerr and ermax for every input without NaNs (whose
+// quadratures are NaN either way), at O(log n) dependent loads instead of O(n).
+// qage calls it with nrmax = 1, where the reference's first loop runs no trips.
 __device__ void q_qpsrt(int limit, int last, int &maxerr, float &ermax, const float *elist, int *iord, int &nrmax)
 {
 #define EL(i) elist[(i) - 1]
@@ -182,30 +197,28 @@ __device__ void q_qpsrt(int limit, int last, int &maxerr, float &ermax, const fl
         if (limit / 2 + 2 < last) jupbn = limit + 3 - last;
         const float errmin = EL(last);
         const int jbnd = jupbn - 1, ibeg = nrmax + 1;
-        int i = ibeg;
-        for (; i <= jbnd; ++i) {
-            const int isucc = IO(i);
-            if (EL(isucc) <= errmax) break;
-            IO(i - 1) = isucc;
+        int lo = ibeg, hi = jbnd + 1;   // first i with EL(IO(i)) <= errmax
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (EL(IO(mid)) <= errmax) hi = mid;
+            else lo = mid + 1;
         }
+        const int i = lo;
+        for (int q = ibeg; q < i; ++q) IO(q - 1) = IO(q);
         if (i > jbnd) {
             IO(jbnd) = maxerr;
             IO(jupbn) = last;
         } else {
             IO(i - 1) = maxerr;
-            int k = jbnd;
-            bool placed = false;
-            for (int j = i; j <= jbnd; ++j) {
-                const int isucc = IO(k);
-                if (errmin < EL(isucc)) {
-                    IO(k + 1) = last;
-                    placed = true;
-                    break;
-                }
-                IO(k + 1) = isucc;
-                k -= 1;
+            int l2 = i, h2 = jbnd + 1;   // first k with !(errmin < EL(IO(k)))
+            while (l2 < h2) {
+                const int mid = (l2 + h2) >> 1;
+                if (errmin < EL(IO(mid))) l2 = mid + 1;
+                else h2 = mid;
             }
-            if (!placed) IO(i) = last;
+            const int k = l2 - 1;
+            for (int q = jbnd; q > k; --q) IO(q + 1) = IO(q);
+            IO(k + 1) = last;
         }
     }
     maxerr = IO(nrmax);
@@ -225,16 +238,20 @@ __device__ float q_qag(const double *f, int n, float a, float b, char *ws, int *
     const float span = fs(b, a);
     float result, abserr, defabs, resabs;
     int ier = 0;
+    bool bad = false;
     alist[0] = a;
     blist[0] = b;
-    q_qk61(f, n, span, a, b, result, abserr, defabs, resabs, st);
+    q_qk61(f, n, span, a, b, result, abserr, defabs, resabs, bad);
     rlist[0] = result;
     elist[0] = abserr;
     iord[0] = 1;
     float errbnd = fm(epsrel, fabsf(result));
     if (epsabs > errbnd) errbnd = epsabs;
     if (abserr <= fm(fm(50.0f, FLT_EPSILON), defabs) && errbnd < abserr) ier = 2;
-    if (ier != 0 || (abserr <= errbnd && abserr != resabs) || abserr == 0.0f) return result;
+    if (ier != 0 || (abserr <= errbnd && abserr != resabs) || abserr == 0.0f) {
+        if (bad) atomicOr(st + QST_INDEX, 1);
+        return result;
+    }
     float errmax = abserr, area = result, errsum = abserr;
     int maxerr = 1, nrmax = 1, iroff1 = 0, iroff2 = 0, last = 2;
     for (; last <= QAG_LIMIT; ++last) {
@@ -242,8 +259,8 @@ __device__ float q_qag(const double *f, int n, float a, float b, char *ws, int *
         const float b1 = fm(0.5f, fa(alist[maxerr - 1], blist[maxerr - 1]));
         const float a2 = b1, b2 = blist[maxerr - 1];
         float area1, error1, defab1, area2, error2, defab2, ra;
-        q_qk61(f, n, span, a1, b1, area1, error1, ra, defab1, st);
-        q_qk61(f, n, span, a2, b2, area2, error2, ra, defab2, st);
+        q_qk61(f, n, span, a1, b1, area1, error1, ra, defab1, bad);
+        q_qk61(f, n, span, a2, b2, area2, error2, ra, defab2, bad);
         const float area12 = fa(area1, area2), erro12 = fa(error1, error2);
         errsum = fs(fa(errsum, erro12), errmax);
         area = fs(fa(area, area12), rlist[maxerr - 1]);
@@ -281,6 +298,7 @@ __device__ float q_qag(const double *f, int n, float a, float b, char *ws, int *
         if (ier != 0 || errsum <= errbnd) break;
     }
     if (last > QAG_LIMIT) last = QAG_LIMIT;
+    if (bad) atomicOr(st + QST_INDEX, 1);
     float s = 0.0f;
     for (int k = 0; k < last; ++k) s = fa(s, rlist[k]);
     return s;
@@ -390,17 +408,19 @@ __global__ void k_q_dir(QParams p, const double2 *__restrict__ S, const Dir4 *__
 // Receiver quadratures.  'un': one QAG per (transmitter, integrand, phi column)
 // over theta, result in fy; other rules: one serial sum per (transmitter,
 // integrand), result in qr.
-__global__ void k_q_rx(QParams p, const double *__restrict__ F, const double *__restrict__ w_rx, double *fy,
-                       double *qr, char *ws, int *st)
+__global__ void __launch_bounds__(Q_TPB) k_q_rx(QParams p, const double *__restrict__ F, const double *__restrict__ w_rx,
+                                                double *fy, double *qr, char *ws, int lists_in_smem, int *st)
 {
+    extern __shared__ __align__(16) char qsm[];   // QAG work lists when lists_in_smem
     const int gid = blockIdx.x * blockDim.x + threadIdx.x, nthr = gridDim.x * blockDim.x;
+    char *mine = lists_in_smem ? qsm + (size_t)threadIdx.x * QAG_WS : ws + (size_t)gid * QAG_WS;
     if (p.quad_rx == 0) {
         const long long inst = 2LL * p.ntr * p.nrx_phi;
         for (long long i = gid; i < inst; i += nthr) {
             const long long tk = i / p.nrx_phi;
             const int j = (int)(i % p.nrx_phi);
             const double *col = F + (size_t)tk * p.nrx + (size_t)j * p.nrx_theta;
-            fy[i] = (double)q_qag(col, p.nrx_theta, (float)p.th0, (float)p.th1, ws + (size_t)gid * QAG_WS, st);
+            fy[i] = (double)q_qag(col, p.nrx_theta, (float)p.th0, (float)p.th1, mine, st);
         }
         return;
     }
@@ -418,16 +438,18 @@ __global__ void k_q_rx(QParams p, const double *__restrict__ F, const double *__
 // Per transmitter: the phi quadrature ('un') and Q_sca, g
 // (Compute_Scattering_Quantities.f90:214-355, 768-860); q_dir row = Q_ext,
 // Q_abs, Q_sca, Q_bks, g (the Qidtable columns, :383-392).
-__global__ void k_q_rx_fin(QParams p, const double *fy, const double *qr, const double *qp, double *q_dir, char *ws,
-                           int *st)
+__global__ void __launch_bounds__(Q_TPB) k_q_rx_fin(QParams p, const double *fy, const double *qr, const double *qp,
+                                                    double *q_dir, char *ws, int lists_in_smem, int *st)
 {
+    extern __shared__ __align__(16) char qsm[];   // QAG work lists when lists_in_smem
     const int gid = blockIdx.x * blockDim.x + threadIdx.x, nthr = gridDim.x * blockDim.x;
+    char *mine = lists_in_smem ? qsm + (size_t)threadIdx.x * QAG_WS : ws + (size_t)gid * QAG_WS;
     for (int t = gid; t < p.ntr; t += nthr) {
         double q[2];
         for (int k = 0; k < 2; ++k) {
             if (p.quad_rx == 0) {
                 const double *y = fy + (size_t)(2 * t + k) * p.nrx_phi;
-                q[k] = p.nrx_phi > 1 ? (double)q_qag(y, p.nrx_phi, (float)p.ph0, (float)p.ph1, ws + (size_t)gid * QAG_WS, st)
+                q[k] = p.nrx_phi > 1 ? (double)q_qag(y, p.nrx_phi, (float)p.ph0, (float)p.ph1, mine, st)
                                      : y[0];
             } else {
                 q[k] = qr[2 * t + k];
@@ -462,7 +484,7 @@ __global__ void k_q_rx_fin(QParams p, const double *fy, const double *qr, const 
 
 // Averages over the transmitters (Compute_Scattering_Quantities.f90:436-526, 937-968).
 // One CTA; G holds 5 ntr doubles, gy 5 ntr_phi, ws blockDim.x work lists.
-__global__ void k_q_avg(QParams p, const double *q_dir, const double *s_tr, const double *w_tr, double *G,
+__global__ void __launch_bounds__(256) k_q_avg(QParams p, const double *q_dir, const double *s_tr, const double *w_tr, double *G,
                         double *gy, double *q_avg, char *ws, int *st)
 {
     const int tid = threadIdx.x;
@@ -655,12 +677,33 @@ int scattering_quantities(midas_gpu_ctx *c, int quad_tr, int quad_rx, int ntr_th
     const void *dS;
     MIDAS_TRY(to_device(c, S, sizeof(double2) * (size_t)nrx_tot * 4 * p.ntr, S_IN0, &dS));
     const long long inst_rx = quad_rx == MIDAS_QUAD_UN ? 2LL * p.ntr * nrx_phi : 2LL * p.ntr;
-    const int workers = (int)std::min<long long>(std::max<long long>(inst_rx, p.ntr), QAG_WORKERS);
-    const int avg_threads = 256, tpb = QAG_TPB, blocks = (workers + tpb - 1) / tpb;
+    const int sms = device_sms(c), avg_threads = 256;
+    // launch shapes (grid-stride loops): quadratures with shared-memory lists (one
+    // block of 20 per SM) while they fit in two such rounds, else 128-thread blocks
+    // with global lists (one block per SM for quadratures, 8 for plain sums)
+    size_t ws_slots = 0;
+    auto shape = [&](long long inst, bool qag, int &grid, int &tpb, int &smem) {
+        const bool in_smem = qag && inst <= 2LL * sms * QAG_SM_TPB;
+        tpb = in_smem ? QAG_SM_TPB : Q_TPB;
+        smem = in_smem ? QAG_SMEM : 0;
+        const long long want = (inst + tpb - 1) / tpb;
+        grid = (int)std::max<long long>(1, std::min<long long>(want, qag ? sms : 8LL * sms));
+        if (qag && !in_smem) ws_slots = std::max(ws_slots, (size_t)grid * tpb);
+    };
+    int g_rx, t_rx, m_rx, g_fin, t_fin, m_fin;
+    shape(inst_rx, quad_rx == MIDAS_QUAD_UN, g_rx, t_rx, m_rx);
+    shape(p.ntr, quad_rx == MIDAS_QUAD_UN && nrx_phi > 1, g_fin, t_fin, m_fin);
+    static PerDeviceOnce attr_once;
+    MIDAS_CUDA(c, attr_once.run(c->device, [] {
+        cudaError_t e = cudaFuncSetAttribute(k_q_rx, cudaFuncAttributeMaxDynamicSharedMemorySize, QAG_SMEM);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_q_rx_fin, cudaFuncAttributeMaxDynamicSharedMemorySize, QAG_SMEM);
+        return e;
+    }));
     const size_t nF = 2 * (size_t)p.ntr * p.nrx, nfy = 2 * (size_t)p.ntr * nrx_phi, nqr = 2 * (size_t)p.ntr,
                  nqp = 8 * (size_t)p.ntr, nqd = 5 * (size_t)p.ntr, nG = 5 * (size_t)p.ntr, ngy = 5 * (size_t)ntr_phi;
     const size_t dbl = n_tab + nF + nfy + nqr + nqp + nqd + nG + ngy + 8;
-    const size_t ws_bytes = (size_t)std::max(blocks * tpb, avg_threads) * QAG_WS;   // one list per launched thread
+    const size_t ws_bytes = std::max(ws_slots, (size_t)avg_threads) * QAG_WS;   // global work lists
     void *base;
     MIDAS_TRY(ensure(c, S_QWS, sizeof(double) * dbl + ws_bytes + 64, &base));
     double *d_tab = (double *)base;
@@ -677,9 +720,9 @@ int scattering_quantities(midas_gpu_ctx *c, int quad_tr, int quad_rx, int ntr_th
                                           d_tab + o_rth, d_tab + o_rph, d_tab + o_wrx, d_tab + o_cex, d_tab + o_cab,
                                           dF, dqp, dst);
     MIDAS_CUDA(c, cudaGetLastError());
-    k_q_rx<<<blocks, tpb, 0, c->stream>>>(p, dF, d_tab + o_wrx, dfy, dqr, ws, dst);
+    k_q_rx<<<g_rx, t_rx, m_rx, c->stream>>>(p, dF, d_tab + o_wrx, dfy, dqr, ws, m_rx > 0, dst);
     MIDAS_CUDA(c, cudaGetLastError());
-    k_q_rx_fin<<<blocks, tpb, 0, c->stream>>>(p, dfy, dqr, dqp, dqd, ws, dst);
+    k_q_rx_fin<<<g_fin, t_fin, m_fin, c->stream>>>(p, dfy, dqr, dqp, dqd, ws, m_fin > 0, dst);
     MIDAS_CUDA(c, cudaGetLastError());
     k_q_avg<<<1, avg_threads, 0, c->stream>>>(p, dqd, d_tab + o_str, d_tab + o_wtr, dG, dgy, dqa, ws, dst);
     MIDAS_CUDA(c, cudaGetLastError());

@@ -125,7 +125,7 @@ def _post_scene(name, tr_grid, rx_grid, seed=3):
     cosang = (np.cos(r(rth))[:, None] * np.cos(r(tth))[None, :]
               + (np.sin(r(rth))[:, None] * np.sin(r(tth))[None, :]) * np.cos(r(rph[:, None] - tph[None, :])))
     amp = 0.3 + 2.0 * np.exp(2.0 * (cosang - 1.0))
-    S = np.empty((len(rth), 4 * ntr), np.complex128)
+    S = np.empty((len(rth), 4 * ntr), np.complex128, order="F")   # the C-ABI layout (column-major)
     for k, scale in enumerate((1.0, 0.1, 0.1, 1.0)):
         S[:, k::4] = scale * amp * np.exp(2j * np.pi * rng.random(amp.shape))
     return {"name": name, "method": "post", "tr_grid": tr_grid, "rx_grid": rx_grid, "tr_th": tth, "tr_ph": tph,
