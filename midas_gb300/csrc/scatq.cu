@@ -360,7 +360,7 @@ __global__ void k_q_dir(QParams p, const double2 *__restrict__ S, const Dir4 *__
         const Dir4 d = drx[r];
         const double cg = da(da(dmu(ki.x, d.x), dmu(ki.y, d.y)), dmu(ki.z, d.z));
         double v;
-        if (p.list_rx) v = p.quad_rx == 4 /* lb */ ? dmu(w_rx[r], sit) : sit;
+        if (p.list_rx) v = p.quad_rx == MIDAS_QUAD_LB ? dmu(w_rx[r], sit) : sit;
         else v = dmu(sit, d.w);
         fx[r] = v;
         fg[r] = dmu(v, cg);
@@ -383,7 +383,7 @@ __global__ void k_q_dir(QParams p, const double2 *__restrict__ S, const Dir4 *__
         if (bk != INT_MAX) atomicMin(&s_bk, bk);
     } else if (threadIdx.x == 0) {   // positional (Compute_Scattering_Quantities.f90:760-764, 866-870)
         const bool same = p.ntr == p.nrx;
-        const int fw = (same && (p.quad_rx == 4 || p.quad_rx == 3)) ? t : p.nrx + t;
+        const int fw = (same && (p.quad_rx == MIDAS_QUAD_LB || p.quad_rx == MIDAS_QUAD_SD)) ? t : p.nrx + t;
         const int bk = (same && p.list_rx) ? p.nrx + t : p.nrx + p.ntr + t;
         if (fw < p.nrx_tot) s_fw = fw;
         if (bk < p.nrx_tot) s_bk = bk;
@@ -414,7 +414,7 @@ __global__ void __launch_bounds__(Q_TPB) k_q_rx(QParams p, const double *__restr
     extern __shared__ __align__(16) char qsm[];   // QAG work lists when lists_in_smem
     const int gid = blockIdx.x * blockDim.x + threadIdx.x, nthr = gridDim.x * blockDim.x;
     char *mine = lists_in_smem ? qsm + (size_t)threadIdx.x * QAG_WS : ws + (size_t)gid * QAG_WS;
-    if (p.quad_rx == 0) {
+    if (p.quad_rx == MIDAS_QUAD_UN) {
         const long long inst = 2LL * p.ntr * p.nrx_phi;
         for (long long i = gid; i < inst; i += nthr) {
             const long long tk = i / p.nrx_phi;
@@ -427,8 +427,8 @@ __global__ void __launch_bounds__(Q_TPB) k_q_rx(QParams p, const double *__restr
     for (long long i = gid; i < 2LL * p.ntr; i += nthr) {
         const double *f = F + (size_t)i * p.nrx;
         double q = 0;
-        if (p.quad_rx == 1) q = q_trap2d(f, p.th0, p.th1, p.ph0, p.ph1, p.nrx_theta, p.nrx_phi);
-        else if (p.quad_rx == 2) q = q_gl2d(f, w_rx, w_rx + p.nrx_theta, p.nrx_theta, p.nrx_phi);
+        if (p.quad_rx == MIDAS_QUAD_TR) q = q_trap2d(f, p.th0, p.th1, p.ph0, p.ph1, p.nrx_theta, p.nrx_phi);
+        else if (p.quad_rx == MIDAS_QUAD_GL) q = q_gl2d(f, w_rx, w_rx + p.nrx_theta, p.nrx_theta, p.nrx_phi);
         else
             for (int r = 0; r < p.nrx; ++r) q = da(q, f[r]);
         qr[i] = q;
@@ -447,7 +447,7 @@ __global__ void __launch_bounds__(Q_TPB) k_q_rx_fin(QParams p, const double *fy,
     for (int t = gid; t < p.ntr; t += nthr) {
         double q[2];
         for (int k = 0; k < 2; ++k) {
-            if (p.quad_rx == 0) {
+            if (p.quad_rx == MIDAS_QUAD_UN) {
                 const double *y = fy + (size_t)(2 * t + k) * p.nrx_phi;
                 q[k] = p.nrx_phi > 1 ? (double)q_qag(y, p.nrx_phi, (float)p.ph0, (float)p.ph1, mine, st)
                                      : y[0];
@@ -457,11 +457,11 @@ __global__ void __launch_bounds__(Q_TPB) k_q_rx_fin(QParams p, const double *fy,
         }
         const double c2 = dmu(2.0, dmu(p.k0, p.k0));
         double qs, g;
-        if (p.quad_rx == 4) {   // 'lb'
+        if (p.quad_rx == MIDAS_QUAD_LB) {
             const double csca = dmu(ddv(1.0, c2), q[0]);
             qs = dmu(ddv(dmu(4.0, p.Pi), dmu(dmu(dmu(2.0, p.Pi), p.X), p.X)), q[0]);
             g = dmu(ddv(1.0, dmu(c2, csca)), q[1]);
-        } else if (p.quad_rx == 3 || p.quad_rx == 5) {   // 'sd' / 'rf'
+        } else if (p.quad_rx == MIDAS_QUAD_SD || p.quad_rx == MIDAS_QUAD_RF) {
             const double w = ddv(dmu(4.0, p.Pi), (double)p.nrx);
             const double qsd = dmu(w, q[0]);
             const double csca = dmu(ddv(1.0, c2), qsd);
@@ -495,7 +495,7 @@ __global__ void __launch_bounds__(256) k_q_avg(QParams p, const double *q_dir, c
     if (p.list_tr) {
         if (tid < 5) {
             double s = 0;
-            if (p.quad_tr == 4)
+            if (p.quad_tr == MIDAS_QUAD_LB)
                 for (int t = 0; t < p.ntr; ++t) s = da(s, dmu(w_tr[t], q_dir[5 * (size_t)t + tid]));
             else {
                 for (int t = 0; t < p.ntr; ++t) s = da(s, q_dir[5 * (size_t)t + tid]);
@@ -510,7 +510,7 @@ __global__ void __launch_bounds__(256) k_q_avg(QParams p, const double *q_dir, c
         G[i] = dmu(q_dir[5 * (size_t)t + k], s_tr[t % p.ntr_theta]);
     }
     __syncthreads();
-    if (p.quad_tr == 0) {
+    if (p.quad_tr == MIDAS_QUAD_UN) {
         for (int i = tid; i < 5 * p.ntr_phi; i += blockDim.x) {
             const int k = i / p.ntr_phi, j = i % p.ntr_phi;
             gy[i] = (double)q_qag(G + (size_t)k * p.ntr + (size_t)j * p.ntr_theta, p.ntr_theta, (float)p.tth0,
@@ -521,11 +521,11 @@ __global__ void __launch_bounds__(256) k_q_avg(QParams p, const double *q_dir, c
     if (tid < 5) {
         const double *g = G + (size_t)tid * p.ntr;
         double q;
-        if (p.quad_tr == 0)
+        if (p.quad_tr == MIDAS_QUAD_UN)
             q = p.ntr_phi > 1 ? (double)q_qag(gy + (size_t)tid * p.ntr_phi, p.ntr_phi, (float)p.tph0, (float)p.tph1,
                                               ws + (size_t)tid * QAG_WS, st)
                               : gy[(size_t)tid * p.ntr_phi];
-        else if (p.quad_tr == 1)   // 'tr' passes TrPh_min as both phi limits (:509-513)
+        else if (p.quad_tr == MIDAS_QUAD_TR)   // 'tr' passes TrPh_min as both phi limits (:509-513)
             q = q_trap2d(g, p.tth0, p.tth1, p.tph0, p.tph0, p.ntr_theta, p.ntr_phi);
         else
             q = q_gl2d(g, w_tr, w_tr + p.ntr_theta, p.ntr_theta, p.ntr_phi);
