@@ -271,3 +271,94 @@ def gauss_legendre_directions(th0: float, th1: float, nth: int, ph0: float, ph1:
         xp, wp = np.array([math.radians(ph0)]), np.array([1.0])
     th, ph = np.degrees(xt), np.degrees(xp)
     return np.tile(th, nph), np.repeat(ph, nth), np.concatenate([wt, wp])
+
+
+def list_receivers_with_extras(rx_th, rx_ph, tr_th, tr_ph):
+    """Receiver list of the 'sd' / 'lb' / 'rf' rules: the NRx directions, then the
+    forward direction of every transmitter, then every backward direction
+    (src/get_trans_Receiv.f90:527-550) -- the positional layout that
+    Compute_Scattering_Quantities_2 indexes (NRx + t, NRx + NTr + t)."""
+    tr_th, tr_ph = np.asarray(tr_th, np.float64), np.asarray(tr_ph, np.float64)
+    return (np.concatenate([np.asarray(rx_th, np.float64), tr_th, 180.0 - tr_th]),
+            np.concatenate([np.asarray(rx_ph, np.float64), tr_ph, np.fmod(tr_ph + 180.0, 360.0)]))
+
+
+def _unit(rng) -> np.ndarray:
+    v = rng.normal(size=3)
+    return v / np.linalg.norm(v)
+
+
+def fractal_aggregate(n_mono: int, a: float = 1.0, df: float = 1.8, kf: float = 1.3, seed: int = 0,
+                      tries: int = 400) -> np.ndarray:
+    """Monomer centres of a seeded aggregate of n_mono touching spheres of radius a,
+    grown by tunable particle-cluster aggregation: each new monomer is placed at
+    the distance Gamma from the cluster's centre of mass that keeps the fractal law
+    N = kf (Rg / a)^df exact, touching one monomer and overlapping none.  With
+    Rg_N^2 the mean squared distance of the N centres from their centroid, adding
+    one centre at distance Gamma gives (N+1) Rg_{N+1}^2 = N Rg_N^2 + N Gamma^2/(N+1),
+    so Gamma^2 = (N+1)/N ((N+1) Rg_{N+1}^2 - N Rg_N^2).  Where no touching position
+    reaches Gamma (small N, or a crowded shell), the touching, non-overlapping
+    position closest to it is taken."""
+    rng = np.random.default_rng(seed)
+    pos = [np.zeros(3), 2.0 * a * _unit(rng)]
+    d_min = 2.0 * a * (1.0 - 1e-9)
+    while len(pos) < n_mono:
+        P = np.array(pos)
+        N = len(P)
+        c = P.mean(axis=0)
+        rg2 = float(np.mean(np.sum((P - c) ** 2, axis=1)))
+        target = a * a * ((N + 1) / kf) ** (2.0 / df)
+        gamma = math.sqrt(max((N + 1) / N * ((N + 1) * target - N * rg2), 0.0))
+        dist = np.linalg.norm(P - c, axis=1)
+        cand = np.flatnonzero((np.abs(dist - gamma) <= 2.0 * a) & (dist > 1e-12))
+        placed = None
+        for _ in range(tries if cand.size else 0):
+            j = int(rng.choice(cand))
+            D = dist[j]
+            e = (P[j] - c) / D
+            h = (D * D + gamma * gamma - 4.0 * a * a) / (2.0 * D)   # circle of the two spheres
+            rho = math.sqrt(max(gamma * gamma - h * h, 0.0))
+            u = np.cross(e, _unit(rng))
+            u /= np.linalg.norm(u)
+            v = np.cross(e, u)
+            phi = rng.uniform(0.0, 2.0 * math.pi)
+            p = c + h * e + rho * (math.cos(phi) * u + math.sin(phi) * v)
+            if np.min(np.linalg.norm(P - p, axis=1)) >= d_min:
+                placed = p
+                break
+        if placed is None:   # closest feasible touching position
+            best, best_err = None, math.inf
+            for _ in range(tries):
+                p = P[int(rng.integers(N))] + 2.0 * a * _unit(rng)
+                if np.min(np.linalg.norm(P - p, axis=1)) < d_min:
+                    continue
+                err = abs(np.linalg.norm(p - c) - gamma)
+                if err < best_err:
+                    best, best_err = p, err
+            placed = best
+        if placed is None:
+            raise RuntimeError("fractal_aggregate: no free touching position")
+        pos.append(placed)
+    P = np.array(pos)
+    return P - P.mean(axis=0)
+
+
+def voxelise_spheres(centres: np.ndarray, a: float, cells_per_diameter: int = 6):
+    """Cubic cells of edge 2a / cells_per_diameter whose centres lie strictly inside
+    one of the spheres (the reference's inside test for its sphere voxeliser,
+    src/Discretization.f90:246-310).  Returns (xyz, edge)."""
+    d = 2.0 * a / cells_per_diameter
+    lo = centres.min(axis=0) - a
+    dims = np.ceil((centres.max(axis=0) + a - lo) / d).astype(int) + 1
+    mask = np.zeros(dims, bool)
+    r = int(math.ceil(a / d)) + 1
+    off = np.arange(-r, r + 1)
+    for cen in centres:
+        base = np.floor((cen - lo) / d).astype(int)
+        idx = [np.clip(base[k] + off, 0, dims[k] - 1) for k in range(3)]
+        gx, gy, gz = np.meshgrid(*idx, indexing="ij")
+        px, py, pz = (lo[k] + (g + 0.5) * d for k, g in enumerate((gx, gy, gz)))
+        inside = (px - cen[0]) ** 2 + (py - cen[1]) ** 2 + (pz - cen[2]) ** 2 < a * a
+        mask[gx[inside], gy[inside], gz[inside]] = True
+    ijk = np.argwhere(mask)
+    return lo + (ijk + 0.5) * d, d

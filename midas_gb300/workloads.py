@@ -145,9 +145,40 @@ def post_avg():
     return _post_scene("post_un_19x37tr_181x25rx", (19, 37), (181, 25))
 
 
+def c4_instance(wl, k):
+    """Cells of aggregate k of a C4 workload: (xyz, edge)."""
+    from . import geometry as G
+    P = G.fractal_aggregate(int(wl["n_mono"][k]), a=wl["a"], df=wl["df"], kf=wl["kf"], seed=int(wl["seeds"][k]))
+    return G.voxelise_spheres(P, wl["a"], wl["cells_per_diameter"])
+
+
+def c4(n_instances=256, ndir=48, nrx=194, seed=11):
+    """Batched uneven instances: n_instances seeded aggregates of 4-64 touching
+    spheres of radius 0.8 lambda / 2 pi (k0 a = 0.8), m = 1.33 + 0.001i, grown by
+    tunable particle-cluster aggregation (fractal dimension 1.8, prefactor 1.3) and
+    voxelised at 6 cells per monomer diameter (113 cells per monomer: 1.4k-22k
+    unknowns); ndir seeded incident directions x 2 polarisations each, and nrx
+    seeded scattering directions with equal weights for Q_sca and g ('rf' rules,
+    Compute_Scattering_Quantities_2).  Instances are built by c4_instance."""
+    from . import geometry as G
+    rng = np.random.default_rng(seed)
+    th, ph = G.random_directions(ndir, seed=seed + 1)
+    rth, rph = G.random_directions(nrx, seed=seed + 2)
+    rth, rph = G.list_receivers_with_extras(rth, rph, th, ph)
+    return {"name": f"c4_{n_instances}_aggregates_df1.8_{ndir}dirs", "method": "batch", "a": 1.0, "k0": 0.8,
+            "m": 1.33 + 0.001j, "df": 1.8, "kf": 1.3, "cells_per_diameter": 6,
+            "n_mono": rng.integers(4, 65, n_instances), "seeds": rng.integers(1 << 30, size=n_instances),
+            "th": th, "ph": ph, "rx_th": rth, "rx_ph": rph, "nrx": nrx}
+
+
+def c4_small():
+    """Eight C4 aggregates: the batch path at a size that runs in seconds."""
+    return c4(n_instances=8)
+
+
 WORKLOADS = {"mom_c1": mom_c1, "mom_c3": mom_c3, "mom_c3_small": mom_c3_small, "mom_tiny": mom_tiny,
              "cbfm_c2": cbfm_c2, "cbfm_c2_small": cbfm_c2_small, "cbfm_c2_mid": cbfm_c2_mid,
-             "post_sphere": post_sphere, "post_avg": post_avg}
+             "post_sphere": post_sphere, "post_avg": post_avg, "c4": c4, "c4_small": c4_small}
 
 
 def cbfm_args(wl):
@@ -156,6 +187,39 @@ def cbfm_args(wl):
     eo = np.ascontiguousarray(np.concatenate([[0], np.cumsum([len(e) for e in wl["ext"]])]), np.int32)
     ei = np.ascontiguousarray(np.concatenate(wl["ext"]), np.int32)
     return bo, eo, ei
+
+
+def run_batch(ctx, wl, steps):
+    """C4: every aggregate solved for all directions (fill, mixed LU, refinement),
+    then its S matrix, Cext / Cabs and orientation averages; prints the
+    orientation-averaged solves/s (directions x instances / wall time) and the
+    averages over the instances."""
+    cells = [c4_instance(wl, k) for k in range(len(wl["n_mono"]))]   # scene preparation, not timed
+    th, ph, rth, rph = wl["th"], wl["ph"], wl["rx_th"], wl["rx_ph"]
+    ntr, eps = len(th), wl["m"] ** 2
+    unknowns = [3 * len(x) for x, _ in cells]
+    for step in range(steps):
+        t0 = time.perf_counter()
+        acc = np.zeros(5)
+        cext = cabs = 0.0
+        for xyz, d in cells:
+            ctx.set_cells(xyz, d, eps, wl["k0"])
+            E = ctx.mom_solve(th, ph)
+            S = ctx.smatrix(rth, rph, E)
+            ce, ca = ctx.cext_cabs(th, ph, E)
+            dm = 2.0 * (3.0 * len(xyz) * d ** 3 / (4.0 * math.pi)) ** (1.0 / 3.0)   # volume-equivalent
+            _, qa = ctx.scattering_quantities("rf", "rf", (ntr, 1), (wl["nrx"], 1), th, ph, rth, rph, S, ce, ca,
+                                              dm, wl["k0"])
+            acc += qa
+            cext += float(np.mean(ce))
+            cabs += float(np.mean(ca))
+        dt = time.perf_counter() - t0
+        n = len(cells)
+        print(f"{wl['name']}: step {step} {dt:.3f} s, {ntr * n / dt:.2f} orientation-averaged solves/s "
+              f"({n} instances, {min(unknowns)}-{max(unknowns)} unknowns), <Cext> {cext / n:.5g}, "
+              f"<Cabs> {cabs / n:.5g}, <g> {acc[4] / n:.4f}", flush=True)
+    ctx.close()
+    return 0
 
 
 def main(argv=None):
@@ -185,6 +249,8 @@ def main(argv=None):
                   f"<Q_ext, Q_abs, Q_sca, Q_bks, g> = {np.array2string(qa, precision=5)}", flush=True)
         ctx.close()
         return 0
+    if wl["method"] == "batch":
+        return run_batch(ctx, wl, args.steps)
     ctx.set_cells(wl["xyz"], wl["sc"], wl["eps"], wl["k0"])
     for step in range(args.steps):
         t0 = time.perf_counter()

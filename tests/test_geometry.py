@@ -41,3 +41,36 @@ def test_gaussian_sphere_seeded():
 
 def test_nipws():
     assert G.init_nipws(0.3) == 91 and G.init_nipws(2.5) == 190 and G.init_nipws(12) == 231
+
+
+@pytest.mark.parametrize("n", [4, 23, 64])
+def test_fractal_aggregate(n):
+    """Touching, non-overlapping monomers on the fractal law N = kf (Rg/a)^df."""
+    P = G.fractal_aggregate(n, a=1.0, df=1.8, kf=1.3, seed=n)
+    assert P.shape == (n, 3) and np.allclose(P.mean(axis=0), 0.0, atol=1e-12)
+    D = np.linalg.norm(P[:, None] - P[None], axis=2) + np.eye(n) * 1e9
+    assert D.min() >= 2.0 * (1 - 1e-9)                       # no overlaps
+    assert np.all(D.min(axis=1) <= 2.0 * (1 + 1e-9))          # every monomer touches one
+    rg = np.sqrt(np.mean(np.sum(P ** 2, axis=1)))
+    assert abs(rg - (n / 1.3) ** (1 / 1.8)) < 1e-6 * rg      # the law holds wherever it was reachable
+    assert np.array_equal(P, G.fractal_aggregate(n, a=1.0, df=1.8, kf=1.3, seed=n))   # seeded
+
+
+def test_voxelise_spheres():
+    P = G.fractal_aggregate(12, seed=3)
+    xyz, d = G.voxelise_spheres(P, 1.0, 6)
+    assert d == 1.0 / 3.0
+    dist = np.min(np.linalg.norm(xyz[:, None] - P[None], axis=2), axis=1)
+    assert np.all(dist < 1.0)                                   # every cell centre inside a monomer
+    assert abs(len(xyz) - 12 * 4 / 3 * np.pi * 27) < 0.05 * len(xyz)
+    g = (xyz - xyz.min(axis=0)) / d                             # on one lattice, no duplicates
+    assert np.allclose(g, np.round(g), atol=1e-9) and len(np.unique(np.round(g), axis=0)) == len(xyz)
+    single, _ = G.voxelise_spheres(np.zeros((1, 3)), 1.0, 6)   # a lone sphere: 6 cells across
+    assert np.ptp(single[:, 0]) == pytest.approx(5 * d)
+
+
+def test_list_receivers_layout():
+    th, ph = np.array([10.0, 100.0]), np.array([30.0, 300.0])
+    rth, rph = G.list_receivers_with_extras([0.0, 45.0, 90.0], [0.0, 90.0, 180.0], th, ph)
+    assert np.array_equal(rth, [0.0, 45.0, 90.0, 10.0, 100.0, 170.0, 80.0])
+    assert np.array_equal(rph, [0.0, 90.0, 180.0, 30.0, 300.0, 210.0, 120.0])

@@ -32,3 +32,15 @@ def test_dense_cube_scenes():
     assert np.all((wl["eps"].real >= 1.5) & (wl["eps"].real <= 3.5))
     assert np.all((wl["eps"].imag >= 0) & (wl["eps"].imag <= 0.2))
     assert len(mom_c3_small()["xyz"]) == 4000
+
+
+def test_c4_batch_scene():
+    """C4: 256 seeded aggregates of 4-64 monomers, 48 directions, 'rf' receivers with the
+    positional forward / backward extras; instances built on demand."""
+    from midas_gb300 import workloads as W
+    wl = W.c4()
+    assert len(wl["n_mono"]) == 256 and wl["n_mono"].min() >= 4 and wl["n_mono"].max() <= 64
+    assert len(wl["th"]) == 48 and len(wl["rx_th"]) == wl["nrx"] + 2 * 48
+    xyz, d = W.c4_instance(wl, 0)
+    assert d == 1.0 / 3.0 and 90 * wl["n_mono"][0] < len(xyz) < 130 * wl["n_mono"][0]
+    assert np.array_equal(xyz, W.c4_instance(wl, 0)[0])
