@@ -256,6 +256,17 @@ int midas_gpu_bench_gemm_ex(midas_gpu_ctx *ctx, int M, int N, int K, int iters, 
 long long midas_gpu_launch_count(const midas_gpu_ctx *ctx);
 /* The context's CUDA stream (a cudaStream_t): every kernel of the context runs on it. */
 void *midas_gpu_stream(const midas_gpu_ctx *ctx);
+/* Stream ordering without a host wait (the asynchronous form of the boundary; no
+ * counterpart in the reference, whose calls are blocking).  midas_gpu_wait_event
+ * makes all work the context issues after it -- its own stream, and the CBFM lanes,
+ * which start from that stream -- wait for `event` (a cudaEvent_t the caller
+ * recorded, e.g. after producing device-resident inputs on its own stream).
+ * midas_gpu_record_event records `event` (a cudaEvent_t) on the context stream
+ * after the work issued so far, for a caller's stream to wait on.  The solve entry
+ * points themselves return when their results are complete: the refinement reads
+ * its convergence test on the host. */
+int midas_gpu_wait_event(midas_gpu_ctx *ctx, void *event);
+int midas_gpu_record_event(midas_gpu_ctx *ctx, void *event);
 
 /* Kernel classes timed by the profiler below. */
 #define MIDAS_KC_GEMM_TC   0   /* tcgen05 GEMM: LU trailing-matrix updates (and untagged GEMMs) */

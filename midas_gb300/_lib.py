@@ -32,7 +32,7 @@ EXPORTS = [
     "midas_gpu_get_cell_params", "midas_gpu_mom_fill", "midas_gpu_mom_rhs", "midas_gpu_incident_field",
     "midas_gpu_block_fill", "midas_gpu_sr_fill", "midas_gpu_set_fsr", "midas_gpu_aca", "midas_gpu_dense_solve",
     "midas_gpu_mom_solve", "midas_gpu_cbfm_solve", "midas_gpu_dense_solve_noalloc", "midas_gpu_cext_cabs", "midas_gpu_smatrix",
-    "midas_gpu_scattering_quantities",
+    "midas_gpu_scattering_quantities", "midas_gpu_wait_event", "midas_gpu_record_event",
     "midas_gpu_gemm_selftest", "midas_gpu_gemm_engine", "midas_gpu_launch_count", "midas_gpu_stream",
     "midas_gpu_bench_gemm", "midas_gpu_bench_gemm_ex", "midas_gpu_heev", "midas_gpu_zgemm_x3", "midas_gpu_profile", "midas_gpu_profile_query",
 ]
@@ -100,6 +100,8 @@ def load(path: str = LIB_PATH):
         "midas_gpu_gemm_engine": (ctypes.c_char_p, []),
         "midas_gpu_launch_count": (ctypes.c_longlong, [vp]),
         "midas_gpu_stream": (ctypes.c_void_p, [vp]),
+        "midas_gpu_wait_event": (i, [vp, vp]),
+        "midas_gpu_record_event": (i, [vp, vp]),
         "midas_gpu_bench_gemm": (i, [vp, i, i, i, i, ctypes.POINTER(ctypes.c_double)]),
         "midas_gpu_bench_gemm_ex": (i, [vp, i, i, i, i, i, ctypes.POINTER(ctypes.c_double)]),
         "midas_gpu_profile": (i, [vp, i]),

@@ -916,4 +916,22 @@ int midas_gpu_profile_query(midas_gpu_ctx *c, int kclass, double *ms, double *fl
 
 void *midas_gpu_stream(const midas_gpu_ctx *c) { return c ? (void *)c->stream : nullptr; }
 
+int midas_gpu_wait_event(midas_gpu_ctx *c, void *event)
+{
+    if (!c) return MIDAS_ERR_ARG;
+    c->err = Err();
+    if (!event) return c->err.set(MIDAS_ERR_ARG, "wait_event: null event");
+    MIDAS_CUDA(c, cudaStreamWaitEvent(c->stream, (cudaEvent_t)event, 0));
+    return MIDAS_OK;
+}
+
+int midas_gpu_record_event(midas_gpu_ctx *c, void *event)
+{
+    if (!c) return MIDAS_ERR_ARG;
+    c->err = Err();
+    if (!event) return c->err.set(MIDAS_ERR_ARG, "record_event: null event");
+    MIDAS_CUDA(c, cudaEventRecord((cudaEvent_t)event, c->stream));
+    return MIDAS_OK;
+}
+
 }  // extern "C"

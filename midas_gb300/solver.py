@@ -238,6 +238,15 @@ class Context:
                 out[name] = {"ms": ms.value, "flops": fl.value, "bytes": by.value, "launches": n.value}
         return out
 
+    def wait_event(self, event: int):
+        """Order the context's later work after a caller's cudaEvent_t (an integer handle,
+        e.g. torch.cuda.Event().cuda_event once recorded) without a host wait."""
+        self._ck(self.L.midas_gpu_wait_event(self.h, ctypes.c_void_p(event)))
+
+    def record_event(self, event: int):
+        """Record a caller's cudaEvent_t on the context stream after the work issued so far."""
+        self._ck(self.L.midas_gpu_record_event(self.h, ctypes.c_void_p(event)))
+
     def stream_handle(self) -> int:
         """cudaStream_t of the context (wrap with torch.cuda.ExternalStream to time on it)."""
         return int(self.L.midas_gpu_stream(self.h) or 0)

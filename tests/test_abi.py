@@ -38,4 +38,5 @@ def test_init_rejects_bad_opts(gpulib):
     h = ctypes.c_void_p()
     assert gpulib.midas_gpu_init(ctypes.byref(o), ctypes.byref(h)) == 1   # MIDAS_ERR_ARG, before any device call
     assert gpulib.midas_gpu_free(None) == 0
+    assert gpulib.midas_gpu_wait_event(None, None) == 1 and gpulib.midas_gpu_record_event(None, None) == 1
     assert gpulib.midas_gpu_last_error(None) == b"null context"
