@@ -193,7 +193,12 @@ def run_batch(ctx, wl, steps):
     """C4: every aggregate solved for all directions (fill, mixed LU, refinement),
     then its S matrix, Cext / Cabs and orientation averages; prints the
     orientation-averaged solves/s (directions x instances / wall time) and the
-    averages over the instances."""
+    averages over the instances.  <Cext> is the optical-theorem (far-field)
+    extinction: the reference's internal-field cross sections sum the three field
+    components before the products (Compute_ExtAbsCsec_fromIntField.f90:52-59),
+    which holds only for axis-aligned incidence, and these directions are random.
+    <Cabs> is the reference's internal-field value all the same (its Q_abs always
+    is)."""
     cells = [c4_instance(wl, k) for k in range(len(wl["n_mono"]))]   # scene preparation, not timed
     th, ph, rth, rph = wl["th"], wl["ph"], wl["rx_th"], wl["rx_ph"]
     ntr, eps = len(th), wl["m"] ** 2
@@ -211,7 +216,7 @@ def run_batch(ctx, wl, steps):
             _, qa = ctx.scattering_quantities("rf", "rf", (ntr, 1), (wl["nrx"], 1), th, ph, rth, rph, S, ce, ca,
                                               dm, wl["k0"])
             acc += qa
-            cext += float(np.mean(ce))
+            cext += float(qa[0]) * math.pi * (dm / 2.0) ** 2    # far-field Q_ext (cext_intfields = 0)
             cabs += float(np.mean(ca))
         dt = time.perf_counter() - t0
         n = len(cells)

@@ -142,3 +142,42 @@ def test_reference_error_cases(oracle):
     c3["rx_th"] = np.where(c3["rx_th"] < 180.0 - 1e-9, c3["rx_th"] * 0.5 + 40.0, c3["rx_th"])
     st, _, _ = C.oracle_call(oracle, c3)
     assert st != 0
+
+
+def test_aggregate_pipeline_energy_balance(oracle):
+    """The C4 pipeline on a small aggregate ('rf' lists, positional forward /
+    backward receivers): the Monte-Carlo Q_sca over 1,500 directions matches the
+    optical-theorem Q_ext minus Q_abs.  (The internal-field Q_ext is not compared:
+    the reference sums the field components before the products, exact only for
+    axis-aligned incidence.)"""
+    from midas_gb300 import geometry as G
+    P = G.fractal_aggregate(5, seed=3)
+    xyz, d = G.voxelise_spheres(P, 1.0, 4)
+    k0, m = 0.8, 1.33 + 0.001j
+    th, ph = G.random_directions(6, seed=1)
+    rth, rph = G.list_receivers_with_extras(*G.random_directions(1500, seed=2), th, ph)
+    res = oracle.mom_solve(oracle.Cells(xyz, d, m * m, k0), th, ph, rth, rph)
+    dm = 2.0 * (3.0 * len(xyz) * d ** 3 / (4.0 * math.pi)) ** (1.0 / 3.0)
+    st, qd, qa = oracle.scattering_quantities("rf", "rf", (6, 1), (1500, 1), th, ph, rth, rph, res["S"],
+                                              res["cext"], res["cabs"], dm, k0)
+    assert st == 0
+    q_ext, q_abs, q_sca = qa[0], qa[1], qa[2]
+    assert abs(q_sca - (q_ext - q_abs)) / q_sca < 0.05
+    assert np.allclose(qa, qd.mean(axis=0), rtol=1e-14)
+
+
+def test_internal_field_cross_sections_sum_components(oracle):
+    """The reference's Cext from the internal field sums E's three components before
+    the product with the conjugated incident field (src/Compute_ExtAbsCsec_fromIntField.f90:52-59):
+    on a sphere it agrees with the optical theorem for incidence along a coordinate
+    axis and not for oblique incidence.  Kept for parity."""
+    m, a, k0 = 1.5 + 0.01j, 1.0, 2.0
+    sc = a / 4.775
+    cells = oracle.Cells(oracle.sphere_cells(2 * a, sc), sc, m * m, k0)
+    th, ph = np.array([0.0, 90.0, 30.0]), np.array([0.0, 90.0, 0.0])
+    res = oracle.mom_solve(cells, th, ph, th, ph)
+    S, X, pi = res["S"], k0 * a, oracle.ref_pi()
+    q_ff = [(2 / (X * X)) * (abs(S[t, 4 * t + 3].imag) + abs(S[t, 4 * t].imag)) for t in range(3)]
+    q_int = res["cext"] / (pi * a * a)
+    assert abs(q_int[0] / q_ff[0] - 1) < 0.03 and abs(q_int[1] / q_ff[1] - 1) < 0.03
+    assert q_int[2] / q_ff[2] < 0.7
