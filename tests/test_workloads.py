@@ -44,3 +44,43 @@ def test_c4_batch_scene():
     xyz, d = W.c4_instance(wl, 0)
     assert d == 1.0 / 3.0 and 90 * wl["n_mono"][0] < len(xyz) < 130 * wl["n_mono"][0]
     assert np.array_equal(xyz, W.c4_instance(wl, 0)[0])
+
+
+def test_c4_batch_runner_calls(capsys):
+    """The batch runner's host logic with a stand-in context: every aggregate is set,
+    solved for all directions, and its efficiencies requested with 'rf' lists whose
+    receiver array carries the positional forward / backward blocks."""
+    from midas_gb300 import workloads as W
+    wl = W.c4(n_instances=3, ndir=4, nrx=10)
+    calls = []
+
+    class FakeCtx:
+        def set_cells(self, xyz, sc, eps, k0):
+            self.n = len(xyz)
+            calls.append(("cells", len(xyz), sc, k0))
+            return self
+
+        def mom_solve(self, th, ph):
+            return np.ones((3 * self.n, 2 * len(th)), complex)
+
+        def smatrix(self, rth, rph, E):
+            return np.ones((len(rth), 2 * E.shape[1]), complex)
+
+        def cext_cabs(self, th, ph, E):
+            return np.full(len(th), 2.0), np.full(len(th), 0.5)
+
+        def scattering_quantities(self, qt, qr, tg, rg, th, ph, rth, rph, S, ce, ca, dm, k0):
+            assert (qt, qr) == ("rf", "rf") and tg == (len(th), 1) and rg == (10, 1)
+            assert len(rth) == 10 + 2 * len(th) and S.shape == (len(rth), 4 * len(th))
+            assert np.allclose(rth[10:10 + len(th)], th) and np.allclose(rth[10 + len(th):], 180.0 - th)
+            assert dm > 0 and k0 == wl["k0"]
+            calls.append(("q", dm))
+            return np.zeros((len(th), 5)), np.array([1.0, 0.1, 0.9, 0.05, 0.3])
+
+        def close(self):
+            calls.append(("close",))
+
+    assert W.run_batch(FakeCtx(), wl, 1) == 0
+    assert [c[0] for c in calls] == ["cells", "q"] * 3 + ["close"]
+    out = capsys.readouterr().out
+    assert "orientation-averaged solves/s" in out and "3 instances" in out
