@@ -217,18 +217,21 @@ int midas_gpu_scattering_quantities(midas_gpu_ctx *ctx, int quad_tr, int quad_rx
                                     const double *w_tr, const double *w_rx, double *q_dir, double *q_avg);
 
 /* Dense complex solve that allocates no device memory (no counterpart in the
- * reference).  For callers that cannot call cudaMalloc -- code running while a
- * stream is captured into a CUDA graph, plug-ins whose host application owns and
- * caps all device memory, latency-critical paths -- it solves A X = B (A n x n,
- * B n x nrhs, column-major complex, host or device memory; B is overwritten by X)
- * with the same mixed-precision LU + FP64 refinement as midas_gpu_dense_solve,
- * on `stream` (a cudaStream_t; NULL = the legacy default stream) of `device`.
+ * reference).  For callers that cannot call cudaMalloc: plug-ins whose host
+ * application owns and caps all device memory, and latency-critical paths where
+ * an allocation could block.  It solves A X = B (A n x n, B n x nrhs,
+ * column-major complex, host or device memory; B is overwritten by X) with the
+ * same mixed-precision LU + FP64 refinement as midas_gpu_dense_solve, on
+ * `stream` (a cudaStream_t; NULL = the legacy default stream) of `device`.
  * No context is needed.  All scratch comes from one static 24 MiB device array
- * inside the library, which every GPU that loads the library holds until exit.
+ * inside the library, which every GPU that loads the library holds until exit;
+ * a scratch request beyond it returns MIDAS_ERR_ALLOC, never a cudaMalloc.
  * Limits: n <= 512, nrhs <= 32 (larger sizes return MIDAS_ERR_ARG).  All calls
  * share the array: calls that overlap on the GPU race, so serialise them.  The
- * first call on a device looks up the array's device address
- * (cudaGetSymbolAddress); make it before any stream capture starts.
+ * call is synchronous (it waits on `stream` and reads the refinement's
+ * convergence on the host); on a stream that is being captured it returns
+ * MIDAS_ERR_ARG without issuing work.  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress) and caches it.
  * *backward_error (may be NULL) receives the final normwise backward error. */
 int midas_gpu_dense_solve_noalloc(int device, void *stream, int n, int nrhs, const double *A, double *B,
                                   double *backward_error);
@@ -239,6 +242,11 @@ int midas_gpu_dense_solve_noalloc(int device, void *stream, int n, int nrhs, con
 int midas_gpu_gemm_selftest(midas_gpu_ctx *ctx);
 /* Name of the GEMM engine in use ("tcgen05"). */
 const char *midas_gpu_gemm_engine(void);
+/* Check of the bounded device waits: one kernel waits, with `limit` polls
+ * (1..2^20), on an mbarrier that nothing arrives at, through the same wait
+ * routine as the tensor-core kernels.  The wait expires, *expired is set to 1 and
+ * the call returns MIDAS_ERR_DEVICE_TIMEOUT; the context stays usable. */
+int midas_gpu_wait_selftest(midas_gpu_ctx *ctx, int limit, int *expired);
 /* Hermitian eigen-decomposition on the device (the CBF singular-value step):
  * A is m x m row-major complex; W receives the eigenvalues in descending order and
  * V (row-major m x m) the eigenvectors as columns. */

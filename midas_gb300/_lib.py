@@ -33,7 +33,7 @@ EXPORTS = [
     "midas_gpu_block_fill", "midas_gpu_sr_fill", "midas_gpu_set_fsr", "midas_gpu_aca", "midas_gpu_dense_solve",
     "midas_gpu_mom_solve", "midas_gpu_cbfm_solve", "midas_gpu_dense_solve_noalloc", "midas_gpu_cext_cabs", "midas_gpu_smatrix",
     "midas_gpu_scattering_quantities", "midas_gpu_wait_event", "midas_gpu_record_event",
-    "midas_gpu_gemm_selftest", "midas_gpu_gemm_engine", "midas_gpu_launch_count", "midas_gpu_stream",
+    "midas_gpu_gemm_selftest", "midas_gpu_gemm_engine", "midas_gpu_wait_selftest", "midas_gpu_launch_count", "midas_gpu_stream",
     "midas_gpu_bench_gemm", "midas_gpu_bench_gemm_ex", "midas_gpu_heev", "midas_gpu_zgemm_x3", "midas_gpu_profile", "midas_gpu_profile_query",
 ]
 
@@ -98,6 +98,7 @@ def load(path: str = LIB_PATH):
         "midas_gpu_scattering_quantities": (i, [vp, i, i, i, i, P, P, i, i, i, P, P, P, P, P, d, d, i, P, P, P, P]),
         "midas_gpu_gemm_selftest": (i, [vp]),
         "midas_gpu_gemm_engine": (ctypes.c_char_p, []),
+        "midas_gpu_wait_selftest": (i, [vp, i, ctypes.POINTER(ctypes.c_int)]),
         "midas_gpu_launch_count": (ctypes.c_longlong, [vp]),
         "midas_gpu_stream": (ctypes.c_void_p, [vp]),
         "midas_gpu_wait_event": (i, [vp, vp]),

@@ -149,6 +149,9 @@ struct midas_gpu_ctx {
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     bool allow_side = true;   // false for the allocation-free entry point
+    // true for the allocation-free entry point: its slots are carved from a static
+    // array, and a request beyond a slot's capacity is an error, never a cudaMalloc
+    bool no_alloc = false;
     void *cusolver = nullptr;
     void *cublas = nullptr;
 };

@@ -12,8 +12,8 @@
 // 128 x BN accumulator in tensor memory; four epilogue warps drain TMEM with
 // tcgen05.ld and apply alpha/beta.  Every mbarrier wait is bounded: on expiry
 // the kernel raises DEV_TIMEOUT in the context flag and unwinds (TMEM freed).
-// Engine "simt": a register-tiled CUDA-core kernel used to validate the tensor
-// path on the device (gemm_selftest) and selectable with MIDAS_GEMM=simt.
+// A register-tiled CUDA-core kernel (k_gemm_simt) is the device-side check of the
+// tensor path in gemm_selftest; no product of the library runs on it.
 #include <cuda.h>
 #include <cuda_fp16.h>
 #include <atomic>
@@ -108,10 +108,11 @@ __device__ __forceinline__ bool mbar_try(uint64_t *bar, uint32_t parity)
     return ok != 0;
 }
 
-// bounded wait: returns false (and raises the abort flag) when the limit expires
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag, int *gflag)
+// bounded wait: returns false (and raises the abort flag) when `limit` polls expire
+__device__ __forceinline__ bool mbar_wait_n(uint64_t *bar, uint32_t parity, volatile int *abort_flag, int *gflag,
+                                            uint32_t limit)
 {
-    for (uint32_t i = 0; i < TC_SPIN_LIMIT; ++i) {
+    for (uint32_t i = 0; i < limit; ++i) {
         if (mbar_try(bar, parity)) return true;
         if (*abort_flag) return false;
         if (i > 64) __nanosleep(64);
@@ -119,6 +120,11 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volati
     *abort_flag = 1;
     atomicOr(gflag, DEV_TIMEOUT);
     return false;
+}
+
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag, int *gflag)
+{
+    return mbar_wait_n(bar, parity, abort_flag, gflag, TC_SPIN_LIMIT);
 }
 
 __device__ __forceinline__ void mbar_arrive_tx(uint64_t *bar, uint32_t bytes)
@@ -643,20 +649,9 @@ static int make_map(midas_gpu_ctx *c, CUtensorMap *m, const void *base, int rows
     return MIDAS_OK;
 }
 
-// 0 simt, 1 tcgen05 (MIDAS_GEMM=simt selects the CUDA-core engine); read once,
-// thread-safe (function-local static initialisation)
-static int pick_engine()
-{
-    static const int engine = [] {
-        const char *e = getenv("MIDAS_GEMM");
-        return (e && strcmp(e, "simt") == 0) ? 0 : 1;
-    }();
-    return engine;
-}
+const char *gemm_engine() { return "tcgen05"; }
 
-const char *gemm_engine() { return pick_engine() == 0 ? "simt" : "tcgen05"; }
-
-bool gemm_tc_engine() { return pick_engine() == 1; }
+bool gemm_tc_engine() { return true; }
 
 // algorithmic bytes of one real GEMM: A and Bt once, D written (and read when beta != 0)
 static double gemm_bytes(const GemmArgs &g)
@@ -779,8 +774,7 @@ int gemm_tf32(midas_gpu_ctx *c, const GemmArgs &g, bool precise)
 {
     if (g.M <= 0 || g.N <= 0) return MIDAS_OK;
     if (g.K <= 0) return c->err.set(MIDAS_ERR_ARG, "gemm_tf32: K must be positive");
-    if (g.h16 && !pick_engine()) return c->err.set(MIDAS_ERR_ARG, "gemm_tf32: fp16 operands need the tcgen05 engine");
-    return pick_engine() ? gemm_tc(c, g, precise) : gemm_simt(c, g);
+    return gemm_tc(c, g, precise);
 }
 
 // ---------------------------------------------------------------------------
@@ -887,13 +881,52 @@ int gemm_selftest(midas_gpu_ctx *c)
     return MIDAS_OK;
 }
 
+// ---------------------------------------------------------------------------
+// bounded-wait check: one CTA waits on an mbarrier that nothing arrives at, with
+// `limit` polls, through the same mbar_wait_n the tensor-core kernels use.  The
+// wait must expire, raise DEV_TIMEOUT in the context flag and let the kernel
+// return; no asynchronous copy or TMEM allocation is in flight.
+// ---------------------------------------------------------------------------
+__global__ void k_wait_expire(uint32_t limit, int *gflag, int *polled)
+{
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ int abort_flag;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const bool ok = mbar_wait_n(&bar, 0, &abort_flag, gflag, limit);
+        *polled = ok ? 0 : 1;
+    }
+    __syncthreads();
+}
+
+int wait_selftest(midas_gpu_ctx *c, int limit, int *expired)
+{
+    if (limit <= 0 || limit > (1 << 20)) return c->err.set(MIDAS_ERR_ARG, "wait_selftest: limit outside 1..2^20");
+    void *buf;
+    MIDAS_TRY(ensure(c, S_T32, 256, &buf));
+    int *polled = (int *)buf;
+    MIDAS_CUDA(c, cudaMemsetAsync(polled, 0, sizeof(int), c->stream));
+    ++c->launches;
+    k_wait_expire<<<1, 32, 0, c->stream>>>((uint32_t)limit, c->d_flag, polled);
+    MIDAS_CUDA(c, cudaGetLastError());
+    int h = 0;
+    MIDAS_CUDA(c, cudaMemcpyAsync(&h, polled, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    MIDAS_CUDA(c, cudaStreamSynchronize(c->stream));
+    *expired = h;
+    return check_flag(c, "wait_selftest");
+}
+
 // Time `iters` launches of one M x N x K GEMM (D = D - A Bt^T) with CUDA events on
 // the context stream; returns the average device time per launch in *ms.
 int gemm_bench(midas_gpu_ctx *c, int M, int N, int K, int iters, double *ms, bool f16)
 {
     if (M <= 0 || N <= 0 || K <= 0 || iters <= 0) return c->err.set(MIDAS_ERR_ARG, "bench_gemm: bad sizes");
-    if (f16 && (K % 8 || !gemm_tc_engine()))
-        return c->err.set(MIDAS_ERR_ARG, "bench_gemm: fp16 operands need K % 8 == 0 and the tcgen05 engine");
+    if (f16 && K % 8) return c->err.set(MIDAS_ERR_ARG, "bench_gemm: fp16 operands need K % 8 == 0");
     size_t na = (size_t)M * K, nb = (size_t)N * K, nd = (size_t)M * N;
     void *buf;
     MIDAS_TRY(ensure(c, S_T32, sizeof(float) * (na + nb + nd + 64) + sizeof(__half) * (na + nb) + 256, &buf));

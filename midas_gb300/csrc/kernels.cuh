@@ -90,6 +90,7 @@ int expand_b(midas_gpu_ctx *c, int k, int n, const float2 *B, long long rsb, lon
 // which GEMM engine is active ("tcgen05" or "simt")
 const char *gemm_engine();
 int gemm_selftest(midas_gpu_ctx *c);
+int wait_selftest(midas_gpu_ctx *c, int limit, int *expired);
 int gemm_bench(midas_gpu_ctx *c, int M, int N, int K, int iters, double *ms, bool f16 = false);
 
 // dense.cu

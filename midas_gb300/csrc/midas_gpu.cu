@@ -34,6 +34,12 @@ int ensure(midas_gpu_ctx *ctx, int slot, size_t bytes, void **out)
 {
     if (slot < 0 || slot >= (int)ctx->pool.size()) return ctx->err.set(MIDAS_ERR_ARG, "bad pool slot");
     DBuf &b = ctx->pool[slot];
+    if (b.bytes < bytes && ctx->no_alloc) {
+        char m[160];
+        snprintf(m, sizeof m, "pool slot %d holds %zu bytes but %zu were requested on the allocation-free path", slot,
+                 b.bytes, bytes);
+        return ctx->err.set(MIDAS_ERR_ALLOC, m);
+    }
     if (b.bytes < bytes) {
         if (b.p) { cudaStreamSynchronize(ctx->stream); cudaFree(b.p); b.p = nullptr; b.bytes = 0; }
         size_t want = bytes + bytes / 8 + 256;
@@ -833,6 +839,13 @@ int midas_gpu_gemm_selftest(midas_gpu_ctx *c)
 }
 
 const char *midas_gpu_gemm_engine(void) { return gemm_engine(); }
+
+int midas_gpu_wait_selftest(midas_gpu_ctx *c, int limit, int *expired)
+{
+    if (!c || !expired) return MIDAS_ERR_ARG;
+    c->err = Err();
+    return wait_selftest(c, limit, expired);
+}
 
 int midas_gpu_heev(midas_gpu_ctx *c, int m, const double *A, double *W, double *V)
 {

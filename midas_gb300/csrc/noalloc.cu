@@ -1,14 +1,22 @@
 // noalloc.cu -- dense complex solve that allocates no device memory.
 //
-// Some callers cannot call cudaMalloc: code running while a CUDA stream is
-// being captured into a graph (allocation calls are not capturable), plug-ins
-// that run inside a host application which owns and caps all device memory,
-// or real-time paths where an allocation could block.  For them
-// midas_gpu_dense_solve_noalloc() solves A X = B with the same mixed-precision
-// LU + FP64 refinement as midas_gpu_dense_solve(), taking every byte of device
-// scratch from one file-scope static __device__ array of NOALLOC_BYTES.  That
-// array is part of the loaded library: every GPU that loads it holds the
-// 24 MiB until the process exits, and all calls share it.
+// Some callers cannot call cudaMalloc: plug-ins that run inside a host
+// application which owns and caps all device memory (the host hands out
+// buffers, and an allocation behind its back can fail or break its
+// accounting), and real-time paths where an allocation could block on the
+// driver.  For them midas_gpu_dense_solve_noalloc() solves A X = B with the
+// same mixed-precision LU + FP64 refinement as midas_gpu_dense_solve(), taking
+// every byte of device scratch from one file-scope static __device__ array of
+// NOALLOC_BYTES.  That array is part of the loaded library: every GPU that
+// loads it holds the 24 MiB until the process exits, and all calls share it.
+// The context it builds on the host stack has `no_alloc` set, so a scratch
+// request larger than its carved slot fails with MIDAS_ERR_ALLOC instead of
+// reaching cudaMalloc.
+//
+// The call is synchronous: it waits on the caller's stream and reads the
+// refinement's convergence test on the host, as midas_gpu_dense_solve() does.
+// A call on a stream that is being captured returns MIDAS_ERR_ARG before it
+// issues any work, so the caller's capture is left intact.
 //
 // Limits: n <= NOALLOC_NMAX (512) unknowns and nrhs <= NOALLOC_RMAX (32)
 // right-hand sides; larger requests return MIDAS_ERR_ARG before any device work.
@@ -16,8 +24,9 @@
 // start at zero is cleared on each call.  Calls that overlap on the GPU (two
 // host threads, or two streams) race on the shared array and must be
 // serialised by the caller.  The first call on a device looks up the array's
-// device address with cudaGetSymbolAddress (once per device, with that device
-// current); make that first call before any stream capture begins.
+// device address with cudaGetSymbolAddress (with that device current) and
+// caches it; a cached address that no longer names device memory (after a
+// cudaDeviceReset) is looked up again.
 #include <cstring>
 
 #include "common.cuh"
@@ -31,8 +40,23 @@ constexpr size_t NOALLOC_BYTES = (size_t)24 << 20;   // n = 512, nrhs = 32 needs
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
 
-// device address of the scratch array per device (host-side cache)
-static void *g_noalloc_addr[64];
+// Device address of the scratch array, per device.  In host code the array's name
+// is only a host-side stand-in: kernels must be given this address instead.
+// Atomic entries, because two host threads may make their first call at once
+// (both then look up the same address).
+static std::atomic<void *> g_noalloc_addr[64];
+
+static int noalloc_scratch_address(int device, void **out)
+{
+    void *p = g_noalloc_addr[device].load(std::memory_order_acquire);
+    if (p && is_device_ptr(p)) { *out = p; return MIDAS_OK; }
+    p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) { cudaGetLastError(); return MIDAS_ERR_CUDA; }
+    g_noalloc_addr[device].store(p, std::memory_order_release);
+    *out = p;
+    return MIDAS_OK;
+}
 
 __global__ void k_na_transpose(const double2 *A, int n, double2 *Z64, float2 *Z32, long long ld)
 {
@@ -103,12 +127,15 @@ extern "C" int midas_gpu_dense_solve_noalloc(int device, void *stream, int n, in
         int d;
         ~Restore() { if (d >= 0) cudaSetDevice(d); }
     } restore{prev};
-    if (!g_noalloc_addr[device]) {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) { cudaGetLastError(); return MIDAS_ERR_CUDA; }
-        g_noalloc_addr[device] = p;
+    {
+        // refuse a capturing stream before issuing anything on it: the solve waits on
+        // the stream and reads convergence on the host, neither of which a capture allows
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing((cudaStream_t)stream, &cs) != cudaSuccess) { cudaGetLastError(); return MIDAS_ERR_ARG; }
+        if (cs != cudaStreamCaptureStatusNone) return MIDAS_ERR_ARG;
     }
+    void *scratch = nullptr;
+    if (noalloc_scratch_address(device, &scratch) != MIDAS_OK) return MIDAS_ERR_CUDA;
     // a context that lives on the host stack; its scratch slots point into the array
     midas_gpu_ctx c;
     midas_gpu_default_opts(&c.opts);
@@ -116,10 +143,11 @@ extern "C" int midas_gpu_dense_solve_noalloc(int device, void *stream, int n, in
     c.device = device;
     c.stream = (cudaStream_t)stream;
     c.allow_side = false;   // no stream or event creation on this path
+    c.no_alloc = true;      // a slot request beyond its carve is an error, not a cudaMalloc
     c.pi = ref_pi_host();
     c.pool.resize(S_NSLOTS);
     const int np = (n + 63) / 64 * 64;
-    Carver cv{(char *)g_noalloc_addr[device], 0, NOALLOC_BYTES};
+    Carver cv{(char *)scratch, 0, NOALLOC_BYTES};
     c.d_flag = (int *)cv.take(256);
     auto slot = [&](int s, size_t bytes) {
         c.pool[s].p = cv.take(bytes);
