@@ -116,6 +116,12 @@ int midas_gpu_mom_rhs(midas_gpu_ctx *ctx, int ntr, const double *theta, const do
  * (idx NULL = all cells), 3ncell x 2ntr: Incident_Field (src/Incident_Field.f90:1-63). */
 int midas_gpu_incident_field(midas_gpu_ctx *ctx, int ncell, const int *idx, int ntr, const double *theta,
                              const double *phi, double *E);
+/* Spherical-wave CBF excitation field with the reference's complex(4) locals on
+ * the cells idx[0..ncell) (idx NULL = all cells), 3ncell x 2ntr: sources at
+ * 10 block radii from the cells' mean centroid in the directions (theta, phi),
+ * Incident_Field_Spherical (src/Incident_Field.f90:65-166). */
+int midas_gpu_incident_field_spherical(midas_gpu_ctx *ctx, int ncell, const int *idx, int ntr, const double *theta,
+                                       const double *phi, double *E);
 /* Block-pair interaction matrix 3n1 x 3n2 (complex(4)-rounded values stored in
  * complex(8)): Green_s_tr_partial (src/Green_functions.f90:96-173). */
 int midas_gpu_block_fill(midas_gpu_ctx *ctx, int n1, const int *idx1, int n2, const int *idx2, double *Z);
@@ -150,7 +156,9 @@ enum midas_cbfm_flags {
     MIDAS_CBFM_SR = 1,      /* threshold the extended-block matrices (SR = 1, the reference default) */
     MIDAS_CBFM_HOMOG = 2,   /* homogeneous scatterer (homogs = 1): PARDISO mtype 6 symmetric storage */
     MIDAS_CBFM_ACA = 4,     /* off-diagonal reduced blocks from ACA factors (Use_ACA = 1) */
-    MIDAS_CBFM_FAST_CBF = 8 /* CBF block solves refined with an FP32-grade residual instead of double-float */
+    MIDAS_CBFM_FAST_CBF = 8, /* CBF block solves refined with an FP32-grade residual instead of double-float */
+    MIDAS_CBFM_SPHERICAL = 16 /* CBF excitations are spherical waves (type_iws = 2/3, Incident_Field_Spherical,
+                                 src/Compute_EFields_CBFME.f90:363-368); plane waves (type_iws = 1) otherwise */
 };
 
 /* CBFM-E solve: Compute_EFields_CBFME (src/Compute_EFields_CBFME.f90:1-1006) or,

@@ -19,7 +19,7 @@ STATUS = {0: "MIDAS_OK", 1: "MIDAS_ERR_ARG", 2: "MIDAS_ERR_CUDA", 3: "MIDAS_ERR_
           8: "MIDAS_ERR_UNSUPPORTED"}
 SOLVE_MIXED, SOLVE_FP64 = 0, 1
 FILL_FAITHFUL, FILL_FAST = 0, 1
-CBFM_SR, CBFM_HOMOG, CBFM_ACA, CBFM_FAST_CBF = 1, 2, 4, 8
+CBFM_SR, CBFM_HOMOG, CBFM_ACA, CBFM_FAST_CBF, CBFM_SPHERICAL = 1, 2, 4, 8, 16
 # integration rules NumIntType_t / NumIntType_r (MIDAS_QUAD_* in the header)
 QUAD = {"un": 0, "tr": 1, "gl": 2, "sd": 3, "lb": 4, "rf": 5}
 # kernel classes of midas_gpu_profile_query (MIDAS_KC_* in the header)
@@ -30,6 +30,7 @@ KCLASSES = ["gemm_trail", "gemm_simt", "fill", "sr_scan", "diag_lu", "trsv", "re
 EXPORTS = [
     "midas_gpu_default_opts", "midas_gpu_init", "midas_gpu_free", "midas_gpu_last_error", "midas_gpu_set_cells",
     "midas_gpu_get_cell_params", "midas_gpu_mom_fill", "midas_gpu_mom_rhs", "midas_gpu_incident_field",
+    "midas_gpu_incident_field_spherical",
     "midas_gpu_block_fill", "midas_gpu_sr_fill", "midas_gpu_set_fsr", "midas_gpu_aca", "midas_gpu_dense_solve",
     "midas_gpu_mom_solve", "midas_gpu_cbfm_solve", "midas_gpu_dense_solve_noalloc", "midas_gpu_cext_cabs", "midas_gpu_smatrix",
     "midas_gpu_scattering_quantities", "midas_gpu_wait_event", "midas_gpu_record_event",
@@ -83,6 +84,7 @@ def load(path: str = LIB_PATH):
         "midas_gpu_mom_fill": (i, [vp, i, i, i, i, P]),
         "midas_gpu_mom_rhs": (i, [vp, i, P, P, P]),
         "midas_gpu_incident_field": (i, [vp, i, P, i, P, P, P]),
+        "midas_gpu_incident_field_spherical": (i, [vp, i, P, i, P, P, P]),
         "midas_gpu_block_fill": (i, [vp, i, P, i, P, P]),
         "midas_gpu_sr_fill": (i, [vp, i, P, d, i, P, ctypes.POINTER(ctypes.c_longlong),
                                   ctypes.POINTER(ctypes.c_double)]),

@@ -165,6 +165,7 @@ struct CbfShared {
     double2 *Gall;                 // device: Gram matrices (output)
     size_t mm;
     int *srefine;                  // host: refinement steps per block (output)
+    bool spherical;                // CBF excitations by Incident_Field_Spherical (type_iws = 2/3)
 };
 
 static int cbf_block(midas_gpu_ctx *c, const CbfShared &S, int b)
@@ -220,7 +221,12 @@ static int cbf_block(midas_gpu_ctx *c, const CbfShared &S, int b)
             MIDAS_CUDA(c, cudaMemcpyAsync(Zsr, Zlu, sizeof(float2) * (size_t)sp * sp, cudaMemcpyDeviceToDevice,
                                           c->stream));
         MIDAS_CUDA(c, cudaMemsetAsync(Bm, 0, sizeof(float2) * (size_t)sp * m, c->stream));
-        MIDAS_TRY(launch_incident4<float2>(c, s, idx, ncbf, d_cth, d_cph, Bm, 1, (size_t)sp));
+        // CBF excitations: plane waves (type_iws = 1) or spherical waves (type_iws = 2/3),
+        // src/Compute_EFields_CBFME.f90:363-368
+        if (S.spherical)
+            MIDAS_TRY(launch_incident_sph<float2>(c, s, idx, ncbf, d_cth, d_cph, Bm, 1, (size_t)sp));
+        else
+            MIDAS_TRY(launch_incident4<float2>(c, s, idx, ncbf, d_cth, d_cph, Bm, 1, (size_t)sp));
         DenseLU lu;
         lu.n = sp;
         lu.A = Zlu;
@@ -528,7 +534,7 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
     // ---- 1. CBF generation: blocks run concurrently on the lanes ----------------
     {
         CbfShared S{bo.data(), xo.data(), d_xall, d_cth, d_cph, ncbf, m, sr, homog, res_sr, cbf_tol, Xall,
-                    xoff.data(), Gall, mm, srefine.data()};
+                    xoff.data(), Gall, mm, srefine.data(), (flags & MIDAS_CBFM_SPHERICAL) != 0};
         MIDAS_TRY(cbf_generate(c, nb, S));
         for (int b = 0; b < nb; ++b) ir_max = std::max(ir_max, srefine[b]);
     }

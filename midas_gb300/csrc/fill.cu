@@ -207,6 +207,98 @@ __global__ void k_incident4(int ncell, const int *idx, const double *x, const do
 }
 
 // ---------------------------------------------------------------------------
+// a8: Incident_Field_Spherical (src/Incident_Field.f90:65-166), the CBF
+// excitations of type_iws = 2/3.  k_sph_centre (one CTA) forms the block
+// centre -- the mean centroid, summed in cell order by one thread as the
+// reference's sum() is read -- and the source radius Rsource = 10 max(Rbl,
+// 2 Pi / k0) from the largest centroid distance (a max: any order).
+// geo = (Xc, Yc, Zc, Rsource).  Every FP64 operation is an explicitly rounded
+// intrinsic, so no product is fused into a sum.
+// ---------------------------------------------------------------------------
+__global__ void k_sph_centre(int ncell, const int *idx, const double *x, const double *y, const double *z,
+                             double k0, double Pi, double *geo)
+{
+    __shared__ double cen[3];
+    __shared__ double red[256];
+    if (threadIdx.x == 0) {
+        double sx = 0, sy = 0, sz = 0;
+        for (int c = 0; c < ncell; ++c) {
+            const int g = idx ? idx[c] : c;
+            sx = __dadd_rn(sx, x[g]);
+            sy = __dadd_rn(sy, y[g]);
+            sz = __dadd_rn(sz, z[g]);
+        }
+        cen[0] = __ddiv_rn(sx, (double)ncell);
+        cen[1] = __ddiv_rn(sy, (double)ncell);
+        cen[2] = __ddiv_rn(sz, (double)ncell);
+    }
+    __syncthreads();
+    double m2 = 0;
+    for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+        const int g = idx ? idx[c] : c;
+        const double dx = __dsub_rn(x[g], cen[0]), dy = __dsub_rn(y[g], cen[1]), dz = __dsub_rn(z[g], cen[2]);
+        m2 = fmax(m2, __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+    }
+    red[threadIdx.x] = m2;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + o]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double rbl = __dsqrt_rn(red[0]);
+        const double lam = __ddiv_rn(__dmul_rn(2.0, Pi), k0);
+        geo[0] = cen[0];
+        geo[1] = cen[1];
+        geo[2] = cen[2];
+        geo[3] = __dmul_rn(10.0, fmax(rbl, lam));
+    }
+}
+
+// E[(3c+p)*rs + col*cs]; column t = V, t + ntr = H.  Per cell: the complex(4)
+// phase exp(i k0 R) / R (:139), the local angles acos(ux), atan2(uz, uy)
+// (:142-143), and complex(4) x real(8) products evaluated left to right in FP64
+// and rounded to float at the assignment (:146-157).
+template <typename T>
+__global__ void k_incident_sph(int ncell, const int *idx, const double *x, const double *y, const double *z,
+                               double k0, double Pi, int ntr, const double *th, const double *ph, const double *geo,
+                               T *E, size_t rs, size_t cs)
+{
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    int t = blockIdx.y;
+    if (c >= ncell) return;
+    const int g = idx ? idx[c] : c;
+    const double rsrc = geo[3];
+    const double tr = th[t] * Pi / 180., pr = ph[t] * Pi / 180.;
+    const double str = sin(tr), ctr = cos(tr), spr = sin(pr), cpr = cos(pr);
+    const double xs = __dadd_rn(geo[0], __dmul_rn(rsrc, ctr));
+    const double ys = __dadd_rn(geo[1], __dmul_rn(__dmul_rn(rsrc, str), cpr));
+    const double zs = __dadd_rn(geo[2], __dmul_rn(__dmul_rn(rsrc, str), spr));
+    const double dx = __dsub_rn(x[g], xs), dy = __dsub_rn(y[g], ys), dz = __dsub_rn(z[g], zs);
+    const double R = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+    const double ux = __ddiv_rn(dx, R), uy = __ddiv_rn(dy, R), uz = __ddiv_rn(dz, R);
+    double sa, ca;
+    sincos(__dmul_rn(k0, R), &sa, &ca);
+    const double pre = (double)(float)__ddiv_rn(ca, R), pim = (double)(float)__ddiv_rn(sa, R);
+    const double the = acos(ux), phi = atan2(uz, uy);
+    double st, ct, sp, cp;
+    sincos(the, &st, &ct);
+    sincos(phi, &sp, &cp);
+    const float2 ex = make_float2((float)__dmul_rn(-pre, st), (float)__dmul_rn(-pim, st));
+    const float2 ey = make_float2((float)__dmul_rn(__dmul_rn(pre, ct), cp), (float)__dmul_rn(__dmul_rn(pim, ct), cp));
+    const float2 ez = make_float2((float)__dmul_rn(__dmul_rn(pre, ct), sp), (float)__dmul_rn(__dmul_rn(pim, ct), sp));
+    const float2 hy = make_float2((float)__dmul_rn(-pre, sp), (float)__dmul_rn(-pim, sp));
+    const float2 hz = make_float2((float)__dmul_rn(pre, cp), (float)__dmul_rn(pim, cp));
+    const size_t rv = (size_t)t * cs, rh = (size_t)(t + ntr) * cs;
+    E[(size_t)(3 * c) * rs + rv] = mkz<T>(ex.x, ex.y);
+    E[(size_t)(3 * c + 1) * rs + rv] = mkz<T>(ey.x, ey.y);
+    E[(size_t)(3 * c + 2) * rs + rv] = mkz<T>(ez.x, ez.y);
+    E[(size_t)(3 * c) * rs + rh] = mkz<T>(0, 0);
+    E[(size_t)(3 * c + 1) * rs + rh] = mkz<T>(hy.x, hy.y);
+    E[(size_t)(3 * c + 2) * rs + rh] = mkz<T>(hz.x, hz.y);
+}
+
+// ---------------------------------------------------------------------------
 // a4/a6: complex(4)-local block fill over cell lists idx1 (rows) x idx2 (cols).
 //   mode 0: Green_s_tr_partial (all entries; self 3x3 = diag(1 - Znnpp)).
 //   mode 1: SR_Green_s_tr_partial dense form: keep |g| > thr (float abs), self
@@ -481,6 +573,27 @@ int launch_mom_rhs(midas_gpu_ctx *c, int ntr, const double *th, const double *ph
     return MIDAS_OK;
 }
 template int launch_mom_rhs<double2>(midas_gpu_ctx *, int, const double *, const double *, double2 *, size_t, size_t);
+
+template <typename T>
+int launch_incident_sph(midas_gpu_ctx *c, int ncell, const int *idx, int ntr, const double *th, const double *ph,
+                        T *E, size_t rs, size_t cs)
+{
+    if (ncell <= 0 || ntr <= 0) return MIDAS_OK;
+    void *p;
+    MIDAS_TRY(ensure(c, S_SPH, sizeof(double) * 4, &p));
+    double *geo = (double *)p;
+    c->launches += 2;
+    k_sph_centre<<<1, 256, 0, c->stream>>>(ncell, idx, c->x, c->y, c->z, c->k0, c->pi, geo);
+    dim3 grd((ncell + 127) / 128, ntr);
+    k_incident_sph<T><<<grd, 128, 0, c->stream>>>(ncell, idx, c->x, c->y, c->z, c->k0, c->pi, ntr, th, ph, geo, E, rs,
+                                                   cs);
+    MIDAS_CUDA(c, cudaGetLastError());
+    return MIDAS_OK;
+}
+template int launch_incident_sph<double2>(midas_gpu_ctx *, int, const int *, int, const double *, const double *,
+                                          double2 *, size_t, size_t);
+template int launch_incident_sph<float2>(midas_gpu_ctx *, int, const int *, int, const double *, const double *,
+                                         float2 *, size_t, size_t);
 
 template <typename T>
 int launch_incident4(midas_gpu_ctx *c, int ncell, const int *idx, int ntr, const double *th, const double *ph, T *E,

@@ -58,6 +58,9 @@ template <typename T>
 int launch_incident4(midas_gpu_ctx *c, int ncell, const int *idx, int ntr, const double *th, const double *ph, T *E,
                      size_t rs, size_t cs);
 template <typename T>
+int launch_incident_sph(midas_gpu_ctx *c, int ncell, const int *idx, int ntr, const double *th, const double *ph,
+                        T *E, size_t rs, size_t cs);
+template <typename T>
 int launch_block_fill4(midas_gpu_ctx *c, int n1, const int *idx1, int n2, const int *idx2, int mode, double thr,
                        int homog, T *out, size_t rs, size_t cs);
 // Z(idx1 rows, idx2 cols) (mode 0) written as the split-TF32 A operand (hi | hi | lo)

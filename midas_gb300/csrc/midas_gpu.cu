@@ -473,6 +473,31 @@ int midas_gpu_incident_field(midas_gpu_ctx *c, int ncell, const int *idx, int nt
     return copy_out(c, E, out, bytes);
 }
 
+int midas_gpu_incident_field_spherical(midas_gpu_ctx *c, int ncell, const int *idx, int ntr, const double *theta,
+                                       const double *phi, double *E)
+{
+    if (!c) return MIDAS_ERR_ARG;
+    c->err = Err();
+    MIDAS_TRY(need_cells(c));
+    if (ntr <= 0 || !theta || !phi || !E || (idx && ncell <= 0))
+        return c->err.set(MIDAS_ERR_ARG, "incident_field_spherical");
+    if (!idx) ncell = c->n;
+    const int *didx = nullptr;
+    if (idx) MIDAS_TRY(idx_to_device(c, idx, ncell, S_IN2, &didx));
+    const void *th, *ph;
+    MIDAS_TRY(to_device(c, theta, sizeof(double) * ntr, S_IN0, &th));
+    MIDAS_TRY(to_device(c, phi, sizeof(double) * ntr, S_IN1, &ph));
+    size_t N = 3 * (size_t)ncell, bytes = sizeof(double2) * N * 2 * ntr;
+    double2 *out = (double2 *)E;
+    if (!is_device_ptr(E)) {
+        void *p;
+        MIDAS_TRY(ensure(c, S_OUT0, bytes, &p));
+        out = (double2 *)p;
+    }
+    MIDAS_TRY(launch_incident_sph<double2>(c, ncell, didx, ntr, (const double *)th, (const double *)ph, out, 1, N));
+    return copy_out(c, E, out, bytes);
+}
+
 int midas_gpu_block_fill(midas_gpu_ctx *c, int n1, const int *idx1, int n2, const int *idx2, double *Z)
 {
     if (!c) return MIDAS_ERR_ARG;

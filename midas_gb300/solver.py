@@ -111,6 +111,18 @@ class Context:
         self._ck(self.L.midas_gpu_incident_field(self.h, nc, addr(idx), len(th), addr(th), addr(ph), addr(E)))
         return E.T
 
+    def incident_field_spherical(self, th, ph, idx=None):
+        """Incident_Field_Spherical with complex(4) locals (src/Incident_Field.f90:65-166):
+        spherical waves from sources at 10 block radii around the cells' centroid."""
+        th, ph = _c(th, np.float64), _c(ph, np.float64)
+        if idx is not None:
+            idx = _c(idx, np.int32)
+        nc = self.n if idx is None else len(idx)
+        E = np.zeros((2 * len(th), 3 * nc), np.complex128)
+        self._ck(self.L.midas_gpu_incident_field_spherical(self.h, nc, addr(idx), len(th), addr(th), addr(ph),
+                                                           addr(E)))
+        return E.T
+
     def block_fill(self, idx1, idx2):
         """Green_s_tr_partial (src/Green_functions.f90:96-173)."""
         idx1, idx2 = _c(idx1, np.int32), _c(idx2, np.int32)

@@ -282,6 +282,74 @@ void or_incident_c4(int n, const int *idx, const double *x, const double *y, con
 }
 
 /* ------------------------------------------------------------------------- */
+/* a8: Incident_Field_Spherical (src/Incident_Field.f90:65-166), the CBF      */
+/* excitation of type_iws = 2/3 (src/Compute_EFields_CBFME.f90:365-368).      */
+/* Cells are idx[0..n) in the order of Cells_in; transmitters tr0..tr1-1.     */
+/* Centre Cbl = the cells' mean centroid (sum in cell order, :91-93), Rbl the */
+/* largest centroid distance (:94), Rsource = 10 max(Rbl, 2 Pi / k0) (:97).   */
+/* Per cell: the complex(4) local phase = exp(i k0 R) / R rounded to float    */
+/* (:139), local angles acos(ux), atan2(uz, uy) in FP64 (:142-143), and the   */
+/* complex(4) field components from complex(4) x real(8) products evaluated   */
+/* left to right in FP64 and rounded at assignment (:146-157).                */
+/* E is 3n x 2*(tr1-tr0) column-major: V block then H block.                  */
+/* ------------------------------------------------------------------------- */
+void or_incident_sph(int n, const int *idx, const double *x, const double *y, const double *z,
+                     double k0, const double *th, const double *ph, int tr0, int tr1, double *E)
+{
+    const double Pi = ref_pi();
+    double cx = 0, cy = 0, cz = 0;
+    for (int c = 0; c < n; ++c) {
+        int g = idx ? idx[c] : c;
+        cx += x[g];
+        cy += y[g];
+        cz += z[g];
+    }
+    cx /= n;
+    cy /= n;
+    cz /= n;
+    double m2 = 0;
+    for (int c = 0; c < n; ++c) {
+        int g = idx ? idx[c] : c;
+        double dx = x[g] - cx, dy = y[g] - cy, dz = z[g] - cz;
+        double d2 = dx * dx + dy * dy + dz * dz;
+        if (d2 > m2) m2 = d2;
+    }
+    const double rbl = sqrt(m2);
+    const double lam = 2.0 * Pi / k0;
+    const double rsrc = 10.0 * (rbl > lam ? rbl : lam);
+    int nt = tr1 - tr0;
+#pragma omp parallel for schedule(static)
+    for (int t = 0; t < nt; ++t) {
+        double tr = th[tr0 + t] * Pi / 180., pr = ph[tr0 + t] * Pi / 180.;
+        double xs = cx + rsrc * cos(tr);
+        double ys = cy + rsrc * sin(tr) * cos(pr);
+        double zs = cz + rsrc * sin(tr) * sin(pr);
+        for (int c = 0; c < n; ++c) {
+            int g = idx ? idx[c] : c;
+            double dx = x[g] - xs, dy = y[g] - ys, dz = z[g] - zs;
+            double R = sqrt(dx * dx + dy * dy + dz * dz);
+            double ux = dx / R, uy = dy / R, uz = dz / R;
+            double a = k0 * R;
+            zc4 phs = z4of8(z8(cos(a) / R, sin(a) / R));
+            double the = acos(ux), phi = atan2(uz, uy);
+            double st = sin(the), ct = cos(the), sp = sin(phi), cp = cos(phi);
+            double pre = phs.re, pim = phs.im;
+            double *ov = E + 2 * ((size_t)t * 3 * n + 3 * c);
+            double *oh = E + 2 * ((size_t)(t + nt) * 3 * n + 3 * c);
+            /* V: Ex = -phase*sin(theta), Ey = phase*cos(theta)*cos(phi), Ez = phase*cos(theta)*sin(phi) */
+            zc4 ex = z4of8(z8(-pre * st, -pim * st));
+            zc4 ey = z4of8(z8((pre * ct) * cp, (pim * ct) * cp));
+            zc4 ez = z4of8(z8((pre * ct) * sp, (pim * ct) * sp));
+            ov[0] = ex.re; ov[1] = ex.im; ov[2] = ey.re; ov[3] = ey.im; ov[4] = ez.re; ov[5] = ez.im;
+            /* H: Ex = 0, Ey = -phase*sin(phi), Ez = phase*cos(phi) */
+            zc4 hy = z4of8(z8(-pre * sp, -pim * sp));
+            zc4 hz = z4of8(z8(pre * cp, pim * cp));
+            oh[0] = 0; oh[1] = 0; oh[2] = hy.re; oh[3] = hy.im; oh[4] = hz.re; oh[5] = hz.im;
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------- */
 /* a4: Green_s_tr_partial (src/Green_functions.f90:96-173)                    */
 /* Z is 3n1 x 3n2 column-major.  Cells are identified by global index; equal  */
 /* global indices give the self term 1 - Znnpp (the n_cell test, :125-127).   */

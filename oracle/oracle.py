@@ -60,6 +60,7 @@ def lib():
             "or_mom_fill": (None, [i, _dp, _dp, _dp, _dp, _dp, _dp, d, i, i, i, i, _dp]),
             "or_mom_rhs": (None, [i, _dp, _dp, _dp, d, i, _dp, _dp, _dp]),
             "or_incident_c4": (None, [i, _ip, _dp, _dp, _dp, d, _dp, _dp, i, i, _dp]),
+            "or_incident_sph": (None, [i, _ip, _dp, _dp, _dp, d, _dp, _dp, i, i, _dp]),
             "or_green_partial": (None, [i, _ip, i, _ip, _dp, _dp, _dp, _dp, _dp, _dp, d, _dp]),
             "or_green_partial_fn": (d, [i, _ip, i, _ip, i, _dp, _dp, _dp, _dp, _dp, _dp, d]),
             "or_sr_dense": (l, [i, _ip, d, i, _dp, _dp, _dp, _dp, _dp, _dp, d, _dp, _dp]),
@@ -187,6 +188,20 @@ def incident_c4(c: Cells, th, ph, idx=None) -> np.ndarray:
         n, ip = len(idx), _i(idx)
     E = np.zeros((2 * len(th), 3 * n), np.complex128)
     lib().or_incident_c4(n, ip, *c.geo(), c.k0, _d(th), _d(ph), 0, len(th), _d(E.view(np.float64)))
+    return E.T
+
+
+def incident_sph(c: Cells, th, ph, idx=None) -> np.ndarray:
+    """Incident_Field_Spherical (src/Incident_Field.f90:65-166) on the cells idx
+    (all cells when None), complex(4) locals: (3n_sel, 2 NTr)."""
+    th, ph = _f64(th), _f64(ph)
+    if idx is None:
+        n, ip = c.n, None
+    else:
+        idx = _i32(idx)
+        n, ip = len(idx), _i(idx)
+    E = np.zeros((2 * len(th), 3 * n), np.complex128)
+    lib().or_incident_sph(n, ip, *c.geo(), c.k0, _d(th), _d(ph), 0, len(th), _d(E.view(np.float64)))
     return E.T
 
 
@@ -369,17 +384,18 @@ class Partition:
 
 
 def cbf_generate(c: Cells, part: Partition, th_cbfm, ph_cbfm, thr: float, sr: int = 1, homog: int = 0,
-                 res_sr: float = RES_SR_DEFAULT, keep=None):
+                 res_sr: float = RES_SR_DEFAULT, keep=None, spherical: bool = False):
     """CBF generation loop (src/Compute_EFields_CBFME.f90:221-449).
 
     Returns the list of C_b (3 n_b x K_b) and K_b.  ``keep`` (dict) receives the
-    per-block fSR, nnz and singular values when given.
+    per-block fSR, nnz and singular values when given.  ``spherical`` selects the
+    spherical-wave excitations of type_iws = 2/3 (:363-368).
     """
     Cs, Ks = [], []
     for b in range(part.nblocks):
         ext = part.extended(b)
         nb = part.blk_offsets[b + 1] - part.blk_offsets[b]
-        Eref = incident_c4(c, th_cbfm, ph_cbfm, idx=ext)
+        Eref = (incident_sph if spherical else incident_c4)(c, th_cbfm, ph_cbfm, idx=ext)
         if sr:
             fsr, nnz = set_fsr(c, ext, homog, res_sr)
             Zb, nnz2, _ = sr_dense(c, ext, fsr, homog)
@@ -425,12 +441,15 @@ def reduced_matrix(c: Cells, part: Partition, Cs, use_aca=False, eps_aca=EPS_ACA
 
 def cbfm_solve(c: Cells, part: Partition, th, ph, niws: int, use_aca: bool = False, sr: int = 1,
                homog: int = 0, thr: float | None = None, res_sr: float = RES_SR_DEFAULT,
-               eps_aca: float = EPS_ACA_DEFAULT, itmax: int = NB_IT_MAX_DEFAULT, keep=None):
-    """Compute_EFields_CBFME (or _ACA): returns dict(E, K, Zc, Vc, alpha)."""
+               eps_aca: float = EPS_ACA_DEFAULT, itmax: int = NB_IT_MAX_DEFAULT, keep=None,
+               spherical: bool = False):
+    """Compute_EFields_CBFME (or _ACA): returns dict(E, K, Zc, Vc, alpha).
+    ``spherical``: CBF excitations by Incident_Field_Spherical (type_iws = 2/3)."""
     th_c, ph_c = transmitters_un(niws)
     if thr is None:
         thr = THR_ACA_DRIVER if use_aca else cbf_threshold(c)
-    Cs, Ks = cbf_generate(c, part, th_c, ph_c, thr, sr=sr, homog=homog, res_sr=res_sr, keep=keep)
+    Cs, Ks = cbf_generate(c, part, th_c, ph_c, thr, sr=sr, homog=homog, res_sr=res_sr, keep=keep,
+                          spherical=spherical)
     Zc, off = reduced_matrix(c, part, Cs, use_aca=use_aca, eps_aca=eps_aca, itmax=itmax, stats=keep)
     ntr = len(th)
     Vc = np.zeros((off[-1], 2 * ntr), np.complex128)

@@ -9,6 +9,7 @@ assignment to a complex(4)/real(4) local, following
   src/Compute_EFields_MoM.f90:433-598 (FP64 element and RHS),
   src/Green_functions.f90:96-173 (complex(4) block element),
   src/Incident_Field.f90:1-63 (complex(4) incident field),
+  src/Incident_Field.f90:65-166 (spherical-wave incident field),
   src/getParameters_CBFM.f90:34-75,294-348 and src/Discretization.f90:246-310.
 The C oracle (oracle/midas_oracle.c) must reproduce them exactly; the GPU
 library is then compared with the C oracle.
@@ -147,6 +148,38 @@ def main():
             E4[3 * c + 1, t + 2] = r4(complex(-(e4.real * sp), -(e4.imag * sp)))
             E4[3 * c + 2, t + 2] = r4(complex(e4.real * cp, e4.imag * cp))
     g["th"], g["ph"] = th, ph
+    # Incident_Field_Spherical (src/Incident_Field.f90:65-166) on the cells in the
+    # order [2, 0, 3, 1]: centre = mean centroid summed in that order, Rsource =
+    # 10 max(Rbl, 2 Pi / k0), complex(4) phase exp(i k0 R) / R, FP64 local angles
+    order = [2, 0, 3, 1]
+    pts = [xyz[i] for i in order]
+    cen = [0.0, 0.0, 0.0]
+    for q in pts:
+        for k in range(3):
+            cen[k] += q[k]
+    cen = [v / len(pts) for v in cen]
+    rbl = math.sqrt(max((q[0] - cen[0]) ** 2 + (q[1] - cen[1]) ** 2 + (q[2] - cen[2]) ** 2 for q in pts))
+    rsrc = 10.0 * max(rbl, 2.0 * PI / k0)
+    r4 = lambda v: complex(float(F(v.real)), float(F(v.imag)))
+    ES = np.zeros((3 * n, 4), complex)
+    for t in range(2):
+        tr, pr = th[t] * PI / 180.0, ph[t] * PI / 180.0
+        src = (cen[0] + rsrc * math.cos(tr), cen[1] + rsrc * math.sin(tr) * math.cos(pr),
+               cen[2] + rsrc * math.sin(tr) * math.sin(pr))
+        for c, q in enumerate(pts):
+            d = [q[k] - src[k] for k in range(3)]
+            R = math.sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2])
+            u = [v / R for v in d]
+            phase = r4(complex(math.cos(k0 * R) / R, math.sin(k0 * R) / R))
+            the, phi = math.acos(u[0]), math.atan2(u[2], u[1])
+            st, ct, sp, cp = math.sin(the), math.cos(the), math.sin(phi), math.cos(phi)
+            ES[3 * c, t] = r4(complex(-phase.real * st, -phase.imag * st))
+            ES[3 * c + 1, t] = r4(complex((phase.real * ct) * cp, (phase.imag * ct) * cp))
+            ES[3 * c + 2, t] = r4(complex((phase.real * ct) * sp, (phase.imag * ct) * sp))
+            ES[3 * c + 1, t + 2] = r4(complex(-phase.real * sp, -phase.imag * sp))
+            ES[3 * c + 2, t + 2] = r4(complex(phase.real * cp, phase.imag * cp))
+    g["sph_order"] = order
+    g["E4_sph"] = [[ES.real[i].tolist(), ES.imag[i].tolist()] for i in range(3 * n)]
     g["V8"] = [[V8.real[i].tolist(), V8.imag[i].tolist()] for i in range(3 * n)]
     g["E4"] = [[E4.real[i].tolist(), E4.imag[i].tolist()] for i in range(3 * n)]
     # 'un' transmitters (counts and a few angles) and Niws table lookups

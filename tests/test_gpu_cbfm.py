@@ -51,6 +51,33 @@ def test_cbfm_matches_oracle(gpulib, oracle, nbx, inhom, fill):
     ctx.close()
 
 
+@pytest.mark.parametrize("inhom", [False, True])
+def test_cbfm_spherical_cbfs_match_oracle(gpulib, oracle, inhom):
+    """CBFs from spherical-wave excitations (type_iws = 2/3, Incident_Field_Spherical,
+    src/Compute_EFields_CBFME.f90:363-368): same K per block, field and cross sections
+    within the CBFM bars."""
+    from midas_gb300 import _lib, geometry as G
+    from midas_gb300.solver import Context
+    xyz, sc, eps, k0, offs, ext = _case(oracle, (2, 2, 1), inhom)
+    th, ph = np.array([90.0, 35.0]), np.array([90.0, 120.0])
+    niws = 91
+    homog = 0 if inhom else 1
+    cells = oracle.Cells(xyz, sc, eps, k0)
+    ref = oracle.cbfm_solve(cells, oracle.Partition(offs, ext), th, ph, niws, homog=homog, spherical=True)
+    cth, cph = G.transmitters_un(niws)
+    ctx = Context(fill_mode=_lib.FILL_FAST).set_cells(xyz, sc, eps, k0)
+    flags = _lib.CBFM_SR | _lib.CBFM_SPHERICAL | (_lib.CBFM_HOMOG if homog else 0)
+    E, K = ctx.cbfm_solve(offs, ext, cth, cph, th, ph, flags=flags)
+    assert np.array_equal(K, ref["K"]), (K, ref["K"])
+    rel = np.linalg.norm(E - ref["E"]) / np.linalg.norm(ref["E"])
+    assert rel < 1e-6, rel
+    ce, ca = ctx.cext_cabs(th, ph, E)
+    ce_o, ca_o = oracle.cext_cabs(cells, th, ph, ref["E"])
+    assert np.max(np.abs(ce - ce_o) / np.abs(ce_o)) < 1e-6
+    assert np.max(np.abs(ca - ca_o) / np.abs(ca_o)) < 1e-6
+    ctx.close()
+
+
 def test_cbfm_rejects_bad_partition(gpulib, oracle):
     from midas_gb300._lib import MidasError
     from midas_gb300 import geometry as G

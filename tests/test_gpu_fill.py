@@ -76,6 +76,18 @@ def test_incident_field_complex4(pair, oracle):
     assert np.mean(u > 0) < 1e-3
 
 
+def test_incident_field_spherical_complex4(pair, oracle):
+    """Incident_Field_Spherical (src/Incident_Field.f90:65-166) on a cell subset in a
+    permuted order (the block centre is a sum in cell order) and on all cells."""
+    ctx, cells, _ = pair
+    th, ph = [90.0, 33.0, 150.0, 0.0], [90.0, 250.0, 10.0, 0.0]
+    for idx in (np.arange(cells.n - 1, 4, -3, dtype=np.int32), None):
+        Eg, Eo = ctx.incident_field_spherical(th, ph, idx), oracle.incident_sph(cells, th, ph, idx)
+        u = ulps32(Eg, Eo)
+        assert u.max() <= 1.0, u.max()
+        assert np.mean(u > 0) < 1e-3
+
+
 def test_block_fill_complex4(pair, oracle):
     ctx, cells, mode = pair
     i1 = np.arange(0, cells.n, 2, dtype=np.int32)

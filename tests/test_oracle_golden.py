@@ -64,3 +64,11 @@ def test_sphere_counts(oracle):
     for key, cnt in G["sphere_counts"].items():
         dm, s = (float(v) for v in key.split("_"))
         assert len(oracle.sphere_cells(dm, s)) == cnt
+
+
+def test_incident_spherical_exact(oracle):
+    """Incident_Field_Spherical (src/Incident_Field.f90:65-166) against the independent
+    restatement, on the cells in a permuted order (the block centre sums in cell order)."""
+    c = _cells(oracle)
+    E = oracle.incident_sph(c, G["th"], G["ph"], idx=np.array(G["sph_order"], np.int32))
+    assert np.array_equal(E, _mat(G["E4_sph"]))
