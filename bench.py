@@ -426,6 +426,14 @@ def run_ours(args, wl, world, rank, local, pg):
                     "speedup": value / (ntr / t64), "field_rel_err_vs_fp64": relerr}
             c64.close()
 
+    # the answer of the timed steps against the oracle's fixture of the same scene
+    # (tests/golden/cfg_*.npz), outside the timed regions
+    parity = None
+    fx_name = {"cbfm_c2": "c2", "mom_c1": "c1", "mom_tiny": "c1_lit"}.get(args.workload)
+    if rank == 0 and fx_name:
+        parity = check_parity(ctx, wl, fx_name, E_d.cpu().numpy().view(np.complex128).reshape(2 * ntr, N).T,
+                              Kb if cbfm else None)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         if cbfm:
@@ -462,7 +470,7 @@ def run_ours(args, wl, world, rank, local, pg):
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": dtype,
                 "data": "synthetic (seeded voxelised scatterer)",
-                "config": cfg, "roofline": roof, "cpu_baseline": cpu,
+                "config": cfg, "roofline": roof, "cpu_baseline": cpu, "parity": parity,
                 "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": d2h},
                 "gpu_launches": launches, "clocks": clk.summary(), "fp64_mom_gpu": fp64,
@@ -473,6 +481,28 @@ def run_ours(args, wl, world, rank, local, pg):
         print(json.dumps(line), flush=True)
     ctx.close()
     return 0
+
+
+def check_parity(ctx, wl, fx_name, E, K):
+    """Compare a solved scene with the oracle's fixture: internal field (seeded row
+    subset and column norms) <= 1e-6, Cext / Cabs <= 1e-6, S <= 1e-5 of max |S|,
+    K per block identical.  E: (N, 2 ntr) complex."""
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    import cfg_digest as D
+    path = D.fixture_path(fx_name)
+    if not os.path.exists(path):
+        return {"fixture": os.path.relpath(path, ROOT), "ok": False, "error": "fixture missing"}
+    fx = np.load(path)
+    rx = "polar181" if fx_name.startswith("c1") else "grid37x2"
+    ce, ca = ctx.cext_cabs(wl["th"], wl["ph"], E)
+    S = ctx.smatrix(*D.receivers(rx), E)
+    res = D.compare(fx, E, ce, ca, S, K)
+    scene_ok = bool(np.array_equal(D.scene_signature(wl), fx["signature"]))
+    ok = (scene_ok and res["E_rows_rel"] <= 1e-6 and res["colnorm_rel"] <= 1e-6 and res["cext_rel"] <= 1e-6
+          and res["cabs_rel"] <= 1e-6 and res["S_rel"] <= 1e-5 and res.get("K_equal", True))
+    return {"fixture": os.path.relpath(path, ROOT), "scene_matches": scene_ok, **res,
+            "tolerances": {"E": 1e-6, "cext_cabs": 1e-6, "S": 1e-5}, "oracle_seconds": float(fx["seconds"]),
+            "ok": bool(ok)}
 
 
 def fp64_mom_extrapolated(local, wl, value):

@@ -105,6 +105,39 @@ int midas_gpu_set_cells(midas_gpu_ctx *ctx, int n, const double *xc, const doubl
 /* Read back the per-cell parameters (any output may be NULL); che/znnpp are complex (2n doubles). */
 int midas_gpu_get_cell_params(midas_gpu_ctx *ctx, double *a_n, double *che, double *znnpp, double *kappa);
 
+/* Scene preparation on the device.  The reference builds these inputs on the
+ * host before the solve; here they are flag passes plus order-preserving
+ * compactions, with outputs in the host loops' order.  Output arrays may be
+ * host or device memory; index outputs use opts.index_base.
+ * midas_gpu_voxelise_sphere: the sphere voxeliser of Discretization
+ * (src/Discretization.f90:246-310) for diameter dm and cell edge sc; *ncell
+ * receives the count, and up to cap centroids go to xc, yc, zc (NULL = count
+ * only). */
+int midas_gpu_voxelise_sphere(midas_gpu_ctx *ctx, double dm, double sc, long long cap, double *xc, double *yc,
+                              double *zc, long long *ncell);
+/* Union of nsph spheres of radius a (centres: 3 doubles each) on one lattice
+ * of edge 2a / cells_per_diameter: cells whose centre lies strictly inside a
+ * sphere (the reference's inside test), lattice order x slowest (no counterpart
+ * in the reference, which reads aggregate shapes from files). */
+int midas_gpu_voxelise_spheres(midas_gpu_ctx *ctx, int nsph, const double *centres, double a, int cells_per_diameter,
+                               long long cap, double *xc, double *yc, double *zc, long long *ncell, double *edge);
+/* Bounding-box split into nx x ny x nz blocks (a partitioner of this library;
+ * the reference divides with its own octree, src/Division_blocks.f90): perm
+ * (n) lists the cells block by block, stable within a block, and
+ * blk_offsets (up to nx ny nz + 1 entries) the non-empty blocks' ranges in the
+ * permuted order (the contiguous-by-block ordering of src/Division_blocks.f90:582). */
+int midas_gpu_box_partition(midas_gpu_ctx *ctx, int n, const double *xc, const double *yc, const double *zc, int nx,
+                            int ny, int nz, int *perm, int *blk_offsets, int *nblocks);
+/* Extend_blocks (src/Extend_blocks.f90:46-151) on block-ordered cells: block
+ * contours as SetBlockCtrs (src/Division_blocks.f90:1616-1662), neighbours by
+ * bounding-sphere distance <= r_b + r_b' + ext_length, and every neighbour cell
+ * inside the block's box grown by ext_length + sc / 2.  ext_offsets (nblocks +
+ * 1) and up to cap extension cell indices (ext_idx) in the layout
+ * midas_gpu_cbfm_solve takes; *ntotal = all extension cells. */
+int midas_gpu_extend_blocks(midas_gpu_ctx *ctx, int n, const double *xc, const double *yc, const double *zc,
+                            int nblocks, const int *blk_offsets, double ext_length, double sc, int *ext_offsets,
+                            long long cap, int *ext_idx, long long *ntotal);
+
 /* Rows [r0, r0+nr) x columns [c0, c0+nc) (0-based unknown indices) of the FP64
  * MoM matrix, column-major nr x nc: compute_Green_s_tr_single_element
  * (src/Compute_EFields_MoM.f90:433-523). */
@@ -145,6 +178,31 @@ int midas_gpu_aca(midas_gpu_ctx *ctx, int row0, int nrows, int col0, int ncols, 
  * (src/Compute_EFields_MoM.f90:173, src/Compute_EFields_CBFME.f90:912). */
 int midas_gpu_dense_solve(midas_gpu_ctx *ctx, int n, int nrhs, const double *A, double *B,
                           midas_gpu_info *info);
+
+/* Y = Z X with the MoM matrix Z of compute_Green_s_tr_single_element
+ * (src/Compute_EFields_MoM.f90:433-523) applied as an FFT convolution, for cells
+ * that lie on one uniform lattice (no counterpart in the reference, which
+ * forms Z densely): X and Y are 3n x nrhs column-major complex (host or device).
+ * FP64 transforms; returns MIDAS_ERR_UNSUPPORTED when the cells are not on a
+ * lattice or a lattice axis spans more than 256 cells. */
+int midas_gpu_lattice_matvec(midas_gpu_ctx *ctx, int nrhs, const double *X, double *Y);
+
+/* Krylov solve of the MoM system for cells on one lattice (no counterpart in
+ * the reference, whose PZGESV, src/Compute_EFields_MoM.f90:153-198, this
+ * complements for systems too large for a dense matrix): GMRES(restart) on the
+ * FFT operator of midas_gpu_lattice_matvec, right-hand sides the FP64 incident
+ * field of Incident_Field_single_element (src/Compute_EFields_MoM.f90:529-598),
+ * all 2ntr columns in lockstep.  E0 (3n x 2ntr, may be NULL = zero) is the
+ * initial guess, e.g. a learned predictor's output.  Converged when the TRUE
+ * relative residual ||b - Z E|| / ||b|| of every column, recomputed in FP64
+ * at each restart, is <= tol.  flags: MIDAS_GMRES_JACOBI right-preconditions
+ * with 1 / (1 - Znnpp) per cell.  info->ir_iters = Arnoldi steps taken,
+ * info->backward_error = the final true relative residual.  Returns
+ * MIDAS_ERR_NOT_CONVERGED after maxit steps (E then holds the last iterate; the
+ * dense midas_gpu_mom_solve is the fallback). */
+enum midas_gmres_flags { MIDAS_GMRES_JACOBI = 1 };
+int midas_gpu_gmres_solve(midas_gpu_ctx *ctx, int ntr, const double *theta, const double *phi, const double *E0,
+                          int restart, int maxit, double tol, int flags, double *E, midas_gpu_info *info);
 
 /* Plain MoM: fill, solve, internal field E (3n x 2ntr).  The field part of
  * Compute_EFields_MoM (src/Compute_EFields_MoM.f90:66-229). */
@@ -299,7 +357,8 @@ int midas_gpu_record_event(midas_gpu_ctx *ctx, void *event);
 #define MIDAS_KC_GEMM_SOLVE 11  /* tcgen05 GEMM: triangular-solve updates */
 #define MIDAS_KC_GEMM_PROD  12  /* tcgen05 GEMM: split-TF32 products (reduced matrix, FP32-grade ZGEMM) */
 #define MIDAS_KC_SPLIT      13  /* split-TF32 operand preparation (hi / lo pieces) */
-#define MIDAS_KC_COUNT     14
+#define MIDAS_KC_LATTICE   14  /* FFT lattice operator (scatter, FFTs, spectral product, gather) */
+#define MIDAS_KC_COUNT     15
 /* enable = 1 clears the per-class totals and starts timing every instrumented
  * launch with CUDA events on the context stream; 0 stops.  Timing adds one event
  * record before and after each instrumented launch. */

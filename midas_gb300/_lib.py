@@ -20,19 +20,21 @@ STATUS = {0: "MIDAS_OK", 1: "MIDAS_ERR_ARG", 2: "MIDAS_ERR_CUDA", 3: "MIDAS_ERR_
 SOLVE_MIXED, SOLVE_FP64 = 0, 1
 FILL_FAITHFUL, FILL_FAST = 0, 1
 CBFM_SR, CBFM_HOMOG, CBFM_ACA, CBFM_FAST_CBF, CBFM_SPHERICAL = 1, 2, 4, 8, 16
+GMRES_JACOBI = 1
 # integration rules NumIntType_t / NumIntType_r (MIDAS_QUAD_* in the header)
 QUAD = {"un": 0, "tr": 1, "gl": 2, "sd": 3, "lb": 4, "rf": 5}
 # kernel classes of midas_gpu_profile_query (MIDAS_KC_* in the header)
 KCLASSES = ["gemm_trail", "gemm_simt", "fill", "sr_scan", "diag_lu", "trsv", "resid", "zgemm64", "eig", "other",
-            "gemm_panel", "gemm_solve", "gemm_prod", "split"]
+            "gemm_panel", "gemm_solve", "gemm_prod", "split", "lattice"]
 
 # every symbol the header declares (checked by the CPU tests)
 EXPORTS = [
     "midas_gpu_default_opts", "midas_gpu_init", "midas_gpu_free", "midas_gpu_last_error", "midas_gpu_set_cells",
     "midas_gpu_get_cell_params", "midas_gpu_mom_fill", "midas_gpu_mom_rhs", "midas_gpu_incident_field",
-    "midas_gpu_incident_field_spherical",
+    "midas_gpu_incident_field_spherical", "midas_gpu_voxelise_sphere", "midas_gpu_voxelise_spheres",
+    "midas_gpu_box_partition", "midas_gpu_extend_blocks",
     "midas_gpu_block_fill", "midas_gpu_sr_fill", "midas_gpu_set_fsr", "midas_gpu_aca", "midas_gpu_dense_solve",
-    "midas_gpu_mom_solve", "midas_gpu_cbfm_solve", "midas_gpu_dense_solve_noalloc", "midas_gpu_cext_cabs", "midas_gpu_smatrix",
+    "midas_gpu_mom_solve", "midas_gpu_lattice_matvec", "midas_gpu_gmres_solve", "midas_gpu_cbfm_solve", "midas_gpu_dense_solve_noalloc", "midas_gpu_cext_cabs", "midas_gpu_smatrix",
     "midas_gpu_scattering_quantities", "midas_gpu_wait_event", "midas_gpu_record_event",
     "midas_gpu_gemm_selftest", "midas_gpu_gemm_engine", "midas_gpu_wait_selftest", "midas_gpu_launch_count", "midas_gpu_stream",
     "midas_gpu_bench_gemm", "midas_gpu_bench_gemm_ex", "midas_gpu_heev", "midas_gpu_zgemm_x3", "midas_gpu_profile", "midas_gpu_profile_query",
@@ -85,6 +87,12 @@ def load(path: str = LIB_PATH):
         "midas_gpu_mom_rhs": (i, [vp, i, P, P, P]),
         "midas_gpu_incident_field": (i, [vp, i, P, i, P, P, P]),
         "midas_gpu_incident_field_spherical": (i, [vp, i, P, i, P, P, P]),
+        "midas_gpu_voxelise_sphere": (i, [vp, d, d, ctypes.c_longlong, P, P, P, ctypes.POINTER(ctypes.c_longlong)]),
+        "midas_gpu_voxelise_spheres": (i, [vp, i, P, d, i, ctypes.c_longlong, P, P, P,
+                                           ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_double)]),
+        "midas_gpu_box_partition": (i, [vp, i, P, P, P, i, i, i, P, P, ctypes.POINTER(ctypes.c_int)]),
+        "midas_gpu_extend_blocks": (i, [vp, i, P, P, P, i, P, d, d, P, ctypes.c_longlong, P,
+                                        ctypes.POINTER(ctypes.c_longlong)]),
         "midas_gpu_block_fill": (i, [vp, i, P, i, P, P]),
         "midas_gpu_sr_fill": (i, [vp, i, P, d, i, P, ctypes.POINTER(ctypes.c_longlong),
                                   ctypes.POINTER(ctypes.c_double)]),
@@ -93,6 +101,8 @@ def load(path: str = LIB_PATH):
         "midas_gpu_aca": (i, [vp, i, i, i, i, d, i, P, P, ctypes.POINTER(ctypes.c_int)]),
         "midas_gpu_dense_solve": (i, [vp, i, i, P, P, ctypes.POINTER(Info)]),
         "midas_gpu_mom_solve": (i, [vp, i, P, P, P, ctypes.POINTER(Info)]),
+        "midas_gpu_lattice_matvec": (i, [vp, i, P, P]),
+        "midas_gpu_gmres_solve": (i, [vp, i, P, P, P, i, i, d, i, P, ctypes.POINTER(Info)]),
         "midas_gpu_dense_solve_noalloc": (i, [i, vp, i, i, P, P, ctypes.POINTER(ctypes.c_double)]),
         "midas_gpu_cbfm_solve": (i, [vp, i, P, P, P, i, P, P, d, d, i, d, i, i, P, P, P, P, ctypes.POINTER(Info)]),
         "midas_gpu_cext_cabs": (i, [vp, i, P, P, P, P, P]),

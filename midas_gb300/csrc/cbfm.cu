@@ -215,7 +215,11 @@ static int cbf_block(midas_gpu_ctx *c, const CbfShared &S, int b)
             k_pad_diag32<<<1, 64, 0, c->stream>>>(Zlu, sp, N3, sp);
         }
         Csr zcsr;
-        if (sr)
+        Bsr3 zb;
+        const bool use_bsr = !getenv("MIDAS_CBF_CSR");
+        if (sr && use_bsr)
+            MIDAS_TRY(bsr3_from_dense(c, s, sp, Zlu, sp, S_CSR, &zb));
+        else if (sr)
             MIDAS_TRY(csr_from_dense(c, sp, Zlu, sp, S_CSR, &zcsr));
         else
             MIDAS_CUDA(c, cudaMemcpyAsync(Zsr, Zlu, sizeof(float2) * (size_t)sp * sp, cudaMemcpyDeviceToDevice,
@@ -251,11 +255,15 @@ static int cbf_block(midas_gpu_ctx *c, const CbfShared &S, int b)
             if (sr && it == 0) {
                 ++c->launches;
                 k_b_to_r64<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(tot, Bm, R64);
-                MIDAS_TRY(residual_csr_update_f32(c, zcsr, m, Drm, R64));
-            } else if (sr && upd)
-                MIDAS_TRY(residual_csr_update_f32(c, zcsr, m, Drm, R64));
-            else if (sr)
-                MIDAS_TRY(residual_csr_df32(c, zcsr, m, Xh, Xl, Bm, R64));
+                if (use_bsr) MIDAS_TRY(residual_bsr_update_f32(c, zb, m, Drm, R64));
+                else MIDAS_TRY(residual_csr_update_f32(c, zcsr, m, Drm, R64));
+            } else if (sr && upd) {
+                if (use_bsr) MIDAS_TRY(residual_bsr_update_f32(c, zb, m, Drm, R64));
+                else MIDAS_TRY(residual_csr_update_f32(c, zcsr, m, Drm, R64));
+            } else if (sr) {
+                if (use_bsr) MIDAS_TRY(residual_bsr_df32(c, zb, m, Xh, Xl, Bm, R64));
+                else MIDAS_TRY(residual_csr_df32(c, zcsr, m, Xh, Xl, Bm, R64));
+            }
             else
                 MIDAS_TRY(residual_df32(c, sp, m, Zsr, sp, Xh, Xl, Bm, R64));
             MIDAS_CUDA(c, cudaMemsetAsync(red, 0, sizeof(unsigned long long) * 2 * m, c->stream));

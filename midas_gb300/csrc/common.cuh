@@ -112,6 +112,16 @@ struct KProf {
     long long n[MIDAS_KC_COUNT] = {};
 };
 
+// FFT form of the MoM operator on a voxel lattice (fft.cu): grid sizes and the
+// dyad spectra of the current cells
+struct LatticeFft {
+    int L[3] = {0, 0, 0}, n[3] = {0, 0, 0};
+    long long npts = 0;
+    double2 *G6 = nullptr;   // 6 spectra, npts each
+    int *lo = nullptr;       // lattice lower corner (device copy)
+    long long version = -1;  // cells version the spectra belong to
+};
+
 }  // namespace midas
 
 // The context (opaque in the C ABI).
@@ -136,6 +146,8 @@ struct midas_gpu_ctx {
     float2 *lat_tab4 = nullptr;    // complex(4) dyad table per lattice offset (6 comps)
     double2 *lat_tab8 = nullptr;   // FP64 dyad table per lattice offset (6 comps)
     int lat_dim[3] = {0, 0, 0};
+    long long cells_version = 0;   // incremented by every midas_gpu_set_cells
+    midas::LatticeFft lfft;
     // scratch pool (grow-only, reused across calls)
     std::vector<midas::DBuf> pool;
     int *d_flag = nullptr;   // device error flag
@@ -201,13 +213,35 @@ int to_device(midas_gpu_ctx *ctx, const void *p, size_t bytes, int slot, const v
 // Device error flag check after a kernel sequence.
 int check_flag(midas_gpu_ctx *ctx, const char *where);
 
+// Lattice FFT operator (fft.cu): Y = Z X, or Y = B - Z X when B is given.
+int lattice_fft_prepare(midas_gpu_ctx *c);
+bool lattice_fft_fits(const midas_gpu_ctx *c);   // cells on a lattice of <= 256 cells per axis
+void lattice_fft_release(midas_gpu_ctx *c);
+int lattice_matvec(midas_gpu_ctx *c, int nrhs, const double2 *X, long long ldx, const double2 *B, long long ldb,
+                   double2 *Y, long long ldy, int slot);
+
+// Restarted GMRES on the lattice operator (krylov.cu); X holds the initial guess.
+int gmres_lattice(midas_gpu_ctx *c, int ncol, const double2 *B, double2 *X, int restart, int maxit, double tol,
+                  bool jacobi, int *iters, double *relres);
+
+// Scene preparation on the device (prep.cu); outputs in device memory.
+int voxelise_sphere(midas_gpu_ctx *c, double dm, double sc, long long cap, double *x, double *y, double *z,
+                    long long *ncell);
+int voxelise_spheres(midas_gpu_ctx *c, int nsph, const double *centres, double a, int cells_per_diameter,
+                     long long cap, double *x, double *y, double *z, long long *ncell, double *edge);
+int box_partition(midas_gpu_ctx *c, int n, const double *x, const double *y, const double *z, int nx, int ny, int nz,
+                  int *perm, int *blk_offsets, int *nblocks);
+int extend_blocks(midas_gpu_ctx *c, int n, const double *x, const double *y, const double *z, int nb,
+                  const int *offs_host, double ext_length, double sc, int *ext_offsets, long long cap, int *ext_idx,
+                  long long *ntotal);
+
 // Pool slots (fixed roles).  A pointer taken from a slot stays valid only until the
 // next ensure() on the same slot, so a caller never holds a slot that a callee grows.
 enum Slot : int {
     S_IN0 = 0, S_IN1, S_IN2, S_IN3, S_IN4, S_IN5, S_OUT0, S_OUT1,
     S_Z32, S_Z64, S_LINV, S_UINV, S_BEXP, S_BEXP2, S_RHS64, S_X64, S_R64, S_T32, S_T32B, S_RED,
     S_CBF0, S_CBF1, S_CBF2, S_CBF3, S_CBF4, S_CBF5, S_CBF6, S_CBF7, S_CBF8, S_CBF9, S_RED2, S_EINC,
-    S_ACA, S_SOLVE, S_CSR, S_RPART, S_H16, S_HEEV, S_ZDF, S_QWS, S_SPH, S_NSLOTS
+    S_ACA, S_SOLVE, S_CSR, S_RPART, S_H16, S_HEEV, S_ZDF, S_QWS, S_SPH, S_LFFT, S_KRYLOV, S_PREP, S_NSLOTS
 };
 
 }  // namespace midas

@@ -891,6 +891,133 @@ int mixed_solve(midas_gpu_ctx *c, int np, float2 *Z32, double2 *Z64, const doubl
 }
 
 
+// ||Z||_inf of the complex64 matrix (row sums of |z| in FP32, as k_z_split forms
+// them from the FP64 matrix), before the factorisation overwrites it
+__global__ void __launch_bounds__(256) k_row_abs_max(int n, long long ldz, const float2 *Z, unsigned *znorm)
+{
+    __shared__ float red[8];
+    for (int row = blockIdx.x; row < n; row += gridDim.x) {
+        const float2 *zr = Z + (long long)row * ldz;
+        float s = 0.f;
+        for (int m = threadIdx.x; m < n; m += blockDim.x) s += hypotf(zr[m].x, zr[m].y);
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float t = 0.f;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+            atomicMax(znorm, __float_as_uint(t));
+        }
+        __syncthreads();
+    }
+}
+
+// Refinement whose every residual b - Z x is the FP64 FFT lattice operator
+// (fft.cu): no FP64 matrix, no double-float pass, no drift bookkeeping -- each
+// residual is FP64-grade.  x0 = LU^-1 b from the TF32 factors, then x += LU^-1 r
+// until the normwise backward error is <= ir_tol.  b, x column-major (ld n, the
+// padded size); rows >= 3 ncell are the identity padding (b = 0 there, so x and
+// r stay 0).
+static int ir_solve_lattice(midas_gpu_ctx *c, const DenseLU &lu, double znorm, const double2 *b, double2 *x,
+                            int nrhs, midas_gpu_info *info)
+{
+    const int n = lu.n;
+    const size_t nn = (size_t)n * nrhs;
+    void *p;
+    MIDAS_TRY(ensure(c, S_R64, sizeof(double2) * nn, &p));
+    double2 *r = (double2 *)p;
+    MIDAS_TRY(ensure(c, S_T32, sizeof(float2) * nn, &p));
+    float2 *d32 = (float2 *)p;
+    MIDAS_TRY(ensure(c, S_RED, sizeof(unsigned long long) * 4 * nrhs + 64, &p));
+    unsigned long long *red = (unsigned long long *)p;   // max|r|, max|x|, max|b|, max|d| per column
+    std::vector<unsigned long long> h(4 * nrhs);
+    auto colmax = [&](int k, int slot) {
+        double v;
+        memcpy(&v, &h[(size_t)slot * nrhs + k], 8);
+        return v;
+    };
+    MIDAS_CUDA(c, cudaMemsetAsync(red, 0, sizeof(unsigned long long) * 4 * nrhs, c->stream));
+    ++c->launches;
+    k_colmax<<<dim3(64, nrhs), 256, 0, c->stream>>>(b, n, nrhs, red + 2 * nrhs);
+    MIDAS_CUDA(c, cudaMemsetAsync(x, 0, sizeof(double2) * nn, c->stream));
+    MIDAS_CUDA(c, cudaMemcpyAsync(r, b, sizeof(double2) * nn, cudaMemcpyDeviceToDevice, c->stream));
+    const double tol = c->opts.ir_tol > 0 ? c->opts.ir_tol : 1e-13;
+    const int itmax = c->opts.ir_max_iter > 0 ? c->opts.ir_max_iter : 30;
+    double berr = 1e300;
+    int it;
+    bool done = false;
+    for (it = 0; it < itmax && !done; ++it) {
+        ++c->launches;
+        k_to32<<<(unsigned)std::min<size_t>((nn + 255) / 256, 65535), 256, 0, c->stream>>>(r, (long long)nn, d32);
+        MIDAS_TRY(lu_solve(c, lu, d32, nrhs));
+        MIDAS_CUDA(c, cudaMemsetAsync(red, 0, sizeof(unsigned long long) * 2 * nrhs, c->stream));
+        ++c->launches;
+        k_add_corr<<<(unsigned)((nn + 255) / 256), 256, 0, c->stream>>>(x, d32, (long long)nn, n, red + 3 * nrhs);
+        ++c->launches;
+        k_colmax<<<dim3(64, nrhs), 256, 0, c->stream>>>(x, n, nrhs, red + nrhs);
+        MIDAS_CUDA(c, cudaGetLastError());
+        MIDAS_TRY(lattice_matvec(c, nrhs, x, n, b, n, r, n, S_LFFT));   // r = b - Z x
+        ++c->launches;
+        k_colmax<<<dim3(64, nrhs), 256, 0, c->stream>>>(r, n, nrhs, red);
+        MIDAS_CUDA(c, cudaMemcpyAsync(h.data(), red, sizeof(unsigned long long) * 4 * nrhs, cudaMemcpyDeviceToHost,
+                                      c->stream));
+        MIDAS_CUDA(c, cudaStreamSynchronize(c->stream));
+        MIDAS_TRY(check_flag(c, "ir_solve_lattice"));
+        berr = 0;
+        for (int k = 0; k < nrhs; ++k) {
+            const double den = znorm * colmax(k, 1) + colmax(k, 2);
+            const double rn = colmax(k, 0);
+            berr = fmax(berr, den > 0 ? rn / den : rn);
+        }
+        if (!(berr == berr)) return c->err.set(MIDAS_ERR_NOT_CONVERGED, "ir_solve_lattice: NaN residual");
+        if (c->opts.verbose)
+            fprintf(stderr, "[midas] ir step %d (FFT lattice residual): backward error %.3e\n", it, berr);
+        done = berr <= tol;
+    }
+    if (info) {
+        info->ir_iters = it;
+        info->backward_error = berr;
+        info->anorm = znorm;
+    }
+    if (!done) {
+        char m[160];
+        snprintf(m, sizeof m, "iterative refinement stalled at backward error %.3e after %d steps", berr, it);
+        return c->err.set(MIDAS_ERR_NOT_CONVERGED, m);
+    }
+    return MIDAS_OK;
+}
+
+// Mixed solve of the MoM system of lattice cells: Z32 (row-major np x np, padded
+// with an identity) factorised in place, residuals from the FFT operator.
+int mixed_solve_lattice(midas_gpu_ctx *c, int np, float2 *Z32, const double2 *b, double2 *x, int nrhs,
+                        midas_gpu_info *info)
+{
+    void *p;
+    MIDAS_TRY(ensure(c, S_RED2, 64, &p));
+    unsigned *dnorm = (unsigned *)p;
+    MIDAS_CUDA(c, cudaMemsetAsync(dnorm, 0, sizeof(unsigned), c->stream));
+    ++c->launches;
+    k_row_abs_max<<<std::min(np, 4 * device_sms(c)), 256, 0, c->stream>>>(np, np, Z32, dnorm);
+    unsigned hn = 0;
+    MIDAS_CUDA(c, cudaMemcpyAsync(&hn, dnorm, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+    MIDAS_TRY(lattice_fft_prepare(c));
+    DenseLU lu;
+    lu.n = np;
+    lu.A = Z32;
+    lu.lda = np;
+    Timer tf(c->stream);
+    MIDAS_TRY(lu_factor_nopiv(c, lu));
+    MIDAS_TRY(check_flag(c, "lu_factor"));
+    float tfac = tf.stop();
+    float znf;
+    memcpy(&znf, &hn, 4);
+    Timer ts(c->stream);
+    int st = ir_solve_lattice(c, lu, (double)znf, b, x, nrhs, info);
+    float tsol = ts.stop();
+    if (info) { info->t_factor_ms = tfac; info->t_solve_ms = tsol; }
+    return st;
+}
+
 void destroy_cusolver(void *h) { cusolverDnDestroy((cusolverDnHandle_t)h); }
 
 }  // namespace midas

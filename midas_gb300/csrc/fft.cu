@@ -1,0 +1,346 @@
+// fft.cu -- the MoM operator on a voxel lattice as an FFT convolution (sm_103a).
+//
+// When every cell centroid sits on one uniform lattice, the MoM matrix of
+// compute_Green_s_tr_single_element (src/Compute_EFields_MoM.f90:433-523)
+// depends on a cell pair only through the lattice offset of the two cells:
+//
+//   (Z x)_o,p = (1 - Znnpp_o) x_o,p - sum_{s != o} sum_q F_pq(r_o - r_s) kc_s x_s,q
+//
+// with kc = f_kapChe = kappa Che.  The sum is a 3-D linear convolution of the
+// six unique dyad components with w_q = kc x_q, evaluated here with zero-padded
+// FFTs in FP64: grids of L_a >= 2 n_a - 1 points per axis (powers of two), the
+// dyad spectra computed once per set of cells, and per right-hand side three
+// forward transforms, a 3 x 3 pointwise product and three inverse transforms.
+// The refinement residuals of the mixed MoM solve and the Krylov solver use it:
+// an O(N log N) product instead of the O(N^2) dense residual, with no FP64
+// matrix in memory.
+//
+// The transforms are radix-2 decimation-in-time FFTs along one axis at a time,
+// several lines per CTA in shared memory (bit-reversed load, log2 L butterfly
+// stages).  Lines that are all zero in the padded input (the padding region of
+// the axes not yet transformed) are skipped on the way in, and lines whose
+// outputs are never read are skipped on the way out.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+#include "green.cuh"
+#include "kernels.cuh"
+
+namespace midas {
+
+constexpr int FFT_THREADS = 256;
+constexpr int FFT_TILE = 2048;   // complex points per CTA (lines x length)
+constexpr int FFT_LMAX = 512;
+
+// twiddles w_k = exp(-2 pi i k / FFT_LMAX), k < FFT_LMAX / 2 (host libm, once per device)
+static double2 *g_tw[64];
+
+static int twiddles(midas_gpu_ctx *c, const double2 **out)
+{
+    static std::atomic<int> ready[64];
+    const int dv = c->device & 63;
+    if (!ready[dv].load(std::memory_order_acquire)) {
+        std::vector<double2> h(FFT_LMAX / 2);
+        for (int k = 0; k < FFT_LMAX / 2; ++k) {
+            const double a = -2.0 * M_PI * k / FFT_LMAX;
+            h[k] = make_double2(cos(a), sin(a));
+        }
+        double2 *d = nullptr;
+        MIDAS_CUDA(c, cudaMalloc(&d, sizeof(double2) * h.size()));
+        MIDAS_CUDA(c, cudaMemcpy(d, h.data(), sizeof(double2) * h.size(), cudaMemcpyHostToDevice));
+        int expect = 0;
+        if (ready[dv].compare_exchange_strong(expect, 1, std::memory_order_acq_rel)) {
+            g_tw[dv] = d;
+        } else {
+            cudaFree(d);   // another thread won; its table is the one in use
+        }
+    }
+    *out = g_tw[dv];
+    return MIDAS_OK;
+}
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b)
+{
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// One radix-2 FFT pass along axis `ax` of a batch of L0 x L1 x L2 grids (x fastest).
+// The lines along ax are indexed by (a, b): for ax = 0, a = y and b = z; for
+// ax = 1, a = x and b = z; for ax = 2, a = x and b = y.  Only lines with
+// a < na and b < nb are transformed.  sign = -1 forward, +1 inverse
+// (unnormalised).  blockIdx.y selects the grid of the batch.
+template <int LOGL>
+__global__ void __launch_bounds__(FFT_THREADS) k_fft_axis(double2 *data, long long gstride, int ax, int L0, int L1,
+                                                          int na, int nb, int sign, const double2 *tw)
+{
+    constexpr int L = 1 << LOGL;
+    constexpr int G = FFT_TILE / L;   // lines per CTA
+    constexpr int LP = L + 1;         // padded line length in shared memory
+    extern __shared__ double2 sm[];
+    double2 *stw = sm + G * LP;
+    const int tid = threadIdx.x;
+    for (int k = tid; k < L / 2; k += FFT_THREADS) {
+        const double2 w = tw[k * (FFT_LMAX / L)];
+        stw[k] = make_double2(w.x, sign > 0 ? -w.y : w.y);
+    }
+    const int ntile = (na + G - 1) / G;
+    const int a0 = (blockIdx.x % ntile) * G, b = blockIdx.x / ntile;
+    if (b >= nb) return;
+    long long sa, sb, es;
+    if (ax == 0) { sa = L0; sb = (long long)L0 * L1; es = 1; }
+    else if (ax == 1) { sa = 1; sb = (long long)L0 * L1; es = L0; }
+    else { sa = 1; sb = L0; es = (long long)L0 * L1; }
+    double2 *g = data + (long long)blockIdx.y * gstride + (long long)b * sb;
+    // load, bit-reversing the position along the line
+    for (int idx = tid; idx < G * L; idx += FFT_THREADS) {
+        int gl, k;
+        if (ax == 0) { gl = idx / L; k = idx % L; } else { gl = idx % G; k = idx / G; }
+        const int a = a0 + gl;
+        if (a < na) sm[gl * LP + (__brev(k) >> (32 - LOGL))] = g[(long long)a * sa + (long long)k * es];
+    }
+    __syncthreads();
+#pragma unroll 1
+    for (int s = 0; s < LOGL; ++s) {
+        const int h = 1 << s;
+        for (int j = tid; j < G * (L / 2); j += FFT_THREADS) {
+            const int gl = j / (L / 2), bj = j % (L / 2);
+            const int grp = bj >> s, pos = bj & (h - 1);
+            const int i0 = gl * LP + grp * 2 * h + pos, i1 = i0 + h;
+            const double2 t = cmul(stw[pos << (LOGL - 1 - s)], sm[i1]);
+            const double2 u = sm[i0];
+            sm[i0] = make_double2(u.x + t.x, u.y + t.y);
+            sm[i1] = make_double2(u.x - t.x, u.y - t.y);
+        }
+        __syncthreads();
+    }
+    for (int idx = tid; idx < G * L; idx += FFT_THREADS) {
+        int gl, k;
+        if (ax == 0) { gl = idx / L; k = idx % L; } else { gl = idx % G; k = idx / G; }
+        const int a = a0 + gl;
+        if (a < na) g[(long long)a * sa + (long long)k * es] = sm[gl * LP + k];
+    }
+}
+
+static int fft_pass(midas_gpu_ctx *c, double2 *data, long long gstride, int ngrids, int ax, const int L[3], int na,
+                    int nb, int sign, const double2 *tw)
+{
+    const int len = L[ax];
+    const int logl = 31 - __builtin_clz(len);
+    const int G = FFT_TILE / len;
+    const int ntile = (na + G - 1) / G;
+    const dim3 grd((unsigned)(ntile * nb), (unsigned)ngrids);
+    const size_t smem = sizeof(double2) * ((size_t)G * (len + 1) + len / 2);
+    ++c->launches;
+    switch (logl) {
+#define FFT_CASE(LG)                                                                                              \
+    case LG:                                                                                                      \
+        k_fft_axis<LG><<<grd, FFT_THREADS, smem, c->stream>>>(data, gstride, ax, L[0], L[1], na, nb, sign, tw); \
+        break;
+        FFT_CASE(3) FFT_CASE(4) FFT_CASE(5) FFT_CASE(6) FFT_CASE(7) FFT_CASE(8) FFT_CASE(9)
+#undef FFT_CASE
+    default: return c->err.set(MIDAS_ERR_UNSUPPORTED, "lattice fft: axis length outside 8..512");
+    }
+    MIDAS_CUDA(c, cudaGetLastError());
+    return MIDAS_OK;
+}
+
+// 3-D transform of `ngrids` grids whose nonzero input occupies [0,n0) x [0,n1) x [0,n2)
+// (forward) or whose needed output is that box (inverse).
+static int fft3(midas_gpu_ctx *c, double2 *data, long long gstride, int ngrids, const int L[3], const int n[3],
+                int sign, const double2 *tw)
+{
+    if (sign < 0) {
+        MIDAS_TRY(fft_pass(c, data, gstride, ngrids, 0, L, n[1], n[2], sign, tw));   // x lines with y < n1, z < n2
+        MIDAS_TRY(fft_pass(c, data, gstride, ngrids, 1, L, L[0], n[2], sign, tw));   // y lines with z < n2
+        MIDAS_TRY(fft_pass(c, data, gstride, ngrids, 2, L, L[0], L[1], sign, tw));   // every z line
+    } else {
+        MIDAS_TRY(fft_pass(c, data, gstride, ngrids, 2, L, L[0], L[1], sign, tw));
+        MIDAS_TRY(fft_pass(c, data, gstride, ngrids, 1, L, L[0], n[2], sign, tw));
+        MIDAS_TRY(fft_pass(c, data, gstride, ngrids, 0, L, n[1], n[2], sign, tw));
+    }
+    return MIDAS_OK;
+}
+
+// dyad components on the circular offset grid: offset (di, dj, dk) at index
+// (di mod L0, dj mod L1, dk mod L2) for |d| < n per axis, zero elsewhere and at 0
+__global__ void k_dyad_grid(int L0, int L1, int L2, int n0, int n1, int n2, double d, double k0, double Pi,
+                            double2 *G6, long long gstride)
+{
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long tot = (long long)L0 * L1 * L2;
+    if (t >= tot) return;
+    const int i = (int)(t % L0), j = (int)((t / L0) % L1), k = (int)(t / ((long long)L0 * L1));
+    const int di = i < L0 / 2 ? i : i - L0, dj = j < L1 / 2 ? j : j - L1, dk = k < L2 / 2 ? k : k - L2;
+    double2 F[6];
+    if ((di == 0 && dj == 0 && dk == 0) || abs(di) >= n0 || abs(dj) >= n1 || abs(dk) >= n2) {
+#pragma unroll
+        for (int q = 0; q < 6; ++q) F[q] = make_double2(0, 0);
+    } else {
+        dyadF8(di * d, dj * d, dk * d, k0, Pi, F);
+    }
+#pragma unroll
+    for (int q = 0; q < 6; ++q) G6[q * gstride + t] = F[q];
+}
+
+// w_q = kc_s x_{3s+q} scattered into three zeroed grids per column
+__global__ void k_lat_scatter(int ncell, const int *ijk, const int *lo, int L0, int L1, const double2 *fk8,
+                              const double2 *X, long long ldx, int col0, double2 *grids, long long gstride)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= ncell) return;
+    const int col = col0 + blockIdx.y;
+    const long long gi = ((long long)(ijk[3 * s + 2] - lo[2]) * L1 + (ijk[3 * s + 1] - lo[1])) * L0 +
+                         (ijk[3 * s] - lo[0]);
+    const double2 f = fk8[s];
+    double2 *g = grids + (long long)blockIdx.y * 3 * gstride;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) g[q * gstride + gi] = cmul(f, X[(long long)col * ldx + 3 * s + q]);
+}
+
+// Y_p = sum_q F^_pq W_q at every frequency, for every column of the batch (the
+// spectra are read once per point and kept in registers across the columns)
+__global__ void k_lat_pointwise(long long npts, const double2 *G6, long long gstride, double2 *grids, int ncol)
+{
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= npts) return;
+    double2 F[6];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) F[q] = G6[q * gstride + t];
+    for (int col = 0; col < ncol; ++col) {
+        double2 *g = grids + (long long)col * 3 * gstride + t;
+        const double2 wx = g[0], wy = g[gstride], wz = g[2 * gstride];
+        const double2 yx = cmul(F[0], wx), yy = cmul(F[1], wy), yz = cmul(F[2], wz);
+        const double2 xy = cmul(F[3], wy), xz = cmul(F[5], wz);
+        const double2 yx2 = cmul(F[3], wx), yz2 = cmul(F[4], wz);
+        const double2 zx = cmul(F[5], wx), zy = cmul(F[4], wy);
+        g[0] = make_double2(yx.x + xy.x + xz.x, yx.y + xy.y + xz.y);
+        g[gstride] = make_double2(yx2.x + yy.x + yz2.x, yx2.y + yy.y + yz2.y);
+        g[2 * gstride] = make_double2(zx.x + zy.x + yz.x, zx.y + zy.y + yz.y);
+    }
+}
+
+// Y = (1 - Znnpp) X - conv / Ntot, or, with B given, R = B - that (the residual)
+__global__ void k_lat_gather(int ncell, const int *ijk, const int *lo, int L0, int L1, const double2 *znnpp,
+                             const double2 *X, long long ldx, const double2 *B, long long ldb, double2 *Y,
+                             long long ldy, int col0, const double2 *grids, long long gstride, double scale)
+{
+    const int o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= ncell) return;
+    const int col = col0 + blockIdx.y;
+    const long long gi = ((long long)(ijk[3 * o + 2] - lo[2]) * L1 + (ijk[3 * o + 1] - lo[1])) * L0 +
+                         (ijk[3 * o] - lo[0]);
+    const double2 dg = make_double2(1.0 - znnpp[o].x, -znnpp[o].y);
+    const double2 *g = grids + (long long)blockIdx.y * 3 * gstride;
+#pragma unroll
+    for (int p = 0; p < 3; ++p) {
+        const double2 cv = g[p * gstride + gi];
+        const double2 dx = cmul(dg, X[(long long)col * ldx + 3 * o + p]);
+        double2 y = make_double2(dx.x - cv.x * scale, dx.y - cv.y * scale);
+        if (B) {
+            const double2 bb = B[(long long)col * ldb + 3 * o + p];
+            y = make_double2(bb.x - y.x, bb.y - y.y);
+        }
+        Y[(long long)col * ldy + 3 * o + p] = y;
+    }
+}
+
+static int next_pow2(int v)
+{
+    int p = 8;
+    while (p < v) p <<= 1;
+    return p;
+}
+
+bool lattice_fft_fits(const midas_gpu_ctx *c)
+{
+    if (!c->lattice || !c->lat_ijk) return false;
+    for (int a = 0; a < 3; ++a)
+        if (next_pow2(2 * (c->lat_hi[a] - c->lat_lo[a] + 1) - 1) > FFT_LMAX) return false;
+    return true;
+}
+
+// Lattice FFT set-up of the current cells: grid sizes, dyad spectra (6 grids).
+int lattice_fft_prepare(midas_gpu_ctx *c)
+{
+    if (!c->lattice || !c->lat_ijk) return c->err.set(MIDAS_ERR_UNSUPPORTED, "lattice fft: cells are not on a lattice");
+    if (c->lfft.G6 && c->lfft.version == c->cells_version) return MIDAS_OK;
+    LatticeFft &f = c->lfft;
+    for (int a = 0; a < 3; ++a) {
+        f.n[a] = c->lat_hi[a] - c->lat_lo[a] + 1;
+        f.L[a] = next_pow2(2 * f.n[a] - 1);
+        if (f.L[a] > FFT_LMAX) return c->err.set(MIDAS_ERR_UNSUPPORTED, "lattice fft: lattice wider than 256 cells along an axis");
+    }
+    f.npts = (long long)f.L[0] * f.L[1] * f.L[2];
+    if (f.G6) cudaFree(f.G6);
+    f.G6 = nullptr;
+    if (!f.lo) MIDAS_CUDA(c, cudaMalloc(&f.lo, sizeof(int) * 4));
+    MIDAS_CUDA(c, cudaMemcpyAsync(f.lo, c->lat_lo, sizeof(int) * 3, cudaMemcpyHostToDevice, c->stream));
+    MIDAS_CUDA(c, cudaMalloc(&f.G6, sizeof(double2) * 6 * (size_t)f.npts));
+    const double2 *tw;
+    MIDAS_TRY(twiddles(c, &tw));
+    ++c->launches;
+    k_dyad_grid<<<(unsigned)((f.npts + 255) / 256), 256, 0, c->stream>>>(f.L[0], f.L[1], f.L[2], f.n[0], f.n[1],
+                                                                          f.n[2], c->lat_d, c->k0, c->pi, f.G6,
+                                                                          f.npts);
+    MIDAS_CUDA(c, cudaGetLastError());
+    // the dyad grid is nonzero over the whole circular grid: full transforms
+    const int full[3] = {f.L[0], f.L[1], f.L[2]};
+    MIDAS_TRY(fft3(c, f.G6, f.npts, 6, f.L, full, -1, tw));
+    f.version = c->cells_version;
+    return MIDAS_OK;
+}
+
+void lattice_fft_release(midas_gpu_ctx *c)
+{
+    if (c->lfft.G6) cudaFree(c->lfft.G6);
+    if (c->lfft.lo) cudaFree(c->lfft.lo);
+    c->lfft = LatticeFft();
+}
+
+// Y = Z X (B == nullptr) or Y = B - Z X, for nrhs columns (column-major, FP64;
+// rows 3 * ncell of each column are read / written).  Scratch from `slot`.
+int lattice_matvec(midas_gpu_ctx *c, int nrhs, const double2 *X, long long ldx, const double2 *B, long long ldb,
+                   double2 *Y, long long ldy, int slot)
+{
+    MIDAS_TRY(lattice_fft_prepare(c));
+    LatticeFft &f = c->lfft;
+    const double2 *tw;
+    MIDAS_TRY(twiddles(c, &tw));
+    // columns per batch: three grids each, batch scratch bounded to ~1 GB
+    const size_t per_col = sizeof(double2) * 3 * (size_t)f.npts;
+    const int batch = (int)std::max<size_t>(1, std::min<size_t>((size_t)nrhs, ((size_t)1 << 30) / per_col));
+    void *p;
+    MIDAS_TRY(ensure(c, slot, per_col * batch, &p));
+    double2 *grids = (double2 *)p;
+    const int ncell = c->n;
+    const double scale = 1.0 / (double)f.npts;
+    const int kp = kp_begin(c);
+    for (int col0 = 0; col0 < nrhs; col0 += batch) {
+        const int nb = std::min(batch, nrhs - col0);
+        MIDAS_CUDA(c, cudaMemsetAsync(grids, 0, per_col * nb, c->stream));
+        const dim3 grd((unsigned)((ncell + 127) / 128), (unsigned)nb);
+        ++c->launches;
+        k_lat_scatter<<<grd, 128, 0, c->stream>>>(ncell, c->lat_ijk, f.lo, f.L[0], f.L[1], c->fk8, X, ldx, col0,
+                                                  grids, f.npts);
+        MIDAS_CUDA(c, cudaGetLastError());
+        MIDAS_TRY(fft3(c, grids, f.npts, 3 * nb, f.L, f.n, -1, tw));
+        ++c->launches;
+        k_lat_pointwise<<<(unsigned)((f.npts + 127) / 128), 128, 0, c->stream>>>(f.npts, f.G6, f.npts, grids, nb);
+        MIDAS_CUDA(c, cudaGetLastError());
+        MIDAS_TRY(fft3(c, grids, f.npts, 3 * nb, f.L, f.n, +1, tw));
+        ++c->launches;
+        k_lat_gather<<<grd, 128, 0, c->stream>>>(ncell, c->lat_ijk, f.lo, f.L[0], f.L[1], c->znnpp, X, ldx, B, ldb, Y,
+                                                 ldy, col0, grids, f.npts, scale);
+        MIDAS_CUDA(c, cudaGetLastError());
+    }
+    // algorithmic work: 6 complex FFTs (5 N log2 N each) + 9 complex MACs per point, per column;
+    // bytes: X, Y (and B) once
+    const double lg = log2((double)f.npts);
+    kp_end(c, kp, MIDAS_KC_LATTICE, nrhs * (6 * 5.0 * f.npts * lg + 72.0 * f.npts),
+           16.0 * 3 * ncell * nrhs * (B ? 3 : 2));
+    return MIDAS_OK;
+}
+
+}  // namespace midas

@@ -337,6 +337,7 @@ int midas_gpu_free(midas_gpu_ctx *c)
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     free_cells(c);
+    lattice_fft_release(c);
     for (auto &b : c->pool)
         if (b.p) cudaFree(b.p);
     if (c->d_flag) cudaFree(c->d_flag);
@@ -393,6 +394,7 @@ int midas_gpu_set_cells(midas_gpu_ctx *c, int n, const double *xc, const double 
     c->k0 = k0;
     MIDAS_TRY(launch_set_cells(c));
     detect_lattice(c, hx, hy, hz, hs);
+    ++c->cells_version;   // the lattice FFT spectra of the previous cells are stale
     MIDAS_CUDA(c, cudaStreamSynchronize(c->stream));
     return MIDAS_OK;
 }
@@ -745,6 +747,35 @@ int midas_gpu_mom_solve(midas_gpu_ctx *c, int ntr, const double *theta, const do
         float tlu = tl.stop();
         if (info) { info->t_fill_ms = tfill; info->t_factor_ms = tlu; }
         if (st == MIDAS_OK) st = copy_out(c, E, pb, sizeof(double2) * (size_t)n * nrhs);
+    } else if (lattice_fft_fits(c)) {
+        // cells on a lattice: the residuals come from the FFT operator, so only the
+        // complex64 matrix (the factorisation's operand) is formed
+        int np = (n + 63) / 64 * 64;
+        void *p32, *pb, *px;
+        MIDAS_TRY(ensure(c, S_Z32, sizeof(float2) * (size_t)np * np, &p32));
+        MIDAS_TRY(ensure(c, S_RHS64, sizeof(double2) * (size_t)np * nrhs, &pb));
+        MIDAS_TRY(ensure(c, S_X64, sizeof(double2) * (size_t)np * nrhs, &px));
+        Timer tf(c->stream);
+        if (np > n) {
+            MIDAS_CUDA(c, cudaMemsetAsync(p32, 0, sizeof(float2) * (size_t)np * np, c->stream));
+            ++c->launches;
+            k_pad_identity<<<1, 64, 0, c->stream>>>(nullptr, (float2 *)p32, np, n, np);
+            MIDAS_CUDA(c, cudaMemsetAsync(pb, 0, sizeof(double2) * (size_t)np * nrhs, c->stream));
+        }
+        MIDAS_TRY(launch_mom_fill(c, 0, n, 0, n, nullptr, (float2 *)p32, (size_t)np, 1));   // row-major
+        MIDAS_TRY(launch_mom_rhs<double2>(c, ntr, (const double *)th, (const double *)ph, (double2 *)pb, 1, np));
+        float tfill = tf.stop();
+        if (info) info->t_fill_ms = tfill;
+        st = mixed_solve_lattice(c, np, (float2 *)p32, (const double2 *)pb, (double2 *)px, nrhs, info);
+        if (st == MIDAS_OK) {
+            void *pout;
+            MIDAS_TRY(ensure(c, S_OUT0, sizeof(double2) * (size_t)n * nrhs, &pout));
+            long long t2 = (long long)n * nrhs;
+            ++c->launches;
+            k_copy_unpad<<<(unsigned)((t2 + 255) / 256), 256, 0, c->stream>>>((const double2 *)px, n, np, nrhs,
+                                                                              (double2 *)pout);
+            st = copy_out(c, E, pout, sizeof(double2) * (size_t)n * nrhs);
+        }
     } else {
         int np = (n + 63) / 64 * 64;
         void *p64, *p32, *pb, *px;
@@ -779,6 +810,68 @@ int midas_gpu_mom_solve(midas_gpu_ctx *c, int ntr, const double *theta, const do
     }
     if (info) {
         info->status = st;
+        info->t_total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
+    return st;
+}
+
+int midas_gpu_lattice_matvec(midas_gpu_ctx *c, int nrhs, const double *X, double *Y)
+{
+    if (!c) return MIDAS_ERR_ARG;
+    c->err = Err();
+    MIDAS_TRY(need_cells(c));
+    if (nrhs <= 0 || !X || !Y) return c->err.set(MIDAS_ERR_ARG, "lattice_matvec: bad arguments");
+    cudaSetDevice(c->device);
+    const size_t N = 3 * (size_t)c->n, bytes = sizeof(double2) * N * nrhs;
+    const void *dx;
+    MIDAS_TRY(to_device(c, X, bytes, S_IN3, &dx));
+    double2 *out = (double2 *)Y;
+    if (!is_device_ptr(Y)) {
+        void *p;
+        MIDAS_TRY(ensure(c, S_OUT0, bytes, &p));
+        out = (double2 *)p;
+    }
+    MIDAS_TRY(lattice_matvec(c, nrhs, (const double2 *)dx, (long long)N, nullptr, 0, out, (long long)N, S_LFFT));
+    MIDAS_TRY(copy_out(c, Y, out, bytes));
+    return check_flag(c, "lattice_matvec");
+}
+
+int midas_gpu_gmres_solve(midas_gpu_ctx *c, int ntr, const double *theta, const double *phi, const double *E0,
+                          int restart, int maxit, double tol, int flags, double *E, midas_gpu_info *info)
+{
+    if (!c) return MIDAS_ERR_ARG;
+    c->err = Err();
+    auto t0 = std::chrono::steady_clock::now();
+    MIDAS_TRY(need_cells(c));
+    if (ntr <= 0 || !theta || !phi || !E || restart <= 0 || restart > 500 || maxit <= 0 || !(tol > 0))
+        return c->err.set(MIDAS_ERR_ARG, "gmres_solve: bad arguments");
+    if (!lattice_fft_fits(c)) return c->err.set(MIDAS_ERR_UNSUPPORTED, "gmres_solve: cells are not on a lattice");
+    cudaSetDevice(c->device);
+    if (info) memset(info, 0, sizeof(*info));
+    const int n = 3 * c->n, nrhs = 2 * ntr;
+    const size_t bytes = sizeof(double2) * (size_t)n * nrhs;
+    const void *th, *ph;
+    MIDAS_TRY(to_device(c, theta, sizeof(double) * ntr, S_IN0, &th));
+    MIDAS_TRY(to_device(c, phi, sizeof(double) * ntr, S_IN1, &ph));
+    void *pb, *px;
+    MIDAS_TRY(ensure(c, S_RHS64, bytes, &pb));
+    MIDAS_TRY(ensure(c, S_X64, bytes, &px));
+    MIDAS_TRY(launch_mom_rhs<double2>(c, ntr, (const double *)th, (const double *)ph, (double2 *)pb, 1, n));
+    if (E0) MIDAS_CUDA(c, cudaMemcpyAsync(px, E0, bytes, cudaMemcpyDefault, c->stream));
+    else MIDAS_CUDA(c, cudaMemsetAsync(px, 0, bytes, c->stream));
+    int iters = 0;
+    double rel = 0;
+    Timer ts(c->stream);
+    int st = gmres_lattice(c, nrhs, (const double2 *)pb, (double2 *)px, restart, maxit, tol,
+                           (flags & MIDAS_GMRES_JACOBI) != 0, &iters, &rel);
+    const float tsol = ts.stop();
+    const int cst = copy_out(c, E, px, bytes);
+    if (st == MIDAS_OK) st = cst;
+    if (info) {
+        info->status = st;
+        info->ir_iters = iters;
+        info->backward_error = rel;
+        info->t_solve_ms = tsol;
         info->t_total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     }
     return st;

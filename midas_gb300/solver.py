@@ -173,6 +173,36 @@ class Context:
         self._ck(self.L.midas_gpu_mom_solve(self.h, len(th), addr(th), addr(ph), addr(E), ctypes.byref(self.info)))
         return E.T if out is None else E
 
+    def lattice_matvec(self, X):
+        """Y = Z X with the MoM matrix of compute_Green_s_tr_single_element
+        (src/Compute_EFields_MoM.f90:433-523) applied as an FFT convolution on the
+        cells' lattice.  X: (3n, nrhs) complex."""
+        X = np.asarray(X, np.complex128)
+        if X.ndim == 1:
+            X = X[:, None]
+        Xc = np.ascontiguousarray(X.T)   # column-major (3n, nrhs) = row-major (nrhs, 3n)
+        Y = np.zeros_like(Xc)
+        self._ck(self.L.midas_gpu_lattice_matvec(self.h, X.shape[1], addr(Xc), addr(Y)))
+        return Y.T
+
+    def gmres_solve(self, th, ph, E0=None, restart=50, maxit=2000, tol=1e-8, jacobi=False, check=True):
+        """GMRES(restart) on the FFT lattice operator for the MoM system of
+        Compute_EFields_MoM (src/Compute_EFields_MoM.f90:153-198): (E, iterations,
+        true relative residual).  E0 (3n, 2ntr) is the initial guess.  With
+        check=False a run that stops at maxit returns its last iterate instead
+        of raising."""
+        th, ph = _c(th, np.float64), _c(ph, np.float64)
+        E = np.zeros((2 * len(th), 3 * self.n), np.complex128)
+        e0 = None
+        if E0 is not None:
+            e0 = np.ascontiguousarray(np.asarray(E0, np.complex128).T)
+        st = self.L.midas_gpu_gmres_solve(self.h, len(th), addr(th), addr(ph), addr(e0), int(restart), int(maxit),
+                                          float(tol), _lib.GMRES_JACOBI if jacobi else 0, addr(E),
+                                          ctypes.byref(self.info))
+        if st != 0 and (check or st != 5):
+            self._ck(st)
+        return E.T, self.info.ir_iters, self.info.backward_error
+
     def cbfm_solve(self, blk_offsets, ext_lists, cbf_th, cbf_ph, th, ph, flags=_lib.CBFM_SR, thr_cbf=0.0,
                    res_sr=0.0, eps_aca=float(np.float32(1e-4)), aca_itmax=50, out=None):
         """Compute_EFields_CBFME(_ACA) (src/Compute_EFields_CBFME.f90:1-1006): (E, K)."""
@@ -190,6 +220,55 @@ class Context:
                                              int(aca_itmax), len(th), addr(th), addr(ph), addr(E), addr(K),
                                              ctypes.byref(self.info)))
         return (E.T if out is None else E), K
+
+    # -- scene preparation on the device --------------------------------------
+    def voxelise_sphere(self, dm: float, sc: float) -> np.ndarray:
+        """Discretization's sphere voxeliser (src/Discretization.f90:246-310): (n, 3) centroids."""
+        n = ctypes.c_longlong(0)
+        self._ck(self.L.midas_gpu_voxelise_sphere(self.h, float(dm), float(sc), 0, None, None, None, ctypes.byref(n)))
+        xyz = np.zeros((3, n.value))
+        self._ck(self.L.midas_gpu_voxelise_sphere(self.h, float(dm), float(sc), n.value, addr(xyz[0]), addr(xyz[1]),
+                                                  addr(xyz[2]), ctypes.byref(n)))
+        return np.ascontiguousarray(xyz.T)
+
+    def voxelise_spheres(self, centres, a: float, cells_per_diameter: int = 6):
+        """Cells inside a union of spheres: ((n, 3) centroids, edge)."""
+        cen = _c(centres, np.float64).reshape(-1, 3)
+        n, e = ctypes.c_longlong(0), ctypes.c_double(0)
+        self._ck(self.L.midas_gpu_voxelise_spheres(self.h, len(cen), addr(cen), float(a), int(cells_per_diameter), 0,
+                                                   None, None, None, ctypes.byref(n), ctypes.byref(e)))
+        xyz = np.zeros((3, n.value))
+        self._ck(self.L.midas_gpu_voxelise_spheres(self.h, len(cen), addr(cen), float(a), int(cells_per_diameter),
+                                                   n.value, addr(xyz[0]), addr(xyz[1]), addr(xyz[2]), ctypes.byref(n),
+                                                   ctypes.byref(e)))
+        return np.ascontiguousarray(xyz.T), e.value
+
+    def box_partition(self, xyz, nx: int, ny: int, nz: int):
+        """Bounding-box blocks: (perm, blk_offsets) -- xyz[perm] is block-contiguous."""
+        xyz = np.asarray(xyz, np.float64).reshape(-1, 3)
+        x, y, z = (_c(xyz[:, i], np.float64) for i in range(3))
+        perm = np.zeros(len(xyz), np.int32)
+        offs = np.zeros(nx * ny * nz + 1, np.int32)
+        nb = ctypes.c_int(0)
+        self._ck(self.L.midas_gpu_box_partition(self.h, len(xyz), addr(x), addr(y), addr(z), nx, ny, nz, addr(perm),
+                                                addr(offs), ctypes.byref(nb)))
+        return perm, offs[: nb.value + 1].copy()
+
+    def extend_blocks(self, xyz, blk_offsets, ext_length: float, sc: float):
+        """Extend_blocks (src/Extend_blocks.f90:46-151): list of extension-cell index arrays."""
+        xyz = np.asarray(xyz, np.float64).reshape(-1, 3)
+        x, y, z = (_c(xyz[:, i], np.float64) for i in range(3))
+        bo = _c(blk_offsets, np.int32)
+        nb = len(bo) - 1
+        eo = np.zeros(nb + 1, np.int32)
+        tot = ctypes.c_longlong(0)
+        self._ck(self.L.midas_gpu_extend_blocks(self.h, len(xyz), addr(x), addr(y), addr(z), nb, addr(bo),
+                                                float(ext_length), float(sc), addr(eo), 0, None, ctypes.byref(tot)))
+        ei = np.zeros(max(tot.value, 1), np.int32)
+        self._ck(self.L.midas_gpu_extend_blocks(self.h, len(xyz), addr(x), addr(y), addr(z), nb, addr(bo),
+                                                float(ext_length), float(sc), addr(eo), tot.value, addr(ei),
+                                                ctypes.byref(tot)))
+        return [ei[eo[b]:eo[b + 1]].copy() for b in range(nb)]
 
     # -- post-processing ---------------------------------------------------
     def cext_cabs(self, th, ph, E):

@@ -58,7 +58,7 @@ def mom_c3_small():
 
 def mom_tiny():
     """The reference's literal sphere case: x = 2, m = 1.5 + 0.01i, a/d = 4.775
-    (447 cells), +z incidence, V + H -- small enough for CPU tests."""
+    (489 cells), +z incidence, V + H -- small enough for CPU tests."""
     from . import geometry as G
     a, x, m = 1.0, 2.0, 1.5 + 0.01j
     sc = a / 4.775
@@ -236,6 +236,8 @@ def main(argv=None):
     ap.add_argument("--fill", default="fast", choices=["fast", "faithful"])
     ap.add_argument("--verbose", "-v", action="count", default=0,
                     help="library trace: -v refinement steps and CBFM lanes, -vv per-block detail")
+    ap.add_argument("--classes", action="store_true",
+                    help="after the steps, one more step with per-kernel-class CUDA-event timing (one lane)")
     args = ap.parse_args(argv)
     wl = WORKLOADS[args.workload]()
     ctx = Context(device=0, fill_mode=_lib.FILL_FAST if args.fill == "fast" else _lib.FILL_FAITHFUL,
@@ -266,6 +268,22 @@ def main(argv=None):
             E = ctx.mom_solve(wl["th"], wl["ph"])
         dt = time.perf_counter() - t0
         print(f"{wl['name']}: step {step} {dt:.3f} s, {ctx.launch_count()} launches so far", flush=True)
+    if args.classes:
+        ctx.profile(True)
+        t0 = time.perf_counter()
+        if wl["method"] == "cbfm":
+            ctx.cbfm_solve(wl["offs"], wl["ext"], wl["cth"], wl["cph"], wl["th"], wl["ph"], flags=flags)
+        else:
+            ctx.mom_solve(wl["th"], wl["ph"])
+        dt = time.perf_counter() - t0
+        prof = ctx.profile_query()
+        ctx.profile(False)
+        print(f"{wl['name']}: profiled step {dt:.3f} s; kernel classes (ms, launches, TFLOP/s, GB/s):")
+        for k, v in sorted(prof.items(), key=lambda kv: -kv[1]["ms"]):
+            if v["launches"]:
+                sec = v["ms"] * 1e-3
+                print(f"  {k:11s} {v['ms']:9.2f} {v['launches']:7d} {v['flops'] / sec / 1e12:8.2f} "
+                      f"{v['bytes'] / sec / 1e9:8.1f}", flush=True)
     ctx.close()
     return 0
 

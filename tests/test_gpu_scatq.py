@@ -42,7 +42,7 @@ def test_rules_match_oracle(ctx, oracle, tr, rx, kw, intf):
 
 def test_sphere_end_to_end(gpulib, oracle):
     """The reference's sphere example layout (one incident direction, theta 0..180
-    x phi 0..360 receivers, 'un'/'un') on a 447-cell sphere solved on the GPU:
+    x phi 0..360 receivers, 'un'/'un') on a 489-cell sphere solved on the GPU:
     S and Cext/Cabs from the GPU, then the efficiencies, against the oracle's
     whole chain (internal fields agree to 1e-10, so the float quadratures agree
     to 1e-6)."""

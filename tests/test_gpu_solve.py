@@ -94,6 +94,26 @@ def test_mom_solve_matches_oracle(gpulib, oracle, mode):
     c.close()
 
 
+def test_mom_solve_off_lattice_dense_residuals(gpulib, oracle):
+    """Cells off any lattice (jittered centroids): the mixed solve refines with the
+    dense double-float residuals instead of the FFT lattice operator."""
+    from midas_gb300.solver import Context
+    m, sc, k0 = 1.5 + 0.01j, 0.2, 2.0
+    rng = np.random.default_rng(5)
+    xyz = oracle.sphere_cells(2.0, sc)
+    xyz = xyz + rng.uniform(-0.01, 0.01, xyz.shape)
+    cells = oracle.Cells(xyz, sc, m * m, k0)
+    th, ph = [90.0, 40.0], [90.0, 200.0]
+    ref = oracle.mom_solve(cells, th, ph)
+    c = Context().set_cells(xyz, sc, m * m, k0)
+    E = c.mom_solve(th, ph)
+    assert np.linalg.norm(E - ref["E"]) / np.linalg.norm(ref["E"]) < 1e-10
+    assert c.info.backward_error <= 1e-13
+    with pytest.raises(Exception):
+        c.lattice_matvec(np.ones((3 * len(xyz), 1), complex))
+    c.close()
+
+
 def test_mom_solve_inhomogeneous_fast_fill(gpulib, oracle):
     from midas_gb300 import _lib, geometry as G
     from midas_gb300.solver import Context

@@ -61,7 +61,7 @@ def test_qag_on_sampled_columns(oracle):
 
 def test_sphere_energy_balance_and_mie(oracle):
     """The reference's sphere example layout (one incident direction, theta 0..180,
-    phi 0..360 receivers) on a solved 447-cell sphere: optical theorem vs internal
+    phi 0..360 receivers) on a solved 489-cell sphere: optical theorem vs internal
     field, Q_sca vs Q_ext - Q_abs, adaptive vs trapezoid, and Mie."""
     from midas_gb300 import geometry as G
     m, a, k0 = 1.5 + 0.01j, 1.0, 2.0
