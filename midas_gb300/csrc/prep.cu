@@ -265,7 +265,7 @@ __global__ void k_block_id(int n, const double *x, const double *y, const double
     for (int a = 0; a < 3; ++a) {
         const double span = mm[3 + a] > mm[a] ? __dsub_rn(mm[3 + a], mm[a]) : 1.0;
         const double f = __dmul_rn(__ddiv_rn(__dsub_rn(p[a], mm[a]), span), (double)ns[a]);
-        ijk[a] = min((int)f, ns[a] - 1);
+        ijk[a] = f >= 0.0 ? min((int)fmin(f, (double)ns[a]), ns[a] - 1) : 0;   // NaN or negative -> block 0
     }
     bid[i] = (ijk[2] * ny + ijk[1]) * nx + ijk[0];
 }
