@@ -77,6 +77,18 @@ __global__ void k_ir_update(long long tot, int n, int m, double2 *X64, const flo
     if (Drm) Drm[o] = d32[i];   // the correction, for the FP32 residual update
 }
 
+// d = fp32(r) and x += d, for the correction of the reduced solution
+__global__ void k_c64_to_c32(long long tot, const double2 *r, float2 *d)
+{
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < tot) d[i] = make_float2((float)r[i].x, (float)r[i].y);
+}
+__global__ void k_add_c32(long long tot, const float2 *d, double2 *x)
+{
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < tot) x[i] = make_double2(x[i].x + d[i].x, x[i].y + d[i].y);
+}
+
 // R = B (FP64 copy of the FP32 right-hand sides)
 __global__ void k_b_to_r64(long long tot, const float2 *B, double2 *R)
 {
@@ -215,11 +227,7 @@ static int cbf_block(midas_gpu_ctx *c, const CbfShared &S, int b)
             k_pad_diag32<<<1, 64, 0, c->stream>>>(Zlu, sp, N3, sp);
         }
         Csr zcsr;
-        Bsr3 zb;
-        const bool use_bsr = !getenv("MIDAS_CBF_CSR");
-        if (sr && use_bsr)
-            MIDAS_TRY(bsr3_from_dense(c, s, sp, Zlu, sp, S_CSR, &zb));
-        else if (sr)
+        if (sr)
             MIDAS_TRY(csr_from_dense(c, sp, Zlu, sp, S_CSR, &zcsr));
         else
             MIDAS_CUDA(c, cudaMemcpyAsync(Zsr, Zlu, sizeof(float2) * (size_t)sp * sp, cudaMemcpyDeviceToDevice,
@@ -255,15 +263,11 @@ static int cbf_block(midas_gpu_ctx *c, const CbfShared &S, int b)
             if (sr && it == 0) {
                 ++c->launches;
                 k_b_to_r64<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(tot, Bm, R64);
-                if (use_bsr) MIDAS_TRY(residual_bsr_update_f32(c, zb, m, Drm, R64));
-                else MIDAS_TRY(residual_csr_update_f32(c, zcsr, m, Drm, R64));
-            } else if (sr && upd) {
-                if (use_bsr) MIDAS_TRY(residual_bsr_update_f32(c, zb, m, Drm, R64));
-                else MIDAS_TRY(residual_csr_update_f32(c, zcsr, m, Drm, R64));
-            } else if (sr) {
-                if (use_bsr) MIDAS_TRY(residual_bsr_df32(c, zb, m, Xh, Xl, Bm, R64));
-                else MIDAS_TRY(residual_csr_df32(c, zcsr, m, Xh, Xl, Bm, R64));
-            }
+                MIDAS_TRY(residual_csr_update_f32(c, zcsr, m, Drm, R64));
+            } else if (sr && upd)
+                MIDAS_TRY(residual_csr_update_f32(c, zcsr, m, Drm, R64));
+            else if (sr)
+                MIDAS_TRY(residual_csr_df32(c, zcsr, m, Xh, Xl, Bm, R64));
             else
                 MIDAS_TRY(residual_df32(c, sp, m, Zsr, sp, Xh, Xl, Bm, R64));
             MIDAS_CUDA(c, cudaMemsetAsync(red, 0, sizeof(unsigned long long) * 2 * m, c->stream));
@@ -688,7 +692,8 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
     }
     midas_gpu_info sinfo;
     memset(&sinfo, 0, sizeof(sinfo));
-    MIDAS_TRY(mixed_solve(c, npd, (float2 *)p32, (double2 *)p64, Vc, (double2 *)px, nr, &sinfo));
+    DenseLU rlu;
+    MIDAS_TRY(mixed_solve(c, npd, (float2 *)p32, (double2 *)p64, Vc, (double2 *)px, nr, &sinfo, &rlu));
     // E = C alpha per block
     double2 *Eout = E_user;
     void *peo = nullptr;
@@ -697,10 +702,46 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
         MIDAS_TRY(ensure(c, S_OUT0, sizeof(double2) * (size_t)3 * n * nr, &peo));
         Eout = (double2 *)peo;
     }
-    for (int b = 0; b < nb; ++b) {
-        const int nbc = bo[b + 1] - bo[b];
-        MIDAS_TRY(zgemm_df(c, 3 * nbc, nr, Kb[b], Call + coff[b], 1, 3 * nbc, (const double2 *)px + koff[b], 1, npd,
-                           Eout + 3 * (size_t)bo[b], 1, 3LL * n));
+    auto reconstruct = [&]() -> int {
+        for (int b = 0; b < nb; ++b) {
+            const int nbc = bo[b + 1] - bo[b];
+            MIDAS_TRY(zgemm_df(c, 3 * nbc, nr, Kb[b], Call + coff[b], 1, 3 * nbc, (const double2 *)px + koff[b], 1,
+                               npd, Eout + 3 * (size_t)bo[b], 1, 3LL * n));
+        }
+        return MIDAS_OK;
+    };
+    MIDAS_TRY(reconstruct());
+    // One correction against the FP64 reduced residual.  The reduced matrix above
+    // is FP32-grade (split-TF32 tensor products summed in FP32), which moves alpha
+    // by ~1e-6 on a 27-block scene.  For lattice cells the exact reduced residual
+    //   rho_b = C_b^T (Einc - Z E)_b,  E = C alpha,
+    // costs one FFT product with the complex(4) dyads of Green_s_tr_partial (their
+    // products with f_kapChe and E in FP64); alpha += Zc^-1 rho with the TF32
+    // factors then leaves ~1e-3.5 of the error.  With ACA the reduced matrix is
+    // itself an approximation of these blocks, so no correction is made.
+    if (!use_aca && lattice_fft_fits(c)) {
+        const size_t nf = (size_t)3 * n * nr;
+        void *pf;
+        MIDAS_TRY(ensure(c, S_CREF, sizeof(double2) * 2 * nf + sizeof(float2) * (size_t)npd * nr + 1024, &pf));
+        double2 *Ef = (double2 *)pf, *Rf = Ef + nf;
+        float2 *d32 = (float2 *)(((uintptr_t)(Rf + nf) + 255) & ~(uintptr_t)255);
+        MIDAS_TRY(launch_incident4<double2>(c, n, d_all, ntr, d_th, d_ph, Ef, 1, (size_t)3 * n));
+        MIDAS_TRY(lattice_matvec(c, nr, Eout, 3LL * n, Ef, 3LL * n, Rf, 3LL * n, S_LFFT, true));
+        double2 *rho = Vc;   // Vc is no longer needed: the reduced residual takes its place
+        MIDAS_CUDA(c, cudaMemsetAsync(rho, 0, sizeof(double2) * (size_t)npd * nr, c->stream));
+        for (int b = 0; b < nb; ++b) {
+            const int nbc = bo[b + 1] - bo[b];
+            MIDAS_TRY(zgemm_df(c, Kb[b], nr, 3 * nbc, Call + coff[b], 3 * nbc, 1, Rf + 3 * (size_t)bo[b], 1, 3LL * n,
+                               rho + koff[b], 1, npd));
+        }
+        const long long tot = (long long)npd * nr;
+        ++c->launches;
+        k_c64_to_c32<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(tot, rho, d32);
+        MIDAS_TRY(lu_solve(c, rlu, d32, nr));
+        ++c->launches;
+        k_add_c32<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(tot, d32, (double2 *)px);
+        MIDAS_CUDA(c, cudaGetLastError());
+        MIDAS_TRY(reconstruct());
     }
     cudaEventRecord(e3, c->stream);
     MIDAS_CUDA(c, cudaStreamSynchronize(c->stream));

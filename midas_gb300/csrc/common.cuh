@@ -117,7 +117,8 @@ struct KProf {
 struct LatticeFft {
     int L[3] = {0, 0, 0}, n[3] = {0, 0, 0};
     long long npts = 0;
-    double2 *G6 = nullptr;   // 6 spectra, npts each
+    double2 *G6 = nullptr;   // 6 spectra of the FP64 dyads, npts each
+    double2 *G6c4 = nullptr; // 6 spectra of the complex(4)-rounded dyads
     int *lo = nullptr;       // lattice lower corner (device copy)
     long long version = -1;  // cells version the spectra belong to
 };
@@ -214,11 +215,11 @@ int to_device(midas_gpu_ctx *ctx, const void *p, size_t bytes, int slot, const v
 int check_flag(midas_gpu_ctx *ctx, const char *where);
 
 // Lattice FFT operator (fft.cu): Y = Z X, or Y = B - Z X when B is given.
-int lattice_fft_prepare(midas_gpu_ctx *c);
+int lattice_fft_prepare(midas_gpu_ctx *c, bool c4 = false);
 bool lattice_fft_fits(const midas_gpu_ctx *c);   // cells on a lattice of <= 256 cells per axis
 void lattice_fft_release(midas_gpu_ctx *c);
 int lattice_matvec(midas_gpu_ctx *c, int nrhs, const double2 *X, long long ldx, const double2 *B, long long ldb,
-                   double2 *Y, long long ldy, int slot);
+                   double2 *Y, long long ldy, int slot, bool c4 = false);
 
 // Restarted GMRES on the lattice operator (krylov.cu); X holds the initial guess.
 int gmres_lattice(midas_gpu_ctx *c, int ncol, const double2 *B, double2 *X, int restart, int maxit, double tol,
@@ -241,7 +242,7 @@ enum Slot : int {
     S_IN0 = 0, S_IN1, S_IN2, S_IN3, S_IN4, S_IN5, S_OUT0, S_OUT1,
     S_Z32, S_Z64, S_LINV, S_UINV, S_BEXP, S_BEXP2, S_RHS64, S_X64, S_R64, S_T32, S_T32B, S_RED,
     S_CBF0, S_CBF1, S_CBF2, S_CBF3, S_CBF4, S_CBF5, S_CBF6, S_CBF7, S_CBF8, S_CBF9, S_RED2, S_EINC,
-    S_ACA, S_SOLVE, S_CSR, S_RPART, S_H16, S_HEEV, S_ZDF, S_QWS, S_SPH, S_LFFT, S_KRYLOV, S_PREP, S_NSLOTS
+    S_ACA, S_SOLVE, S_CSR, S_RPART, S_H16, S_HEEV, S_ZDF, S_QWS, S_SPH, S_LFFT, S_KRYLOV, S_PREP, S_CREF, S_NSLOTS
 };
 
 }  // namespace midas

@@ -873,7 +873,7 @@ int zgesv_fp64(midas_gpu_ctx *c, int n, int nrhs, double2 *A, double2 *B, midas_
 // Mixed solve of a system whose FP64 row-major matrix Z64 and complex64 copy Z32
 // (np x np, padded) are already in the pool slots; b/x are np x nrhs (ld np).
 int mixed_solve(midas_gpu_ctx *c, int np, float2 *Z32, double2 *Z64, const double2 *b, double2 *x,
-                              int nrhs, midas_gpu_info *info)
+                              int nrhs, midas_gpu_info *info, DenseLU *lu_out)
 {
     DenseLU lu;
     lu.n = np;
@@ -887,6 +887,7 @@ int mixed_solve(midas_gpu_ctx *c, int np, float2 *Z32, double2 *Z64, const doubl
     int st = ir_solve(c, lu, Z64, np, b, x, nrhs, info);
     float tsol = ts.stop();
     if (info) { info->t_factor_ms = tfac; info->t_solve_ms = tsol; }
+    if (lu_out) *lu_out = lu;
     return st;
 }
 

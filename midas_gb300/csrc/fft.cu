@@ -166,7 +166,7 @@ static int fft3(midas_gpu_ctx *c, double2 *data, long long gstride, int ngrids, 
 // dyad components on the circular offset grid: offset (di, dj, dk) at index
 // (di mod L0, dj mod L1, dk mod L2) for |d| < n per axis, zero elsewhere and at 0
 __global__ void k_dyad_grid(int L0, int L1, int L2, int n0, int n1, int n2, double d, double k0, double Pi,
-                            double2 *G6, long long gstride)
+                            int c4, double2 *G6, long long gstride)
 {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const long long tot = (long long)L0 * L1 * L2;
@@ -177,6 +177,11 @@ __global__ void k_dyad_grid(int L0, int L1, int L2, int n0, int n1, int n2, doub
     if ((di == 0 && dj == 0 && dk == 0) || abs(di) >= n0 || abs(dj) >= n1 || abs(dk) >= n2) {
 #pragma unroll
         for (int q = 0; q < 6; ++q) F[q] = make_double2(0, 0);
+    } else if (c4) {
+        float2 F4[6];
+        dyadF4(di * d, dj * d, dk * d, k0, Pi, F4);
+#pragma unroll
+        for (int q = 0; q < 6; ++q) F[q] = make_double2(F4[q].x, F4[q].y);
     } else {
         dyadF8(di * d, dj * d, dk * d, k0, Pi, F);
     }
@@ -186,14 +191,15 @@ __global__ void k_dyad_grid(int L0, int L1, int L2, int n0, int n1, int n2, doub
 
 // w_q = kc_s x_{3s+q} scattered into three zeroed grids per column
 __global__ void k_lat_scatter(int ncell, const int *ijk, const int *lo, int L0, int L1, const double2 *fk8,
-                              const double2 *X, long long ldx, int col0, double2 *grids, long long gstride)
+                              const float2 *fk4, const double2 *X, long long ldx, int col0, double2 *grids,
+                              long long gstride)
 {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= ncell) return;
     const int col = col0 + blockIdx.y;
     const long long gi = ((long long)(ijk[3 * s + 2] - lo[2]) * L1 + (ijk[3 * s + 1] - lo[1])) * L0 +
                          (ijk[3 * s] - lo[0]);
-    const double2 f = fk8[s];
+    const double2 f = fk4 ? make_double2(fk4[s].x, fk4[s].y) : fk8[s];
     double2 *g = grids + (long long)blockIdx.y * 3 * gstride;
 #pragma unroll
     for (int q = 0; q < 3; ++q) g[q * gstride + gi] = cmul(f, X[(long long)col * ldx + 3 * s + q]);
@@ -261,33 +267,39 @@ bool lattice_fft_fits(const midas_gpu_ctx *c)
     return true;
 }
 
-// Lattice FFT set-up of the current cells: grid sizes, dyad spectra (6 grids).
-int lattice_fft_prepare(midas_gpu_ctx *c)
+// Lattice FFT set-up of the current cells: grid sizes and the dyad spectra (6
+// grids) -- FP64 dyads (the MoM element) or, with c4, the complex(4)-rounded
+// dyads of Green_s_tr_partial (src/Green_functions.f90:139-157).
+int lattice_fft_prepare(midas_gpu_ctx *c, bool c4)
 {
     if (!c->lattice || !c->lat_ijk) return c->err.set(MIDAS_ERR_UNSUPPORTED, "lattice fft: cells are not on a lattice");
-    if (c->lfft.G6 && c->lfft.version == c->cells_version) return MIDAS_OK;
     LatticeFft &f = c->lfft;
+    if (f.version != c->cells_version) {   // new cells: both spectra sets are stale
+        if (f.G6) cudaFree(f.G6);
+        if (f.G6c4) cudaFree(f.G6c4);
+        f.G6 = f.G6c4 = nullptr;
+    }
+    if (c4 ? f.G6c4 : f.G6) return MIDAS_OK;
     for (int a = 0; a < 3; ++a) {
         f.n[a] = c->lat_hi[a] - c->lat_lo[a] + 1;
         f.L[a] = next_pow2(2 * f.n[a] - 1);
         if (f.L[a] > FFT_LMAX) return c->err.set(MIDAS_ERR_UNSUPPORTED, "lattice fft: lattice wider than 256 cells along an axis");
     }
     f.npts = (long long)f.L[0] * f.L[1] * f.L[2];
-    if (f.G6) cudaFree(f.G6);
-    f.G6 = nullptr;
     if (!f.lo) MIDAS_CUDA(c, cudaMalloc(&f.lo, sizeof(int) * 4));
     MIDAS_CUDA(c, cudaMemcpyAsync(f.lo, c->lat_lo, sizeof(int) * 3, cudaMemcpyHostToDevice, c->stream));
-    MIDAS_CUDA(c, cudaMalloc(&f.G6, sizeof(double2) * 6 * (size_t)f.npts));
+    double2 *&G = c4 ? f.G6c4 : f.G6;
+    MIDAS_CUDA(c, cudaMalloc(&G, sizeof(double2) * 6 * (size_t)f.npts));
     const double2 *tw;
     MIDAS_TRY(twiddles(c, &tw));
     ++c->launches;
     k_dyad_grid<<<(unsigned)((f.npts + 255) / 256), 256, 0, c->stream>>>(f.L[0], f.L[1], f.L[2], f.n[0], f.n[1],
-                                                                          f.n[2], c->lat_d, c->k0, c->pi, f.G6,
-                                                                          f.npts);
+                                                                          f.n[2], c->lat_d, c->k0, c->pi, c4 ? 1 : 0,
+                                                                          G, f.npts);
     MIDAS_CUDA(c, cudaGetLastError());
     // the dyad grid is nonzero over the whole circular grid: full transforms
     const int full[3] = {f.L[0], f.L[1], f.L[2]};
-    MIDAS_TRY(fft3(c, f.G6, f.npts, 6, f.L, full, -1, tw));
+    MIDAS_TRY(fft3(c, G, f.npts, 6, f.L, full, -1, tw));
     f.version = c->cells_version;
     return MIDAS_OK;
 }
@@ -295,16 +307,19 @@ int lattice_fft_prepare(midas_gpu_ctx *c)
 void lattice_fft_release(midas_gpu_ctx *c)
 {
     if (c->lfft.G6) cudaFree(c->lfft.G6);
+    if (c->lfft.G6c4) cudaFree(c->lfft.G6c4);
     if (c->lfft.lo) cudaFree(c->lfft.lo);
     c->lfft = LatticeFft();
 }
 
 // Y = Z X (B == nullptr) or Y = B - Z X, for nrhs columns (column-major, FP64;
 // rows 3 * ncell of each column are read / written).  Scratch from `slot`.
+// c4: the matrix of Green_s_tr_partial (complex(4)-rounded dyads and f_kapChe,
+// their products formed in FP64) instead of the FP64 MoM element.
 int lattice_matvec(midas_gpu_ctx *c, int nrhs, const double2 *X, long long ldx, const double2 *B, long long ldb,
-                   double2 *Y, long long ldy, int slot)
+                   double2 *Y, long long ldy, int slot, bool c4)
 {
-    MIDAS_TRY(lattice_fft_prepare(c));
+    MIDAS_TRY(lattice_fft_prepare(c, c4));
     LatticeFft &f = c->lfft;
     const double2 *tw;
     MIDAS_TRY(twiddles(c, &tw));
@@ -322,12 +337,13 @@ int lattice_matvec(midas_gpu_ctx *c, int nrhs, const double2 *X, long long ldx, 
         MIDAS_CUDA(c, cudaMemsetAsync(grids, 0, per_col * nb, c->stream));
         const dim3 grd((unsigned)((ncell + 127) / 128), (unsigned)nb);
         ++c->launches;
-        k_lat_scatter<<<grd, 128, 0, c->stream>>>(ncell, c->lat_ijk, f.lo, f.L[0], f.L[1], c->fk8, X, ldx, col0,
-                                                  grids, f.npts);
+        k_lat_scatter<<<grd, 128, 0, c->stream>>>(ncell, c->lat_ijk, f.lo, f.L[0], f.L[1], c->fk8,
+                                                  c4 ? c->fk4 : nullptr, X, ldx, col0, grids, f.npts);
         MIDAS_CUDA(c, cudaGetLastError());
         MIDAS_TRY(fft3(c, grids, f.npts, 3 * nb, f.L, f.n, -1, tw));
         ++c->launches;
-        k_lat_pointwise<<<(unsigned)((f.npts + 127) / 128), 128, 0, c->stream>>>(f.npts, f.G6, f.npts, grids, nb);
+        k_lat_pointwise<<<(unsigned)((f.npts + 127) / 128), 128, 0, c->stream>>>(f.npts, c4 ? f.G6c4 : f.G6, f.npts,
+                                                                                  grids, nb);
         MIDAS_CUDA(c, cudaGetLastError());
         MIDAS_TRY(fft3(c, grids, f.npts, 3 * nb, f.L, f.n, +1, tw));
         ++c->launches;

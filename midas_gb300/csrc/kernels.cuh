@@ -46,18 +46,6 @@ int csr_from_dense(midas_gpu_ctx *c, int n, const float2 *Z, long long ldz, int 
 int residual_csr_df32(midas_gpu_ctx *c, const Csr &Z, int m, const float2 *Xh_rm, const float2 *Xl_rm,
                       const float2 *B, double2 *R);
 int residual_csr_update_f32(midas_gpu_ctx *c, const Csr &Z, int m, const float2 *D_rm, double2 *R);
-// sparse.cu: 3 x 3 cell-pair block form of the thresholded block (nc block rows
-// over the cells; rows [3 nc, n) are identity padding)
-struct Bsr3 {
-    int nc = 0, n = 0;
-    long long nb = 0, nnz = 0;   // stored blocks; nonzero entries (0 = not counted)
-    int *bptr = nullptr, *bcol = nullptr;
-    float2 *bval = nullptr;      // 9 complex values per block, row-major inside the block
-};
-int bsr3_from_dense(midas_gpu_ctx *c, int nc, int n, const float2 *Z, long long ldz, int slot, Bsr3 *out);
-int residual_bsr_df32(midas_gpu_ctx *c, const Bsr3 &Z, int m, const float2 *Xh_rm, const float2 *Xl_rm,
-                      const float2 *B, double2 *R);
-int residual_bsr_update_f32(midas_gpu_ctx *c, const Bsr3 &Z, int m, const float2 *D_rm, double2 *R);
 
 // fill.cu
 int launch_set_cells(midas_gpu_ctx *c);
@@ -148,7 +136,7 @@ void destroy_cusolver(void *h);
 int mixed_solve_lattice(midas_gpu_ctx *c, int np, float2 *Z32, const double2 *b, double2 *x, int nrhs,
                         midas_gpu_info *info);
 int mixed_solve(midas_gpu_ctx *c, int np, float2 *Z32, double2 *Z64, const double2 *b, double2 *x, int nrhs,
-                midas_gpu_info *info);
+                midas_gpu_info *info, DenseLU *lu_out = nullptr);
 
 // refinement residuals on the FP32 cores (resid.cu)
 size_t resid_scratch_bytes(int n, int nrhs);   // slot S_RPART

@@ -251,322 +251,4 @@ int residual_csr_update_f32(midas_gpu_ctx *c, const Csr &Z, int m, const float2 
     return MIDAS_OK;
 }
 
-// ---------------------------------------------------------------------------
-// 3 x 3 block form (BSR3) of the thresholded extended-block matrix.  The unknowns
-// of one cell are three consecutive rows / columns, so the matrix is a grid of
-// cell-pair blocks.  A block is stored (column cell, 9 complex values, zeros kept)
-// when any of its 9 entries survives the threshold; nc block rows cover the cells
-// and rows [3 nc, n) are the identity padding of the factorised matrix.  The
-// residual kernels below take a warp per cell (3 output rows): each X row they
-// load serves the three rows, and the per-entry work is only the arithmetic.
-// ---------------------------------------------------------------------------
-__global__ void k_bsr_count(int nc, const float2 *Z, long long ldz, int *cnt, unsigned long long *nnz)
-{
-    const int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (r >= nc) return;
-    const float2 *z0 = Z + (long long)(3 * r) * ldz;
-    int c = 0, ne = 0;
-    for (int cb = lane; cb < nc; cb += 32) {
-        int k = 0;
-#pragma unroll
-        for (int p = 0; p < 3; ++p)
-#pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                const float2 v = z0[(long long)p * ldz + 3 * cb + q];
-                k += (v.x != 0.f || v.y != 0.f);
-            }
-        c += k > 0;
-        ne += k;
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-        c += __shfl_down_sync(0xffffffffu, c, o);
-        ne += __shfl_down_sync(0xffffffffu, ne, o);
-    }
-    if (lane == 0) {
-        cnt[r] = c;
-        atomicAdd(nnz, (unsigned long long)ne);
-    }
-}
-
-// block columns ascending within a block row; values row-major inside a block
-__global__ void k_bsr_fill(int nc, const float2 *Z, long long ldz, const int *bptr, int *bcol, float2 *bval)
-{
-    const int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (r >= nc) return;
-    const float2 *z0 = Z + (long long)(3 * r) * ldz;
-    int pos = bptr[r];
-    for (int c0 = 0; c0 < nc; c0 += 32) {
-        const int cb = c0 + lane;
-        float2 v[9];
-        bool nz = false;
-#pragma unroll
-        for (int e = 0; e < 9; ++e) {
-            v[e] = cb < nc ? z0[(long long)(e / 3) * ldz + 3 * cb + e % 3] : make_float2(0.f, 0.f);
-            nz |= (v[e].x != 0.f || v[e].y != 0.f);
-        }
-        const unsigned mk = __ballot_sync(0xffffffffu, nz);
-        if (nz) {
-            const int pb = pos + __popc(mk & ((1u << lane) - 1u));
-            bcol[pb] = cb;
-#pragma unroll
-            for (int e = 0; e < 9; ++e) bval[(long long)pb * 9 + e] = v[e];
-        }
-        pos += __popc(mk);
-    }
-}
-
-int bsr3_from_dense(midas_gpu_ctx *c, int nc, int n, const float2 *Z, long long ldz, int slot, Bsr3 *out)
-{
-    void *p;
-    MIDAS_TRY(ensure(c, S_RED, sizeof(int) * ((size_t)2 * nc + 16), &p));
-    unsigned long long *d_nnz = (unsigned long long *)p;
-    int *cnt = (int *)p + 4, *bp_tmp = cnt + nc + 4;
-    const unsigned blocks = (unsigned)(((long long)nc * 32 + 255) / 256);
-    MIDAS_CUDA(c, cudaMemsetAsync(d_nnz, 0, sizeof(unsigned long long), c->stream));
-    ++c->launches;
-    k_bsr_count<<<blocks, 256, 0, c->stream>>>(nc, Z, ldz, cnt, d_nnz);
-    ++c->launches;
-    k_scan_rowptr<<<1, 1024, 0, c->stream>>>(nc, cnt, bp_tmp);
-    MIDAS_CUDA(c, cudaGetLastError());
-    int nb = 0;
-    unsigned long long nnz = 0;
-    MIDAS_CUDA(c, cudaMemcpyAsync(&nb, bp_tmp + nc, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-    MIDAS_CUDA(c, cudaMemcpyAsync(&nnz, d_nnz, sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->stream));
-    MIDAS_CUDA(c, cudaStreamSynchronize(c->stream));
-    if (nb < 0) return c->err.set(MIDAS_ERR_UNSUPPORTED, "bsr3: more than 2^31 blocks");
-    const size_t bp_bytes = ((sizeof(int) * ((size_t)nc + 1)) + 255) & ~(size_t)255;
-    const size_t col_bytes = ((sizeof(int) * (size_t)nb) + 255) & ~(size_t)255;
-    MIDAS_TRY(ensure(c, slot, bp_bytes + col_bytes + sizeof(float2) * 9 * (size_t)nb, &p));
-    out->nc = nc;
-    out->n = n;
-    out->nb = nb;
-    out->bptr = (int *)p;
-    out->bcol = (int *)((char *)p + bp_bytes);
-    out->bval = (float2 *)((char *)p + bp_bytes + col_bytes);
-    MIDAS_CUDA(c, cudaMemcpyAsync(out->bptr, bp_tmp, sizeof(int) * ((size_t)nc + 1), cudaMemcpyDeviceToDevice,
-                                  c->stream));
-    ++c->launches;
-    k_bsr_fill<<<blocks, 256, 0, c->stream>>>(nc, Z, ldz, out->bptr, out->bcol, out->bval);
-    MIDAS_CUDA(c, cudaGetLastError());
-    out->nnz = (long long)nnz;   // nonzero entries: the algorithmic counts of the residual kernels
-    return MIDAS_OK;
-}
-
-constexpr int BSR_T = 3;                 // right-hand-side columns per lane
-constexpr int BSR_COLS = 32 * BSR_T;     // columns per warp pass (blockIdx.y selects the group)
-constexpr int BSR_STAGE = 16;            // blocks staged in shared memory per warp
-constexpr int BSR_WARPS = 8;
-
-// (hi, lo) += a (bh + bl): the product with bh exactly (FMA residue, TwoSum into
-// hi), the product with bl (2^-24 smaller) in FP32 into lo.
-__device__ __forceinline__ void df_axpy(float &hi, float &lo, float a, float bh, float bl)
-{
-    const float p = __fmul_rn(a, bh);
-    const float pe = fmaf(a, bh, -p);
-    float s, e;
-    ef_two_sum(hi, p, s, e);
-    hi = s;
-    lo = fmaf(a, bl, __fadd_rn(lo, __fadd_rn(e, pe)));
-}
-
-// r = B - Z (Xh + Xl), Z in BSR3 form.  Xh, Xl row-major (n x m), B column-major
-// float (ld n), R column-major FP64 (ld n).  Warp per block row; lanes over
-// BSR_COLS right-hand sides.
-__global__ void __launch_bounds__(BSR_WARPS * 32) k_resid_bsr_df32(int nc, int n, int m, const int *bptr,
-                                                                   const int *bcol, const float2 *bval,
-                                                                   const float2 *Xh, const float2 *Xl,
-                                                                   const float2 *B, double2 *R)
-{
-    __shared__ float2 sz[BSR_WARPS][BSR_STAGE * 9];
-    __shared__ int sk[BSR_WARPS][BSR_STAGE];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int r = blockIdx.x * BSR_WARPS + warp;
-    const int npad = (n - 3 * nc + 2) / 3;
-    if (r >= nc + npad) return;
-    const int c0 = blockIdx.y * BSR_COLS;
-    if (r >= nc) {   // identity rows of the padding
-#pragma unroll
-        for (int p = 0; p < 3; ++p) {
-            const int row = 3 * r + p;
-            if (row >= n) break;
-#pragma unroll
-            for (int t = 0; t < BSR_T; ++t) {
-                const int cc = c0 + lane + 32 * t;
-                if (cc < m) {
-                    const float2 b = B[(long long)cc * n + row];
-                    const float2 h = Xh[(long long)row * m + cc], l = Xl[(long long)row * m + cc];
-                    R[(long long)cc * n + row] = make_double2(((double)b.x - h.x) - l.x, ((double)b.y - h.y) - l.y);
-                }
-            }
-        }
-        return;
-    }
-    float rh[3][BSR_T], rl[3][BSR_T], ih[3][BSR_T], il[3][BSR_T];
-#pragma unroll
-    for (int p = 0; p < 3; ++p)
-#pragma unroll
-        for (int t = 0; t < BSR_T; ++t) rh[p][t] = rl[p][t] = ih[p][t] = il[p][t] = 0.f;
-    bool live[BSR_T];
-#pragma unroll
-    for (int t = 0; t < BSR_T; ++t) live[t] = c0 + lane + 32 * t < m;
-    const int p1 = bptr[r + 1];
-    for (int p0 = bptr[r]; p0 < p1; p0 += BSR_STAGE) {
-        const int cnt = min(BSR_STAGE, p1 - p0);
-        __syncwarp();
-        for (int e = lane; e < cnt * 9; e += 32) sz[warp][e] = bval[(long long)p0 * 9 + e];
-        if (lane < cnt) sk[warp][lane] = bcol[p0 + lane];
-        __syncwarp();
-        for (int q = 0; q < cnt; ++q) {
-            const int k = sk[warp][q];
-            float2 xh[3][BSR_T], xl[3][BSR_T];
-#pragma unroll
-            for (int b = 0; b < 3; ++b) {
-                const long long o = (long long)(3 * k + b) * m + c0 + lane;
-#pragma unroll
-                for (int t = 0; t < BSR_T; ++t) {
-                    xh[b][t] = live[t] ? Xh[o + 32 * t] : make_float2(0.f, 0.f);
-                    xl[b][t] = live[t] ? Xl[o + 32 * t] : make_float2(0.f, 0.f);
-                }
-            }
-#pragma unroll
-            for (int e = 0; e < 9; ++e) {
-                const float2 z = sz[warp][q * 9 + e];
-                if (z.x == 0.f && z.y == 0.f) continue;   // warp-uniform: dropped entry of the block
-                const int a = e / 3, b = e % 3;
-#pragma unroll
-                for (int t = 0; t < BSR_T; ++t) {
-                    df_axpy(rh[a][t], rl[a][t], z.x, xh[b][t].x, xl[b][t].x);
-                    df_axpy(rh[a][t], rl[a][t], -z.y, xh[b][t].y, xl[b][t].y);
-                    df_axpy(ih[a][t], il[a][t], z.x, xh[b][t].y, xl[b][t].y);
-                    df_axpy(ih[a][t], il[a][t], z.y, xh[b][t].x, xl[b][t].x);
-                }
-            }
-        }
-    }
-#pragma unroll
-    for (int p = 0; p < 3; ++p)
-#pragma unroll
-        for (int t = 0; t < BSR_T; ++t) {
-            const int cc = c0 + lane + 32 * t;
-            if (cc < m) {
-                const int row = 3 * r + p;
-                const float2 b = B[(long long)cc * n + row];
-                const double zr = (double)rh[p][t] + (double)rl[p][t];
-                const double zi = (double)ih[p][t] + (double)il[p][t];
-                R[(long long)cc * n + row] = make_double2((double)b.x - zr, (double)b.y - zi);
-            }
-        }
-}
-
-// r -= Z d in FP32 (the refinement's residual update), Z in BSR3 form; d
-// row-major (n x m), r column-major FP64.  Padding rows: r -= d.
-__global__ void __launch_bounds__(BSR_WARPS * 32) k_bsr_sub_f32(int nc, int n, int m, const int *bptr,
-                                                                const int *bcol, const float2 *bval,
-                                                                const float2 *D, double2 *R)
-{
-    __shared__ float2 sz[BSR_WARPS][BSR_STAGE * 9];
-    __shared__ int sk[BSR_WARPS][BSR_STAGE];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int r = blockIdx.x * BSR_WARPS + warp;
-    const int npad = (n - 3 * nc + 2) / 3;
-    if (r >= nc + npad) return;
-    const int c0 = blockIdx.y * BSR_COLS;
-    if (r >= nc) {
-#pragma unroll
-        for (int p = 0; p < 3; ++p) {
-            const int row = 3 * r + p;
-            if (row >= n) break;
-#pragma unroll
-            for (int t = 0; t < BSR_T; ++t) {
-                const int cc = c0 + lane + 32 * t;
-                if (cc < m) {
-                    const float2 d = D[(long long)row * m + cc];
-                    double2 *o = R + (long long)cc * n + row;
-                    *o = make_double2(o->x - (double)d.x, o->y - (double)d.y);
-                }
-            }
-        }
-        return;
-    }
-    float ar[3][BSR_T], ai[3][BSR_T];
-#pragma unroll
-    for (int p = 0; p < 3; ++p)
-#pragma unroll
-        for (int t = 0; t < BSR_T; ++t) ar[p][t] = ai[p][t] = 0.f;
-    bool live[BSR_T];
-#pragma unroll
-    for (int t = 0; t < BSR_T; ++t) live[t] = c0 + lane + 32 * t < m;
-    const int p1 = bptr[r + 1];
-    for (int p0 = bptr[r]; p0 < p1; p0 += BSR_STAGE) {
-        const int cnt = min(BSR_STAGE, p1 - p0);
-        __syncwarp();
-        for (int e = lane; e < cnt * 9; e += 32) sz[warp][e] = bval[(long long)p0 * 9 + e];
-        if (lane < cnt) sk[warp][lane] = bcol[p0 + lane];
-        __syncwarp();
-        for (int q = 0; q < cnt; ++q) {
-            const int k = sk[warp][q];
-            float2 d[3][BSR_T];
-#pragma unroll
-            for (int b = 0; b < 3; ++b) {
-                const long long o = (long long)(3 * k + b) * m + c0 + lane;
-#pragma unroll
-                for (int t = 0; t < BSR_T; ++t) d[b][t] = live[t] ? D[o + 32 * t] : make_float2(0.f, 0.f);
-            }
-#pragma unroll
-            for (int e = 0; e < 9; ++e) {
-                const float2 z = sz[warp][q * 9 + e];
-                const int a = e / 3, b = e % 3;
-#pragma unroll
-                for (int t = 0; t < BSR_T; ++t) {
-                    ar[a][t] = fmaf(z.x, d[b][t].x, fmaf(-z.y, d[b][t].y, ar[a][t]));
-                    ai[a][t] = fmaf(z.x, d[b][t].y, fmaf(z.y, d[b][t].x, ai[a][t]));
-                }
-            }
-        }
-    }
-#pragma unroll
-    for (int p = 0; p < 3; ++p)
-#pragma unroll
-        for (int t = 0; t < BSR_T; ++t) {
-            const int cc = c0 + lane + 32 * t;
-            if (cc < m) {
-                double2 *o = R + (long long)cc * n + 3 * r + p;
-                *o = make_double2(o->x - (double)ar[p][t], o->y - (double)ai[p][t]);
-            }
-        }
-}
-
-static dim3 bsr_grid(const Bsr3 &Z, int m)
-{
-    const int rows = Z.nc + (Z.n - 3 * Z.nc + 2) / 3;
-    return dim3((unsigned)((rows + BSR_WARPS - 1) / BSR_WARPS), (unsigned)((m + BSR_COLS - 1) / BSR_COLS));
-}
-
-int residual_bsr_df32(midas_gpu_ctx *c, const Bsr3 &Z, int m, const float2 *Xh_rm, const float2 *Xl_rm,
-                      const float2 *B, double2 *R)
-{
-    ++c->launches;
-    int kp = kp_begin(c);
-    k_resid_bsr_df32<<<bsr_grid(Z, m), BSR_WARPS * 32, 0, c->stream>>>(Z.nc, Z.n, m, Z.bptr, Z.bcol, Z.bval, Xh_rm,
-                                                                       Xl_rm, B, R);
-    // algorithmic work: the stored blocks' 9 entries (dropped entries are skipped, not counted)
-    const double nnz = Z.nnz > 0 ? (double)Z.nnz : 9.0 * (double)Z.nb;
-    kp_end(c, kp, MIDAS_KC_RESID, 8.0 * nnz * m,
-           76.0 * (double)Z.nb + 16.0 * (double)Z.n * m + 8.0 * (double)Z.n * m + 16.0 * (double)Z.n * m);
-    MIDAS_CUDA(c, cudaGetLastError());
-    return MIDAS_OK;
-}
-
-int residual_bsr_update_f32(midas_gpu_ctx *c, const Bsr3 &Z, int m, const float2 *D_rm, double2 *R)
-{
-    ++c->launches;
-    int kp = kp_begin(c);
-    k_bsr_sub_f32<<<bsr_grid(Z, m), BSR_WARPS * 32, 0, c->stream>>>(Z.nc, Z.n, m, Z.bptr, Z.bcol, Z.bval, D_rm, R);
-    const double nnz = Z.nnz > 0 ? (double)Z.nnz : 9.0 * (double)Z.nb;
-    kp_end(c, kp, MIDAS_KC_RESID, 8.0 * nnz * m,
-           76.0 * (double)Z.nb + 8.0 * (double)Z.n * m + 32.0 * (double)Z.n * m);
-    MIDAS_CUDA(c, cudaGetLastError());
-    return MIDAS_OK;
-}
-
 }  // namespace midas
