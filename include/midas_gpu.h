@@ -204,6 +204,36 @@ enum midas_gmres_flags { MIDAS_GMRES_JACOBI = 1 };
 int midas_gpu_gmres_solve(midas_gpu_ctx *ctx, int ntr, const double *theta, const double *phi, const double *E0,
                           int restart, int maxit, double tol, int flags, double *E, midas_gpu_info *info);
 
+/* Learned initial guess for midas_gpu_gmres_solve (no counterpart in the
+ * reference).  A 3-D convolutional network on a grid^3 voxel grid (grid even,
+ * <= 128): 8 input channels per voxel -- Re, Im of chi = eps - 1 (0 outside the
+ * scatterer) and Re, Im of the three incident-field components -- and the
+ * prediction E = E_inc + mask * net(...), 6 channels (Re, Im of Ex, Ey, Ez).
+ * Four 3x3x3 convolutions (8 -> 32 -> 32 -> 32 -> 6, ReLU), fp16 operands on the
+ * tensor cores with FP32 accumulation, FP32 master weights, Adam.  Arrays are
+ * voxel-major, x fastest then y then z, one sample after another:
+ * inputs [batch][grid^3][8], mask [batch][grid^3] (1 inside, 0 outside), target
+ * and E [batch][grid^3][6]; host or device memory.  batch <= 64 and
+ * batch * grid^3 <= 2^22.  Parameters are laid out layer by layer, weights
+ * [cout][27 taps (dz, dy, dx = -1..1, dx fastest)][cin] then biases [cout], with
+ * the last layer's cout padded to 8 (rows 6, 7 stay zero). */
+typedef struct midas_gpu_nn midas_gpu_nn;
+int midas_gpu_nn_create(midas_gpu_ctx *ctx, int grid, unsigned long long seed, midas_gpu_nn **net);
+int midas_gpu_nn_free(midas_gpu_nn *net);
+long long midas_gpu_nn_param_count(const midas_gpu_nn *net);
+/* set = 0 reads the parameters (grads = 1: the gradients of the last
+ * midas_gpu_nn_gradients / train_step) into buf; set = 1 writes them. */
+int midas_gpu_nn_params(midas_gpu_ctx *ctx, midas_gpu_nn *net, int set, float *buf, int grads);
+int midas_gpu_nn_forward(midas_gpu_ctx *ctx, midas_gpu_nn *net, int batch, const float *inputs, const float *mask,
+                         float *E);
+/* Loss L = mean over the batch of sum(mask |E_pred - target|^2) / sum(mask |target|^2)
+ * and the gradient of every parameter (read them with midas_gpu_nn_params). */
+int midas_gpu_nn_gradients(midas_gpu_ctx *ctx, midas_gpu_nn *net, int batch, const float *inputs, const float *mask,
+                           const float *target, double *loss);
+/* One Adam step (beta 0.9 / 0.999, eps 1e-8) at learning rate lr on that loss. */
+int midas_gpu_nn_train_step(midas_gpu_ctx *ctx, midas_gpu_nn *net, int batch, const float *inputs, const float *mask,
+                            const float *target, float lr, double *loss);
+
 /* Plain MoM: fill, solve, internal field E (3n x 2ntr).  The field part of
  * Compute_EFields_MoM (src/Compute_EFields_MoM.f90:66-229). */
 int midas_gpu_mom_solve(midas_gpu_ctx *ctx, int ntr, const double *theta, const double *phi, double *E,
@@ -358,7 +388,8 @@ int midas_gpu_record_event(midas_gpu_ctx *ctx, void *event);
 #define MIDAS_KC_GEMM_PROD  12  /* tcgen05 GEMM: split-TF32 products (reduced matrix, FP32-grade ZGEMM) */
 #define MIDAS_KC_SPLIT      13  /* split-TF32 operand preparation (hi / lo pieces) */
 #define MIDAS_KC_LATTICE   14  /* FFT lattice operator (scatter, FFTs, spectral product, gather) */
-#define MIDAS_KC_COUNT     15
+#define MIDAS_KC_NN        15  /* tcgen05 GEMMs of the learned initial guess's convolutions */
+#define MIDAS_KC_COUNT     16
 /* enable = 1 clears the per-class totals and starts timing every instrumented
  * launch with CUDA events on the context stream; 0 stops.  Timing adds one event
  * record before and after each instrumented launch. */

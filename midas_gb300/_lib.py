@@ -25,7 +25,7 @@ GMRES_JACOBI = 1
 QUAD = {"un": 0, "tr": 1, "gl": 2, "sd": 3, "lb": 4, "rf": 5}
 # kernel classes of midas_gpu_profile_query (MIDAS_KC_* in the header)
 KCLASSES = ["gemm_trail", "gemm_simt", "fill", "sr_scan", "diag_lu", "trsv", "resid", "zgemm64", "eig", "other",
-            "gemm_panel", "gemm_solve", "gemm_prod", "split", "lattice"]
+            "gemm_panel", "gemm_solve", "gemm_prod", "split", "lattice", "nn"]
 
 # every symbol the header declares (checked by the CPU tests)
 EXPORTS = [
@@ -34,7 +34,9 @@ EXPORTS = [
     "midas_gpu_incident_field_spherical", "midas_gpu_voxelise_sphere", "midas_gpu_voxelise_spheres",
     "midas_gpu_box_partition", "midas_gpu_extend_blocks",
     "midas_gpu_block_fill", "midas_gpu_sr_fill", "midas_gpu_set_fsr", "midas_gpu_aca", "midas_gpu_dense_solve",
-    "midas_gpu_mom_solve", "midas_gpu_lattice_matvec", "midas_gpu_gmres_solve", "midas_gpu_cbfm_solve", "midas_gpu_dense_solve_noalloc", "midas_gpu_cext_cabs", "midas_gpu_smatrix",
+    "midas_gpu_mom_solve", "midas_gpu_lattice_matvec", "midas_gpu_gmres_solve", "midas_gpu_nn_create", "midas_gpu_nn_free",
+    "midas_gpu_nn_param_count", "midas_gpu_nn_params", "midas_gpu_nn_forward", "midas_gpu_nn_gradients",
+    "midas_gpu_nn_train_step", "midas_gpu_cbfm_solve", "midas_gpu_dense_solve_noalloc", "midas_gpu_cext_cabs", "midas_gpu_smatrix",
     "midas_gpu_scattering_quantities", "midas_gpu_wait_event", "midas_gpu_record_event",
     "midas_gpu_gemm_selftest", "midas_gpu_gemm_engine", "midas_gpu_wait_selftest", "midas_gpu_launch_count", "midas_gpu_stream",
     "midas_gpu_bench_gemm", "midas_gpu_bench_gemm_ex", "midas_gpu_heev", "midas_gpu_zgemm_x3", "midas_gpu_profile", "midas_gpu_profile_query",
@@ -103,6 +105,13 @@ def load(path: str = LIB_PATH):
         "midas_gpu_mom_solve": (i, [vp, i, P, P, P, ctypes.POINTER(Info)]),
         "midas_gpu_lattice_matvec": (i, [vp, i, P, P]),
         "midas_gpu_gmres_solve": (i, [vp, i, P, P, P, i, i, d, i, P, ctypes.POINTER(Info)]),
+        "midas_gpu_nn_create": (i, [vp, i, ctypes.c_ulonglong, ctypes.POINTER(vp)]),
+        "midas_gpu_nn_free": (i, [vp]),
+        "midas_gpu_nn_param_count": (ctypes.c_longlong, [vp]),
+        "midas_gpu_nn_params": (i, [vp, vp, i, P, i]),
+        "midas_gpu_nn_forward": (i, [vp, vp, i, P, P, P]),
+        "midas_gpu_nn_gradients": (i, [vp, vp, i, P, P, P, ctypes.POINTER(ctypes.c_double)]),
+        "midas_gpu_nn_train_step": (i, [vp, vp, i, P, P, P, ctypes.c_float, ctypes.POINTER(ctypes.c_double)]),
         "midas_gpu_dense_solve_noalloc": (i, [i, vp, i, i, P, P, ctypes.POINTER(ctypes.c_double)]),
         "midas_gpu_cbfm_solve": (i, [vp, i, P, P, P, i, P, P, d, d, i, d, i, i, P, P, P, P, ctypes.POINTER(Info)]),
         "midas_gpu_cext_cabs": (i, [vp, i, P, P, P, P, P]),

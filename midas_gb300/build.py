@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libmidas_gpu.so")
 OBJDIR = os.path.join(HERE, "_build")
-SOURCES = ["midas_gpu.cu", "fill.cu", "gemm.cu", "dense.cu", "post.cu", "cbfm.cu", "blas.cu", "noalloc.cu", "aca.cu", "sparse.cu", "resid.cu", "scatq.cu", "fft.cu", "krylov.cu", "prep.cu"]
+SOURCES = ["midas_gpu.cu", "fill.cu", "gemm.cu", "dense.cu", "post.cu", "cbfm.cu", "blas.cu", "noalloc.cu", "aca.cu", "sparse.cu", "resid.cu", "scatq.cu", "fft.cu", "krylov.cu", "prep.cu", "nn.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 

@@ -242,7 +242,7 @@ enum Slot : int {
     S_IN0 = 0, S_IN1, S_IN2, S_IN3, S_IN4, S_IN5, S_OUT0, S_OUT1,
     S_Z32, S_Z64, S_LINV, S_UINV, S_BEXP, S_BEXP2, S_RHS64, S_X64, S_R64, S_T32, S_T32B, S_RED,
     S_CBF0, S_CBF1, S_CBF2, S_CBF3, S_CBF4, S_CBF5, S_CBF6, S_CBF7, S_CBF8, S_CBF9, S_RED2, S_EINC,
-    S_ACA, S_SOLVE, S_CSR, S_RPART, S_H16, S_HEEV, S_ZDF, S_QWS, S_SPH, S_LFFT, S_KRYLOV, S_PREP, S_CREF, S_NSLOTS
+    S_ACA, S_SOLVE, S_CSR, S_RPART, S_H16, S_HEEV, S_ZDF, S_QWS, S_SPH, S_LFFT, S_KRYLOV, S_PREP, S_CREF, S_NN, S_NSLOTS
 };
 
 }  // namespace midas
