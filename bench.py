@@ -245,10 +245,19 @@ def run_reference(args, wl, world, rank, pg):
         return 0
     from oracle import oracle as O
     O.build()
-    cells = O.Cells(wl["xyz"], wl["sc"], wl["eps"], wl["k0"])
     model, walls = [], []
     desc = None
-    for it in range(args.warmup + args.steps):
+    if wl["method"] == "batch":
+        from midas_gb300.workloads import c4_instance
+        c4cells = [c4_instance(wl, k) for k in range(len(wl["n_mono"]))]
+        for it in range(args.warmup + args.steps):
+            dt, tw, desc = c4_cpu_sample(wl, c4cells)
+            if it >= args.warmup:
+                model.append(dt / len(c4cells))   # per instance: the value below counts all instances
+                walls.append(tw)
+        wl = dict(wl, xyz=np.zeros((sum(len(x) for x, _ in c4cells), 3)))
+    cells = None if wl["method"] == "batch" else O.Cells(wl["xyz"], wl["sc"], wl["eps"], wl["k0"])
+    for it in range(0 if wl["method"] == "batch" else args.warmup + args.steps):
         t0 = time.perf_counter()
         if wl["method"] == "mom" and 3 * len(wl["xyz"]) > 20000:
             dt, _, desc = mom_cpu_sample(wl)
@@ -562,6 +571,130 @@ def check_parity(ctx, wl, fx_name, E, K):
             "ok": bool(ok)}
 
 
+def c4_cpu_sample(wl, cells):
+    """Bounded CPU sample of the C4 batch: the oracle pipeline (C fill, LAPACK
+    zgesv, S matrix, cross sections, list-rule averages) on the smallest and a
+    median instance; per-instance time modelled as a N^2 + b N^3 (fill and
+    averaging; the dense solve) through those two points and summed over all
+    instances.  Returns (modelled seconds of the batch, sample wall seconds,
+    description)."""
+    from oracle import oracle as O
+    O.build()
+    th, ph, rth, rph = wl["th"], wl["ph"], wl["rx_th"], wl["rx_ph"]
+    ntr = len(th)
+    sizes = np.array([3 * len(x) for x, _ in cells], float)
+    order = np.argsort(sizes)
+    pick = [int(order[0]), int(order[len(order) // 2])]
+    pts = []
+    t_all = time.perf_counter()
+    for k in pick:
+        xyz, d = cells[k]
+        c = O.Cells(xyz, d, wl["m"] ** 2, wl["k0"])
+        t0 = time.perf_counter()
+        r = O.mom_solve(c, th, ph, rth, rph)
+        dm = 2.0 * (3.0 * len(xyz) * d ** 3 / (4.0 * math.pi)) ** (1.0 / 3.0)
+        O.scattering_quantities("rf", "rf", (ntr, 1), (wl["nrx"], 1), th, ph, rth, rph, r["S"], r["cext"], r["cabs"],
+                                dm, wl["k0"])
+        pts.append((sizes[k], time.perf_counter() - t0))
+    wall = time.perf_counter() - t_all
+    (n0, t0), (n1, t1) = pts
+    A = np.array([[n0 ** 2, n0 ** 3], [n1 ** 2, n1 ** 3]])
+    a, b = np.linalg.solve(A, np.array([t0, t1]))
+    a, b = max(a, 0.0), max(b, 0.0)
+    T = float(np.sum(a * sizes ** 2 + b * sizes ** 3))
+    desc = (f"oracle pipeline on instances of {int(n0)} and {int(n1)} unknowns ({t0:.2f} s, {t1:.2f} s), "
+            f"per-instance time a N^2 + b N^3 through them, summed over all {len(sizes)} instances "
+            f"({int(sizes.min())}-{int(sizes.max())} unknowns)")
+    return T, wall, desc
+
+
+def run_batch_bench(args, wl, world, rank, local, pg):
+    """C4 line: all instances per step on concurrent lanes (contexts), through the
+    library's public entry points.  The per-instance inputs (cell lists of at most
+    a few hundred kB) are host arrays, so `value` already includes their copies;
+    `e2e` is the same measurement."""
+    import torch
+    from midas_gb300 import _lib
+    from midas_gb300.solver import Context
+    from midas_gb300.workloads import batch_step, c4_instance
+    torch.cuda.set_device(local)
+    cells = [c4_instance(wl, k) for k in range(len(wl["n_mono"]))]
+    ntr, n = len(wl["th"]), len(cells)
+    ctx = Context(device=local, fill_mode=_lib.FILL_FAST)
+    contexts = [ctx] + [ctx.sibling() for _ in range(args.lanes - 1)]
+    for _ in range(args.warmup):
+        batch_step(contexts, wl, cells)
+    torch.cuda.synchronize()
+    barrier(pg)
+    l0 = sum(c.launch_count() for c in contexts)
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            res = batch_step(contexts, wl, cells)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+    launches = sum(c.launch_count() for c in contexts) - l0
+    dt = allmax(pg, dt)
+    value = world * ntr * n * args.steps / dt
+    # one more step with per-kernel-class CUDA events on every lane
+    for c in contexts:
+        c.profile(True)
+    tp = time.perf_counter()
+    batch_step(contexts, wl, cells)
+    tp = time.perf_counter() - tp
+    kprof = {}
+    for c in contexts:
+        for k, v in c.profile_query().items():
+            e = kprof.setdefault(k, {"ms": 0.0, "flops": 0.0, "bytes": 0.0, "launches": 0})
+            for f in e:
+                e[f] += v[f]
+        c.profile(False)
+    peaks = load_peaks()
+    top = max(kprof, key=lambda k: kprof[k]["ms"])
+    kp = kprof[top]
+    sec = kp["ms"] * 1e-3
+    f16 = top == "gemm_trail"
+    tf_peak = peaks["bf16_tflops"] if f16 else peaks["bf16_tflops"] / 2.0
+    if top.startswith("gemm_"):
+        ach = kp["flops"] / sec / 1e12
+        roof = {"bound": "tensor", "achieved": ach, "peak": tf_peak, "unit": "TFLOP/s", "frac": ach / tf_peak}
+    else:
+        ach = kp["bytes"] / sec / 1e9
+        roof = {"bound": "hbm", "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": ach / peaks["hbm_gbs"]}
+    roof.update({"traffic": None, "kernel_class": top, "launches": kp["launches"], "peak_src": peaks["src"],
+                 "note": "class time summed over the lanes (kernels of different lanes overlap)"})
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        tc, tw, desc = c4_cpu_sample(wl, cells)
+        cpu = {"value": ntr * n / tc, "unit": "solves/s", "cores": os.cpu_count(), "kind": "port", "sample": desc,
+               "modelled_full_batch_s": tc, "sample_wall_s": tw}
+    if rank == 0:
+        sizes = [3 * len(x) for x, _ in cells]
+        acc = sum(r[0] for r in res) / n
+        line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "c64 tf32-tensor LU + f64 FFT-residual refinement",
+                "data": "synthetic (seeded fractal aggregates)",
+                "config": {"workload": wl["name"], "instances": n, "unknowns_min_max": [min(sizes), max(sizes)],
+                           "directions": ntr, "polarisations": 2, "lanes": args.lanes,
+                           "parallelism": f"replicas x{world}",
+                           "l2": "inputs larger than L2 (per-instance complex64 matrices up to 3.9 GB)"},
+                "roofline": roof, "cpu_baseline": cpu,
+                "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": int(sum(56 * len(x) for x, _ in cells)),
+                        "d2h_bytes_per_step": int(sum(16 * 2 * ntr * s for s in sizes))},
+                "gpu_launches": launches, "clocks": clk.summary(),
+                "averages": {"Q_ext": float(acc[0]), "Q_abs": float(acc[1]), "Q_sca": float(acc[2]),
+                             "g": float(acc[4])},
+                "profiled_step_s": tp,
+                "kernel_classes": {k: {"ms_per_step": v["ms"], "launches_per_step": v["launches"]}
+                                   for k, v in kprof.items()}}
+        print(json.dumps(line), flush=True)
+    for c in contexts:
+        c.close()
+    return 0
+
+
 def fp64_mom_extrapolated(local, wl, value):
     """Plain FP64 MoM (FP64 fill + cuSOLVER zgetrf/zgetrs) timed on this GPU on the
     sphere x = 2 scene (12,672 unknowns) and scaled to the workload's unknowns by
@@ -610,6 +743,7 @@ def main():
     ap.add_argument("--workload", default="cbfm_c2", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--lanes", type=int, default=4, help="concurrent contexts of a batch workload")
     ap.add_argument("--fp64-measure", action="store_true",
                     help="time the plain FP64 MoM (cuSOLVER) on the workload itself, whatever its size")
     args = ap.parse_args()
@@ -619,6 +753,8 @@ def main():
     wl = WORKLOADS[args.workload]()
     if args.impl == "reference":
         rc = run_reference(args, wl, world, rank, pg)
+    elif wl["method"] == "batch":
+        rc = run_batch_bench(args, wl, world, rank, local, pg)
     else:
         rc = run_ours(args, wl, world, rank, local, pg)
     if pg is not None:

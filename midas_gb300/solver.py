@@ -47,6 +47,12 @@ class Context:
         self.n = 0
         self.info = Info()
         self._keep = []
+        self._opts = dict(device=device, solve_mode=solve_mode, fill_mode=fill_mode, index_base=index_base,
+                          ir_tol=ir_tol, ir_max_iter=ir_max_iter, verbose=verbose)
+
+    def sibling(self):
+        """A new context with the same options (its own stream and scratch)."""
+        return Context(**self._opts)
 
     def close(self):
         if self.h:

@@ -189,7 +189,57 @@ def cbfm_args(wl):
     return bo, eo, ei
 
 
-def run_batch(ctx, wl, steps):
+def batch_instance(ctx, wl, xyz, d):
+    """One C4 aggregate through the library: MoM solve for every direction, S
+    matrix, cross sections and the list-rule orientation averages.  Returns
+    (Q averages [5], far-field <Cext>, internal-field <Cabs>)."""
+    th, ph, rth, rph = wl["th"], wl["ph"], wl["rx_th"], wl["rx_ph"]
+    ntr = len(th)
+    ctx.set_cells(xyz, d, wl["m"] ** 2, wl["k0"])
+    E = ctx.mom_solve(th, ph)
+    S = ctx.smatrix(rth, rph, E)
+    ce, ca = ctx.cext_cabs(th, ph, E)
+    dm = 2.0 * (3.0 * len(xyz) * d ** 3 / (4.0 * math.pi)) ** (1.0 / 3.0)   # volume-equivalent
+    _, qa = ctx.scattering_quantities("rf", "rf", (ntr, 1), (wl["nrx"], 1), th, ph, rth, rph, S, ce, ca, dm,
+                                      wl["k0"])
+    return qa, float(qa[0]) * math.pi * (dm / 2.0) ** 2, float(np.mean(ca))
+
+
+def batch_step(contexts, wl, cells):
+    """Every instance once, largest first, pulled by len(contexts) concurrent lanes
+    (one host thread and one context -- its own CUDA stream -- per lane).  Returns
+    the per-instance results in instance order."""
+    import threading
+    order = sorted(range(len(cells)), key=lambda k: -len(cells[k][0]))
+    out = [None] * len(cells)
+    nxt = [0]
+    lock = threading.Lock()
+    err = []
+
+    def lane(ctx):
+        while True:
+            with lock:
+                if nxt[0] >= len(order) or err:
+                    return
+                k = order[nxt[0]]
+                nxt[0] += 1
+            try:
+                out[k] = batch_instance(ctx, wl, *cells[k])
+            except Exception as e:   # reported after the lanes join
+                err.append(e)
+                return
+
+    ths = [threading.Thread(target=lane, args=(c,)) for c in contexts]
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    if err:
+        raise err[0]
+    return out
+
+
+def run_batch(ctx, wl, steps, lanes=4):
     """C4: every aggregate solved for all directions (fill, mixed LU, refinement),
     then its S matrix, Cext / Cabs and orientation averages; prints the
     orientation-averaged solves/s (directions x instances / wall time) and the
@@ -198,32 +248,24 @@ def run_batch(ctx, wl, steps):
     components before the products (Compute_ExtAbsCsec_fromIntField.f90:52-59),
     which holds only for axis-aligned incidence, and these directions are random.
     <Cabs> is the reference's internal-field value all the same (its Q_abs always
-    is)."""
+    is).  Instances run on `lanes` concurrent contexts."""
     cells = [c4_instance(wl, k) for k in range(len(wl["n_mono"]))]   # scene preparation, not timed
-    th, ph, rth, rph = wl["th"], wl["ph"], wl["rx_th"], wl["rx_ph"]
-    ntr, eps = len(th), wl["m"] ** 2
+    ntr = len(wl["th"])
     unknowns = [3 * len(x) for x, _ in cells]
+    contexts = [ctx] + [ctx.sibling() for _ in range(lanes - 1)]
     for step in range(steps):
         t0 = time.perf_counter()
-        acc = np.zeros(5)
-        cext = cabs = 0.0
-        for xyz, d in cells:
-            ctx.set_cells(xyz, d, eps, wl["k0"])
-            E = ctx.mom_solve(th, ph)
-            S = ctx.smatrix(rth, rph, E)
-            ce, ca = ctx.cext_cabs(th, ph, E)
-            dm = 2.0 * (3.0 * len(xyz) * d ** 3 / (4.0 * math.pi)) ** (1.0 / 3.0)   # volume-equivalent
-            _, qa = ctx.scattering_quantities("rf", "rf", (ntr, 1), (wl["nrx"], 1), th, ph, rth, rph, S, ce, ca,
-                                              dm, wl["k0"])
-            acc += qa
-            cext += float(qa[0]) * math.pi * (dm / 2.0) ** 2    # far-field Q_ext (cext_intfields = 0)
-            cabs += float(np.mean(ca))
+        res = batch_step(contexts, wl, cells)
         dt = time.perf_counter() - t0
         n = len(cells)
+        acc = sum(r[0] for r in res)
+        cext = sum(r[1] for r in res)
+        cabs = sum(r[2] for r in res)
         print(f"{wl['name']}: step {step} {dt:.3f} s, {ntr * n / dt:.2f} orientation-averaged solves/s "
-              f"({n} instances, {min(unknowns)}-{max(unknowns)} unknowns), <Cext> {cext / n:.5g}, "
+              f"({n} instances, {min(unknowns)}-{max(unknowns)} unknowns, {lanes} lanes), <Cext> {cext / n:.5g}, "
               f"<Cabs> {cabs / n:.5g}, <g> {acc[4] / n:.4f}", flush=True)
-    ctx.close()
+    for c in contexts:
+        c.close()
     return 0
 
 
@@ -236,6 +278,7 @@ def main(argv=None):
     ap.add_argument("--fill", default="fast", choices=["fast", "faithful"])
     ap.add_argument("--verbose", "-v", action="count", default=0,
                     help="library trace: -v refinement steps and CBFM lanes, -vv per-block detail")
+    ap.add_argument("--lanes", type=int, default=4, help="concurrent contexts of the C4 batch")
     ap.add_argument("--classes", action="store_true",
                     help="after the steps, one more step with per-kernel-class CUDA-event timing (one lane)")
     args = ap.parse_args(argv)
@@ -257,7 +300,7 @@ def main(argv=None):
         ctx.close()
         return 0
     if wl["method"] == "batch":
-        return run_batch(ctx, wl, args.steps)
+        return run_batch(ctx, wl, args.steps, lanes=args.lanes)
     ctx.set_cells(wl["xyz"], wl["sc"], wl["eps"], wl["k0"])
     for step in range(args.steps):
         t0 = time.perf_counter()

@@ -80,7 +80,7 @@ def test_c4_batch_runner_calls(capsys):
         def close(self):
             calls.append(("close",))
 
-    assert W.run_batch(FakeCtx(), wl, 1) == 0
+    assert W.run_batch(FakeCtx(), wl, 1, lanes=1) == 0
     assert [c[0] for c in calls] == ["cells", "q"] * 3 + ["close"]
     out = capsys.readouterr().out
     assert "orientation-averaged solves/s" in out and "3 instances" in out
