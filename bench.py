@@ -108,8 +108,29 @@ NCU_TRAFFIC_PER_ALG_BYTE = {}
 # by each phase's order.  Full oracle solves of the same 40,992-cell scene check
 # that model: (machine, cores, full solve measured, the model's prediction there).
 CPU_MODEL_CHECKS = {
-    "cbfm": [{"machine": "x86-64 build host", "cores": 8, "full_solve_s": 827.9, "model_s": 826.1}],
+    "cbfm": [{"machine": "x86_64", "cores": 8, "full_solve_s": 827.9, "model_s": 826.1},
+             {"machine": "aarch64", "cores": 16, "full_solve_s": 784.3, "model_s": 508.5,
+              "note": "GB300 box host (Grace); the full solve shared the host with GPU jobs for part of its run, "
+                      "the model is the benchmark's own sample on an idle host"}],
 }
+
+
+def cpu_model_calibration(method):
+    """Full-solve / model ratio measured on this machine's architecture (1 when unknown)."""
+    import platform
+    for chk in CPU_MODEL_CHECKS.get(method, []):
+        if chk["machine"] == platform.machine():
+            return chk["full_solve_s"] / chk["model_s"], chk
+    return 1.0, None
+
+
+# The plain FP64 MoM (FP64 fill + cuSOLVER zgetrf / zgetrs) measured on GB300 at the
+# largest size that fits a benchmark call: the 60,000-unknown inhomogeneous cube with
+# 64 right-hand sides (bench.py --workload mom_c3 --fp64-measure).  Larger systems
+# are scaled from this point: factorisation by N^3, fill by N^2.
+FP64_MEASURED = {"workload": "mom_c3 (20,000 voxels, 60,000 unknowns, 64 right-hand sides)", "unknowns": 60000,
+                 "seconds": 528.88, "fill_ms": 187.4, "factor_ms": 528688.4,
+                 "mixed_solves_per_s_same_matrix": 31.42, "field_rel_err_mixed_vs_fp64": 3.6e-9}
 
 
 def load_peaks():
@@ -270,6 +291,8 @@ def run_reference(args, wl, world, rank, pg):
             model.append(dt)
             walls.append(time.perf_counter() - t0)
     per = float(np.mean(model))
+    cal, chk = cpu_model_calibration("cbfm") if wl["method"] == "cbfm" else (1.0, None)
+    per *= cal
     value = len(wl["th"]) / per
     wall = float(np.mean(walls))
     cores = os.cpu_count()
@@ -281,8 +304,8 @@ def run_reference(args, wl, world, rank, pg):
             "scaling": "weak", "vs_baseline": None, "dtype": "c128 (fp64)", "data": "synthetic",
             "config": {"workload": wl["name"], "cells": int(len(wl["xyz"])), "directions": int(len(wl["th"]))},
             "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port", "sample": sample,
-                             "modelled_full_solve_s": per, "sample_wall_s": wall,
-                             "model_checks": CPU_MODEL_CHECKS.get(wl["method"])},
+                             "modelled_full_solve_s": per, "calibration": cal, "calibrated_by": chk,
+                             "sample_wall_s": wall},
             "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -482,8 +505,10 @@ def run_ours(args, wl, world, rank, local, pg):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         if cbfm:
             tc, tw, desc = cbfm_cpu_sample(wl)
-            cpu = {"value": ntr / tc, "unit": "solves/s", "cores": os.cpu_count(), "kind": "port", "sample": desc,
-                   "modelled_full_solve_s": tc, "sample_wall_s": tw, "model_checks": CPU_MODEL_CHECKS.get("cbfm")}
+            cal, chk = cpu_model_calibration("cbfm")
+            cpu = {"value": ntr / (tc * cal), "unit": "solves/s", "cores": os.cpu_count(), "kind": "port",
+                   "sample": desc, "modelled_full_solve_s": tc, "calibration": cal, "calibrated_by": chk,
+                   "sample_wall_s": tw}
         elif N > 20000:
             tc, tw, desc = mom_cpu_sample(wl)
             cpu = {"value": ntr / tc, "unit": "solves/s", "cores": os.cpu_count(), "kind": "port", "sample": desc,
@@ -696,37 +721,31 @@ def run_batch_bench(args, wl, world, rank, local, pg):
 
 
 def fp64_mom_extrapolated(local, wl, value):
-    """Plain FP64 MoM (FP64 fill + cuSOLVER zgetrf/zgetrs) timed on this GPU on the
-    sphere x = 2 scene (12,672 unknowns) and scaled to the workload's unknowns by
-    phase: fill N^2, factorisation N^3, solves N^2 x right-hand sides.  A measured
-    full-size FP64 run does not fit the benchmark's time (the FP64 LU of ~123k
-    unknowns is ~5e15 flops at the part's FP64 rate)."""
+    """Plain FP64 MoM (FP64 fill + cuSOLVER zgetrf/zgetrs) for a system too large to
+    factor within the benchmark: scaled from the measured 60,000-unknown point
+    (FP64_MEASURED) by N^3 (factorisation) and N^2 (fill).  A cross-check is timed
+    here on the 12,672-unknown sphere and scaled the same way."""
     from midas_gb300 import _lib
     from midas_gb300.solver import Context
+    n1 = 3 * len(wl["xyz"])
+    r = n1 / FP64_MEASURED["unknowns"]
+    t = FP64_MEASURED["factor_ms"] * 1e-3 * r ** 3 + FP64_MEASURED["fill_ms"] * 1e-3 * r ** 2
+    ntr = len(wl["th"])
     ref = workload_mom_c1()
     c64 = Context(device=local, solve_mode=_lib.SOLVE_FP64)
     c64.set_cells(ref["xyz"], ref["sc"], ref["eps"], ref["k0"])
     th = np.asarray(wl["th"], float)
     ph = np.asarray(wl["ph"], float)
     c64.mom_solve(th, ph)
-    t0 = time.perf_counter()
     c64.mom_solve(th, ph)
-    t_meas = time.perf_counter() - t0
     inf = c64.info.as_dict()
     c64.close()
-    n0, n1 = 3 * len(ref["xyz"]), 3 * len(wl["xyz"])
-    r = n1 / n0
-    t_fill = inf["t_fill_ms"] * 1e-3 * r ** 2
-    t_fac = inf["t_factor_ms"] * 1e-3 * r ** 3
-    t_sol = inf["t_solve_ms"] * 1e-3 * r ** 2
-    t = t_fill + t_fac + t_sol
-    ntr = len(th)
+    n0 = 3 * len(ref["xyz"])
+    t_c1 = inf["t_factor_ms"] * 1e-3 * (n1 / n0) ** 3 + inf["t_fill_ms"] * 1e-3 * (n1 / n0) ** 2
     return {"value": ntr / t, "unit": "solves/s", "impl": "cuSOLVER zgetrf/zgetrs FP64 + FP64 fill",
-            "measured_on": f"{ref['name']} ({n0} unknowns, {ntr} directions x 2 pol): {t_meas:.2f} s "
-                           f"(fill {inf['t_fill_ms']:.0f} ms, factor {inf['t_factor_ms']:.0f} ms, "
-                           f"solve {inf['t_solve_ms']:.0f} ms)",
-            "extrapolated_to_unknowns": n1, "extrapolated_s": t, "speedup": value / (ntr / t),
-            "memory_gb_fp64_matrix": 16.0 * n1 * n1 / 1e9}
+            "measured_on": FP64_MEASURED, "scaled_to_unknowns": n1, "scale_factor_n3": r ** 3, "seconds": t,
+            "speedup": value / (ntr / t), "memory_gb_fp64_matrix": 16.0 * n1 * n1 / 1e9,
+            "cross_check_from_12672_unknowns": {"factor_ms_measured": inf["t_factor_ms"], "scaled_s": t_c1}}
 
 
 def ctypes_byref(x):

@@ -206,13 +206,15 @@ int midas_gpu_gmres_solve(midas_gpu_ctx *ctx, int ntr, const double *theta, cons
 
 /* Learned initial guess for midas_gpu_gmres_solve (no counterpart in the
  * reference).  A 3-D convolutional network on a grid^3 voxel grid (grid even,
- * <= 128): 8 input channels per voxel -- Re, Im of chi = eps - 1 (0 outside the
- * scatterer) and Re, Im of the three incident-field components -- and the
- * prediction E = E_inc + mask * net(...), 6 channels (Re, Im of Ex, Ey, Ez).
- * Four 3x3x3 convolutions (8 -> 32 -> 32 -> 32 -> 6, ReLU), fp16 operands on the
+ * <= 128): 16 input channels per voxel -- Re, Im of chi = eps - 1 (0 outside
+ * the scatterer) in channels 0-1, Re, Im of the three incident-field components
+ * in channels 2-7, Re, Im of chi times each component in 8-13, the mask in 14
+ * and 0 in 15 -- and the prediction E = E_inc + mask * net(...), 6 channels
+ * (Re, Im of Ex, Ey, Ez).  Four 3x3x3 convolutions (16 -> 32 -> 32 -> 32 -> 6,
+ * ReLU), fp16 operands on the
  * tensor cores with FP32 accumulation, FP32 master weights, Adam.  Arrays are
  * voxel-major, x fastest then y then z, one sample after another:
- * inputs [batch][grid^3][8], mask [batch][grid^3] (1 inside, 0 outside), target
+ * inputs [batch][grid^3][16], mask [batch][grid^3] (1 inside, 0 outside), target
  * and E [batch][grid^3][6]; host or device memory.  batch <= 64 and
  * batch * grid^3 <= 2^22.  Parameters are laid out layer by layer, weights
  * [cout][27 taps (dz, dy, dx = -1..1, dx fastest)][cin] then biases [cout], with

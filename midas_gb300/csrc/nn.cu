@@ -2,13 +2,16 @@
 // convolutional network trained and evaluated by this library's own kernels.
 //
 // The network maps, on a G^3 voxel grid, the per-voxel contrast chi = eps - 1
-// (real, imaginary) and the incident field (three complex components) -- 8
-// input channels -- to the scattered part of the internal field, 6 output
-// channels; the prediction is E = E_inc + mask * net(...).  Four 3 x 3 x 3
-// convolutions with zero padding, 8 -> 32 -> 32 -> 32 -> 6 channels (the last
-// padded to 8), ReLU between them.  The reference has no learned component;
-// the dense LU / CBFM solve stays the fallback and the judge of its error, and
-// the Krylov solve it starts checks its residual in FP64.
+// (real, imaginary), the incident field (three complex components), their
+// products chi E_inc and the scatterer mask -- 16 input channels -- to the
+// scattered part of the internal field, 6 output channels; the prediction is
+// E = E_inc + mask * net(...).  Four 3 x 3 x 3 convolutions with zero padding,
+// 16 -> 32 -> 32 -> 32 -> 6 channels (the last padded to 8), ReLU between them.
+// The products chi E_inc are inputs because a ReLU stack represents a product
+// of two inputs only coarsely, and the internal field is, to first order, that
+// product rescaled.  The reference has no learned component; the dense LU /
+// CBFM solve stays the fallback and the judge of its error, and the Krylov
+// solve it starts checks its residual in FP64.
 //
 // Arithmetic: every convolution is an fp16 im2col (channel-last activations,
 // the 27 neighbour offsets x input channels contiguous) multiplied on the
@@ -37,9 +40,9 @@
 namespace midas {
 
 constexpr int NN_LAYERS = 4;
-constexpr int NN_CIN0 = 8;    // input channels
+constexpr int NN_CIN0 = 16;   // input channels
 constexpr int NN_COUT = 6;    // output channels (complex field)
-static const int NN_CI[NN_LAYERS] = {8, 32, 32, 32};
+static const int NN_CI[NN_LAYERS] = {16, 32, 32, 32};
 static const int NN_CO[NN_LAYERS] = {32, 32, 32, 8};   // last layer: 6 real + 2 zero rows
 
 }  // namespace midas
@@ -275,7 +278,7 @@ static int nn_workspace(midas_gpu_ctx *c, long long M, NnWork &w)
     const size_t a = al256(sizeof(__half) * M * 27 * 32);
     const size_t part = al256(sizeof(float) * (M / NN_ROWS + 2) * 32);
     const size_t tot = NN_LAYERS * (x16 + z32) + 2 * a + 2 * z32 + 2 * x16 + 3 * 256 + part + al256(sizeof(double) * 64) +
-                       al256(sizeof(float) * M * 8) + al256(sizeof(float) * M) + al256(sizeof(float) * M * 6) + 1024;
+                       al256(sizeof(float) * M * NN_CIN0) + al256(sizeof(float) * M) + al256(sizeof(float) * M * 6) + 1024;
     void *p;
     MIDAS_TRY(ensure(c, S_NN, tot, &p));
     char *q = (char *)p;
@@ -295,7 +298,7 @@ static int nn_workspace(midas_gpu_ctx *c, long long M, NnWork &w)
     w.loss = (double *)take(64);
     w.part = (float *)take(part);
     w.den = (double *)take(sizeof(double) * 64);
-    w.in32 = (float *)take(sizeof(float) * M * 8);
+    w.in32 = (float *)take(sizeof(float) * M * NN_CIN0);
     w.mask32 = (float *)take(sizeof(float) * M);
     w.tgt32 = (float *)take(sizeof(float) * M * 6);
     return MIDAS_OK;
@@ -319,7 +322,7 @@ static int nn_forward(midas_gpu_ctx *c, midas_gpu_nn *net, int B, NnWork &w)
     const int G = net->grid;
     const long long M = (long long)B * G * G * G;
     ++c->launches;
-    k_nn_f32_to_f16<<<nb(M * 8), 256, 0, c->stream>>>(M * 8, w.in32, w.X16[0]);
+    k_nn_f32_to_f16<<<nb(M * NN_CIN0), 256, 0, c->stream>>>(M * NN_CIN0, w.in32, w.X16[0]);
     for (int l = 0; l < NN_LAYERS; ++l) {
         const int ci = NN_CI[l], co = NN_CO[l];
         ++c->launches;
@@ -390,13 +393,13 @@ static int nn_refresh16(midas_gpu_ctx *c, midas_gpu_nn *net)
     return MIDAS_OK;
 }
 
-// stage a batch: inputs [B][V][8], mask [B][V], target [B][V][6] (host or device);
+// stage a batch: inputs [B][V][16], mask [B][V], target [B][V][6] (host or device);
 // per-sample denominators sum(mask target^2) on the host
 static int nn_stage(midas_gpu_ctx *c, midas_gpu_nn *net, int B, const float *in, const float *mask, const float *tgt,
                     NnWork &w)
 {
     const long long V = (long long)net->grid * net->grid * net->grid, M = B * V;
-    MIDAS_CUDA(c, cudaMemcpyAsync(w.in32, in, sizeof(float) * M * 8, cudaMemcpyDefault, c->stream));
+    MIDAS_CUDA(c, cudaMemcpyAsync(w.in32, in, sizeof(float) * M * NN_CIN0, cudaMemcpyDefault, c->stream));
     MIDAS_CUDA(c, cudaMemcpyAsync(w.mask32, mask, sizeof(float) * M, cudaMemcpyDefault, c->stream));
     if (tgt) {
         MIDAS_CUDA(c, cudaMemcpyAsync(w.tgt32, tgt, sizeof(float) * M * 6, cudaMemcpyDefault, c->stream));

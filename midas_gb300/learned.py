@@ -1,6 +1,6 @@
 """Learned initial guess for the Krylov solve of voxel scatterers.
 
-    python -m midas_gb300.learned [--grid 32] [--train 2000] [--test 500] [--epochs 8]
+    python -m midas_gb300.learned [--grid 32] [--train 2000] [--test 500] [--epochs 30]
 
 Workflow (all arithmetic in the library: GMRES on the FFT lattice operator,
 the network's forward, backward and Adam kernels; numpy only assembles arrays):
@@ -34,7 +34,7 @@ from . import _lib
 from . import geometry as G
 from ._lib import addr
 
-IN_CH, OUT_CH = 8, 6
+IN_CH, OUT_CH = 16, 6
 
 
 class Net:
@@ -169,7 +169,8 @@ def incident_grid(sc) -> np.ndarray:
 
 
 def grid_inputs(sc):
-    """Network inputs [2, V, 8] and mask [2, V] (float32)."""
+    """Network inputs [2, V, 16] and mask [2, V] (float32): chi = eps - 1 (0 outside),
+    the incident field, chi times each incident component, the mask, 0."""
     V = sc["grid"] ** 3
     chi = np.zeros(V, complex)
     chi[sc["mask"]] = sc["eps"] - 1.0
@@ -180,6 +181,10 @@ def grid_inputs(sc):
         for q in range(3):
             inp[pol, :, 2 + 2 * q] = einc[pol, :, q].real
             inp[pol, :, 3 + 2 * q] = einc[pol, :, q].imag
+            prod = chi * einc[pol, :, q]
+            inp[pol, :, 8 + 2 * q] = prod.real
+            inp[pol, :, 9 + 2 * q] = prod.imag
+        inp[pol, :, 14] = sc["mask"]
     mask = np.repeat(sc["mask"][None].astype(np.float32), 2, axis=0)
     return inp, mask
 
@@ -241,6 +246,7 @@ def generate(ctx, scene_list, tol=1e-6, log=None):
 
 
 def train(net, data, epochs=8, batch=8, lr=2e-3, seed=0, log=None):
+    """Adam over shuffled batches; the learning rate falls as a cosine to 5 % of lr."""
     inputs, mask, target = data
     rng = np.random.default_rng(seed)
     hist = []
@@ -248,7 +254,7 @@ def train(net, data, epochs=8, batch=8, lr=2e-3, seed=0, log=None):
     for ep in range(epochs):
         order = rng.permutation(len(inputs))
         losses = []
-        lr_ep = lr * (0.5 ** (ep // 3))
+        lr_ep = lr * (0.05 + 0.95 * 0.5 * (1.0 + math.cos(math.pi * ep / max(1, epochs))))
         for b in range(nb):
             sel = order[b * batch:(b + 1) * batch]
             losses.append(net.train_step(inputs[sel], mask[sel], target[sel], lr_ep))
@@ -309,7 +315,7 @@ def main(argv=None):
     ap.add_argument("--grid", type=int, default=32)
     ap.add_argument("--train", type=int, default=2000, help="training pairs (two per scene)")
     ap.add_argument("--test", type=int, default=500, help="held-out scenes")
-    ap.add_argument("--epochs", type=int, default=8)
+    ap.add_argument("--epochs", type=int, default=30)
     ap.add_argument("--judge", type=int, default=20, help="held-out scenes also solved densely")
     ap.add_argument("--tol", type=float, default=1e-6)
     args = ap.parse_args(argv)

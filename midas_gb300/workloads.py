@@ -279,6 +279,7 @@ def main(argv=None):
     ap.add_argument("--verbose", "-v", action="count", default=0,
                     help="library trace: -v refinement steps and CBFM lanes, -vv per-block detail")
     ap.add_argument("--lanes", type=int, default=4, help="concurrent contexts of the C4 batch")
+    ap.add_argument("--aca", action="store_true", help="CBFM: off-diagonal reduced blocks from ACA factors")
     ap.add_argument("--classes", action="store_true",
                     help="after the steps, one more step with per-kernel-class CUDA-event timing (one lane)")
     args = ap.parse_args(argv)
@@ -305,7 +306,7 @@ def main(argv=None):
     for step in range(args.steps):
         t0 = time.perf_counter()
         if wl["method"] == "cbfm":
-            flags = _lib.CBFM_SR | (_lib.CBFM_HOMOG if wl.get("homog") else 0)
+            flags = _lib.CBFM_SR | (_lib.CBFM_HOMOG if wl.get("homog") else 0) | (_lib.CBFM_ACA if args.aca else 0)
             E, K = ctx.cbfm_solve(wl["offs"], wl["ext"], wl["cth"], wl["cph"], wl["th"], wl["ph"], flags=flags)
         else:
             E = ctx.mom_solve(wl["th"], wl["ph"])

@@ -3,7 +3,7 @@
 The reference has no learned component; this file is the checker of the
 library's network kernels (midas_gb300/csrc/nn.cu): a float64 numpy
 restatement of the same computation -- four 3x3x3 zero-padded convolutions,
-8 -> 32 -> 32 -> 32 -> 8 channels (the last two output channels zero), ReLU
+16 -> 32 -> 32 -> 32 -> 8 channels (the last two output channels zero), ReLU
 between them, the prediction E = E_inc + mask * out[:, :6] and the loss
 
     L = mean_b  sum(mask |E_pred - target|^2) / sum(mask |target|^2)
@@ -22,7 +22,7 @@ from __future__ import annotations
 
 import numpy as np
 
-CI = (8, 32, 32, 32)
+CI = (16, 32, 32, 32)
 CO = (32, 32, 32, 8)
 NOUT = 6
 
@@ -90,7 +90,7 @@ def conv_wgrad(dZ, X, G):
 
 
 def loss_and_grads(theta, inputs, mask, target, G, fp16=True):
-    """inputs [B, V, 8], mask [B, V], target [B, V, 6]; returns (loss, gradient of theta)."""
+    """inputs [B, V, 16], mask [B, V], target [B, V, 6]; returns (loss, gradient of theta)."""
     r = _f16 if fp16 else (lambda a: np.asarray(a, np.float64))
     params = unpack(np.asarray(theta, np.float64))
     B = inputs.shape[0]

@@ -17,7 +17,7 @@ def _random_batch(G, B, seed):
     rng = np.random.default_rng(seed)
     V = G ** 3
     mask = (rng.random((B, V)) < 0.5).astype(np.float32)
-    inp = (rng.standard_normal((B, V, 8)) * 0.5).astype(np.float32)
+    inp = (rng.standard_normal((B, V, 16)) * 0.5).astype(np.float32)
     inp[:, :, :2] *= mask[:, :, None]
     tgt = (inp[:, :, 2:8] + 0.3 * rng.standard_normal((B, V, 6))).astype(np.float32)
     return inp, mask, tgt
@@ -81,10 +81,10 @@ def test_training_lowers_loss_and_guess_saves_gmres_iterations(gpulib):
     from midas_gb300.solver import Context
     ctx = Context()
     G = 16
-    data, its = LG.generate(ctx, LG.scenes(21, 48, G), tol=1e-6)
-    assert len(data[0]) >= 80
+    data, its = LG.generate(ctx, LG.scenes(21, 64, G), tol=1e-6)
+    assert len(data[0]) >= 100
     net = LG.Net(ctx, G, seed=5)
-    hist = LG.train(net, data, epochs=12, batch=8, lr=3e-3)
+    hist = LG.train(net, data, epochs=30, batch=8, lr=3e-3)
     print("loss history", hist)
     assert hist[-1] < 0.5 * hist[0]
     rows = LG.evaluate(ctx, net, LG.scenes(99, 8, G), tol=1e-8, judge=8)

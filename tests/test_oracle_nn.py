@@ -12,7 +12,7 @@ from oracle import nn_oracle as N
 def _case(G=4, B=2, seed=0):
     rng = np.random.default_rng(seed)
     V = G ** 3
-    inputs = rng.standard_normal((B, V, 8)) * 0.5
+    inputs = rng.standard_normal((B, V, 16)) * 0.5
     mask = (rng.random((B, V)) < 0.6).astype(float)
     inputs[:, :, 0:2] *= mask[:, :, None]
     target = rng.standard_normal((B, V, 6))
