@@ -391,7 +391,8 @@ int midas_gpu_record_event(midas_gpu_ctx *ctx, void *event);
 #define MIDAS_KC_SPLIT      13  /* split-TF32 operand preparation (hi / lo pieces) */
 #define MIDAS_KC_LATTICE   14  /* FFT lattice operator (scatter, FFTs, spectral product, gather) */
 #define MIDAS_KC_NN        15  /* tcgen05 GEMMs of the learned initial guess's convolutions */
-#define MIDAS_KC_COUNT     16
+#define MIDAS_KC_RESID32   16  /* FP32 residual updates r -= Z d of the refinements */
+#define MIDAS_KC_COUNT     17
 /* enable = 1 clears the per-class totals and starts timing every instrumented
  * launch with CUDA events on the context stream; 0 stops.  Timing adds one event
  * record before and after each instrumented launch. */

@@ -25,7 +25,7 @@ GMRES_JACOBI = 1
 QUAD = {"un": 0, "tr": 1, "gl": 2, "sd": 3, "lb": 4, "rf": 5}
 # kernel classes of midas_gpu_profile_query (MIDAS_KC_* in the header)
 KCLASSES = ["gemm_trail", "gemm_simt", "fill", "sr_scan", "diag_lu", "trsv", "resid", "zgemm64", "eig", "other",
-            "gemm_panel", "gemm_solve", "gemm_prod", "split", "lattice", "nn"]
+            "gemm_panel", "gemm_solve", "gemm_prod", "split", "lattice", "nn", "resid32"]
 
 # every symbol the header declares (checked by the CPU tests)
 EXPORTS = [

@@ -113,7 +113,7 @@ int zgemm_x3(midas_gpu_ctx *c, int M, int N, int K, const TA *A, long long ars, 
 // written by launch_block_fill4_a3)
 template <typename TB>
 int zgemm_x3_a3(midas_gpu_ctx *c, int M, int N, int K, const float *A3, long long K6, const TB *B, long long brs,
-                long long bcs, float *D, long long ldd, float alpha, float beta)
+                long long bcs, float *D, long long ldd, float alpha, float beta, int kclass)
 {
     if (M <= 0 || N <= 0 || K <= 0) return MIDAS_OK;
     if (K6 != (6LL * K + 3) / 4 * 4) return c->err.set(MIDAS_ERR_ARG, "zgemm_x3_a3: bad A3 stride");
@@ -126,11 +126,57 @@ int zgemm_x3_a3(midas_gpu_ctx *c, int M, int N, int K, const float *A3, long lon
                                                                                             K6);
     kp_end(c, kp, MIDAS_KC_SPLIT, 0.0, (double)N * K * sizeof(TB) + 8.0 * N * K6);
     MIDAS_CUDA(c, cudaGetLastError());
-    GemmArgs g{M, 2 * N, (int)K6, A3, K6, B3, K6, D, ldd, alpha, beta, 0, MIDAS_KC_GEMM_PROD};
+    GemmArgs g{M, 2 * N, (int)K6, A3, K6, B3, K6, D, ldd, alpha, beta, 0, kclass};
     return gemm_tf32(c, g, true);
 }
 template int zgemm_x3_a3<double2>(midas_gpu_ctx *, int, int, int, const float *, long long, const double2 *,
-                                  long long, long long, float *, long long, float, float);
+                                  long long, long long, float *, long long, float, float, int);
+template int zgemm_x3_a3<float2>(midas_gpu_ctx *, int, int, int, const float *, long long, const float2 *,
+                                 long long, long long, float *, long long, float, float, int);
+
+// A3 = (hi | hi | lo) split of a row-major complex64 M x K matrix (K6 = 6K, a
+// multiple of 4 floats): the A operand of zgemm_x3_a3, formed once for a matrix
+// that several products reuse.
+int zsplit_a3(midas_gpu_ctx *c, int M, int K, const float2 *A, long long lda, float *A3, long long K6)
+{
+    if (M <= 0 || K <= 0) return MIDAS_OK;
+    if (K6 != (6LL * K + 3) / 4 * 4) return c->err.set(MIDAS_ERR_ARG, "zsplit_a3: bad A3 stride");
+    ++c->launches;
+    int kp = kp_begin(c);
+    k_split_a<float2><<<dim3((K + 127) / 128, std::min(M, 65535)), 128, 0, c->stream>>>(M, K, A, lda, 1, 0, A3, K6);
+    kp_end(c, kp, MIDAS_KC_SPLIT, 0.0, 8.0 * M * K + 4.0 * M * K6);
+    MIDAS_CUDA(c, cudaGetLastError());
+    return MIDAS_OK;
+}
+
+// R[j * n + i] -= P[i][2j] + i P[i][2j + 1]   (P row-major n x 2m, FP32; R column-major FP64)
+__global__ void k_sub_rowmajor(int n, int m, const float *P, double2 *R)
+{
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= (long long)n * m) return;
+    const int i = (int)(t % n), j = (int)(t / n);
+    const float2 p = *(const float2 *)(P + (long long)i * 2 * m + 2 * j);
+    double2 r = R[t];
+    r.x -= (double)p.x;
+    r.y -= (double)p.y;
+    R[t] = r;
+}
+
+// R -= Z D with Z given by its split A3 (n x n) and D row-major n x m complex64:
+// the FP32-grade product (hi*hi + hi*lo + lo*hi, relative error ~2^-22) on the
+// tensor cores.  P (n x 2m floats) is scratch.
+int resid_update_x3(midas_gpu_ctx *c, int n, int m, const float *A3, long long K6, const float2 *D, float *P,
+                    double2 *R)
+{
+    MIDAS_TRY(zgemm_x3_a3<float2>(c, n, m, n, A3, K6, D, m, 1, P, 2LL * m, 1.f, 0.f, MIDAS_KC_RESID32));
+    ++c->launches;
+    int kp = kp_begin(c);
+    const long long tot = (long long)n * m;
+    k_sub_rowmajor<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(n, m, P, R);
+    kp_end(c, kp, MIDAS_KC_RESID32, 2.0 * tot, 40.0 * tot);
+    MIDAS_CUDA(c, cudaGetLastError());
+    return MIDAS_OK;
+}
 
 template int zgemm_x3<float2, double2>(midas_gpu_ctx *, int, int, int, const float2 *, long long, long long, int,
                                        const double2 *, long long, long long, float *, long long, float, float);

@@ -42,7 +42,10 @@ int zgemm_x3(midas_gpu_ctx *c, int M, int N, int K, const TA *A, long long ars, 
              const TB *B, long long brs, long long bcs, float *D, long long ldd, float alpha, float beta);
 template <typename TB>
 int zgemm_x3_a3(midas_gpu_ctx *c, int M, int N, int K, const float *A3, long long K6, const TB *B, long long brs,
-                long long bcs, float *D, long long ldd, float alpha, float beta);
+                long long bcs, float *D, long long ldd, float alpha, float beta, int kclass = MIDAS_KC_GEMM_PROD);
+int zsplit_a3(midas_gpu_ctx *c, int M, int K, const float2 *A, long long lda, float *A3, long long K6);
+int resid_update_x3(midas_gpu_ctx *c, int n, int m, const float *A3, long long K6, const float2 *D, float *P,
+                    double2 *R);
 int residual_df32(midas_gpu_ctx *c, int n, int nrhs, const float2 *Z, long long ldz, const float2 *Xh,
                   const float2 *Xl, const float2 *B, double2 *R);
 int heev_dev(midas_gpu_ctx *c, int batch, int m, double2 *A, long long lda, long long sa, double2 *H, double2 *V,
@@ -226,10 +229,19 @@ static int cbf_block(midas_gpu_ctx *c, const CbfShared &S, int b)
             ++c->launches;
             k_pad_diag32<<<1, 64, 0, c->stream>>>(Zlu, sp, N3, sp);
         }
+        // With SR, the thresholded block is kept twice before the LU overwrites it:
+        // in CSR form for the double-float residual (CUDA cores, a sixth of the
+        // dense work) and as the split-TF32 operand A3 for the FP32-grade residual
+        // updates r -= Z d (dense, on the tensor cores).
         Csr zcsr;
-        if (sr)
+        float *A3z = nullptr;
+        const long long K6z = 6LL * sp;
+        if (sr) {
             MIDAS_TRY(csr_from_dense(c, sp, Zlu, sp, S_CSR, &zcsr));
-        else
+            MIDAS_TRY(ensure(c, S_CBF2, sizeof(float) * (size_t)sp * (size_t)K6z, &p2));
+            A3z = (float *)p2;
+            MIDAS_TRY(zsplit_a3(c, sp, sp, Zlu, sp, A3z, K6z));
+        } else
             MIDAS_CUDA(c, cudaMemcpyAsync(Zsr, Zlu, sizeof(float2) * (size_t)sp * sp, cudaMemcpyDeviceToDevice,
                                           c->stream));
         MIDAS_CUDA(c, cudaMemsetAsync(Bm, 0, sizeof(float2) * (size_t)sp * m, c->stream));
@@ -252,20 +264,21 @@ static int cbf_block(midas_gpu_ctx *c, const CbfShared &S, int b)
         k_ir_update<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(tot, sp, m, X64, d32, Xh, Xl,
                                                                           sr ? Drm : nullptr, 1, sr);
         // Residuals.  The first, B - Z x0, is needed only to ~1e-3 of itself (x0 from
-        // the TF32 factors is ~1e-3.5 off), so it is formed in FP32 on the CSR matrix.
-        // Then double-float B - Z x while the corrections are large; once the
-        // relative residual is below 1e-5 every later correction d is ~1e-5 |x| or
-        // smaller, and r - Z d in FP32 (error ~1e-6 |Z||d| over a row's ~3k
-        // nonzeros) keeps the computed residual within ~1e-11 |x| of the true one.
+        // the TF32 factors is ~1e-3.5 off), so it is formed as an FP32-grade
+        // split-TF32 product on the tensor cores.  Then double-float B - Z x on the
+        // CSR form while the corrections are large; once the relative residual is
+        // below 1e-5 every later correction d is ~1e-5 |x| or smaller, and r - Z d
+        // as the same split-TF32 product (relative error ~2^-22 of |Z||d|) keeps the
+        // computed residual within ~1e-11 |x| of the true one.
         int it;
         bool upd = false;
         for (it = 0; it < 12; ++it) {
             if (sr && it == 0) {
                 ++c->launches;
                 k_b_to_r64<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(tot, Bm, R64);
-                MIDAS_TRY(residual_csr_update_f32(c, zcsr, m, Drm, R64));
+                MIDAS_TRY(resid_update_x3(c, sp, m, A3z, K6z, Drm, (float *)d32, R64));
             } else if (sr && upd)
-                MIDAS_TRY(residual_csr_update_f32(c, zcsr, m, Drm, R64));
+                MIDAS_TRY(resid_update_x3(c, sp, m, A3z, K6z, Drm, (float *)d32, R64));
             else if (sr)
                 MIDAS_TRY(residual_csr_df32(c, zcsr, m, Xh, Xl, Bm, R64));
             else

@@ -217,6 +217,7 @@ int check_flag(midas_gpu_ctx *ctx, const char *where);
 // Lattice FFT operator (fft.cu): Y = Z X, or Y = B - Z X when B is given.
 int lattice_fft_prepare(midas_gpu_ctx *c, bool c4 = false);
 bool lattice_fft_fits(const midas_gpu_ctx *c);   // cells on a lattice of <= 256 cells per axis
+bool lattice_fft_preferred(const midas_gpu_ctx *c, long long np);   // FFT residuals cheaper than dense ones
 void lattice_fft_release(midas_gpu_ctx *c);
 int lattice_matvec(midas_gpu_ctx *c, int nrhs, const double2 *X, long long ldx, const double2 *B, long long ldb,
                    double2 *Y, long long ldy, int slot, bool c4 = false);

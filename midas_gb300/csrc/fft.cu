@@ -267,6 +267,22 @@ bool lattice_fft_fits(const midas_gpu_ctx *c)
     return true;
 }
 
+// The MoM solve takes its refinement residuals from the FFT operator when that
+// is the cheaper product: per right-hand side the FP64 transforms of a padded
+// grid of V points cost ~15 V log2 V double-float-MAC equivalents (six
+// transforms of 5 V log2 V flops, ~1.75 of three passes each way, at the part's
+// ~1 TFLOP/s FP64 against ~0.67e12 double-float complex MACs/s of the dense
+// residual), the dense residual np^2.  Compact scatterers (spheres, cubes) have
+// V ~ 8 n and take the FFT; sparse aggregates, whose bounding box pads to grids
+// far larger than their cell count, take the dense residual.
+bool lattice_fft_preferred(const midas_gpu_ctx *c, long long np)
+{
+    if (!lattice_fft_fits(c)) return false;
+    double V = 1.0;
+    for (int a = 0; a < 3; ++a) V *= next_pow2(2 * (c->lat_hi[a] - c->lat_lo[a] + 1) - 1);
+    return 15.0 * V * std::log2(V) < (double)np * (double)np;
+}
+
 // Lattice FFT set-up of the current cells: grid sizes and the dyad spectra (6
 // grids) -- FP64 dyads (the MoM element) or, with c4, the complex(4)-rounded
 // dyads of Green_s_tr_partial (src/Green_functions.f90:139-157).

@@ -45,7 +45,6 @@ struct Csr {
 int csr_from_dense(midas_gpu_ctx *c, int n, const float2 *Z, long long ldz, int slot, Csr *out);
 int residual_csr_df32(midas_gpu_ctx *c, const Csr &Z, int m, const float2 *Xh_rm, const float2 *Xl_rm,
                       const float2 *B, double2 *R);
-int residual_csr_update_f32(midas_gpu_ctx *c, const Csr &Z, int m, const float2 *D_rm, double2 *R);
 
 // fill.cu
 int launch_set_cells(midas_gpu_ctx *c);

@@ -747,9 +747,9 @@ int midas_gpu_mom_solve(midas_gpu_ctx *c, int ntr, const double *theta, const do
         float tlu = tl.stop();
         if (info) { info->t_fill_ms = tfill; info->t_factor_ms = tlu; }
         if (st == MIDAS_OK) st = copy_out(c, E, pb, sizeof(double2) * (size_t)n * nrhs);
-    } else if (lattice_fft_fits(c)) {
-        // cells on a lattice: the residuals come from the FFT operator, so only the
-        // complex64 matrix (the factorisation's operand) is formed
+    } else if (lattice_fft_preferred(c, (n + 63) / 64 * 64)) {
+        // cells on a compact lattice: the residuals come from the FFT operator, so
+        // only the complex64 matrix (the factorisation's operand) is formed
         int np = (n + 63) / 64 * 64;
         void *p32, *pb, *px;
         MIDAS_TRY(ensure(c, S_Z32, sizeof(float2) * (size_t)np * np, &p32));

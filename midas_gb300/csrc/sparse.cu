@@ -8,8 +8,6 @@
 // the refinement use the CSR form built from it: about 16 % of the entries
 // survive the threshold on the voxel scatterers of interest, so the residual
 // does a sixth of the dense work.
-#include <cstdlib>
-
 #include "common.cuh"
 #include "kernels.cuh"
 
@@ -180,227 +178,15 @@ __global__ void __launch_bounds__(256) k_resid_csr_df32(int n, int m, const int 
     }
 }
 
-// ---------------------------------------------------------------------------
-// The same residual with the lanes over the row's nonzeros: a warp takes one
-// row and RL_T consecutive right-hand sides; each lane walks every 32nd
-// nonzero of the row (one coalesced index and value load) and accumulates its
-// RL_T columns from four float4 loads of Xh and of Xl, so the per-nonzero work
-// is the arithmetic alone.  The 32 lanes' double-float partial sums are then
-// added by a shuffle tree of TwoSums.  m must be even (X rows start on 16-byte
-// boundaries): the CBF right-hand sides come in V / H pairs.
-// ---------------------------------------------------------------------------
-constexpr int RL_T = 8;
-
-// (hi, lo) += a (bh + bl): the product with bh exactly (FMA residue, TwoSum into
-// hi), the product with bl (2^-24 smaller) in FP32 into lo
-__device__ __forceinline__ void df_axpy(float &hi, float &lo, float a, float bh, float bl)
-{
-    const float p = __fmul_rn(a, bh);
-    const float pe = fmaf(a, bh, -p);
-    float sum, err;
-    ef_two_sum(hi, p, sum, err);
-    hi = sum;
-    lo = fmaf(a, bl, __fadd_rn(lo, __fadd_rn(err, pe)));
-}
-
-__device__ __forceinline__ void load_row8(const float2 *X, long long base, int ncols, float2 v[RL_T])
-{
-    if (ncols == RL_T) {
-        const float4 *q = (const float4 *)(X + base);
-#pragma unroll
-        for (int u = 0; u < RL_T / 2; ++u) {
-            const float4 w = q[u];
-            v[2 * u] = make_float2(w.x, w.y);
-            v[2 * u + 1] = make_float2(w.z, w.w);
-        }
-    } else {
-#pragma unroll
-        for (int t = 0; t < RL_T; ++t) v[t] = t < ncols ? X[base + t] : make_float2(0.f, 0.f);
-    }
-}
-
-__global__ void __launch_bounds__(256) k_resid_csr_df32_nz(int n, int m, const int *rowptr, const int *col,
-                                                            const float2 *val, const float2 *Xh, const float2 *Xl,
-                                                            const float2 *B, double2 *R)
-{
-    const long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    const int ntile = (m + RL_T - 1) / RL_T;
-    if (w >= (long long)n * ntile) return;
-    const int i = (int)(w / ntile), c0 = (int)(w % ntile) * RL_T, ncols = min(RL_T, m - c0);
-    float rh[RL_T], rl[RL_T], ih[RL_T], il[RL_T];
-#pragma unroll
-    for (int t = 0; t < RL_T; ++t) rh[t] = rl[t] = ih[t] = il[t] = 0.f;
-    const int p1 = rowptr[i + 1];
-    for (int p = rowptr[i] + lane; p < p1; p += 32) {
-        const int k = col[p];
-        const float2 z = val[p];
-        float2 h[RL_T], l[RL_T];
-        load_row8(Xh, (long long)k * m + c0, ncols, h);
-        load_row8(Xl, (long long)k * m + c0, ncols, l);
-#pragma unroll
-        for (int t = 0; t < RL_T; ++t) {
-            df_axpy(rh[t], rl[t], z.x, h[t].x, l[t].x);
-            df_axpy(rh[t], rl[t], -z.y, h[t].y, l[t].y);
-            df_axpy(ih[t], il[t], z.x, h[t].y, l[t].y);
-            df_axpy(ih[t], il[t], z.y, h[t].x, l[t].x);
-        }
-    }
-    // the lanes' double-float partial sums: a shuffle tree of TwoSums
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-#pragma unroll
-        for (int t = 0; t < RL_T; ++t) {
-            float sum, err;
-            const float oh = __shfl_down_sync(0xffffffffu, rh[t], o), ol = __shfl_down_sync(0xffffffffu, rl[t], o);
-            ef_two_sum(rh[t], oh, sum, err);
-            rh[t] = sum;
-            rl[t] = __fadd_rn(rl[t], __fadd_rn(err, ol));
-            const float jh = __shfl_down_sync(0xffffffffu, ih[t], o), jl = __shfl_down_sync(0xffffffffu, il[t], o);
-            ef_two_sum(ih[t], jh, sum, err);
-            ih[t] = sum;
-            il[t] = __fadd_rn(il[t], __fadd_rn(err, jl));
-        }
-    }
-    if (lane == 0) {
-#pragma unroll
-        for (int t = 0; t < RL_T; ++t)
-            if (t < ncols) {
-                const float2 b = B[(long long)(c0 + t) * n + i];
-                R[(long long)(c0 + t) * n + i] = make_double2((double)b.x - ((double)rh[t] + (double)rl[t]),
-                                                              (double)b.y - ((double)ih[t] + (double)il[t]));
-            }
-    }
-}
-
-// r -= Z d in FP32 with the same lane layout
-__global__ void __launch_bounds__(256) k_csr_sub_f32_nz(int n, int m, const int *rowptr, const int *col,
-                                                         const float2 *val, const float2 *D, double2 *R)
-{
-    const long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    const int ntile = (m + RL_T - 1) / RL_T;
-    if (w >= (long long)n * ntile) return;
-    const int i = (int)(w / ntile), c0 = (int)(w % ntile) * RL_T, ncols = min(RL_T, m - c0);
-    float ar[RL_T], ai[RL_T];
-#pragma unroll
-    for (int t = 0; t < RL_T; ++t) ar[t] = ai[t] = 0.f;
-    const int p1 = rowptr[i + 1];
-    for (int p = rowptr[i] + lane; p < p1; p += 32) {
-        const int k = col[p];
-        const float2 z = val[p];
-        float2 d[RL_T];
-        load_row8(D, (long long)k * m + c0, ncols, d);
-#pragma unroll
-        for (int t = 0; t < RL_T; ++t) {
-            ar[t] = fmaf(z.x, d[t].x, fmaf(-z.y, d[t].y, ar[t]));
-            ai[t] = fmaf(z.x, d[t].y, fmaf(z.y, d[t].x, ai[t]));
-        }
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1)
-#pragma unroll
-        for (int t = 0; t < RL_T; ++t) {
-            ar[t] += __shfl_down_sync(0xffffffffu, ar[t], o);
-            ai[t] += __shfl_down_sync(0xffffffffu, ai[t], o);
-        }
-    if (lane == 0) {
-#pragma unroll
-        for (int t = 0; t < RL_T; ++t)
-            if (t < ncols) {
-                double2 *r = R + (long long)(c0 + t) * n + i;
-                *r = make_double2(r->x - (double)ar[t], r->y - (double)ai[t]);
-            }
-    }
-}
-
-static bool csr_lanes_over_columns()
-{
-    static const bool v = getenv("MIDAS_CSR_COLUMN_LANES") != nullptr;
-    return v;
-}
-
 int residual_csr_df32(midas_gpu_ctx *c, const Csr &Z, int m, const float2 *Xh_rm, const float2 *Xl_rm,
                       const float2 *B, double2 *R)
 {
     const int n = Z.n;
     ++c->launches;
     int kp = kp_begin(c);
-    if (csr_lanes_over_columns() || (m & 1)) {
-        dim3 grd((unsigned)(((long long)n * 32 + 255) / 256), (m + RESID_COLS - 1) / RESID_COLS);
-        k_resid_csr_df32<<<grd, 256, 0, c->stream>>>(n, m, Z.rowptr, Z.col, Z.val, Xh_rm, Xl_rm, B, R);
-    } else {
-        const long long warps = (long long)n * ((m + RL_T - 1) / RL_T);
-        k_resid_csr_df32_nz<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, c->stream>>>(n, m, Z.rowptr, Z.col,
-                                                                                           Z.val, Xh_rm, Xl_rm, B, R);
-    }
+    dim3 grd((unsigned)(((long long)n * 32 + 255) / 256), (m + RESID_COLS - 1) / RESID_COLS);
+    k_resid_csr_df32<<<grd, 256, 0, c->stream>>>(n, m, Z.rowptr, Z.col, Z.val, Xh_rm, Xl_rm, B, R);
     kp_end(c, kp, MIDAS_KC_RESID, 8.0 * Z.nnz * m, 12.0 * Z.nnz + 16.0 * (double)n * m * 2 + 24.0 * (double)n * m);
-    MIDAS_CUDA(c, cudaGetLastError());
-    return MIDAS_OK;
-}
-
-// ---------------------------------------------------------------------------
-// r -= Z d (FP32): the residual of x + d from the residual of x, once the
-// correction d is small -- its FP32 product error is then below the double-float
-// accuracy the refinement needs.  d row-major (n x m), r column-major FP64.
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_csr_sub_f32(int n, int m, const int *rowptr, const int *col,
-                                                      const float2 *val, const float2 *D, double2 *R)
-{
-    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (i >= n) return;
-    const int c0 = blockIdx.y * RESID_COLS;
-    float ar[RESID_T], ai[RESID_T];
-#pragma unroll
-    for (int t = 0; t < RESID_T; ++t) { ar[t] = 0.f; ai[t] = 0.f; }
-    const int p1 = rowptr[i + 1];
-    for (int p0 = rowptr[i]; p0 < p1; p0 += 32) {
-        const int cnt = min(32, p1 - p0);
-        int mk = 0;
-        float2 mz = make_float2(0.f, 0.f);
-        if (lane < cnt) { mk = col[p0 + lane]; mz = val[p0 + lane]; }
-#pragma unroll 4
-        for (int q = 0; q < cnt; ++q) {
-            const int k = __shfl_sync(0xffffffffu, mk, q);
-            float2 z;
-            z.x = __shfl_sync(0xffffffffu, mz.x, q);
-            z.y = __shfl_sync(0xffffffffu, mz.y, q);
-            const float2 *dr = D + (long long)k * m;
-#pragma unroll
-            for (int t = 0; t < RESID_T; ++t) {
-                const int cc = c0 + lane + 32 * t;
-                if (cc < m) {
-                    float2 d = dr[cc];
-                    ar[t] = fmaf(z.x, d.x, fmaf(-z.y, d.y, ar[t]));
-                    ai[t] = fmaf(z.x, d.y, fmaf(z.y, d.x, ai[t]));
-                }
-            }
-        }
-    }
-#pragma unroll
-    for (int t = 0; t < RESID_T; ++t) {
-        const int cc = c0 + lane + 32 * t;
-        if (cc < m) {
-            double2 *r = R + (long long)cc * n + i;
-            *r = make_double2(r->x - (double)ar[t], r->y - (double)ai[t]);
-        }
-    }
-}
-
-int residual_csr_update_f32(midas_gpu_ctx *c, const Csr &Z, int m, const float2 *D_rm, double2 *R)
-{
-    const int n = Z.n;
-    ++c->launches;
-    int kp = kp_begin(c);
-    if (csr_lanes_over_columns() || (m & 1)) {
-        dim3 grd((unsigned)(((long long)n * 32 + 255) / 256), (m + RESID_COLS - 1) / RESID_COLS);
-        k_csr_sub_f32<<<grd, 256, 0, c->stream>>>(n, m, Z.rowptr, Z.col, Z.val, D_rm, R);
-    } else {
-        const long long warps = (long long)n * ((m + RL_T - 1) / RL_T);
-        k_csr_sub_f32_nz<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, c->stream>>>(n, m, Z.rowptr, Z.col, Z.val,
-                                                                                        D_rm, R);
-    }
-    kp_end(c, kp, MIDAS_KC_RESID, 8.0 * Z.nnz * m, 12.0 * Z.nnz + 8.0 * (double)n * m + 32.0 * (double)n * m);
     MIDAS_CUDA(c, cudaGetLastError());
     return MIDAS_OK;
 }

@@ -55,6 +55,79 @@ def test_gradients_match_oracle(gpulib):
     ctx.close()
 
 
+def test_gradients_match_oracle_at_training_size(gpulib):
+    """The training configuration (16^3 grid, batch 8: 32,768 GEMM rows, more
+    output tiles than the GPU has SMs) against the oracle."""
+    from midas_gb300.learned import Net
+    from midas_gb300.solver import Context
+    from oracle import nn_oracle as N
+    ctx = Context()
+    G, B = 16, 8
+    net = Net(ctx, G, seed=3)
+    inp, mask, tgt = _random_batch(G, B, 11)
+    loss = net.gradients(inp, mask, tgt)
+    g = net.params(grads=True).astype(np.float64)
+    loss_o, g_o = N.loss_and_grads(net.params().astype(np.float64), inp, mask, tgt, G, fp16=True)
+    assert abs(loss - loss_o) <= 1e-4 * loss_o, (loss, loss_o)
+    o = 0
+    for (ws, bs) in N.param_shapes():
+        n = int(np.prod(ws)) + bs[0]
+        a, b = g[o:o + n], g_o[o:o + n]
+        o += n
+        rel = np.linalg.norm(a - b) / np.linalg.norm(b)
+        cos = a @ b / (np.linalg.norm(a) * np.linalg.norm(b))
+        print("layer", ws, "grad rel", rel, "cos", cos)
+        assert rel < 1e-2 and cos > 0.9999   # fp16 operands summed over 32,768 voxels
+    E = net.forward(inp, mask)
+    params = N.unpack(net.params().astype(np.float64))
+    X = N._f16(inp)
+    for l, (W, b) in enumerate(params):
+        z = N.conv(X, N._f16(W), G) + b
+        X = N._f16(np.maximum(z, 0)) if l < 3 else z
+    ref = inp[:, :, 2:8] + mask[:, :, None] * X[:, :, :6]
+    assert np.max(np.abs(E - ref)) <= 1e-3 * max(1.0, np.max(np.abs(ref)))
+    net.close()
+    ctx.close()
+
+
+def test_adam_steps_follow_the_oracle(gpulib):
+    """Five training steps of the library (gradients, Adam, fp16 weight copies)
+    against Adam on the oracle's gradients from the same start."""
+    from midas_gb300.learned import Net
+    from midas_gb300.solver import Context
+    from oracle import nn_oracle as N
+    ctx = Context()
+    G = 8
+    net = Net(ctx, G, seed=9)
+    inp, mask, tgt = _random_batch(G, 2, 5)
+    theta = net.params().astype(np.float64)
+    live = np.ones_like(theta)
+    off = sum(co * 27 * ci + co for ci, co in zip(N.CI[:3], N.CO[:3]))
+    live[off + 6 * 27 * 32:off + 8 * 27 * 32] = 0
+    live[off + 8 * 27 * 32 + 6:] = 0
+    m = np.zeros_like(theta)
+    v = np.zeros_like(theta)
+    lr, b1, b2, eps = 1e-2, 0.9, 0.999, 1e-8
+    losses = []
+    for k in range(1, 6):
+        loss = net.train_step(inp, mask, tgt, lr)
+        loss_o, g = N.loss_and_grads(theta, inp, mask, tgt, G, fp16=True)
+        assert abs(loss - loss_o) <= 2e-3 * loss_o, (k, loss, loss_o)
+        m = b1 * m + (1 - b1) * g
+        v = b2 * v + (1 - b2) * g * g
+        step = lr * (m / (1 - b1 ** k)) / (np.sqrt(v / (1 - b2 ** k)) + eps) * live
+        got = net.params().astype(np.float64)
+        cos = (theta - got) @ step / (np.linalg.norm(theta - got) * np.linalg.norm(step))
+        print("step", k, "loss", loss, loss_o, "update cosine", cos)
+        assert cos > 0.99
+        assert np.all(got[live == 0] == 0)
+        theta = got   # the next oracle step starts where the library is
+        losses.append(loss)
+    assert losses[-1] < losses[0]
+    net.close()
+    ctx.close()
+
+
 def test_forward_prediction_is_incident_field_plus_masked_output(gpulib):
     from midas_gb300.learned import Net
     from midas_gb300.solver import Context
