@@ -210,6 +210,8 @@ int midas_gpu_gmres_solve(midas_gpu_ctx *ctx, int ntr, const double *theta, cons
  * the scatterer) in channels 0-1, Re, Im of the three incident-field components
  * in channels 2-7, Re, Im of chi times each component in 8-13, the mask in 14
  * and 0 in 15 -- and the prediction E = E_inc + mask * net(...), 6 channels
+ * (in general: channels 2-7, the base field the network corrects, plus its
+ * masked output)
  * (Re, Im of Ex, Ey, Ez).  Four 3x3x3 convolutions (16 -> 32 -> 32 -> 32 -> 6,
  * ReLU), fp16 operands on the
  * tensor cores with FP32 accumulation, FP32 master weights, Adam.  Arrays are
@@ -235,6 +237,27 @@ int midas_gpu_nn_gradients(midas_gpu_ctx *ctx, midas_gpu_nn *net, int batch, con
 /* One Adam step (beta 0.9 / 0.999, eps 1e-8) at learning rate lr on that loss. */
 int midas_gpu_nn_train_step(midas_gpu_ctx *ctx, midas_gpu_nn *net, int batch, const float *inputs, const float *mask,
                             const float *target, float lr, double *loss);
+
+/* The network as a learned right preconditioner (no counterpart in the
+ * reference).  The same network, with the 16 input channels holding a cell
+ * vector v on the grid: Re, Im of chi in 0-1, s D^-1 v (D = 1 - Znnpp, the
+ * Jacobi term) in 2-7, s v in 8-13, the mask in 14 and Re 3 / (eps + 2) in 15,
+ * each complex vector as (Re, Im) of x, y, z; the prediction (channels 2-7 plus
+ * the network's output, divided by s) approximates Z^-1 v.  The cells must lie
+ * on one lattice whose box fits the network's grid; the box is centred in it.
+ *
+ * midas_gpu_nn_prec_grid writes these inputs and the mask for ncol cell vectors
+ * V (3n x ncol column-major complex, host or device) at scales scale[ncol]:
+ * the training pairs of the preconditioner (inputs from r = Z e, the target e
+ * read from channels 8-13 of the grid of e at r's scale).
+ *
+ * midas_gpu_fgmres_solve is midas_gpu_gmres_solve with the network as its
+ * right preconditioner (flexible GMRES: the preconditioned vectors are kept);
+ * convergence is judged on the FP64 true residual as there. */
+int midas_gpu_nn_prec_grid(midas_gpu_ctx *ctx, midas_gpu_nn *net, int ncol, const double *V, const double *scale,
+                           float *inputs, float *mask);
+int midas_gpu_fgmres_solve(midas_gpu_ctx *ctx, midas_gpu_nn *net, int ntr, const double *theta, const double *phi,
+                           const double *E0, int restart, int maxit, double tol, double *E, midas_gpu_info *info);
 
 /* Plain MoM: fill, solve, internal field E (3n x 2ntr).  The field part of
  * Compute_EFields_MoM (src/Compute_EFields_MoM.f90:66-229). */

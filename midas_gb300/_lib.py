@@ -36,7 +36,7 @@ EXPORTS = [
     "midas_gpu_block_fill", "midas_gpu_sr_fill", "midas_gpu_set_fsr", "midas_gpu_aca", "midas_gpu_dense_solve",
     "midas_gpu_mom_solve", "midas_gpu_lattice_matvec", "midas_gpu_gmres_solve", "midas_gpu_nn_create", "midas_gpu_nn_free",
     "midas_gpu_nn_param_count", "midas_gpu_nn_params", "midas_gpu_nn_forward", "midas_gpu_nn_gradients",
-    "midas_gpu_nn_train_step", "midas_gpu_cbfm_solve", "midas_gpu_dense_solve_noalloc", "midas_gpu_cext_cabs", "midas_gpu_smatrix",
+    "midas_gpu_nn_train_step", "midas_gpu_nn_prec_grid", "midas_gpu_fgmres_solve", "midas_gpu_cbfm_solve", "midas_gpu_dense_solve_noalloc", "midas_gpu_cext_cabs", "midas_gpu_smatrix",
     "midas_gpu_scattering_quantities", "midas_gpu_wait_event", "midas_gpu_record_event",
     "midas_gpu_gemm_selftest", "midas_gpu_gemm_engine", "midas_gpu_wait_selftest", "midas_gpu_launch_count", "midas_gpu_stream",
     "midas_gpu_bench_gemm", "midas_gpu_bench_gemm_ex", "midas_gpu_heev", "midas_gpu_zgemm_x3", "midas_gpu_profile", "midas_gpu_profile_query",
@@ -110,6 +110,8 @@ def load(path: str = LIB_PATH):
         "midas_gpu_nn_param_count": (ctypes.c_longlong, [vp]),
         "midas_gpu_nn_params": (i, [vp, vp, i, P, i]),
         "midas_gpu_nn_forward": (i, [vp, vp, i, P, P, P]),
+        "midas_gpu_nn_prec_grid": (i, [vp, vp, i, P, P, P, P]),
+        "midas_gpu_fgmres_solve": (i, [vp, vp, i, P, P, P, i, i, d, P, ctypes.POINTER(Info)]),
         "midas_gpu_nn_gradients": (i, [vp, vp, i, P, P, P, ctypes.POINTER(ctypes.c_double)]),
         "midas_gpu_nn_train_step": (i, [vp, vp, i, P, P, P, ctypes.c_float, ctypes.POINTER(ctypes.c_double)]),
         "midas_gpu_dense_solve_noalloc": (i, [i, vp, i, i, P, P, ctypes.POINTER(ctypes.c_double)]),

@@ -65,19 +65,20 @@ __global__ void k_pad_diag32(float2 *Z, long long ld, int n0, int np)
 }
 
 // X64 += d32 ; Xh = fp32(X64) ; Xl = fp32(X64 - Xh)   (n x m column-major, ld n);
-// with rm = 1, Xh and Xl are written row-major (n x m) for the CSR residual
+// with rm = 1, Xh and Xl are written row-major (n rows of ldx) for the CSR
+// residual and the correction d row-major (n x m) into Drm
 __global__ void k_ir_update(long long tot, int n, int m, double2 *X64, const float2 *d32, float2 *Xh, float2 *Xl,
-                            float2 *Drm, int first, int rm)
+                            float2 *Drm, int first, int rm, int ldx)
 {
     long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i >= tot) return;
     double2 x = first ? make_double2(d32[i].x, d32[i].y) : make_double2(X64[i].x + d32[i].x, X64[i].y + d32[i].y);
     X64[i] = x;
     float2 h = make_float2((float)x.x, (float)x.y);
-    long long o = rm ? (i % n) * m + i / n : i;
+    const long long o = rm ? (i % n) * ldx + i / n : i;
     Xh[o] = h;
     Xl[o] = make_float2((float)(x.x - h.x), (float)(x.y - h.y));
-    if (Drm) Drm[o] = d32[i];   // the correction, for the FP32 residual update
+    if (Drm) Drm[rm ? (i % n) * m + i / n : i] = d32[i];   // the correction, for the FP32 residual update
 }
 
 // d = fp32(r) and x += d, for the correction of the reduced solution
@@ -197,14 +198,18 @@ static int cbf_block(midas_gpu_ctx *c, const CbfShared &S, int b)
         double2 *X64 = S.Xall + S.xoff[b];
         // work buffers of this lane (grow-only; the lane takes its blocks largest first)
         const size_t nrm = (size_t)sp * m;
+        // row stride of the row-major Xh / Xl the CSR residual reads (its column groups, no tail)
+        const int ldx = sr ? csr_resid_ldx(m) : m;
+        const size_t nrx = (size_t)sp * ldx;
         void *p1, *p2 = nullptr, *p3, *pred;
         MIDAS_TRY(ensure(c, S_CBF1, sizeof(float2) * (size_t)sp * sp, &p1));
         if (!sr) MIDAS_TRY(ensure(c, S_CBF2, sizeof(float2) * (size_t)sp * sp, &p2));
-        MIDAS_TRY(ensure(c, S_CBF3, (sizeof(float2) * 5 + sizeof(double2)) * nrm + 8 * 256, &p3));
+        MIDAS_TRY(ensure(c, S_CBF3, (sizeof(float2) * 3 + sizeof(double2)) * nrm + sizeof(float2) * 2 * nrx + 8 * 256,
+                         &p3));
         MIDAS_TRY(ensure(c, S_RED2, sizeof(unsigned long long) * 2 * m + 64, &pred));
         float2 *Zlu = (float2 *)p1, *Zsr = (float2 *)p2;
         Buf b3{c, 0, (char *)p3};
-        float2 *Bm = b3.take<float2>(nrm), *Xh = b3.take<float2>(nrm), *Xl = b3.take<float2>(nrm),
+        float2 *Bm = b3.take<float2>(nrm), *Xh = b3.take<float2>(nrx), *Xl = b3.take<float2>(nrx),
                *d32 = b3.take<float2>(nrm), *Drm = b3.take<float2>(nrm);
         double2 *R64 = b3.take<double2>(nrm);
         unsigned long long *red = (unsigned long long *)pred;
@@ -262,7 +267,7 @@ static int cbf_block(midas_gpu_ctx *c, const CbfShared &S, int b)
         long long tot = (long long)sp * m;
         ++c->launches;
         k_ir_update<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(tot, sp, m, X64, d32, Xh, Xl,
-                                                                          sr ? Drm : nullptr, 1, sr);
+                                                                          sr ? Drm : nullptr, 1, sr, ldx);
         // Residuals.  The first, B - Z x0, is needed only to ~1e-3 of itself (x0 from
         // the TF32 factors is ~1e-3.5 off), so it is formed as an FP32-grade
         // split-TF32 product on the tensor cores.  Then double-float B - Z x on the
@@ -280,7 +285,7 @@ static int cbf_block(midas_gpu_ctx *c, const CbfShared &S, int b)
             } else if (sr && upd)
                 MIDAS_TRY(resid_update_x3(c, sp, m, A3z, K6z, Drm, (float *)d32, R64));
             else if (sr)
-                MIDAS_TRY(residual_csr_df32(c, zcsr, m, Xh, Xl, Bm, R64));
+                MIDAS_TRY(residual_csr_df32(c, zcsr, m, ldx, Xh, Xl, Bm, R64));
             else
                 MIDAS_TRY(residual_df32(c, sp, m, Zsr, sp, Xh, Xl, Bm, R64));
             MIDAS_CUDA(c, cudaMemsetAsync(red, 0, sizeof(unsigned long long) * 2 * m, c->stream));
@@ -303,14 +308,14 @@ static int cbf_block(midas_gpu_ctx *c, const CbfShared &S, int b)
             MIDAS_TRY(lu_solve(c, lu, d32, m));
             ++c->launches;
             k_ir_update<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(tot, sp, m, X64, d32, Xh, Xl,
-                                                                              upd ? Drm : nullptr, 0, sr);
+                                                                              upd ? Drm : nullptr, 0, sr, ldx);
         }
         if (it == 12) return c->err.set(MIDAS_ERR_NOT_CONVERGED, "cbf block solve: refinement did not converge");
         // Gram G = X^H X over the 3s rows of the extended block, in double float from
         // the refinement's hi/lo copies of X (row-major with SR, column-major without)
         void *pg;
         MIDAS_TRY(ensure(c, S_CBF9, gram_df_scratch_bytes(m), &pg));
-        MIDAS_TRY(gram_df(c, m, N3, Xh, Xl, sr ? m : 1, sr ? 1 : sp, S.Gall + S.mm * b, (float4 *)pg));
+        MIDAS_TRY(gram_df(c, m, N3, Xh, Xl, sr ? ldx : 1, sr ? 1 : sp, S.Gall + S.mm * b, (float4 *)pg));
         S.srefine[b] = it;
     }
     return MIDAS_OK;

@@ -223,8 +223,12 @@ int lattice_matvec(midas_gpu_ctx *c, int nrhs, const double2 *X, long long ldx, 
                    double2 *Y, long long ldy, int slot, bool c4 = false);
 
 // Restarted GMRES on the lattice operator (krylov.cu); X holds the initial guess.
+// With net, flexible GMRES right-preconditioned by the network (nn.cu).
 int gmres_lattice(midas_gpu_ctx *c, int ncol, const double2 *B, double2 *X, int restart, int maxit, double tol,
-                  bool jacobi, int *iters, double *relres);
+                  bool jacobi, int *iters, double *relres, midas_gpu_nn *net = nullptr);
+// Zout = P(V): the network preconditioner on unit-norm cell vectors (nn.cu)
+int nn_prec_apply(midas_gpu_ctx *c, midas_gpu_nn *net, int ncol, const double2 *V, long long ldv, double2 *Zout,
+                  long long ldz);
 
 // Scene preparation on the device (prep.cu); outputs in device memory.
 int voxelise_sphere(midas_gpu_ctx *c, double dm, double sc, long long cap, double *x, double *y, double *z,

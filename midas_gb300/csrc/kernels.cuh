@@ -43,7 +43,10 @@ struct Csr {
     float2 *val = nullptr;
 };
 int csr_from_dense(midas_gpu_ctx *c, int n, const float2 *Z, long long ldz, int slot, Csr *out);
-int residual_csr_df32(midas_gpu_ctx *c, const Csr &Z, int m, const float2 *Xh_rm, const float2 *Xl_rm,
+// right-hand sides per warp pass of the CSR residual; X rows are padded to a multiple
+constexpr int CSR_RESID_COLS = 192;
+inline int csr_resid_ldx(int m) { return (m + CSR_RESID_COLS - 1) / CSR_RESID_COLS * CSR_RESID_COLS; }
+int residual_csr_df32(midas_gpu_ctx *c, const Csr &Z, int m, int ldx, const float2 *Xh_rm, const float2 *Xl_rm,
                       const float2 *B, double2 *R);
 
 // fill.cu

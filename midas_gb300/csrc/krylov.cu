@@ -14,7 +14,9 @@
 // least-squares problems (Givens rotations) run on the host.  Every restart
 // recomputes the true residual b - Z x in FP64, and convergence is accepted on
 // that true residual only.  Optional right preconditioner: the inverse of the
-// matrix diagonal, 1 / (1 - Znnpp) per cell (Jacobi).
+// matrix diagonal, 1 / (1 - Znnpp) per cell (Jacobi), or the learned network of
+// nn.cu, which is not linear and makes the method flexible GMRES (FGMRES: the
+// preconditioned vectors P(v_j) are kept and x += sum_j P(v_j) y_j).
 #include <algorithm>
 #include <cmath>
 #include <complex>
@@ -151,8 +153,9 @@ static unsigned kr_blocks(long long n) { return (unsigned)((n + KR_THREADS - 1) 
 // initial guess on entry.  Returns the iterations (Arnoldi steps) and the final
 // true relative residual max_k ||b_k - Z x_k|| / ||b_k||.
 int gmres_lattice(midas_gpu_ctx *c, int ncol, const double2 *B, double2 *X, int restart, int maxit, double tol,
-                  bool jacobi, int *iters, double *relres)
+                  bool jacobi, int *iters, double *relres, midas_gpu_nn *net)
 {
+    if (net) jacobi = false;   // the network's prediction contains the Jacobi term
     MIDAS_TRY(lattice_fft_prepare(c));
     const int N = 3 * c->n;
     const int m = std::max(1, restart);
@@ -160,13 +163,15 @@ int gmres_lattice(midas_gpu_ctx *c, int ncol, const double2 *B, double2 *X, int 
     const int nblk = (N + KR_CHUNK - 1) / KR_CHUNK;
     void *p;
     const size_t vbytes = sizeof(double2) * (size_t)vs;
-    MIDAS_TRY(ensure(c, S_KRYLOV, vbytes * (m + 1) + 3 * vbytes + sizeof(double2) * ((size_t)ncol * (m + 2) * nblk +
+    const int nz = net ? m : 0;   // flexible GMRES keeps the preconditioned vectors P(v_j)
+    MIDAS_TRY(ensure(c, S_KRYLOV, vbytes * (m + 1 + nz) + 3 * vbytes + sizeof(double2) * ((size_t)ncol * (m + 2) * nblk +
                                                                                      (size_t)ncol * (m + 2) + 64) +
                                       sizeof(double) * ncol + sizeof(int) * ncol + 4096,
                       &p));
     char *base = (char *)p;
     auto take = [&](size_t bytes) { char *q = base; base += (bytes + 255) & ~(size_t)255; return q; };
     double2 *V = (double2 *)take(vbytes * (m + 1));
+    double2 *Zp = net ? (double2 *)take(vbytes * m) : nullptr;
     double2 *W = (double2 *)take(vbytes), *R = (double2 *)take(vbytes), *Tz = (double2 *)take(vbytes);
     double2 *partial = (double2 *)take(sizeof(double2) * (size_t)ncol * (m + 2) * nblk);
     double2 *hdev = (double2 *)take(sizeof(double2) * ((size_t)ncol * (m + 2) + 64));
@@ -215,7 +220,10 @@ int gmres_lattice(midas_gpu_ctx *c, int ncol, const double2 *B, double2 *X, int 
             const double2 *vj = V + j * vs;
             // W = Z M^-1 v_j
             const double2 *zin = vj;
-            if (jacobi) {
+            if (net) {
+                MIDAS_TRY(nn_prec_apply(c, net, ncol, vj, N, Zp + j * vs, N));
+                zin = Zp + j * vs;
+            } else if (jacobi) {
                 ++c->launches;
                 k_kr_jacobi<<<dim3(kr_blocks(N), ncol), KR_THREADS, 0, c->stream>>>(c->n, ncol, c->znnpp, vj, Tz);
                 zin = Tz;
@@ -282,7 +290,10 @@ int gmres_lattice(midas_gpu_ctx *c, int ncol, const double2 *B, double2 *X, int 
         }
         MIDAS_CUDA(c, cudaMemcpyAsync(hdev, y.data(), sizeof(double2) * (size_t)ncol * m, cudaMemcpyHostToDevice,
                                       c->stream));
-        if (jacobi) {
+        if (net) {   // x += sum_j P(v_j) y_j
+            ++c->launches;
+            k_kr_axpy<<<gv, KR_THREADS, 0, c->stream>>>(N, ncol, j, Zp, vs, hdev, m, 1.0, adev, X);
+        } else if (jacobi) {
             MIDAS_CUDA(c, cudaMemsetAsync(W, 0, vbytes, c->stream));
             ++c->launches;
             k_kr_axpy<<<gv, KR_THREADS, 0, c->stream>>>(N, ncol, j, V, vs, hdev, m, 1.0, adev, W);

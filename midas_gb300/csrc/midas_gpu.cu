@@ -836,8 +836,8 @@ int midas_gpu_lattice_matvec(midas_gpu_ctx *c, int nrhs, const double *X, double
     return check_flag(c, "lattice_matvec");
 }
 
-int midas_gpu_gmres_solve(midas_gpu_ctx *c, int ntr, const double *theta, const double *phi, const double *E0,
-                          int restart, int maxit, double tol, int flags, double *E, midas_gpu_info *info)
+static int gmres_solve(midas_gpu_ctx *c, midas_gpu_nn *net, int ntr, const double *theta, const double *phi,
+                       const double *E0, int restart, int maxit, double tol, int flags, double *E, midas_gpu_info *info)
 {
     if (!c) return MIDAS_ERR_ARG;
     c->err = Err();
@@ -863,7 +863,7 @@ int midas_gpu_gmres_solve(midas_gpu_ctx *c, int ntr, const double *theta, const 
     double rel = 0;
     Timer ts(c->stream);
     int st = gmres_lattice(c, nrhs, (const double2 *)pb, (double2 *)px, restart, maxit, tol,
-                           (flags & MIDAS_GMRES_JACOBI) != 0, &iters, &rel);
+                           (flags & MIDAS_GMRES_JACOBI) != 0, &iters, &rel, net);
     const float tsol = ts.stop();
     const int cst = copy_out(c, E, px, bytes);
     if (st == MIDAS_OK) st = cst;
@@ -875,6 +875,20 @@ int midas_gpu_gmres_solve(midas_gpu_ctx *c, int ntr, const double *theta, const 
         info->t_total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     }
     return st;
+}
+
+int midas_gpu_gmres_solve(midas_gpu_ctx *c, int ntr, const double *theta, const double *phi, const double *E0,
+                          int restart, int maxit, double tol, int flags, double *E, midas_gpu_info *info)
+{
+    return gmres_solve(c, nullptr, ntr, theta, phi, E0, restart, maxit, tol, flags, E, info);
+}
+
+int midas_gpu_fgmres_solve(midas_gpu_ctx *c, midas_gpu_nn *net, int ntr, const double *theta, const double *phi,
+                           const double *E0, int restart, int maxit, double tol, double *E, midas_gpu_info *info)
+{
+    if (!c) return MIDAS_ERR_ARG;
+    if (!net) return c->err.set(MIDAS_ERR_ARG, "fgmres_solve: no network");
+    return gmres_solve(c, net, ntr, theta, phi, E0, restart, maxit, tol, 0, E, info);
 }
 
 int midas_gpu_cbfm_solve(midas_gpu_ctx *c, int nblocks, const int *blk_offsets, const int *ext_offsets,

@@ -419,6 +419,126 @@ static int nn_stage(midas_gpu_ctx *c, midas_gpu_nn *net, int B, const float *in,
     return MIDAS_OK;
 }
 
+// ---------------------------------------------------------------------------
+// The network as a right preconditioner of flexible GMRES.  A Krylov vector v
+// (cells, 3 complex rows per cell) is placed on the network's grid at its
+// lattice position, as 16 channels per voxel:
+//   0-1  Re, Im chi = eps - 1          2-7   s D^-1 v  (D = 1 - Znnpp, Jacobi)
+//   8-13 s v                           14    mask (1)
+//   15   Re 3 / (eps + 2)              (0 outside the cells)
+// s scales v to O(1) entries.  The network's prediction -- channels 2-7 plus
+// its output -- is the scaled approximation of Z^-1 v, gathered back to the
+// cells and divided by s.  The lattice box is centred in the grid.
+// ---------------------------------------------------------------------------
+struct NnPlace {
+    int ox, oy, oz, lo0, lo1, lo2;
+};
+
+static int nn_place(midas_gpu_ctx *c, const midas_gpu_nn *net, NnPlace *pl)
+{
+    if (!c->lattice || !c->lat_ijk) return c->err.set(MIDAS_ERR_UNSUPPORTED, "nn preconditioner: cells are not on a lattice");
+    int o[3];
+    for (int a = 0; a < 3; ++a) {
+        const int ext = c->lat_hi[a] - c->lat_lo[a] + 1;
+        if (ext > net->grid) return c->err.set(MIDAS_ERR_UNSUPPORTED, "nn preconditioner: lattice wider than the network grid");
+        o[a] = (net->grid - ext) / 2;
+    }
+    *pl = NnPlace{o[0], o[1], o[2], c->lat_lo[0], c->lat_lo[1], c->lat_lo[2]};
+    return MIDAS_OK;
+}
+
+__device__ __forceinline__ long long nn_voxel(const int *ijk, int i, int G, const NnPlace &pl)
+{
+    const int x = ijk[3 * i] - pl.lo0 + pl.ox, y = ijk[3 * i + 1] - pl.lo1 + pl.oy, z = ijk[3 * i + 2] - pl.lo2 + pl.oz;
+    return ((long long)z * G + y) * G + x;
+}
+
+__device__ __forceinline__ double2 nn_cdiv(double2 a, double2 b)
+{
+    const double den = b.x * b.x + b.y * b.y;
+    return make_double2((a.x * b.x + a.y * b.y) / den, (a.y * b.x - a.x * b.y) / den);
+}
+
+// one thread per (cell, column); V column k at V + k ldv; scale[k] (or s_all when scale is null)
+__global__ void k_nn_prec_scatter(int ncell, int ncol, int G, NnPlace pl, const int *ijk, const double2 *eps,
+                                  const double2 *znnpp, const double2 *V, long long ldv, const double *scale,
+                                  double s_all, float *in, float *mask)
+{
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= (long long)ncell * ncol) return;
+    const int i = (int)(t % ncell), k = (int)(t / ncell);
+    const long long r = (long long)k * G * G * G + nn_voxel(ijk, i, G, pl);
+    const double s = scale ? scale[k] : s_all;
+    const double2 e = eps[i], d = make_double2(1.0 - znnpp[i].x, -znnpp[i].y);
+    const double2 cm = nn_cdiv(make_double2(3.0, 0.0), make_double2(e.x + 2.0, e.y));
+    float *row = in + r * NN_CIN0;
+    row[0] = (float)(e.x - 1.0);
+    row[1] = (float)e.y;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        const double2 v = V[(long long)k * ldv + 3 * i + q], w = nn_cdiv(v, d);
+        row[2 + 2 * q] = (float)(s * w.x);
+        row[3 + 2 * q] = (float)(s * w.y);
+        row[8 + 2 * q] = (float)(s * v.x);
+        row[9 + 2 * q] = (float)(s * v.y);
+    }
+    row[14] = 1.f;
+    row[15] = (float)cm.x;
+    mask[r] = 1.f;
+}
+
+// Zout column k = (channels 2-7 + output + bias) / s at each cell
+__global__ void k_nn_prec_gather(int ncell, int ncol, int G, NnPlace pl, const int *ijk, const float *in,
+                                 const float *D, const float *b, double s_all, double2 *Zout, long long ldz)
+{
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= (long long)ncell * ncol) return;
+    const int i = (int)(t % ncell), k = (int)(t / ncell);
+    const long long r = (long long)k * G * G * G + nn_voxel(ijk, i, G, pl);
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        const double re = (double)in[r * NN_CIN0 + 2 + 2 * q] + (double)(D[r * 8 + 2 * q] + b[2 * q]);
+        const double im = (double)in[r * NN_CIN0 + 3 + 2 * q] + (double)(D[r * 8 + 2 * q + 1] + b[2 * q + 1]);
+        Zout[(long long)k * ldz + 3 * i + q] = make_double2(re / s_all, im / s_all);
+    }
+}
+
+static int nn_check(midas_gpu_ctx *c, midas_gpu_nn *net, int B);
+
+static int nn_prec_inputs(midas_gpu_ctx *c, midas_gpu_nn *net, int ncol, const double2 *V, long long ldv,
+                          const double *scale, double s_all, float *in, float *mask, const NnPlace &pl)
+{
+    const long long M = (long long)ncol * net->grid * net->grid * net->grid;
+    MIDAS_CUDA(c, cudaMemsetAsync(in, 0, sizeof(float) * M * NN_CIN0, c->stream));
+    MIDAS_CUDA(c, cudaMemsetAsync(mask, 0, sizeof(float) * M, c->stream));
+    ++c->launches;
+    k_nn_prec_scatter<<<nb((long long)c->n * ncol), 256, 0, c->stream>>>(c->n, ncol, net->grid, pl, c->lat_ijk, c->eps,
+                                                                        c->znnpp, V, ldv, scale, s_all, in, mask);
+    MIDAS_CUDA(c, cudaGetLastError());
+    return MIDAS_OK;
+}
+
+// Zout = P(V) for unit-norm columns V (3n x ncol, ld ldv): the network preconditioner
+int nn_prec_apply(midas_gpu_ctx *c, midas_gpu_nn *net, int ncol, const double2 *V, long long ldv, double2 *Zout,
+                  long long ldz)
+{
+    MIDAS_TRY(nn_check(c, net, ncol));
+    NnPlace pl;
+    MIDAS_TRY(nn_place(c, net, &pl));
+    const long long M = (long long)ncol * net->grid * net->grid * net->grid;
+    NnWork w;
+    MIDAS_TRY(nn_workspace(c, M, w));
+    const double s = sqrt((double)c->n);   // |v| = 1: entries of s v are O(1)
+    MIDAS_TRY(nn_prec_inputs(c, net, ncol, V, ldv, nullptr, s, w.in32, w.mask32, pl));
+    MIDAS_TRY(nn_forward(c, net, ncol, w));
+    ++c->launches;
+    k_nn_prec_gather<<<nb((long long)c->n * ncol), 256, 0, c->stream>>>(c->n, ncol, net->grid, pl, c->lat_ijk, w.in32,
+                                                                       w.Z[NN_LAYERS - 1], net->b[NN_LAYERS - 1], s,
+                                                                       Zout, ldz);
+    MIDAS_CUDA(c, cudaGetLastError());
+    return MIDAS_OK;
+}
+
 static int nn_check(midas_gpu_ctx *c, midas_gpu_nn *net, int B)
 {
     if (!c || !net) return MIDAS_ERR_ARG;
@@ -546,6 +666,32 @@ int midas_gpu_nn_forward(midas_gpu_ctx *c, midas_gpu_nn *net, int batch, const f
     if (out != E) MIDAS_CUDA(c, cudaMemcpyAsync(E, out, sizeof(float) * M * 6, cudaMemcpyDeviceToHost, c->stream));
     MIDAS_CUDA(c, cudaStreamSynchronize(c->stream));
     return check_flag(c, "nn_forward");
+}
+
+int midas_gpu_nn_prec_grid(midas_gpu_ctx *c, midas_gpu_nn *net, int ncol, const double *V, const double *scale,
+                           float *inputs, float *mask)
+{
+    MIDAS_TRY(nn_check(c, net, ncol));
+    if (!V || !scale || !inputs || !mask) return MIDAS_ERR_ARG;
+    c->err = Err();
+    cudaSetDevice(c->device);
+    if (c->n <= 0) return c->err.set(MIDAS_ERR_STATE, "nn_prec_grid: no cells");
+    NnPlace pl;
+    MIDAS_TRY(nn_place(c, net, &pl));
+    const long long M = (long long)ncol * net->grid * net->grid * net->grid;
+    const size_t vb = sizeof(double2) * 3 * (size_t)c->n * ncol;
+    void *pv, *ps, *po;
+    MIDAS_TRY(ensure(c, S_IN2, vb, &pv));
+    MIDAS_TRY(ensure(c, S_IN3, sizeof(double) * ncol, &ps));
+    MIDAS_TRY(ensure(c, S_OUT0, sizeof(float) * M * (NN_CIN0 + 1), &po));
+    MIDAS_CUDA(c, cudaMemcpyAsync(pv, V, vb, cudaMemcpyDefault, c->stream));
+    MIDAS_CUDA(c, cudaMemcpyAsync(ps, scale, sizeof(double) * ncol, cudaMemcpyDefault, c->stream));
+    float *din = (float *)po, *dmask = din + M * NN_CIN0;
+    MIDAS_TRY(nn_prec_inputs(c, net, ncol, (const double2 *)pv, 3LL * c->n, (const double *)ps, 0.0, din, dmask, pl));
+    MIDAS_CUDA(c, cudaMemcpyAsync(inputs, din, sizeof(float) * M * NN_CIN0, cudaMemcpyDefault, c->stream));
+    MIDAS_CUDA(c, cudaMemcpyAsync(mask, dmask, sizeof(float) * M, cudaMemcpyDefault, c->stream));
+    MIDAS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return check_flag(c, "nn_prec_grid");
 }
 
 int midas_gpu_nn_gradients(midas_gpu_ctx *c, midas_gpu_nn *net, int batch, const float *inputs, const float *mask,

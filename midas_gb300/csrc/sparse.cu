@@ -116,76 +116,86 @@ int csr_from_dense(midas_gpu_ctx *c, int n, const float2 *Z, long long ldz, int 
 }
 
 // ---------------------------------------------------------------------------
-// r = B - Z (Xh + Xl) with Z in CSR form.  Xh, Xl row-major (n x m), B
-// column-major float (ld n), r column-major FP64 (ld n).  A warp per row; the
-// lanes run over RESID_COLS right-hand sides (blockIdx.y selects the group),
-// each holding RESID_COLS / 32 double-float accumulators.  The products with
-// Xh are exact (fma residue) and summed in double-float; the products with Xl
-// (2^-24 smaller) are summed in FP32.
+// r = B - Z (Xh + Xl) with Z in CSR form.  Xh, Xl row-major (n rows of ldx, ldx a
+// multiple of CSR_RESID_COLS), B column-major float (ld n), r column-major FP64
+// (ld n).  A warp per row; the lanes run over CSR_RESID_COLS right-hand sides
+// (blockIdx.y selects the group), CSR_T per lane, so the per-nonzero work (the
+// shuffle broadcast of the column offset and the value) is shared by 6 complex
+// multiply-adds.  The products with Xh are exact (FMA TwoProduct) and summed by
+// TwoSum; the products with Xl (2^-24 smaller) are added in FP32 into the same
+// low word.  The padded columns of X are read but never stored.
 // ---------------------------------------------------------------------------
-constexpr int RESID_COLS = 96;
-constexpr int RESID_T = RESID_COLS / 32;
+constexpr int CSR_T = CSR_RESID_COLS / 32;
 
-__global__ void __launch_bounds__(256) k_resid_csr_df32(int n, int m, const int *rowptr, const int *col,
+// (hi, lo) += a (bh + bl) with a exact: a bh exactly, a bl in FP32 into lo
+__device__ __forceinline__ void df_fma_lo(float &hi, float &lo, float a, float bh, float bl)
+{
+    const float p = __fmul_rn(a, bh);
+    float pe = fmaf(a, bh, -p);
+    pe = fmaf(a, bl, pe);
+    float s, e;
+    ef_two_sum(hi, p, s, e);
+    hi = s;
+    lo = __fadd_rn(lo, __fadd_rn(e, pe));
+}
+
+__global__ void __launch_bounds__(256) k_resid_csr_df32(int n, int m, int ldx, const int *rowptr, const int *col,
                                                          const float2 *val, const float2 *Xh, const float2 *Xl,
                                                          const float2 *B, double2 *R)
 {
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (i >= n) return;
-    const int c0 = blockIdx.y * RESID_COLS;
-    float rh[RESID_T], rl[RESID_T], ih[RESID_T], il[RESID_T], cr[RESID_T], ci[RESID_T];
+    const int c0 = blockIdx.y * CSR_RESID_COLS + lane;
+    float rh[CSR_T], rl[CSR_T], ih[CSR_T], il[CSR_T];
 #pragma unroll
-    for (int t = 0; t < RESID_T; ++t) { rh[t] = rl[t] = ih[t] = il[t] = cr[t] = ci[t] = 0.f; }
+    for (int t = 0; t < CSR_T; ++t) rh[t] = rl[t] = ih[t] = il[t] = 0.f;
     const int p1 = rowptr[i + 1];
+    const float2 *xh0 = Xh + c0, *xl0 = Xl + c0;
     // the row's (column, value) pairs are read 32 at a time, one per lane, and
     // broadcast with shuffles, so the X gathers do not wait on index loads
     for (int p0 = rowptr[i]; p0 < p1; p0 += 32) {
         const int cnt = min(32, p1 - p0);
-        int mk = 0;
+        int mk = 0;   // row offset of X (n ldx < 2^31, checked by the launcher)
         float2 mz = make_float2(0.f, 0.f);
-        if (lane < cnt) { mk = col[p0 + lane]; mz = val[p0 + lane]; }
-#pragma unroll 4
+        if (lane < cnt) { mk = col[p0 + lane] * ldx; mz = val[p0 + lane]; }
+#pragma unroll 2
         for (int q = 0; q < cnt; ++q) {
             const int k = __shfl_sync(0xffffffffu, mk, q);
-            float2 z;
-            z.x = __shfl_sync(0xffffffffu, mz.x, q);
-            z.y = __shfl_sync(0xffffffffu, mz.y, q);
-            const float2 *xh = Xh + (long long)k * m, *xl = Xl + (long long)k * m;
+            const float zx = __shfl_sync(0xffffffffu, mz.x, q), zy = __shfl_sync(0xffffffffu, mz.y, q);
+            const float2 *xh = xh0 + k, *xl = xl0 + k;
+            float2 h[CSR_T], l[CSR_T];
 #pragma unroll
-            for (int t = 0; t < RESID_T; ++t) {
-                const int cc = c0 + lane + 32 * t;
-                if (cc < m) {
-                    float2 h = xh[cc], l = xl[cc];
-                    df_fma(rh[t], rl[t], z.x, h.x);
-                    df_fma(rh[t], rl[t], -z.y, h.y);
-                    df_fma(ih[t], il[t], z.x, h.y);
-                    df_fma(ih[t], il[t], z.y, h.x);
-                    cr[t] += z.x * l.x - z.y * l.y;
-                    ci[t] += z.x * l.y + z.y * l.x;
-                }
+            for (int t = 0; t < CSR_T; ++t) { h[t] = xh[32 * t]; l[t] = xl[32 * t]; }
+#pragma unroll
+            for (int t = 0; t < CSR_T; ++t) {
+                df_fma_lo(rh[t], rl[t], zx, h[t].x, l[t].x);
+                df_fma_lo(rh[t], rl[t], -zy, h[t].y, l[t].y);
+                df_fma_lo(ih[t], il[t], zx, h[t].y, l[t].y);
+                df_fma_lo(ih[t], il[t], zy, h[t].x, l[t].x);
             }
         }
     }
 #pragma unroll
-    for (int t = 0; t < RESID_T; ++t) {
-        const int cc = c0 + lane + 32 * t;
+    for (int t = 0; t < CSR_T; ++t) {
+        const int cc = c0 + 32 * t;
         if (cc < m) {
-            double zr = (double)rh[t] + (double)rl[t] + (double)cr[t];
-            double zi = (double)ih[t] + (double)il[t] + (double)ci[t];
-            float2 b = B[(long long)cc * n + i];
-            R[(long long)cc * n + i] = make_double2((double)b.x - zr, (double)b.y - zi);
+            const float2 b = B[(long long)cc * n + i];
+            R[(long long)cc * n + i] = make_double2((double)b.x - ((double)rh[t] + (double)rl[t]),
+                                                    (double)b.y - ((double)ih[t] + (double)il[t]));
         }
     }
 }
 
-int residual_csr_df32(midas_gpu_ctx *c, const Csr &Z, int m, const float2 *Xh_rm, const float2 *Xl_rm,
+int residual_csr_df32(midas_gpu_ctx *c, const Csr &Z, int m, int ldx, const float2 *Xh_rm, const float2 *Xl_rm,
                       const float2 *B, double2 *R)
 {
     const int n = Z.n;
+    if (ldx < m || ldx % CSR_RESID_COLS) return c->err.set(MIDAS_ERR_ARG, "csr residual: bad X row stride");
+    if ((long long)n * ldx >= (1LL << 31)) return c->err.set(MIDAS_ERR_UNSUPPORTED, "csr residual: X above 2^31 entries");
     ++c->launches;
     int kp = kp_begin(c);
-    dim3 grd((unsigned)(((long long)n * 32 + 255) / 256), (m + RESID_COLS - 1) / RESID_COLS);
-    k_resid_csr_df32<<<grd, 256, 0, c->stream>>>(n, m, Z.rowptr, Z.col, Z.val, Xh_rm, Xl_rm, B, R);
+    dim3 grd((unsigned)(((long long)n * 32 + 255) / 256), (m + CSR_RESID_COLS - 1) / CSR_RESID_COLS);
+    k_resid_csr_df32<<<grd, 256, 0, c->stream>>>(n, m, ldx, Z.rowptr, Z.col, Z.val, Xh_rm, Xl_rm, B, R);
     kp_end(c, kp, MIDAS_KC_RESID, 8.0 * Z.nnz * m, 12.0 * Z.nnz + 16.0 * (double)n * m * 2 + 24.0 * (double)n * m);
     MIDAS_CUDA(c, cudaGetLastError());
     return MIDAS_OK;

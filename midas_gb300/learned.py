@@ -1,24 +1,32 @@
-"""Learned initial guess for the Krylov solve of voxel scatterers.
+"""Learned initial guess and learned preconditioner for the Krylov solve of
+voxel scatterers.
 
-    python -m midas_gb300.learned [--grid 32] [--train 2000] [--test 500] [--epochs 30]
+    python -m midas_gb300.learned [--grid 32] [--train 2000] [--prec-scenes 300] [--test 500]
 
-Workflow (all arithmetic in the library: GMRES on the FFT lattice operator,
-the network's forward, backward and Adam kernels; numpy only assembles arrays):
+Workflow (all arithmetic in the library: GMRES and flexible GMRES on the FFT
+lattice operator, the network's forward, backward and Adam kernels; numpy only
+assembles arrays):
 
 1. seeded scenes on a grid^3 voxel grid -- Gaussian random spheres and
    aggregates of touching spheres, per-voxel complex permittivity, size
    parameter 1..8, one incident direction (two polarisations);
-2. training pairs from the solver itself: each scene's internal field from
-   GMRES (midas_gpu_gmres_solve) to a 1e-6 true relative residual;
-3. training of the network (midas_gpu_nn_train_step);
-4. held-out scenes: GMRES from zero against GMRES from the network's
-   prediction, both to the same FP64-checked residual, and the dense mixed
-   solve (LU + refinement to a 1e-13 backward error, the reference's PZGESV
-   answer) as the judge of the field error.
+2. the initial-guess network: training pairs from the solver itself (each
+   scene's internal field from GMRES, midas_gpu_gmres_solve, to a 1e-6 true
+   relative residual), trained on (incident field, permittivity) -> field;
+3. the preconditioner network: pairs (r = Z e, e) with e the Arnoldi vectors
+   of the Jacobi-preconditioned operator (no solve needed), trained to map a
+   Krylov vector to Z^-1 of it; it right-preconditions flexible GMRES
+   (midas_gpu_fgmres_solve);
+4. held-out scenes: GMRES from zero, from the incident field and from the
+   guess, flexible GMRES with the preconditioner from zero and from the guess,
+   all to the same FP64-checked true residual, with the dense mixed solve (LU
+   + refinement to a 1e-13 backward error, the reference's PZGESV answer) as
+   the judge of each field error.
 
 The reference (Compute_EFields_MoM, src/Compute_EFields_MoM.f90:153-198)
-solves these systems densely; nothing here changes that answer -- the network
-only chooses where the Krylov iteration starts.
+solves these systems densely; nothing here changes that answer -- the
+networks only choose where the Krylov iteration starts and which directions
+it explores, and every answer is accepted on its FP64 true residual.
 """
 from __future__ import annotations
 
@@ -79,6 +87,19 @@ class Net:
         self.ctx._ck(self.L.midas_gpu_nn_gradients(self.ctx.h, self.h, inputs.shape[0], addr(_f32(inputs)),
                                                    addr(_f32(mask)), addr(_f32(target)), ctypes.byref(loss)))
         return loss.value
+
+    def prec_grid(self, V, scale, out=None):
+        """Preconditioner inputs [ncol, grid^3, 16] and mask [ncol, grid^3] of cell
+        vectors V (3n, ncol) at scales scale[ncol] (midas_gpu_nn_prec_grid).  out =
+        (inputs, mask) device tensors to write into, else host arrays."""
+        V = np.ascontiguousarray(np.asarray(V, np.complex128).T)
+        ncol = V.shape[0]
+        sc = np.ascontiguousarray(scale, np.float64)
+        if out is None:
+            out = (np.zeros((ncol, self.grid ** 3, IN_CH), np.float32), np.zeros((ncol, self.grid ** 3), np.float32))
+        self.ctx._ck(self.L.midas_gpu_nn_prec_grid(self.ctx.h, self.h, ncol, addr(V), addr(sc), addr(out[0]),
+                                                   addr(out[1])))
+        return out
 
     def train_step(self, inputs, mask, target, lr: float) -> float:
         loss = ctypes.c_double()
@@ -245,8 +266,10 @@ def generate(ctx, scene_list, tol=1e-6, log=None):
     return (np.concatenate(ins), np.concatenate(masks), np.concatenate(tgts)), its
 
 
-def train(net, data, epochs=8, batch=8, lr=2e-3, seed=0, log=None):
-    """Adam over shuffled batches; the learning rate falls as a cosine to 5 % of lr."""
+def train(net, data, epochs=8, batch=8, lr=1e-3, seed=0, log=None):
+    """Adam over shuffled batches; the learning rate falls as a cosine to 5 % of lr.
+    (With He-initialised weights a rate of 3e-3 kills the ReLUs of this network on
+    the 16^3 scenes within two epochs; 1e-3 trains.)"""
     inputs, mask, target = data
     rng = np.random.default_rng(seed)
     hist = []
@@ -256,7 +279,7 @@ def train(net, data, epochs=8, batch=8, lr=2e-3, seed=0, log=None):
         losses = []
         lr_ep = lr * (0.05 + 0.95 * 0.5 * (1.0 + math.cos(math.pi * ep / max(1, epochs))))
         for b in range(nb):
-            sel = order[b * batch:(b + 1) * batch]
+            sel = np.sort(order[b * batch:(b + 1) * batch])
             losses.append(net.train_step(inputs[sel], mask[sel], target[sel], lr_ep))
         hist.append(float(np.mean(losses)))
         if log:
@@ -264,26 +287,103 @@ def train(net, data, epochs=8, batch=8, lr=2e-3, seed=0, log=None):
     return hist
 
 
-def evaluate(ctx, net, scene_list, tol=1e-6, judge=0, log=None):
-    """Per held-out scene: GMRES iterations and time from zero and from the
-    network's guess (same tolerance), and for the first `judge` scenes the field
-    error of both against the dense mixed solve."""
+def krylov_pairs(ctx, net, sc, nvec=16):
+    """Training pairs of the preconditioner for one scene, with no solve: the
+    Arnoldi basis e_1..e_nvec of the Jacobi-preconditioned MoM operator started
+    from each polarisation's incident field (the directions GMRES explores), and
+    r_j = Z e_j from the lattice operator.  The network input is r_j on the grid
+    at scale s_j = sqrt(n) / |r_j| (midas_gpu_nn_prec_grid), the target s_j e_j
+    (channels 8-13 of e_j's grid at the same scale): the network learns Z^-1 on
+    Krylov-like vectors.  Returns float16 inputs, uint8 mask, float16 target."""
+    ctx.set_cells(sc["xyz"], sc["sc"], sc["eps"], sc["k0"])
+    b = ctx.mom_rhs(sc["th"], sc["ph"])                     # (3n, 2)
+    D = np.repeat(1.0 - ctx.cell_params()["znnpp"], 3)
+    V = [b / np.linalg.norm(b, axis=0)]
+    for _ in range(nvec - 1):
+        w = ctx.lattice_matvec(V[-1] / D[:, None])
+        for _pass in range(2):                                # classical Gram-Schmidt, twice
+            for v in V:
+                w = w - v * np.sum(np.conj(v) * w, axis=0)
+        V.append(w / np.linalg.norm(w, axis=0))
+    E = np.concatenate(V, axis=1)                             # (3n, 2 nvec)
+    R = ctx.lattice_matvec(E)
+    s = math.sqrt(sc["n"]) / np.linalg.norm(R, axis=0)
+    inp, mask = net.prec_grid(R, s)
+    tg, _ = net.prec_grid(E, s)
+    return inp.astype(np.float16), mask.astype(np.uint8), tg[:, :, 8:14].astype(np.float16)
+
+
+class _Pairs:
+    """Stored pairs, handed to train() batch by batch as float32."""
+
+    def __init__(self, parts):
+        self.a = [np.concatenate([p[q] for p in parts]) for q in range(3)]
+
+    def __len__(self):
+        return len(self.a[0])
+
+    def view(self, q):
+        arr = self.a[q]
+
+        class _V:
+            def __len__(self_v):
+                return len(arr)
+
+            def __getitem__(self_v, sel):
+                return np.ascontiguousarray(arr[sel], np.float32)
+        return _V()
+
+    def as_data(self):
+        return self.view(0), self.view(1), self.view(2)
+
+
+def generate_prec(ctx, net, scene_list, nvec=16, log=None):
+    parts = []
+    for k, sc in enumerate(scene_list):
+        parts.append(krylov_pairs(ctx, net, sc, nvec))
+        if log and (k + 1) % 100 == 0:
+            log(f"  {k + 1}/{len(scene_list)} scenes of preconditioner pairs")
+    return _Pairs(parts)
+
+
+def evaluate(ctx, scene_list, guess_net=None, prec_net=None, tol=1e-6, judge=0, log=None):
+    """Per held-out scene, all to the same FP64-checked true residual: GMRES
+    (Jacobi) from zero, from the incident field and from the guess network's
+    prediction; flexible GMRES with the preconditioner network from zero and
+    from the guess.  The first `judge` scenes are also solved densely (mixed LU +
+    FP64-grade refinement) as the judge of each answer's field error."""
     rows = []
     for k, sc in enumerate(scene_list):
         inp, m = grid_inputs(sc)
-        t0 = time.perf_counter()
-        guess = grid_to_cells(sc, net.forward(inp, m))
-        t_net = time.perf_counter() - t0
-        E0, it0, rel0, t0s = solve_gmres(ctx, sc, tol=tol)
-        _, iti, _, _ = solve_gmres(ctx, sc, E0=grid_to_cells(sc, inp[:, :, 2:8]), tol=tol)
-        E1, it1, rel1, t1s = solve_gmres(ctx, sc, E0=guess, tol=tol)
-        row = {"kind": sc["kind"], "unknowns": 3 * sc["n"], "x": sc["x"], "its_zero": it0, "its_inc": iti,
-               "its_net": it1, "rel_zero": rel0, "rel_net": rel1, "t_zero": t0s, "t_net": t1s + t_net, "tol": tol}
-        Et = ctx.mom_solve(sc["th"], sc["ph"]) if k < judge else None
-        if Et is not None:
+        row = {"kind": sc["kind"], "unknowns": 3 * sc["n"], "x": sc["x"], "tol": tol}
+        sols = {}
+        E0, row["its_zero"], row["rel_zero"], row["t_zero"] = solve_gmres(ctx, sc, tol=tol)
+        sols["zero"] = E0
+        _, row["its_inc"], _, _ = solve_gmres(ctx, sc, E0=grid_to_cells(sc, inp[:, :, 2:8]), tol=tol)
+        guess = None
+        if guess_net is not None:
+            t0 = time.perf_counter()
+            guess = grid_to_cells(sc, guess_net.forward(inp, m))
+            t_g = time.perf_counter() - t0
+            sols["guess"], row["its_guess"], row["rel_guess"], t = solve_gmres(ctx, sc, E0=guess, tol=tol)
+            row["t_guess"] = t + t_g
+        if prec_net is not None:
+            t0 = time.perf_counter()
+            sols["prec"], row["its_prec"], row["rel_prec"] = ctx.fgmres_solve(prec_net, sc["th"], sc["ph"], tol=tol,
+                                                                              maxit=3000, check=False)
+            row["t_prec"] = time.perf_counter() - t0
+            if guess is not None:
+                t0 = time.perf_counter()
+                sols["both"], row["its_both"], row["rel_both"] = ctx.fgmres_solve(prec_net, sc["th"], sc["ph"], E0=guess,
+                                                                                  tol=tol, maxit=3000, check=False)
+                row["t_both"] = time.perf_counter() - t0 + t_g
+        if k < judge:
+            Et = ctx.mom_solve(sc["th"], sc["ph"])
             nrm = np.linalg.norm(Et)
-            row.update({"err_zero": float(np.linalg.norm(E0 - Et) / nrm), "err_net": float(np.linalg.norm(E1 - Et) / nrm),
-                        "err_guess": float(np.linalg.norm(guess - Et) / nrm)})
+            for key, E in sols.items():
+                row["err_" + key] = float(np.linalg.norm(E - Et) / nrm)
+            if guess is not None:
+                row["err_guess_start"] = float(np.linalg.norm(guess - Et) / nrm)
         rows.append(row)
         if log and (k + 1) % 50 == 0:
             log(f"  {k + 1}/{len(scene_list)} held-out scenes")
@@ -291,21 +391,28 @@ def evaluate(ctx, net, scene_list, tol=1e-6, judge=0, log=None):
 
 
 def summarise(rows):
-    its0 = np.array([r["its_zero"] for r in rows], float)
-    itsi = np.array([r["its_inc"] for r in rows], float)
-    its1 = np.array([r["its_net"] for r in rows], float)
+    out = {"scenes": len(rows)}
+    its0 = sum(r["its_zero"] for r in rows)
     t0 = sum(r["t_zero"] for r in rows)
-    t1 = sum(r["t_net"] for r in rows)
-    out = {"scenes": len(rows), "mean_its_zero": float(its0.mean()), "mean_its_incident_start": float(itsi.mean()),
-           "mean_its_net": float(its1.mean()), "iteration_ratio": float(its1.sum() / its0.sum()),
-           "solves_per_s_zero": len(rows) / t0, "solves_per_s_net": len(rows) / t1,
-           "converged_zero": int(sum(r["rel_zero"] <= r["tol"] for r in rows)),
-           "converged_net": int(sum(r["rel_net"] <= r["tol"] for r in rows))}
-    judged = [r for r in rows if "err_net" in r]
+    out.update({"mean_its_zero": its0 / len(rows), "mean_its_incident_start": float(np.mean([r["its_inc"] for r in rows])),
+                "solves_per_s_zero": len(rows) / t0,
+                "converged_zero": int(sum(r["rel_zero"] <= r["tol"] for r in rows))})
+    for key in ("guess", "prec", "both"):
+        if "its_" + key not in rows[0]:
+            continue
+        its = sum(r["its_" + key] for r in rows)
+        t = sum(r["t_" + key] for r in rows)
+        out.update({f"mean_its_{key}": its / len(rows), f"iteration_ratio_{key}": its / its0,
+                    f"solves_per_s_{key}": len(rows) / t,
+                    f"converged_{key}": int(sum(r["rel_" + key] <= r["tol"] for r in rows))})
+    judged = [r for r in rows if "err_zero" in r]
     if judged:
-        out.update({"judged": len(judged), "max_err_net_vs_dense": max(r["err_net"] for r in judged),
-                    "max_err_zero_vs_dense": max(r["err_zero"] for r in judged),
-                    "mean_err_guess_vs_dense": float(np.mean([r["err_guess"] for r in judged]))})
+        out["judged"] = len(judged)
+        for key in ("zero", "guess", "prec", "both"):
+            if "err_" + key in judged[0]:
+                out[f"max_err_{key}_vs_dense"] = max(r["err_" + key] for r in judged)
+        if "err_guess_start" in judged[0]:
+            out["mean_err_guess_start_vs_dense"] = float(np.mean([r["err_guess_start"] for r in judged]))
     return out
 
 
@@ -313,29 +420,48 @@ def main(argv=None):
     from .solver import Context
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--grid", type=int, default=32)
-    ap.add_argument("--train", type=int, default=2000, help="training pairs (two per scene)")
+    ap.add_argument("--train", type=int, default=2000, help="training pairs of the guess network (two per scene)")
+    ap.add_argument("--prec-scenes", type=int, default=300, help="scenes of preconditioner pairs")
+    ap.add_argument("--nvec", type=int, default=8, help="Arnoldi vectors per polarisation and scene")
     ap.add_argument("--test", type=int, default=500, help="held-out scenes")
     ap.add_argument("--epochs", type=int, default=30)
+    ap.add_argument("--prec-epochs", type=int, default=20)
     ap.add_argument("--judge", type=int, default=20, help="held-out scenes also solved densely")
     ap.add_argument("--tol", type=float, default=1e-6)
+    ap.add_argument("--no-guess", action="store_true", help="preconditioner only")
     args = ap.parse_args(argv)
     log = lambda s: print(s, flush=True)   # noqa: E731
     ctx = Context(fill_mode=_lib.FILL_FAST)
+    summ = {"grid": args.grid}
+    guess_net = None
+    if not args.no_guess:
+        t0 = time.perf_counter()
+        data, its = generate(ctx, scenes(11, args.train // 2, args.grid), tol=args.tol, log=log)
+        t_gen = time.perf_counter() - t0
+        log(f"guess: {len(data[0])} pairs in {t_gen:.1f} s (mean GMRES iterations {np.mean(its):.0f})")
+        guess_net = Net(ctx, args.grid, seed=1)
+        t1 = time.perf_counter()
+        hist = train(guess_net, data, epochs=args.epochs, log=log)
+        summ.update({"guess_pairs": int(len(data[0])), "guess_generate_s": t_gen, "guess_train_s": time.perf_counter() - t1,
+                     "guess_loss_history": hist})
+        del data
+    prec_net = Net(ctx, args.grid, seed=2)
     t0 = time.perf_counter()
-    train_scenes = scenes(11, args.train // 2, args.grid)
-    data, its = generate(ctx, train_scenes, tol=args.tol, log=log)
+    pairs = generate_prec(ctx, prec_net, scenes(13, args.prec_scenes, args.grid), nvec=args.nvec, log=log)
     t_gen = time.perf_counter() - t0
-    log(f"generated {len(data[0])} pairs in {t_gen:.1f} s (mean GMRES iterations {np.mean(its):.0f})")
-    net = Net(ctx, args.grid, seed=1)
+    log(f"preconditioner: {len(pairs)} pairs in {t_gen:.1f} s")
     t1 = time.perf_counter()
-    hist = train(net, data, epochs=args.epochs, log=log)
-    t_train = time.perf_counter() - t1
-    rows = evaluate(ctx, net, scenes(12345, args.test, args.grid), tol=args.tol, judge=args.judge, log=log)
-    summ = summarise(rows)
-    summ.update({"grid": args.grid, "train_pairs": int(len(data[0])), "generate_s": t_gen, "train_s": t_train,
-                 "epochs": args.epochs, "loss_history": hist, "params": net.n})
+    hist = train(prec_net, pairs.as_data(), epochs=args.prec_epochs, batch=16, log=log)
+    summ.update({"prec_pairs": len(pairs), "prec_generate_s": t_gen, "prec_train_s": time.perf_counter() - t1,
+                 "prec_loss_history": hist, "params": prec_net.n})
+    del pairs
+    rows = evaluate(ctx, scenes(12345, args.test, args.grid), guess_net, prec_net, tol=args.tol, judge=args.judge,
+                    log=log)
+    summ.update(summarise(rows))
     print(json.dumps(summ), flush=True)
-    net.close()
+    for nt in (guess_net, prec_net):
+        if nt is not None:
+            nt.close()
     ctx.close()
     return 0
 

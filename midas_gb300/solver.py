@@ -209,6 +209,18 @@ class Context:
             self._ck(st)
         return E.T, self.info.ir_iters, self.info.backward_error
 
+    def fgmres_solve(self, net, th, ph, E0=None, restart=50, maxit=2000, tol=1e-8, check=True):
+        """Flexible GMRES(restart) right-preconditioned by the learned network
+        (midas_gpu_fgmres_solve): (E, iterations, true relative residual)."""
+        th, ph = _c(th, np.float64), _c(ph, np.float64)
+        E = np.zeros((2 * len(th), 3 * self.n), np.complex128)
+        e0 = None if E0 is None else np.ascontiguousarray(np.asarray(E0, np.complex128).T)
+        st = self.L.midas_gpu_fgmres_solve(self.h, net.h, len(th), addr(th), addr(ph), addr(e0), int(restart),
+                                           int(maxit), float(tol), addr(E), ctypes.byref(self.info))
+        if st != 0 and (check or st != 5):
+            self._ck(st)
+        return E.T, self.info.ir_iters, self.info.backward_error
+
     def cbfm_solve(self, blk_offsets, ext_lists, cbf_th, cbf_ph, th, ph, flags=_lib.CBFM_SR, thr_cbf=0.0,
                    res_sr=0.0, eps_aca=float(np.float32(1e-4)), aca_itmax=50, out=None):
         """Compute_EFields_CBFME(_ACA) (src/Compute_EFields_CBFME.f90:1-1006): (E, K)."""
