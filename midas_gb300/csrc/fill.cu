@@ -17,6 +17,8 @@
 // per offset into a table (FP64 and complex(4)-rounded) and the fills become a
 // gather plus one complex product per element, which turns the fill from
 // FP64/SFU-bound into HBM-bound on GB300.
+#include <cmath>
+
 #include "common.cuh"
 #include "green.cuh"
 #include "kernels.cuh"
@@ -441,23 +443,45 @@ __global__ void k_block_fill4_a3(int n1, const int *idx1, int n2, const int *idx
 //   (:564-806).  Per-CTA partials: part[cta * (1 + 2 * NL) + ...].
 // ---------------------------------------------------------------------------
 constexpr int NLAD = 11;
+// The ladder's threshold tests run on the FP32 pipe: an entry's magnitude a is a
+// float, and (double)a > thr exactly when a > thr_f, thr_f = the largest float
+// <= thr (no float lies strictly between the two).  Counts are integers and the
+// squared magnitudes (floats) are summed in double float (TwoSum), which holds
+// the FP64 sum of the same terms to ~2^-48; only the per-thread totals and the
+// block reduction are FP64.  The FP64 form (a double compare and two FP64 adds
+// per entry and threshold) made this scan FP64-bound.
+__device__ __forceinline__ void df_add(float &hi, float &lo, float v)
+{
+    float s, e;
+    ef_two_sum(hi, v, s, e);
+    hi = s;
+    lo = __fadd_rn(lo, e);
+}
+
 template <bool LAT>
 __global__ void k_sr_scan(int s_n, const int *idx, const double *x, const double *y, const double *z,
                           const double2 *znnpp, const float2 *fk4, double k0, double Pi, Lat lat, const float2 *tab4,
-                          int homog, const double *thr, double *part)
+                          int homog, const float *thr_f, double *part)
 {
     __shared__ double sh[32][1 + 2 * NLAD];
-    double acc[1 + 2 * NLAD];
+    float tf[NLAD];
 #pragma unroll
-    for (int j = 0; j < 1 + 2 * NLAD; ++j) acc[j] = 0;
+    for (int j = 0; j < NLAD; ++j) tf[j] = thr_f[j];
+    double acc0 = 0, self_sq = 0;
+    int cnt[NLAD];
+    float qh[NLAD], ql[NLAD];
+#pragma unroll
+    for (int j = 0; j < NLAD; ++j) { cnt[j] = 0; qh[j] = ql[j] = 0.f; }
     size_t npair = (size_t)s_n * s_n;
     for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < npair; t += (size_t)gridDim.x * blockDim.x) {
         int io = (int)(t / s_n), is = (int)(t % s_n);
         int o = idx[io], s = idx[is];
         if (io == is) {
             double a = hypot(1 - znnpp[s].x, -znnpp[s].y);
-            acc[0] += 3. * (a * a);                       // FN of Z (self term)
-            for (int j = 0; j < NLAD; ++j) { acc[1 + j] += 3; acc[1 + NLAD + j] += 3. * (a * a); }
+            acc0 += 3. * (a * a);                       // FN of Z (self term)
+            self_sq += 3. * (a * a);
+#pragma unroll
+            for (int j = 0; j < NLAD; ++j) cnt[j] += 3;
             continue;
         }
         float2 F[6];
@@ -478,7 +502,7 @@ __global__ void k_sr_scan(int s_n, const int *idx, const double *x, const double
             tt = __fadd_rn(tt, __fmul_rn(aF[1], aF[1]));
             tt = __fadd_rn(tt, __fmul_rn(2.f, __fmul_rn(aF[4], aF[4])));
             tt = __fadd_rn(tt, __fmul_rn(aF[2], aF[2]));
-            acc[0] += (double)__fmul_rn(tt, __fmul_rn(afk, afk));
+            acc0 += (double)__fmul_rn(tt, __fmul_rn(afk, afk));
         }
         // SR: homog keeps only Is > Io
         if (!homog || is > io) {
@@ -486,16 +510,20 @@ __global__ void k_sr_scan(int s_n, const int *idx, const double *x, const double
                 for (int q = 0; q < 3; ++q) {
                     float2 g = zmul4_rn(F[comp6(p, q)], fk);
                     float a = absf4(g);
-                    double a2 = (double)__fmul_rn(a, a);
+                    float a2 = __fmul_rn(a, a);
+#pragma unroll
                     for (int j = 0; j < NLAD; ++j)
-                        if ((double)a > thr[j]) { acc[1 + j] += 1; acc[1 + NLAD + j] += a2; }
+                        if (a > tf[j]) { cnt[j] += 1; df_add(qh[j], ql[j], a2); }
                 }
         }
     }
     // block reduction (fixed order)
     int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     for (int j = 0; j < 1 + 2 * NLAD; ++j) {
-        double v = acc[j];
+        double v;
+        if (j == 0) v = acc0;
+        else if (j <= NLAD) v = (double)cnt[j - 1];
+        else v = (double)qh[j - 1 - NLAD] + (double)ql[j - 1 - NLAD] + self_sq;
         for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
         if (lane == 0) sh[wid][j] = v;
     }
@@ -661,12 +689,18 @@ int sr_ladder(midas_gpu_ctx *c, int s_n, const int *d_idx, int first_cell, int h
     MIDAS_CUDA(c, cudaMemcpyAsync(&zn, c->znnpp + first_cell, sizeof(double2), cudaMemcpyDeviceToHost, c->stream));
     MIDAS_CUDA(c, cudaStreamSynchronize(c->stream));
     double vmax = hypot(1 - zn.x, -zn.y);
-    double thr[NLAD];
-    for (int j = 0; j < NLAD; ++j) thr[j] = vmax / ladder[j];
+    float thr[NLAD];   // vmax / ladder rounded down to float (see k_sr_scan)
+    for (int j = 0; j < NLAD; ++j) {
+        const double t = vmax / ladder[j];
+        float f = (float)t;
+        if ((double)f > t) f = std::nextafter(f, -INFINITY);
+        thr[j] = f;
+    }
     const int nblk = 2 * 152, nv = 1 + 2 * NLAD;
     void *buf;
     MIDAS_TRY(ensure(c, S_RED, sizeof(double) * (nblk * nv + NLAD), &buf));
-    double *part = (double *)buf, *dthr = part + nblk * nv;
+    double *part = (double *)buf;
+    float *dthr = (float *)(part + nblk * nv);
     MIDAS_CUDA(c, cudaMemcpyAsync(dthr, thr, sizeof(thr), cudaMemcpyHostToDevice, c->stream));
     Lat l = make_lat(c);
     ++c->launches;
