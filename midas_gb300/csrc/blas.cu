@@ -14,6 +14,7 @@
 //    without the GB300's slow FP64 pipe.
 //  * heev_dev : Hermitian eigen-decomposition (Householder tridiagonalisation +
 //    implicit QL, FP64) of the CBF Gram matrices; one CTA per matrix.
+#include <cuda_fp16.h>
 #include <cmath>
 
 #include <algorithm>
@@ -134,17 +135,159 @@ template int zgemm_x3_a3<double2>(midas_gpu_ctx *, int, int, int, const float *,
 template int zgemm_x3_a3<float2>(midas_gpu_ctx *, int, int, int, const float *, long long, const float2 *,
                                  long long, long long, float *, long long, float, float, int);
 
-// A3 = (hi | hi | lo) split of a row-major complex64 M x K matrix (K6 = 6K, a
-// multiple of 4 floats): the A operand of zgemm_x3_a3, formed once for a matrix
-// that several products reuse.
-int zsplit_a3(midas_gpu_ctx *c, int M, int K, const float2 *A, long long lda, float *A3, long long K6)
+// ---------------------------------------------------------------------------
+// The same split product on fp16 operands (kind::f16: the 11-bit significands of
+// TF32 at half the bytes and twice the MMA rate).  FP16 has a narrow exponent
+// range, so each operand is scaled by a power of two that puts its largest
+// entry in [2^12, 2^13): the hi pieces of entries down to 2^-24 of the maximum
+// stay normal, and what falls out of range is below 2^-37 of the maximum.  The
+// GEMM multiplies by 1 / (sA sB), read from device memory.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_cabsmax(int M, int K, const T *src, long long rs, long long cs, unsigned *out)
+{
+    float m = 0.f;
+    for (int i = blockIdx.x; i < M; i += gridDim.x)
+        for (int k = threadIdx.x; k < K; k += blockDim.x) {
+            const double2 v = ld2<T>(src, (long long)i * rs + (long long)k * cs);
+            m = fmaxf(m, (float)fmax(fabs(v.x), fabs(v.y)));
+        }
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m > 0.f) atomicMax(out, __float_as_uint(m));
+}
+
+// s = 2^(12 - ceil(log2 max)) (1 for an all-zero operand); which = 0: A, 1: B and alpha = 1 / (sA sB)
+__global__ void k_h16_scale(const unsigned *amax, float *sc, int which)
+{
+    const float m = __uint_as_float(*amax);
+    int e = 0;
+    if (m > 0.f) e = 12 - (int)ceilf(log2f(m));
+    e = max(-120, min(120, e));
+    sc[which] = ldexpf(1.f, e);
+    if (which == 1) sc[2] = 1.f / (sc[0] * sc[1]);
+}
+
+__device__ __forceinline__ void split_h16(double v, float s, __half &hi, __half &lo)
+{
+    const double x = v * (double)s;
+    hi = __float2half_rn((float)x);
+    lo = __float2half_rn((float)(x - (double)__half2float(hi)));
+}
+// the same for an FP32 value, in FP32 (x - hi is exact: hi holds x's leading bits)
+__device__ __forceinline__ void split_h16(float v, float s, __half &hi, __half &lo)
+{
+    const float x = v * s;
+    hi = __float2half_rn(x);
+    lo = __float2half_rn(x - __half2float(hi));
+}
+template <typename T> struct SplitIn;
+template <> struct SplitIn<float2> {
+    using V = float2;
+    static __device__ __forceinline__ float2 ld(const float2 *p, long long i) { return p[i]; }
+};
+template <> struct SplitIn<double2> {
+    using V = double2;
+    static __device__ __forceinline__ double2 ld(const double2 *p, long long i) { return p[i]; }
+};
+
+template <typename T>
+__global__ void k_split_a_h16(int M, int K, const T *src, long long rs, long long cs, const float *sc, __half *A3,
+                              long long lda3)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= K) return;
+    const float s = sc[0];
+    for (int i = blockIdx.y; i < M; i += gridDim.y) {
+        const auto v = SplitIn<T>::ld(src, (long long)i * rs + (long long)k * cs);
+        __half hr, lr, hi_, li;
+        split_h16(v.x, s, hr, lr);
+        split_h16(v.y, s, hi_, li);
+        __half *row = A3 + (long long)i * lda3;
+        row[2 * k] = hr; row[2 * k + 1] = hi_;
+        row[2 * K + 2 * k] = hr; row[2 * K + 2 * k + 1] = hi_;
+        row[4 * K + 2 * k] = lr; row[4 * K + 2 * k + 1] = li;
+        if (k == K - 1)
+            for (long long p = 6LL * K; p < lda3; ++p) row[p] = __float2half(0.f);
+    }
+}
+
+template <typename T>
+__global__ void k_split_expand_b_h16(int K, int N, const T *src, long long rs, long long cs, const float *sc,
+                                     __half *B3, long long ldb3)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= K) return;
+    const float s = sc[1];
+    for (int j = blockIdx.y; j < N; j += gridDim.y) {
+        const auto v = SplitIn<T>::ld(src, (long long)k * rs + (long long)j * cs);
+        __half hr, lr, hi_, li;
+        split_h16(v.x, s, hr, lr);
+        split_h16(v.y, s, hi_, li);
+        const __half nhi = __hneg(hi_), nli = __hneg(li);
+        __half *r0 = B3 + (long long)(2 * j) * ldb3, *r1 = r0 + ldb3;
+        r0[2 * k] = hr; r0[2 * k + 1] = nhi; r1[2 * k] = hi_; r1[2 * k + 1] = hr;
+        r0[2 * K + 2 * k] = lr; r0[2 * K + 2 * k + 1] = nli; r1[2 * K + 2 * k] = li; r1[2 * K + 2 * k + 1] = lr;
+        r0[4 * K + 2 * k] = hr; r0[4 * K + 2 * k + 1] = nhi; r1[4 * K + 2 * k] = hi_; r1[4 * K + 2 * k + 1] = hr;
+        if (k == K - 1)
+            for (long long p = 6LL * K; p < ldb3; ++p) { r0[p] = __float2half(0.f); r1[p] = __float2half(0.f); }
+    }
+}
+
+// A3h (fp16 hi | hi | lo rows of K6h = 6K halves rounded up to 8) of a row-major complex64
+// M x K matrix, with its scale in sc[0] (sc: 4 floats of device memory after the split)
+int zsplit_a3_h16(midas_gpu_ctx *c, int M, int K, const float2 *A, long long lda, __half *A3, long long K6h,
+                  float *sc)
 {
     if (M <= 0 || K <= 0) return MIDAS_OK;
-    if (K6 != (6LL * K + 3) / 4 * 4) return c->err.set(MIDAS_ERR_ARG, "zsplit_a3: bad A3 stride");
+    if (K6h != (6LL * K + 7) / 8 * 8) return c->err.set(MIDAS_ERR_ARG, "zsplit_a3_h16: bad A3 stride");
     ++c->launches;
     int kp = kp_begin(c);
-    k_split_a<float2><<<dim3((K + 127) / 128, std::min(M, 65535)), 128, 0, c->stream>>>(M, K, A, lda, 1, 0, A3, K6);
-    kp_end(c, kp, MIDAS_KC_SPLIT, 0.0, 8.0 * M * K + 4.0 * M * K6);
+    MIDAS_CUDA(c, cudaMemsetAsync(sc + 3, 0, sizeof(unsigned), c->stream));
+    k_cabsmax<float2><<<std::min(M, 4096), 256, 0, c->stream>>>(M, K, A, lda, 1, (unsigned *)(sc + 3));
+    k_h16_scale<<<1, 1, 0, c->stream>>>((const unsigned *)(sc + 3), sc, 0);
+    k_split_a_h16<float2><<<dim3((K + 127) / 128, std::min(M, 65535)), 128, 0, c->stream>>>(M, K, A, lda, 1, sc, A3,
+                                                                                             K6h);
+    kp_end(c, kp, MIDAS_KC_SPLIT, 0.0, 16.0 * M * K + 2.0 * M * K6h);
+    MIDAS_CUDA(c, cudaGetLastError());
+    return MIDAS_OK;
+}
+
+// D (M x 2N floats, row-major, ld ldd) = A B with A given as its fp16 split A3h
+// (M rows of K6h = 6K halves rounded up to 8, scale sA in sc[0]) and B (K x N complex, element
+// (k, j) at B[k brs + j bcs]): B is scaled (sc[1]) and split here, the GEMM
+// multiplies by 1 / (sA sB) (sc[2]); sc[3] is scratch.
+template <typename TB>
+int zgemm_x3h_a3(midas_gpu_ctx *c, int M, int N, int K, const __half *A3h, long long K6h, float *sc, const TB *B,
+                 long long brs, long long bcs, float *D, long long ldd, int kclass)
+{
+    if (M <= 0 || N <= 0 || K <= 0) return MIDAS_OK;
+    if (K6h != (6LL * K + 7) / 8 * 8) return c->err.set(MIDAS_ERR_ARG, "zgemm_x3h_a3: bad A3 stride");
+    void *pb;
+    MIDAS_TRY(ensure(c, S_CBF9, sizeof(__half) * (size_t)2 * N * K6h + 256, &pb));
+    __half *B3 = (__half *)pb;
+    ++c->launches;
+    int kp = kp_begin(c);
+    MIDAS_CUDA(c, cudaMemsetAsync(sc + 3, 0, sizeof(unsigned), c->stream));
+    k_cabsmax<TB><<<std::min(K, 4096), 256, 0, c->stream>>>(K, N, B, brs, bcs, (unsigned *)(sc + 3));
+    k_h16_scale<<<1, 1, 0, c->stream>>>((const unsigned *)(sc + 3), sc, 1);
+    k_split_expand_b_h16<TB><<<dim3((K + 127) / 128, std::min(N, 65535)), 128, 0, c->stream>>>(K, N, B, brs, bcs, sc,
+                                                                                               B3, K6h);
+    kp_end(c, kp, MIDAS_KC_SPLIT, 0.0, (double)sizeof(TB) * K * N + 4.0 * N * K6h);
+    MIDAS_CUDA(c, cudaGetLastError());
+    GemmArgs g{M, 2 * N, (int)K6h, (const float *)A3h, K6h, (const float *)B3, K6h, D, ldd, 1.f, 0.f, 0, kclass};
+    g.h16 = 1;
+    g.alpha_dev = sc + 2;
+    return gemm_tf32(c, g, true);
+}
+template int zgemm_x3h_a3<double2>(midas_gpu_ctx *, int, int, int, const __half *, long long, float *,
+                                   const double2 *, long long, long long, float *, long long, int);
+
+// sc[0] = s (a power of two) for a split written by a kernel that knew its scale
+__global__ void k_set_scale(float *sc, float s) { sc[0] = s; }
+int set_h16_scale(midas_gpu_ctx *c, float *sc, float s)
+{
+    ++c->launches;
+    k_set_scale<<<1, 1, 0, c->stream>>>(sc, s);
     MIDAS_CUDA(c, cudaGetLastError());
     return MIDAS_OK;
 }
@@ -162,13 +305,13 @@ __global__ void k_sub_rowmajor(int n, int m, const float *P, double2 *R)
     R[t] = r;
 }
 
-// R -= Z D with Z given by its split A3 (n x n) and D row-major n x m complex64:
-// the FP32-grade product (hi*hi + hi*lo + lo*hi, relative error ~2^-22) on the
-// tensor cores.  P (n x 2m floats) is scratch.
-int resid_update_x3(midas_gpu_ctx *c, int n, int m, const float *A3, long long K6, const float2 *D, float *P,
-                    double2 *R)
+// R -= Z D with Z given by its fp16 split A3h (n x n, scale in sc[0]) and D row-major
+// n x m complex64: the FP32-grade product (hi*hi + hi*lo + lo*hi, relative error
+// ~2^-22) on the tensor cores.  P (n x 2m floats) is scratch.
+int resid_update_x3(midas_gpu_ctx *c, int n, int m, const __half *A3h, long long K6h, float *sc, const float2 *D,
+                    float *P, double2 *R)
 {
-    MIDAS_TRY(zgemm_x3_a3<float2>(c, n, m, n, A3, K6, D, m, 1, P, 2LL * m, 1.f, 0.f, MIDAS_KC_RESID32));
+    MIDAS_TRY(zgemm_x3h_a3<float2>(c, n, m, n, A3h, K6h, sc, D, m, 1, P, 2LL * m, MIDAS_KC_RESID32));
     ++c->launches;
     int kp = kp_begin(c);
     const long long tot = (long long)n * m;

@@ -22,6 +22,8 @@
 //   3. Vc = C^T Einc [829-849], reduced solve (mixed LU + FP64 refinement) [873-943],
 //      E = C alpha [990-1006].
 #include <algorithm>
+#include <cuda_fp16.h>
+
 #include <atomic>
 #include <chrono>
 #include <cmath>
@@ -43,9 +45,14 @@ int zgemm_x3(midas_gpu_ctx *c, int M, int N, int K, const TA *A, long long ars, 
 template <typename TB>
 int zgemm_x3_a3(midas_gpu_ctx *c, int M, int N, int K, const float *A3, long long K6, const TB *B, long long brs,
                 long long bcs, float *D, long long ldd, float alpha, float beta, int kclass = MIDAS_KC_GEMM_PROD);
-int zsplit_a3(midas_gpu_ctx *c, int M, int K, const float2 *A, long long lda, float *A3, long long K6);
-int resid_update_x3(midas_gpu_ctx *c, int n, int m, const float *A3, long long K6, const float2 *D, float *P,
-                    double2 *R);
+int zsplit_a3_h16(midas_gpu_ctx *c, int M, int K, const float2 *A, long long lda, __half *A3, long long K6h,
+                  float *sc);
+int resid_update_x3(midas_gpu_ctx *c, int n, int m, const __half *A3h, long long K6h, float *sc, const float2 *D,
+                    float *P, double2 *R);
+template <typename TB>
+int zgemm_x3h_a3(midas_gpu_ctx *c, int M, int N, int K, const __half *A3h, long long K6h, float *sc, const TB *B,
+                 long long brs, long long bcs, float *D, long long ldd, int kclass);
+int set_h16_scale(midas_gpu_ctx *c, float *sc, float s);
 int residual_df32(midas_gpu_ctx *c, int n, int nrhs, const float2 *Z, long long ldz, const float2 *Xh,
                   const float2 *Xl, const float2 *B, double2 *R);
 int heev_dev(midas_gpu_ctx *c, int batch, int m, double2 *A, long long lda, long long sa, double2 *H, double2 *V,
@@ -239,13 +246,15 @@ static int cbf_block(midas_gpu_ctx *c, const CbfShared &S, int b)
         // dense work) and as the split-TF32 operand A3 for the FP32-grade residual
         // updates r -= Z d (dense, on the tensor cores).
         Csr zcsr;
-        float *A3z = nullptr;
+        __half *A3z = nullptr;
+        float *A3sc = nullptr;   // the split's scales (4 floats after it)
         const long long K6z = 6LL * sp;
         if (sr) {
             MIDAS_TRY(csr_from_dense(c, sp, Zlu, sp, S_CSR, &zcsr));
-            MIDAS_TRY(ensure(c, S_CBF2, sizeof(float) * (size_t)sp * (size_t)K6z, &p2));
-            A3z = (float *)p2;
-            MIDAS_TRY(zsplit_a3(c, sp, sp, Zlu, sp, A3z, K6z));
+            MIDAS_TRY(ensure(c, S_CBF2, sizeof(__half) * (size_t)sp * (size_t)K6z + 256, &p2));
+            A3z = (__half *)p2;
+            A3sc = (float *)(A3z + (size_t)sp * (size_t)K6z);
+            MIDAS_TRY(zsplit_a3_h16(c, sp, sp, Zlu, sp, A3z, K6z, A3sc));
         } else
             MIDAS_CUDA(c, cudaMemcpyAsync(Zsr, Zlu, sizeof(float2) * (size_t)sp * sp, cudaMemcpyDeviceToDevice,
                                           c->stream));
@@ -281,9 +290,9 @@ static int cbf_block(midas_gpu_ctx *c, const CbfShared &S, int b)
             if (sr && it == 0) {
                 ++c->launches;
                 k_b_to_r64<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(tot, Bm, R64);
-                MIDAS_TRY(resid_update_x3(c, sp, m, A3z, K6z, Drm, (float *)d32, R64));
+                MIDAS_TRY(resid_update_x3(c, sp, m, A3z, K6z, A3sc, Drm, (float *)d32, R64));
             } else if (sr && upd)
-                MIDAS_TRY(resid_update_x3(c, sp, m, A3z, K6z, Drm, (float *)d32, R64));
+                MIDAS_TRY(resid_update_x3(c, sp, m, A3z, K6z, A3sc, Drm, (float *)d32, R64));
             else if (sr)
                 MIDAS_TRY(residual_csr_df32(c, zcsr, m, ldx, Xh, Xl, Bm, R64));
             else
@@ -648,6 +657,13 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
     void *pt;
     MIDAS_TRY(ensure(c, S_CBF7, sizeof(float) * (size_t)3 * n * ldT + sizeof(float) * (size_t)Kt * ldT, &pt));
     float *T = (float *)pt, *Zcf = T + (size_t)3 * n * ldT;
+    // With the lattice-table fill the products Z C_j take fp16 operand pieces (kind::f16:
+    // twice the rate and half the bytes of TF32), scaled by a power of two from a bound
+    // of every entry; otherwise TF32 pieces.
+    double zbound = 0.0;
+    MIDAS_TRY(fill4_bound(c, &zbound));
+    const bool h16 = zbound > 0.0;
+    const float hsA = h16 ? ldexpf(1.f, 12 - (int)std::ceil(std::log2(zbound))) : 1.f;
     for (int j = 0; j < nb; ++j) {
         const int nj = bo[j + 1] - bo[j];
         const double2 *Cj = Call + coff[j];
@@ -658,13 +674,24 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
             int i1 = i;
             while (i1 < nb && dense(i1, j)) ++i1;
             const int r0 = bo[i], nr = bo[i1] - bo[i];
-            // the fill writes the split-TF32 A operand (hi | hi | lo) directly
-            const long long K6 = (6LL * 3 * nj + 3) / 4 * 4;
+            // the fill writes the split A operand (hi | hi | lo) directly
             void *pa;
-            MIDAS_TRY(ensure(c, S_CBF8, sizeof(float) * (size_t)3 * nr * K6, &pa));
-            MIDAS_TRY(launch_block_fill4_a3(c, nr, d_all + r0, nj, d_all + bo[j], (float *)pa, K6));
-            MIDAS_TRY(zgemm_x3_a3<double2>(c, 3 * nr, Kb[j], 3 * nj, (const float *)pa, K6, Cj, 1, 3LL * nj,
-                                           T + (size_t)3 * r0 * ldT + 2LL * koff[j], ldT, 1.f, 0.f));
+            if (h16) {
+                const long long K6h = (6LL * 3 * nj + 7) / 8 * 8;
+                MIDAS_TRY(ensure(c, S_CBF8, sizeof(__half) * (size_t)3 * nr * K6h + 256, &pa));
+                __half *A3h = (__half *)pa;
+                float *sc = (float *)(A3h + (size_t)3 * nr * K6h);
+                MIDAS_TRY(launch_block_fill4_a3(c, nr, d_all + r0, nj, d_all + bo[j], nullptr, K6h, A3h, hsA));
+                MIDAS_TRY(set_h16_scale(c, sc, hsA));
+                MIDAS_TRY(zgemm_x3h_a3<double2>(c, 3 * nr, Kb[j], 3 * nj, A3h, K6h, sc, Cj, 1, 3LL * nj,
+                                                T + (size_t)3 * r0 * ldT + 2LL * koff[j], ldT, MIDAS_KC_GEMM_PROD));
+            } else {
+                const long long K6 = (6LL * 3 * nj + 3) / 4 * 4;
+                MIDAS_TRY(ensure(c, S_CBF8, sizeof(float) * (size_t)3 * nr * K6, &pa));
+                MIDAS_TRY(launch_block_fill4_a3(c, nr, d_all + r0, nj, d_all + bo[j], (float *)pa, K6));
+                MIDAS_TRY(zgemm_x3_a3<double2>(c, 3 * nr, Kb[j], 3 * nj, (const float *)pa, K6, Cj, 1, 3LL * nj,
+                                               T + (size_t)3 * r0 * ldT + 2LL * koff[j], ldT, 1.f, 0.f));
+            }
             i = i1;
         }
         // low-rank pairs: T(rows of i, cols of j) = U (V C_j), FP64 products

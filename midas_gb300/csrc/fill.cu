@@ -17,7 +17,10 @@
 // per offset into a table (FP64 and complex(4)-rounded) and the fills become a
 // gather plus one complex product per element, which turns the fill from
 // FP64/SFU-bound into HBM-bound on GB300.
+#include <cuda_fp16.h>
+#include <algorithm>
 #include <cmath>
+#include <cstring>
 
 #include "common.cuh"
 #include "green.cuh"
@@ -368,7 +371,8 @@ __global__ void k_block_fill4(int n1, const int *idx1, int n2, const int *idx2, 
 template <bool LAT>
 __global__ void k_block_fill4_a3(int n1, const int *idx1, int n2, const int *idx2, const double *x, const double *y,
                                  const double *z, const double2 *znnpp, const float2 *fk4, double k0, double Pi,
-                                 Lat lat, const float2 *tab4, float *A3, long long lda3)
+                                 Lat lat, const float2 *tab4, float *A3, long long lda3, __half *A3h,
+                                 float hscale)
 {
     int js = blockIdx.x * blockDim.x + threadIdx.x;
     int io = blockIdx.y * blockDim.y + threadIdx.y;
@@ -405,6 +409,7 @@ __global__ void k_block_fill4_a3(int n1, const int *idx1, int n2, const int *idx
     }
     // stage the CTA's 6 rows x (64 cells x 3) complex entries (hi and lo) in shared
     // memory, then write each row segment as one contiguous run
+    // (with A3h: fp16 pieces of the entries scaled by hscale, a power of two)
     __shared__ float2 sh[6][192], sl[6][192];
     const int tr = threadIdx.y, tc = threadIdx.x;
 #pragma unroll
@@ -412,9 +417,16 @@ __global__ void k_block_fill4_a3(int n1, const int *idx1, int n2, const int *idx
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
             const float2 v = V[p * 3 + q];
-            const float hr = tf32_rna(v.x), hi = tf32_rna(v.y);
-            sh[3 * tr + p][3 * tc + q] = make_float2(hr, hi);
-            sl[3 * tr + p][3 * tc + q] = make_float2(tf32_rna(v.x - hr), tf32_rna(v.y - hi));
+            if (A3h) {
+                const float xr = v.x * hscale, xi = v.y * hscale;
+                const float hr = __half2float(__float2half_rn(xr)), hi = __half2float(__float2half_rn(xi));
+                sh[3 * tr + p][3 * tc + q] = make_float2(hr, hi);
+                sl[3 * tr + p][3 * tc + q] = make_float2(xr - hr, xi - hi);
+            } else {
+                const float hr = tf32_rna(v.x), hi = tf32_rna(v.y);
+                sh[3 * tr + p][3 * tc + q] = make_float2(hr, hi);
+                sl[3 * tr + p][3 * tc + q] = make_float2(tf32_rna(v.x - hr), tf32_rna(v.y - hi));
+            }
         }
     __syncthreads();
     const int js0 = blockIdx.x * blockDim.x, io0 = blockIdx.y * blockDim.y;
@@ -423,16 +435,29 @@ __global__ void k_block_fill4_a3(int n1, const int *idx1, int n2, const int *idx
     const long long kc0 = 3LL * js0;
     for (int t = threadIdx.y * blockDim.x + threadIdx.x; t < nrow * ncol; t += blockDim.x * blockDim.y) {
         const int rr = t / ncol, cc = t % ncol;
-        float2 *row = (float2 *)(A3 + (3LL * io0 + rr) * lda3);
         const float2 h = sh[rr][cc];
-        row[kc0 + cc] = h;
-        row[K + kc0 + cc] = h;
-        row[2 * K + kc0 + cc] = sl[rr][cc];
+        if (A3h) {
+            __half2 *row = (__half2 *)(A3h + (3LL * io0 + rr) * lda3);
+            const __half2 hh = __floats2half2_rn(h.x, h.y);
+            row[kc0 + cc] = hh;
+            row[K + kc0 + cc] = hh;
+            row[2 * K + kc0 + cc] = __floats2half2_rn(sl[rr][cc].x, sl[rr][cc].y);
+        } else {
+            float2 *row = (float2 *)(A3 + (3LL * io0 + rr) * lda3);
+            row[kc0 + cc] = h;
+            row[K + kc0 + cc] = h;
+            row[2 * K + kc0 + cc] = sl[rr][cc];
+        }
     }
     if (js0 + 64 >= n2)   // the CTA holding the last columns zeroes the row padding
         for (int t = threadIdx.y * blockDim.x + threadIdx.x; t < nrow; t += blockDim.x * blockDim.y) {
-            float *row = A3 + (3LL * io0 + t) * lda3;
-            for (long long pad = 6 * K; pad < lda3; ++pad) row[pad] = 0.f;
+            if (A3h) {
+                __half *row = A3h + (3LL * io0 + t) * lda3;
+                for (long long pad = 6 * K; pad < lda3; ++pad) row[pad] = __float2half(0.f);
+            } else {
+                float *row = A3 + (3LL * io0 + t) * lda3;
+                for (long long pad = 6 * K; pad < lda3; ++pad) row[pad] = 0.f;
+            }
         }
 }
 
@@ -658,7 +683,7 @@ int launch_block_fill4(midas_gpu_ctx *c, int n1, const int *idx1, int n2, const 
     return MIDAS_OK;
 }
 int launch_block_fill4_a3(midas_gpu_ctx *c, int n1, const int *idx1, int n2, const int *idx2, float *A3,
-                          long long lda3)
+                          long long lda3, __half *A3h, float hscale)
 {
     dim3 blk(64, 2);
     dim3 grd((n2 + 63) / 64, (n1 + 1) / 2);
@@ -667,11 +692,11 @@ int launch_block_fill4_a3(midas_gpu_ctx *c, int n1, const int *idx1, int n2, con
     int kp = kp_begin(c);
     if (c->opts.fill_mode == MIDAS_FILL_FAST && use_lat(c))
         k_block_fill4_a3<true><<<grd, blk, 0, c->stream>>>(n1, idx1, n2, idx2, c->x, c->y, c->z, c->znnpp, c->fk4,
-                                                           c->k0, c->pi, l, c->lat_tab4, A3, lda3);
+                                                           c->k0, c->pi, l, c->lat_tab4, A3, lda3, A3h, hscale);
     else
         k_block_fill4_a3<false><<<grd, blk, 0, c->stream>>>(n1, idx1, n2, idx2, c->x, c->y, c->z, c->znnpp, c->fk4,
-                                                            c->k0, c->pi, l, nullptr, A3, lda3);
-    kp_end(c, kp, MIDAS_KC_FILL, 0.0, 4.0 * 3 * n1 * (double)lda3);
+                                                            c->k0, c->pi, l, nullptr, A3, lda3, A3h, hscale);
+    kp_end(c, kp, MIDAS_KC_FILL, 0.0, (A3h ? 2.0 : 4.0) * 3 * n1 * (double)lda3);
     MIDAS_CUDA(c, cudaGetLastError());
     return MIDAS_OK;
 }
@@ -679,6 +704,54 @@ template int launch_block_fill4<double2>(midas_gpu_ctx *, int, const int *, int,
                                          double2 *, size_t, size_t);
 template int launch_block_fill4<float2>(midas_gpu_ctx *, int, const int *, int, const int *, int, double, int,
                                         float2 *, size_t, size_t);
+
+// An upper bound of |Z_os| over every cell pair of the lattice-table fill (mode 0):
+// max(max |1 - Znnpp|, max over the table of |F| times max |f_kapChe|) -- the
+// scale of the fp16 operand pieces of the reduced-matrix products.  0 when the
+// fill does not come from the table.
+__global__ void k_fill_bound(long long ntab, const float2 *tab4, int n, const double2 *znnpp, const float2 *fk4,
+                             unsigned *out)
+{
+    float mt = 0.f, mf = 0.f, md = 0.f;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ntab; e += (long long)gridDim.x * blockDim.x)
+        mt = fmaxf(mt, absf4(tab4[e]));
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        mf = fmaxf(mf, absf4(fk4[e]));
+        md = fmaxf(md, (float)hypot(1.0 - znnpp[e].x, -znnpp[e].y));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        mt = fmaxf(mt, __shfl_down_sync(0xffffffffu, mt, o));
+        mf = fmaxf(mf, __shfl_down_sync(0xffffffffu, mf, o));
+        md = fmaxf(md, __shfl_down_sync(0xffffffffu, md, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(out, __float_as_uint(mt));
+        atomicMax(out + 1, __float_as_uint(mf));
+        atomicMax(out + 2, __float_as_uint(md));
+    }
+}
+
+int fill4_bound(midas_gpu_ctx *c, double *bound)
+{
+    *bound = 0.0;
+    if (!(c->opts.fill_mode == MIDAS_FILL_FAST && use_lat(c))) return MIDAS_OK;
+    void *p;
+    MIDAS_TRY(ensure(c, S_RED, 64, &p));
+    unsigned *d = (unsigned *)p;
+    MIDAS_CUDA(c, cudaMemsetAsync(d, 0, 3 * sizeof(unsigned), c->stream));
+    const long long ntab = 6LL * c->lat_dim[0] * c->lat_dim[1] * c->lat_dim[2];
+    ++c->launches;
+    k_fill_bound<<<1024, 256, 0, c->stream>>>(ntab, c->lat_tab4, c->n, c->znnpp, c->fk4, d);
+    MIDAS_CUDA(c, cudaGetLastError());
+    unsigned h[3];
+    MIDAS_CUDA(c, cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    MIDAS_CUDA(c, cudaStreamSynchronize(c->stream));
+    float f[3];
+    memcpy(f, h, sizeof(f));
+    // the complex(4) products round: a 1 % margin covers them
+    *bound = 1.01 * std::max((double)f[0] * (double)f[1], (double)f[2]);
+    return MIDAS_OK;
+}
 
 // setfSR ladder (src/getParameters_CBFM.f90:140-162).  vmax = |1 - Znnpp(first cell)|.
 int sr_ladder(midas_gpu_ctx *c, int s_n, const int *d_idx, int first_cell, int homog, double res_sr, double *fsr_out,

@@ -214,13 +214,18 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float v[32])
 // while the MMA fills the other buffer.  The tensor core's own accumulation
 // (coarser than an FMA chain) then only spans 64 products, which brings long-K
 // products with cancellation (the CBF reduced matrix) to FP32-FMA accuracy.
+// With H16 the operands are fp16 (the same 11-bit significands as TF32, half the
+// bytes, twice the MMA rate): a k-block is 64 elements and every k-block is
+// promoted, so each tensor-core chunk again spans 64 products; alpha may be read
+// from device memory (the inverse of the operands' power-of-two scales).
 constexpr int TC_PROMOTE_KB = 2;
 
-template <bool PROMOTE, int TC_STAGES>
+template <bool PROMOTE, int TC_STAGES, bool H16 = false>
 __global__ void __launch_bounds__(TC_THREADS, TC_STAGES == 2 ? 2 : 1)
     k_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int M, int N, int K,
-              float *D, long long ldd, float alpha, float beta, int rnd, int *gflag)
+              float *D, long long ldd, float alpha, float beta, int rnd, int *gflag, const float *alpha_dev = nullptr)
 {
+    constexpr int BKE = H16 ? 2 * TC_BK : TC_BK;   // elements per k-block (128 bytes of a row)
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t *full = (uint64_t *)(smem + TC_STAGES * TC_STAGE_BYTES);
@@ -233,8 +238,8 @@ __global__ void __launch_bounds__(TC_THREADS, TC_STAGES == 2 ? 2 : 1)
 
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
     const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * TC_BN;
-    const int nk = (K + TC_BK - 1) / TC_BK;
-    const int KC = PROMOTE ? TC_PROMOTE_KB : (nk > 0 ? nk : 1);
+    const int nk = (K + BKE - 1) / BKE;
+    const int KC = PROMOTE ? (H16 ? 1 : TC_PROMOTE_KB) : (nk > 0 ? nk : 1);
     const int nchunk = (nk + KC - 1) / KC;
 
     if (threadIdx.x == 0) {
@@ -265,13 +270,13 @@ __global__ void __launch_bounds__(TC_THREADS, TC_STAGES == 2 ? 2 : 1)
                 uint8_t *sa = smem + s * TC_STAGE_BYTES;
                 uint8_t *sb = sa + TC_A_BYTES;
                 mbar_arrive_tx(&full[s], TC_STAGE_BYTES);
-                tma_load_2d(sa, &tmA, &full[s], kb * TC_BK, m0);
-                tma_load_2d(sb, &tmB, &full[s], kb * TC_BK, n0);
+                tma_load_2d(sa, &tmA, &full[s], kb * BKE, m0);
+                tma_load_2d(sb, &tmB, &full[s], kb * BKE, n0);
             }
         }
     } else if (warp == 1) {
         if (lane == 0) {
-            const uint32_t idesc = idesc_tf32(TC_BM, TC_BN);
+            const uint32_t idesc = H16 ? idesc_f16(TC_BM, TC_BN) : idesc_tf32(TC_BM, TC_BN);
             bool ok = true;
             for (int ch = 0; ch < nchunk && ok; ++ch) {
                 const int buf = PROMOTE ? (ch & 1) : 0;
@@ -287,10 +292,13 @@ __global__ void __launch_bounds__(TC_THREADS, TC_STAGES == 2 ? 2 : 1)
                     uint32_t sa = smem_u32(smem + s * TC_STAGE_BYTES);
                     uint32_t sb = sa + TC_A_BYTES;
 #pragma unroll
-                    for (int k4 = 0; k4 < TC_BK / 8; ++k4) {
+                    for (int k4 = 0; k4 < TC_BK / 8; ++k4) {   // 32 bytes of K per MMA: 8 tf32 or 16 fp16
                         uint64_t ad = smem_desc_sw128(sa + k4 * 32);
                         uint64_t bd = smem_desc_sw128(sb + k4 * 32);
-                        mma_tf32(dst, ad, bd, idesc, (kb > ch * KC || k4 > 0) ? 1u : 0u);
+                        if constexpr (H16)
+                            mma_f16(dst, ad, bd, idesc, (kb > ch * KC || k4 > 0) ? 1u : 0u);
+                        else
+                            mma_tf32(dst, ad, bd, idesc, (kb > ch * KC || k4 > 0) ? 1u : 0u);
                     }
                     mma_commit(&empty[s]);
                 }
@@ -299,6 +307,7 @@ __global__ void __launch_bounds__(TC_THREADS, TC_STAGES == 2 ? 2 : 1)
         }
     } else {
         // epilogue: warp w reads TMEM lanes 32*(w%4) .. +31
+        if (alpha_dev) alpha = *alpha_dev;   // set by an earlier kernel on the stream
         const int lg = warp % 4;
         const int row = m0 + lg * 32 + lane;
         const uint32_t lane_base = (uint32_t)(lg * 32) << 16;
@@ -711,6 +720,25 @@ static int gemm_tc(midas_gpu_ctx *c, const GemmArgs &g, bool precise)
     const int ldm = g.h16 ? 7 : 3;
     if ((((uintptr_t)g.A) & 15) || (((uintptr_t)g.Bt) & 15) || (g.lda & ldm) || (g.ldb & ldm))
         return c->err.set(MIDAS_ERR_ARG, "gemm_tf32: operands must be 16-byte aligned with 16-byte row strides");
+    if (g.h16 && precise) {   // fp16 operands, every k-block promoted to FP32 registers
+        static PerDeviceOnce once_h;
+        MIDAS_CUDA(c, once_h.run(c->device, [] {
+            return cudaFuncSetAttribute(k_gemm_tc<true, 4, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        tc_smem(4));
+        }));
+        CUtensorMap ma, mb;
+        MIDAS_TRY(make_map(c, &ma, g.A, g.M, g.K, g.lda, TC_BM, true));
+        MIDAS_TRY(make_map(c, &mb, g.Bt, g.N, g.K, g.ldb, TC_BN, true));
+        dim3 grd((g.N + TC_BN - 1) / TC_BN, (g.M + TC_BM - 1) / TC_BM);
+        ++c->launches;
+        int kp = kp_begin(c);
+        k_gemm_tc<true, 4, true><<<grd, TC_THREADS, tc_smem(4), c->stream>>>(ma, mb, g.M, g.N, g.K, g.D, g.ldd, g.alpha,
+                                                                             g.beta, 0, c->d_flag, g.alpha_dev);
+        kp_end(c, kp, g.kclass, 2.0 * g.M * g.N * g.K,
+               2.0 * ((double)g.M * g.K + (double)g.N * g.K) + 4.0 * (double)g.M * g.N * (g.beta != 0.f ? 2 : 1));
+        MIDAS_CUDA(c, cudaGetLastError());
+        return MIDAS_OK;
+    }
     if (g.h16) return gemm_tcp_h16(c, g);
     static PerDeviceOnce once_tc;
     MIDAS_CUDA(c, once_tc.run(c->device, [] {

@@ -1,5 +1,7 @@
 // kernels.cuh -- internal launcher prototypes shared between translation units.
 #pragma once
+#include <cuda_fp16.h>
+
 #include "common.cuh"
 
 namespace midas {
@@ -67,7 +69,9 @@ int launch_block_fill4(midas_gpu_ctx *c, int n1, const int *idx1, int n2, const 
                        int homog, T *out, size_t rs, size_t cs);
 // Z(idx1 rows, idx2 cols) (mode 0) written as the split-TF32 A operand (hi | hi | lo)
 int launch_block_fill4_a3(midas_gpu_ctx *c, int n1, const int *idx1, int n2, const int *idx2, float *A3,
-                          long long lda3);
+                          long long lda3, __half *A3h = nullptr, float hscale = 1.f);
+// upper bound of |Z| over the lattice-table fill (0 when the fill is direct)
+int fill4_bound(midas_gpu_ctx *c, double *bound);
 int sr_ladder(midas_gpu_ctx *c, int s_n, const int *d_idx, int first_cell, int homog, double res_sr, double *fsr_out,
               long long *nnz_out, int want_all, double *all_nnz, double *all_fn, double *fnz_out);
 
