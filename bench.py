@@ -646,7 +646,7 @@ def run_batch_bench(args, wl, world, rank, local, pg):
     torch.cuda.set_device(local)
     cells = [c4_instance(wl, k) for k in range(len(wl["n_mono"]))]
     ntr, n = len(wl["th"]), len(cells)
-    ctx = Context(device=local, fill_mode=_lib.FILL_FAST)
+    ctx = Context(device=local, fill_mode=_lib.FILL_FAST, ir_tol=wl.get("ir_tol", 1e-13))
     contexts = [ctx] + [ctx.sibling() for _ in range(args.lanes - 1)]
     for _ in range(args.warmup):
         batch_step(contexts, wl, cells)
@@ -700,10 +700,12 @@ def run_batch_bench(args, wl, world, rank, local, pg):
         acc = sum(r[0] for r in res) / n
         line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "c64 tf32-tensor LU + f64 FFT-residual refinement",
+                "scaling": "weak", "vs_baseline": None,
+                "dtype": "c64 tf32-tensor LU + double-float (or FP64 FFT) residual refinement",
                 "data": "synthetic (seeded fractal aggregates)",
                 "config": {"workload": wl["name"], "instances": n, "unknowns_min_max": [min(sizes), max(sizes)],
                            "directions": ntr, "polarisations": 2, "lanes": args.lanes,
+                           "ir_tol": wl.get("ir_tol", 1e-13),
                            "parallelism": f"replicas x{world}",
                            "l2": "inputs larger than L2 (per-instance complex64 matrices up to 3.9 GB)"},
                 "roofline": roof, "cpu_baseline": cpu,

@@ -159,7 +159,10 @@ def c4(n_instances=256, ndir=48, nrx=194, seed=11):
     voxelised at 6 cells per monomer diameter (113 cells per monomer: 1.4k-22k
     unknowns); ndir seeded incident directions x 2 polarisations each, and nrx
     seeded scattering directions with equal weights for Q_sca and g ('rf' rules,
-    Compute_Scattering_Quantities_2).  Instances are built by c4_instance."""
+    Compute_Scattering_Quantities_2).  Instances are built by c4_instance.  The
+    mixed solves refine to a 1e-10 backward error: the averages need a field
+    accurate to 1e-6, and the 1e-13 default costs a second double-float residual
+    per instance."""
     from . import geometry as G
     rng = np.random.default_rng(seed)
     th, ph = G.random_directions(ndir, seed=seed + 1)
@@ -168,7 +171,7 @@ def c4(n_instances=256, ndir=48, nrx=194, seed=11):
     return {"name": f"c4_{n_instances}_aggregates_df1.8_{ndir}dirs", "method": "batch", "a": 1.0, "k0": 0.8,
             "m": 1.33 + 0.001j, "df": 1.8, "kf": 1.3, "cells_per_diameter": 6,
             "n_mono": rng.integers(4, 65, n_instances), "seeds": rng.integers(1 << 30, size=n_instances),
-            "th": th, "ph": ph, "rx_th": rth, "rx_ph": rph, "nrx": nrx}
+            "th": th, "ph": ph, "rx_th": rth, "rx_ph": rph, "nrx": nrx, "ir_tol": 1e-10}
 
 
 def c4_small():
