@@ -33,8 +33,10 @@ namespace midas {
 constexpr int FFT_THREADS = 256;
 constexpr int FFT_TILE = 2048;   // complex points per CTA (lines x length)
 constexpr int FFT_LMAX = 512;
+constexpr int FFT_L3MAX = 384;   // the largest mixed-radix length 3 * 2^k
 
-// twiddles w_k = exp(-2 pi i k / FFT_LMAX), k < FFT_LMAX / 2 (host libm, once per device)
+// twiddles w_k = exp(-2 pi i k / FFT_LMAX), k < FFT_LMAX / 2, followed by
+// exp(-2 pi i j / FFT_L3MAX), j < 2 FFT_L3MAX / 3 (host libm, once per device)
 static double2 *g_tw[64];
 
 static int twiddles(midas_gpu_ctx *c, const double2 **out)
@@ -42,10 +44,14 @@ static int twiddles(midas_gpu_ctx *c, const double2 **out)
     static std::atomic<int> ready[64];
     const int dv = c->device & 63;
     if (!ready[dv].load(std::memory_order_acquire)) {
-        std::vector<double2> h(FFT_LMAX / 2);
+        std::vector<double2> h(FFT_LMAX / 2 + 2 * FFT_L3MAX / 3);
         for (int k = 0; k < FFT_LMAX / 2; ++k) {
             const double a = -2.0 * M_PI * k / FFT_LMAX;
             h[k] = make_double2(cos(a), sin(a));
+        }
+        for (int j = 0; j < 2 * FFT_L3MAX / 3; ++j) {
+            const double a = -2.0 * M_PI * j / FFT_L3MAX;
+            h[FFT_LMAX / 2 + j] = make_double2(cos(a), sin(a));
         }
         double2 *d = nullptr;
         MIDAS_CUDA(c, cudaMalloc(&d, sizeof(double2) * h.size()));
@@ -123,14 +129,106 @@ __global__ void __launch_bounds__(FFT_THREADS) k_fft_axis(double2 *data, long lo
     }
 }
 
+// The same pass for lines of L = 3 M points (M = 2^LOGM): three radix-2
+// transforms of the sub-sequences x[3n + r] (loaded bit-reversed), then one
+// radix-3 step X[k + qM] = Y0[k] + w^q W^k Y1[k] + w^2q W^2k Y2[k], w = W^M,
+// W = exp(sign 2 pi i / L).  The 3 x 2^k sizes put grids of odd lattice widths
+// closer to 2n - 1 than the next power of two.
+template <int LOGM>
+__global__ void __launch_bounds__(FFT_THREADS) k_fft_axis3(double2 *data, long long gstride, int ax, int L0, int L1,
+                                                           int na, int nb, int sign, const double2 *tw)
+{
+    constexpr int M = 1 << LOGM, L = 3 * M;
+    constexpr int G = FFT_TILE / L;   // lines per CTA
+    constexpr int LP = L + 1;
+    extern __shared__ double2 sm[];
+    double2 *stw = sm + G * LP;   // M / 2 twiddles of the length-M transforms
+    double2 *stw3 = stw + M / 2;  // 2M twiddles W^j of the radix-3 step
+    const double2 *tw3 = tw + FFT_LMAX / 2;
+    const int tid = threadIdx.x;
+    for (int k = tid; k < M / 2; k += FFT_THREADS) {
+        const double2 w = tw[k * (FFT_LMAX / M)];
+        stw[k] = make_double2(w.x, sign > 0 ? -w.y : w.y);
+    }
+    for (int j = tid; j < 2 * M; j += FFT_THREADS) {
+        const double2 w = tw3[j * (FFT_L3MAX / L)];
+        stw3[j] = make_double2(w.x, sign > 0 ? -w.y : w.y);
+    }
+    const int ntile = (na + G - 1) / G;
+    const int a0 = (blockIdx.x % ntile) * G, b = blockIdx.x / ntile;
+    if (b >= nb) return;
+    long long sa, sb, es;
+    if (ax == 0) { sa = L0; sb = (long long)L0 * L1; es = 1; }
+    else if (ax == 1) { sa = 1; sb = (long long)L0 * L1; es = L0; }
+    else { sa = 1; sb = L0; es = (long long)L0 * L1; }
+    double2 *g = data + (long long)blockIdx.y * gstride + (long long)b * sb;
+    // load: point k goes to sub-line k % 3 at the bit-reversed position of k / 3
+    for (int idx = tid; idx < G * L; idx += FFT_THREADS) {
+        int gl, k;
+        if (ax == 0) { gl = idx / L; k = idx % L; } else { gl = idx % G; k = idx / G; }
+        const int a = a0 + gl;
+        if (a < na) sm[gl * LP + (k % 3) * M + (__brev(k / 3) >> (32 - LOGM))] = g[(long long)a * sa + (long long)k * es];
+    }
+    __syncthreads();
+#pragma unroll 1
+    for (int s = 0; s < LOGM; ++s) {
+        const int h = 1 << s;
+        for (int j = tid; j < G * 3 * (M / 2); j += FFT_THREADS) {
+            const int sub = j / (M / 2), bj = j % (M / 2);
+            const int base = (sub / 3) * LP + (sub % 3) * M;
+            const int grp = bj >> s, pos = bj & (h - 1);
+            const int i0 = base + grp * 2 * h + pos, i1 = i0 + h;
+            const double2 t = cmul(stw[pos << (LOGM - 1 - s)], sm[i1]);
+            const double2 u = sm[i0];
+            sm[i0] = make_double2(u.x + t.x, u.y + t.y);
+            sm[i1] = make_double2(u.x - t.x, u.y - t.y);
+        }
+        __syncthreads();
+    }
+    const double c3 = (sign > 0 ? 1.0 : -1.0) * 0.86602540378443864676;   // Im w = sign sin(2 pi / 3)
+    for (int j = tid; j < G * M; j += FFT_THREADS) {
+        const int base = (j / M) * LP, k = j % M;
+        const double2 y0 = sm[base + k], y1 = cmul(stw3[k], sm[base + M + k]), y2 = cmul(stw3[2 * k], sm[base + 2 * M + k]);
+        const double2 sp = make_double2(y1.x + y2.x, y1.y + y2.y), dm = make_double2(y1.x - y2.x, y1.y - y2.y);
+        const double2 h0 = make_double2(y0.x - 0.5 * sp.x, y0.y - 0.5 * sp.y);
+        const double2 rot = make_double2(-c3 * dm.y, c3 * dm.x);   // i Im(w) (y1 - y2)
+        sm[base + k] = make_double2(y0.x + sp.x, y0.y + sp.y);
+        sm[base + M + k] = make_double2(h0.x + rot.x, h0.y + rot.y);
+        sm[base + 2 * M + k] = make_double2(h0.x - rot.x, h0.y - rot.y);
+    }
+    __syncthreads();
+    for (int idx = tid; idx < G * L; idx += FFT_THREADS) {
+        int gl, k;
+        if (ax == 0) { gl = idx / L; k = idx % L; } else { gl = idx % G; k = idx / G; }
+        const int a = a0 + gl;
+        if (a < na) g[(long long)a * sa + (long long)k * es] = sm[gl * LP + k];
+    }
+}
+
 static int fft_pass(midas_gpu_ctx *c, double2 *data, long long gstride, int ngrids, int ax, const int L[3], int na,
                     int nb, int sign, const double2 *tw)
 {
     const int len = L[ax];
-    const int logl = 31 - __builtin_clz(len);
     const int G = FFT_TILE / len;
     const int ntile = (na + G - 1) / G;
     const dim3 grd((unsigned)(ntile * nb), (unsigned)ngrids);
+    if (len % 3 == 0) {   // 3 x 2^k
+        const int m = len / 3, logm = 31 - __builtin_clz(m);
+        const size_t smem = sizeof(double2) * ((size_t)G * (len + 1) + m / 2 + 2 * m);
+        ++c->launches;
+        switch (logm) {
+#define FFT3_CASE(LG)                                                                                              \
+    case LG:                                                                                                       \
+        k_fft_axis3<LG><<<grd, FFT_THREADS, smem, c->stream>>>(data, gstride, ax, L[0], L[1], na, nb, sign, tw); \
+        break;
+            FFT3_CASE(3) FFT3_CASE(4) FFT3_CASE(5) FFT3_CASE(6) FFT3_CASE(7)
+#undef FFT3_CASE
+        default: return c->err.set(MIDAS_ERR_UNSUPPORTED, "lattice fft: mixed-radix axis length outside 24..384");
+        }
+        MIDAS_CUDA(c, cudaGetLastError());
+        return MIDAS_OK;
+    }
+    const int logl = 31 - __builtin_clz(len);
     const size_t smem = sizeof(double2) * ((size_t)G * (len + 1) + len / 2);
     ++c->launches;
     switch (logl) {
@@ -252,10 +350,13 @@ __global__ void k_lat_gather(int ncell, const int *ijk, const int *lo, int L0, i
     }
 }
 
-static int next_pow2(int v)
+// the smallest transform length >= v: a power of two from 8 or 3 x 2^k (24 .. 384)
+static int fft_len(int v)
 {
     int p = 8;
     while (p < v) p <<= 1;
+    for (int q = 24; q <= FFT_L3MAX; q <<= 1)
+        if (q >= v && q < p) return q;
     return p;
 }
 
@@ -263,7 +364,7 @@ bool lattice_fft_fits(const midas_gpu_ctx *c)
 {
     if (!c->lattice || !c->lat_ijk) return false;
     for (int a = 0; a < 3; ++a)
-        if (next_pow2(2 * (c->lat_hi[a] - c->lat_lo[a] + 1) - 1) > FFT_LMAX) return false;
+        if (fft_len(2 * (c->lat_hi[a] - c->lat_lo[a] + 1) - 1) > FFT_LMAX) return false;
     return true;
 }
 
@@ -279,7 +380,7 @@ bool lattice_fft_preferred(const midas_gpu_ctx *c, long long np)
 {
     if (!lattice_fft_fits(c)) return false;
     double V = 1.0;
-    for (int a = 0; a < 3; ++a) V *= next_pow2(2 * (c->lat_hi[a] - c->lat_lo[a] + 1) - 1);
+    for (int a = 0; a < 3; ++a) V *= fft_len(2 * (c->lat_hi[a] - c->lat_lo[a] + 1) - 1);
     return 15.0 * V * std::log2(V) < (double)np * (double)np;
 }
 
@@ -298,7 +399,7 @@ int lattice_fft_prepare(midas_gpu_ctx *c, bool c4)
     if (c4 ? f.G6c4 : f.G6) return MIDAS_OK;
     for (int a = 0; a < 3; ++a) {
         f.n[a] = c->lat_hi[a] - c->lat_lo[a] + 1;
-        f.L[a] = next_pow2(2 * f.n[a] - 1);
+        f.L[a] = fft_len(2 * f.n[a] - 1);
         if (f.L[a] > FFT_LMAX) return c->err.set(MIDAS_ERR_UNSUPPORTED, "lattice fft: lattice wider than 256 cells along an axis");
     }
     f.npts = (long long)f.L[0] * f.L[1] * f.L[2];

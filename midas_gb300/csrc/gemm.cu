@@ -215,9 +215,9 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float v[32])
 // (coarser than an FMA chain) then only spans 64 products, which brings long-K
 // products with cancellation (the CBF reduced matrix) to FP32-FMA accuracy.
 // With H16 the operands are fp16 (the same 11-bit significands as TF32, half the
-// bytes, twice the MMA rate): a k-block is 64 elements and every k-block is
-// promoted, so each tensor-core chunk again spans 64 products; alpha may be read
-// from device memory (the inverse of the operands' power-of-two scales).
+// bytes, twice the MMA rate): a k-block is 64 elements, so a chunk of two
+// k-blocks spans 128 products; alpha may be read from device memory (the
+// inverse of the operands' power-of-two scales).
 constexpr int TC_PROMOTE_KB = 2;
 
 template <bool PROMOTE, int TC_STAGES, bool H16 = false>
@@ -239,7 +239,7 @@ __global__ void __launch_bounds__(TC_THREADS, TC_STAGES == 2 ? 2 : 1)
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
     const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * TC_BN;
     const int nk = (K + BKE - 1) / BKE;
-    const int KC = PROMOTE ? (H16 ? 1 : TC_PROMOTE_KB) : (nk > 0 ? nk : 1);
+    const int KC = PROMOTE ? TC_PROMOTE_KB : (nk > 0 ? nk : 1);
     const int nchunk = (nk + KC - 1) / KC;
 
     if (threadIdx.x == 0) {
