@@ -134,6 +134,15 @@ FP64_MEASURED = {"workload": "mom_c3 (20,000 voxels, 60,000 unknowns, 64 right-h
                  "mixed_solves_per_s_same_matrix": 31.42, "field_rel_err_mixed_vs_fp64": 3.6e-9}
 
 
+def peaks_clock_mhz():
+    """SM clock of the peak measurements (MEASURED_PEAKS.json), else GB300's maximum."""
+    try:
+        with open(PEAKS_PATH) as f:
+            return float(json.load(f).get("sm_max_mhz", 2070.0))
+    except (OSError, ValueError):
+        return 2070.0
+
+
 def load_peaks():
     try:
         with open(PEAKS_PATH) as f:
@@ -460,6 +469,21 @@ def run_ours(args, wl, world, rank, local, pg):
                  "algorithmic_flops_per_launch": kp["flops"] / max(1, kp["launches"]),
                  "share_of_step": kp["ms"] / ms_prof if ms_prof > 0 else None, "tflops": tf_ach, "gbs": gb_ach,
                  "profiled_ms_per_step": ms_prof / args.steps, "ncu": NCU_COUNTERS.get(top)})
+    if top == "diag_lu":
+        roof["note"] = ("the 64 x 64 diagonal-block LUs and their inverses: one CTA per block (1 of 152 SMs), "
+                        "128 barrier-separated pivot phases -- latency-bound; in the timed six-lane step their "
+                        "launches overlap the other lanes' throughput-bound kernels")
+    if top == "resid":
+        # The double-float CSR residual is bound by FP32 instruction issue, not by HBM: its
+        # arithmetic is 44 FP32 operations per complex multiply-add (four TwoProduct +
+        # TwoSum updates), against one FP32 operation per lane per clock on every SM.
+        props = torch.cuda.get_device_properties(local)
+        mhz = clk.summary().get("sm_mhz") or peaks_clock_mhz()
+        peak_ops = props.multi_processor_count * 128 * mhz * 1e6
+        ops = kp["flops"] / 8.0 * 44.0 / sec if sec > 0 else 0.0
+        roof["fp32_issue"] = {"achieved_ops_per_s": ops, "peak_ops_per_s": peak_ops, "frac": ops / peak_ops,
+                              "ops_per_complex_mac": 44, "sm_mhz": mhz,
+                              "peak_src": f"{props.multi_processor_count} SMs x 128 FP32 lanes x SM clock"}
     classes = {k: {"ms_per_step": v["ms"] / args.steps, "launches_per_step": v["launches"] / args.steps,
                    "gbs": v["bytes"] / (v["ms"] * 1e-3) / 1e9 if v["ms"] > 0 else None,
                    "tflops": v["flops"] / (v["ms"] * 1e-3) / 1e12 if v["ms"] > 0 else None}
