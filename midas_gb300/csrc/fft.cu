@@ -72,6 +72,69 @@ __device__ __forceinline__ double2 cmul(double2 a, double2 b)
     return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
+// ---------------------------------------------------------------------------
+// The transforms compute in double float on the FP32 pipe (GB300's FP64 rate is
+// 1/64 of its FP32 rate): a complex value is (re_hi, im_hi, re_lo, im_lo), each
+// part a hi + lo pair of floats, ~2^-48 relative per operation (Dekker's product
+// with FMA, Knuth's TwoSum for the sum).  Data stay FP64 in global memory and are
+// split on load and rejoined on store.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void df_fast2(float s, float e, float &h, float &l)   // |s| >= |e|
+{
+    h = __fadd_rn(s, e);
+    l = __fsub_rn(e, __fsub_rn(h, s));
+}
+__device__ __forceinline__ void dfr_add(float ah, float al, float bh, float bl, float &h, float &l)
+{
+    float s, e;
+    ef_two_sum(ah, bh, s, e);
+    e = __fadd_rn(e, __fadd_rn(al, bl));
+    df_fast2(s, e, h, l);
+}
+__device__ __forceinline__ void dfr_mul(float ah, float al, float bh, float bl, float &h, float &l)
+{
+    const float p = __fmul_rn(ah, bh);
+    float e = fmaf(ah, bh, -p);
+    e = fmaf(ah, bl, e);
+    e = fmaf(al, bh, e);
+    df_fast2(p, e, h, l);
+}
+__device__ __forceinline__ float4 dfc_load(double2 v)
+{
+    const float rh = (float)v.x, ih = (float)v.y;
+    return make_float4(rh, ih, (float)(v.x - (double)rh), (float)(v.y - (double)ih));
+}
+__device__ __forceinline__ double2 dfc_store(float4 v)
+{
+    return make_double2((double)v.x + (double)v.z, (double)v.y + (double)v.w);
+}
+__device__ __forceinline__ float4 dfc_add(float4 a, float4 b)
+{
+    float4 r;
+    dfr_add(a.x, a.z, b.x, b.z, r.x, r.z);
+    dfr_add(a.y, a.w, b.y, b.w, r.y, r.w);
+    return r;
+}
+__device__ __forceinline__ float4 dfc_sub(float4 a, float4 b)
+{
+    float4 r;
+    dfr_add(a.x, a.z, -b.x, -b.z, r.x, r.z);
+    dfr_add(a.y, a.w, -b.y, -b.w, r.y, r.w);
+    return r;
+}
+__device__ __forceinline__ float4 dfc_mul(float4 a, float4 b)
+{
+    float p1h, p1l, p2h, p2l, p3h, p3l, p4h, p4l;
+    dfr_mul(a.x, a.z, b.x, b.z, p1h, p1l);
+    dfr_mul(a.y, a.w, b.y, b.w, p2h, p2l);
+    dfr_mul(a.x, a.z, b.y, b.w, p3h, p3l);
+    dfr_mul(a.y, a.w, b.x, b.z, p4h, p4l);
+    float4 r;
+    dfr_add(p1h, p1l, -p2h, -p2l, r.x, r.z);
+    dfr_add(p3h, p3l, p4h, p4l, r.y, r.w);
+    return r;
+}
+
 // One radix-2 FFT pass along axis `ax` of a batch of L0 x L1 x L2 grids (x fastest).
 // The lines along ax are indexed by (a, b): for ax = 0, a = y and b = z; for
 // ax = 1, a = x and b = z; for ax = 2, a = x and b = y.  Only lines with
@@ -84,12 +147,12 @@ __global__ void __launch_bounds__(FFT_THREADS) k_fft_axis(double2 *data, long lo
     constexpr int L = 1 << LOGL;
     constexpr int G = FFT_TILE / L;   // lines per CTA
     constexpr int LP = L + 1;         // padded line length in shared memory
-    extern __shared__ double2 sm[];
-    double2 *stw = sm + G * LP;
+    extern __shared__ float4 sm[];
+    float4 *stw = sm + G * LP;
     const int tid = threadIdx.x;
     for (int k = tid; k < L / 2; k += FFT_THREADS) {
         const double2 w = tw[k * (FFT_LMAX / L)];
-        stw[k] = make_double2(w.x, sign > 0 ? -w.y : w.y);
+        stw[k] = dfc_load(make_double2(w.x, sign > 0 ? -w.y : w.y));
     }
     const int ntile = (na + G - 1) / G;
     const int a0 = (blockIdx.x % ntile) * G, b = blockIdx.x / ntile;
@@ -104,7 +167,7 @@ __global__ void __launch_bounds__(FFT_THREADS) k_fft_axis(double2 *data, long lo
         int gl, k;
         if (ax == 0) { gl = idx / L; k = idx % L; } else { gl = idx % G; k = idx / G; }
         const int a = a0 + gl;
-        if (a < na) sm[gl * LP + (__brev(k) >> (32 - LOGL))] = g[(long long)a * sa + (long long)k * es];
+        if (a < na) sm[gl * LP + (__brev(k) >> (32 - LOGL))] = dfc_load(g[(long long)a * sa + (long long)k * es]);
     }
     __syncthreads();
 #pragma unroll 1
@@ -114,10 +177,10 @@ __global__ void __launch_bounds__(FFT_THREADS) k_fft_axis(double2 *data, long lo
             const int gl = j / (L / 2), bj = j % (L / 2);
             const int grp = bj >> s, pos = bj & (h - 1);
             const int i0 = gl * LP + grp * 2 * h + pos, i1 = i0 + h;
-            const double2 t = cmul(stw[pos << (LOGL - 1 - s)], sm[i1]);
-            const double2 u = sm[i0];
-            sm[i0] = make_double2(u.x + t.x, u.y + t.y);
-            sm[i1] = make_double2(u.x - t.x, u.y - t.y);
+            const float4 t = dfc_mul(stw[pos << (LOGL - 1 - s)], sm[i1]);
+            const float4 u = sm[i0];
+            sm[i0] = dfc_add(u, t);
+            sm[i1] = dfc_sub(u, t);
         }
         __syncthreads();
     }
@@ -125,7 +188,7 @@ __global__ void __launch_bounds__(FFT_THREADS) k_fft_axis(double2 *data, long lo
         int gl, k;
         if (ax == 0) { gl = idx / L; k = idx % L; } else { gl = idx % G; k = idx / G; }
         const int a = a0 + gl;
-        if (a < na) g[(long long)a * sa + (long long)k * es] = sm[gl * LP + k];
+        if (a < na) g[(long long)a * sa + (long long)k * es] = dfc_store(sm[gl * LP + k]);
     }
 }
 
@@ -141,18 +204,18 @@ __global__ void __launch_bounds__(FFT_THREADS) k_fft_axis3(double2 *data, long l
     constexpr int M = 1 << LOGM, L = 3 * M;
     constexpr int G = FFT_TILE / L;   // lines per CTA
     constexpr int LP = L + 1;
-    extern __shared__ double2 sm[];
-    double2 *stw = sm + G * LP;   // M / 2 twiddles of the length-M transforms
-    double2 *stw3 = stw + M / 2;  // 2M twiddles W^j of the radix-3 step
+    extern __shared__ float4 sm[];
+    float4 *stw = sm + G * LP;   // M / 2 twiddles of the length-M transforms
+    float4 *stw3 = stw + M / 2;  // 2M twiddles W^j of the radix-3 step
     const double2 *tw3 = tw + FFT_LMAX / 2;
     const int tid = threadIdx.x;
     for (int k = tid; k < M / 2; k += FFT_THREADS) {
         const double2 w = tw[k * (FFT_LMAX / M)];
-        stw[k] = make_double2(w.x, sign > 0 ? -w.y : w.y);
+        stw[k] = dfc_load(make_double2(w.x, sign > 0 ? -w.y : w.y));
     }
     for (int j = tid; j < 2 * M; j += FFT_THREADS) {
         const double2 w = tw3[j * (FFT_L3MAX / L)];
-        stw3[j] = make_double2(w.x, sign > 0 ? -w.y : w.y);
+        stw3[j] = dfc_load(make_double2(w.x, sign > 0 ? -w.y : w.y));
     }
     const int ntile = (na + G - 1) / G;
     const int a0 = (blockIdx.x % ntile) * G, b = blockIdx.x / ntile;
@@ -167,7 +230,8 @@ __global__ void __launch_bounds__(FFT_THREADS) k_fft_axis3(double2 *data, long l
         int gl, k;
         if (ax == 0) { gl = idx / L; k = idx % L; } else { gl = idx % G; k = idx / G; }
         const int a = a0 + gl;
-        if (a < na) sm[gl * LP + (k % 3) * M + (__brev(k / 3) >> (32 - LOGM))] = g[(long long)a * sa + (long long)k * es];
+        if (a < na)
+            sm[gl * LP + (k % 3) * M + (__brev(k / 3) >> (32 - LOGM))] = dfc_load(g[(long long)a * sa + (long long)k * es]);
     }
     __syncthreads();
 #pragma unroll 1
@@ -178,30 +242,35 @@ __global__ void __launch_bounds__(FFT_THREADS) k_fft_axis3(double2 *data, long l
             const int base = (sub / 3) * LP + (sub % 3) * M;
             const int grp = bj >> s, pos = bj & (h - 1);
             const int i0 = base + grp * 2 * h + pos, i1 = i0 + h;
-            const double2 t = cmul(stw[pos << (LOGM - 1 - s)], sm[i1]);
-            const double2 u = sm[i0];
-            sm[i0] = make_double2(u.x + t.x, u.y + t.y);
-            sm[i1] = make_double2(u.x - t.x, u.y - t.y);
+            const float4 t = dfc_mul(stw[pos << (LOGM - 1 - s)], sm[i1]);
+            const float4 u = sm[i0];
+            sm[i0] = dfc_add(u, t);
+            sm[i1] = dfc_sub(u, t);
         }
         __syncthreads();
     }
-    const double c3 = (sign > 0 ? 1.0 : -1.0) * 0.86602540378443864676;   // Im w = sign sin(2 pi / 3)
+    // Im w = sign sin(2 pi / 3) as a double float; i Im(w) (y1 - y2) is (-c3 d.im, c3 d.re)
+    const double c3d = (sign > 0 ? 1.0 : -1.0) * 0.86602540378443864676;
+    const float c3h = (float)c3d, c3l = (float)(c3d - (double)c3h);
     for (int j = tid; j < G * M; j += FFT_THREADS) {
         const int base = (j / M) * LP, k = j % M;
-        const double2 y0 = sm[base + k], y1 = cmul(stw3[k], sm[base + M + k]), y2 = cmul(stw3[2 * k], sm[base + 2 * M + k]);
-        const double2 sp = make_double2(y1.x + y2.x, y1.y + y2.y), dm = make_double2(y1.x - y2.x, y1.y - y2.y);
-        const double2 h0 = make_double2(y0.x - 0.5 * sp.x, y0.y - 0.5 * sp.y);
-        const double2 rot = make_double2(-c3 * dm.y, c3 * dm.x);   // i Im(w) (y1 - y2)
-        sm[base + k] = make_double2(y0.x + sp.x, y0.y + sp.y);
-        sm[base + M + k] = make_double2(h0.x + rot.x, h0.y + rot.y);
-        sm[base + 2 * M + k] = make_double2(h0.x - rot.x, h0.y - rot.y);
+        const float4 y0 = sm[base + k], y1 = dfc_mul(stw3[k], sm[base + M + k]),
+                     y2 = dfc_mul(stw3[2 * k], sm[base + 2 * M + k]);
+        const float4 sp = dfc_add(y1, y2), dm = dfc_sub(y1, y2);
+        const float4 h0 = dfc_sub(y0, make_float4(0.5f * sp.x, 0.5f * sp.y, 0.5f * sp.z, 0.5f * sp.w));
+        float4 rot;
+        dfr_mul(-c3h, -c3l, dm.y, dm.w, rot.x, rot.z);
+        dfr_mul(c3h, c3l, dm.x, dm.z, rot.y, rot.w);
+        sm[base + k] = dfc_add(y0, sp);
+        sm[base + M + k] = dfc_add(h0, rot);
+        sm[base + 2 * M + k] = dfc_sub(h0, rot);
     }
     __syncthreads();
     for (int idx = tid; idx < G * L; idx += FFT_THREADS) {
         int gl, k;
         if (ax == 0) { gl = idx / L; k = idx % L; } else { gl = idx % G; k = idx / G; }
         const int a = a0 + gl;
-        if (a < na) g[(long long)a * sa + (long long)k * es] = sm[gl * LP + k];
+        if (a < na) g[(long long)a * sa + (long long)k * es] = dfc_store(sm[gl * LP + k]);
     }
 }
 
