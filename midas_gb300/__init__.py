@@ -4,4 +4,11 @@
 (C ABI in include/midas_gpu.h); ``midas_gb300.geometry`` prepares cells and
 CBFM partitions.
 """
-from . import geometry  # noqa: F401
+import os as _os
+
+# The library's CBFM pipeline runs ~20 CUDA streams; the CUDA default of 8 hardware work
+# queues makes streams share queues, so a long kernel on one holds up the others.  The
+# setting must precede the process's first CUDA context (torch's included).
+_os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
+from . import geometry  # noqa: E402,F401

@@ -736,7 +736,7 @@ __global__ void __launch_bounds__(256) k_heev_tridiag(int m, double2 *Ab, long l
                                                       long long logcap, long long *logn, int *flag)
 {
     extern __shared__ double shm[];
-    double *d = shm, *e = d + m, *rc = e + m, *rs = rc + m, *red = rs + m;   // red: 32 doubles
+    double *d = shm, *e = d + m, *red = e + m;   // red: 32 doubles
     double2 *tau = (double2 *)(red + 32), *v = tau + m, *x = v + m;
     __shared__ double2 s_tau, s_scale;
     __shared__ double s_beta;
@@ -745,7 +745,6 @@ __global__ void __launch_bounds__(256) k_heev_tridiag(int m, double2 *Ab, long l
     double *W = Wb + (long long)blockIdx.x * m;
     int *pos = posb + (long long)blockIdx.x * m;
     double2 *lg = logb + blockIdx.x * logcap;   // per sweep: (mm, nrot), then nrot (s, c)
-    long long lp = 0;                            // log length (thread 0)
     const int tid = threadIdx.x, nt = blockDim.x;
     // ---- tridiagonalisation --------------------------------------------------
     for (int k = 0; k < m - 1; ++k) {
@@ -817,13 +816,16 @@ __global__ void __launch_bounds__(256) k_heev_tridiag(int m, double2 *Ab, long l
                 x[i] = make_double2(x[i].x + al.x * b.x - al.y * b.y, x[i].y + al.x * b.y + al.y * b.x);
             }
             __syncthreads();
-            // A22 -= v w^H + w v^H
-            for (int q = tid; q < L * L; q += nt) {
-                int i = q / L, j = q % L;
-                double2 vi = v[i], wi = x[i], vj = v[j], wj = x[j];
-                double2 *a = A + (long long)(k + 1 + i) * lda + (k + 1 + j);
-                a->x -= (vi.x * wj.x + vi.y * wj.y) + (wi.x * vj.x + wi.y * vj.y);
-                a->y -= (vi.y * wj.x - vi.x * wj.y) + (wi.y * vj.x - wi.x * vj.y);
+            // A22 -= v w^H + w v^H (a warp per row, the lanes along it)
+            for (int i = tid / 32; i < L; i += nt / 32) {
+                const double2 vi = v[i], wi = x[i];
+                double2 *row = A + (long long)(k + 1 + i) * lda + (k + 1);
+                for (int j = tid % 32; j < L; j += 32) {
+                    const double2 vj = v[j], wj = x[j];
+                    double2 *a = row + j;
+                    a->x -= (vi.x * wj.x + vi.y * wj.y) + (wi.x * vj.x + wi.y * vj.y);
+                    a->y -= (vi.y * wj.x - vi.x * wj.y) + (wi.y * vj.x - wi.x * vj.y);
+                }
             }
         }
         if (tid == 0) {
@@ -835,92 +837,98 @@ __global__ void __launch_bounds__(256) k_heev_tridiag(int m, double2 *Ab, long l
     if (tid == 0) { d[m - 1] = A[(long long)(m - 1) * lda + (m - 1)].x; e[m - 1] = 0; }
     if (tid == 0) H[(long long)(m - 1) * m + (m - 1)] = make_double2(0, 0);   // no reflector k = m - 1
     __syncthreads();
-    // ---- implicit QL on (d, e) ------------------------------------------------
+    // ---- implicit QL on (d, e), warp 0 ------------------------------------------
     // deflation: |e| <= eps (|d_i| + |d_i+1|), or |e| <= eps ||T|| -- eigenvalues at the
-    // roundoff level of a rank-deficient Gram matrix never pass the relative test alone
+    // roundoff level of a rank-deficient Gram matrix never pass the relative test alone.
+    // The lanes test 32 off-diagonals at a time for the split point; lane 0 runs each
+    // sweep (the rotation chain is serial) with the next rotation's d and e loaded ahead,
+    // and logs the rotations straight to global memory.
     const double eps = 2.220446049250313e-16;
-    __shared__ double s_tn;
-    if (tid == 0) {
+    if (tid < 32) {
+        const int lane = tid;
         double tn = 0;
-        for (int i = 0; i < m; ++i) tn = fmax(tn, fabs(d[i]) + fabs(e[i]) + (i > 0 ? fabs(e[i - 1]) : 0.0));
-        s_tn = tn;
-    }
-    __syncthreads();
-    const double tnorm = s_tn;
-    for (int l = 0; l < m; ++l) {
-        int iter = 0;
-        while (true) {
-            __shared__ int s_mm;
-            if (tid == 0) {
-                int mm = l;
-                while (mm < m - 1) {
-                    double dd = fabs(d[mm]) + fabs(d[mm + 1]);
-                    if (fabs(e[mm]) <= eps * dd || fabs(e[mm]) <= eps * tnorm) break;
-                    ++mm;
-                }
-                s_mm = mm;
-            }
-            __syncthreads();
-            const int mm = s_mm;
-            if (mm == l) break;
-            if (++iter > 200) {
-                if (tid == 0) atomicOr(flag, DEV_BAD_ARG);
-                break;
-            }
-            if (tid == 0) {
-                // one thread runs the sweep on the FP64 pipe; sqrt(f^2 + g^2) and one
-                // reciprocal per rotation (|g| <= ~1/eps after the deflation test and f,
-                // g are bounded by ||T||, so the squares cannot overflow)
-                double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
-                double r = sqrt(g * g + 1.0);
-                g = d[mm] - d[l] + e[l] / (g + copysign(r, g));
-                double s = 1, c = 1, p = 0;
-                int cnt = 0, broke = 0;
-                for (int i = mm - 1; i >= l; --i) {
-                    double f = s * e[i], b = c * e[i];
-                    r = sqrt(f * f + g * g);
-                    e[i + 1] = r;
-                    if (r == 0.0) { d[i + 1] -= p; e[mm] = 0.0; broke = 1; break; }
-                    const double ir = 1.0 / r;
-                    s = f * ir; c = g * ir;
-                    g = d[i + 1] - p;
-                    r = (d[i] - g) * s + 2.0 * c * b;
-                    p = s * r;
-                    d[i + 1] = g + p;
-                    g = c * r - b;
-                    rs[cnt] = s; rc[cnt] = c;
-                    ++cnt;
-                }
-                if (!broke) { d[l] -= p; e[l] = g; e[mm] = 0.0; }
-                if (cnt > 0) {
-                    if (lp + 1 + cnt > logcap) {
-                        atomicOr(flag, DEV_BAD_ARG);   // rotation log full (not expected: ~1.5 m^2 rotations)
-                    } else {
-                        lg[lp] = make_double2((double)mm, (double)cnt);
-                        for (int q = 0; q < cnt; ++q) lg[lp + 1 + q] = make_double2(rs[q], rc[q]);
-                        lp += 1 + cnt;
+        for (int i = lane; i < m; i += 32) tn = fmax(tn, fabs(d[i]) + fabs(e[i]) + (i > 0 ? fabs(e[i - 1]) : 0.0));
+        for (int o = 16; o > 0; o >>= 1) tn = fmax(tn, __shfl_xor_sync(0xffffffffu, tn, o));
+        const double tnorm = tn;
+        long long lp = 0;   // log length (the same in every lane)
+        bool fail = false;
+        for (int l = 0; l < m && !fail; ++l) {
+            for (int iter = 0;; ++iter) {
+                int mm = -1;   // first split point at or after l (m - 1 at the latest)
+                for (int base = l; mm < 0; base += 32) {
+                    const int q = base + lane;
+                    bool split = true;
+                    if (q < m - 1) {
+                        const double eq = fabs(e[q]);
+                        split = eq <= eps * (fabs(d[q]) + fabs(d[q + 1])) || eq <= eps * tnorm;
                     }
+                    const unsigned bal = __ballot_sync(0xffffffffu, split);
+                    if (bal) mm = base + __ffs(bal) - 1;
                 }
+                if (mm == l) break;
+                if (iter >= 200 || lp + 1 + (mm - l) > logcap) {
+                    // no convergence, or the rotation log is full (not expected: ~1.5 m^2 rotations)
+                    if (lane == 0) atomicOr(flag, DEV_BAD_ARG);
+                    fail = true;
+                    break;
+                }
+                int cnt = 0;
+                if (lane == 0) {
+                    double2 *out = lg + lp + 1;   // per sweep: (mm, nrot), then nrot (s, c)
+                    double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
+                    const double r0 = sqrt(g * g + 1.0);
+                    g = d[mm] - d[l] + e[l] / (g + copysign(r0, g));
+                    double s = 1, c = 1, p = 0;
+                    double ei = e[mm - 1], di = d[mm - 1], dh = d[mm];   // e[i], d[i], d[i+1] (not yet updated)
+                    bool broke = false;
+                    for (int i = mm - 1; i >= l; --i) {
+                        const double en = i > l ? e[i - 1] : 0.0, dn = i > l ? d[i - 1] : 0.0;
+                        const double f = s * ei, b = c * ei;
+                        // r = sqrt(f^2 + g^2) and 1 / r: the FP32 reciprocal square root refined by
+                        // two Newton-Raphson steps y <- y (3/2 - q y^2 / 2) in FP64 (error ~1 ulp),
+                        // a shorter dependent chain than an FP64 square root and divide.  |g| is
+                        // bounded by ~||T|| / eps after the deflation test, so q cannot overflow.
+                        const double q2 = f * f + g * g;
+                        if (q2 == 0.0) { e[i + 1] = 0.0; d[i + 1] = dh - p; broke = true; break; }
+                        const float qf = (float)q2;
+                        double ir = (qf > 1e-37f && qf < 1e37f) ? (double)rsqrtf(qf) : 1.0 / sqrt(q2);
+                        const double hq = 0.5 * q2;
+                        ir = ir * (1.5 - hq * ir * ir);
+                        ir = ir * (1.5 - hq * ir * ir);
+                        e[i + 1] = q2 * ir;
+                        s = f * ir;
+                        c = g * ir;
+                        g = dh - p;
+                        const double r = (di - g) * s + 2.0 * c * b;
+                        p = s * r;
+                        d[i + 1] = g + p;
+                        g = c * r - b;
+                        out[cnt++] = make_double2(s, c);
+                        ei = en; dh = di; di = dn;
+                    }
+                    if (!broke) { d[l] -= p; e[l] = g; }
+                    e[mm] = 0.0;
+                    if (cnt > 0) lg[lp] = make_double2((double)mm, (double)cnt);
+                }
+                __syncwarp();
+                cnt = __shfl_sync(0xffffffffu, cnt, 0);
+                if (cnt > 0) lp += 1 + cnt;
             }
-            __syncthreads();
         }
-    }
-    if (tid == 0) logn[blockIdx.x] = lp;
-    // ---- sort (descending) ------------------------------------------------------
-    __shared__ int ord[1024];
-    if (tid == 0) {
-        for (int i = 0; i < m; ++i) ord[i] = i;
-        for (int i = 0; i < m; ++i) {
-            int bst = i;
-            for (int j = i + 1; j < m; ++j)
-                if (d[ord[j]] > d[ord[bst]]) bst = j;
-            int tmp = ord[i]; ord[i] = ord[bst]; ord[bst] = tmp;
-        }
+        if (lane == 0) logn[blockIdx.x] = fail ? 0 : lp;
     }
     __syncthreads();
+    // ---- sort (descending): each eigenvalue's rank, ties in index order ------------
     for (int i = tid; i < m; i += nt) {
-        W[i] = d[ord[i]];
-        pos[ord[i]] = i;   // eigenvector i goes to column pos[i]
+        const double di = d[i];
+        if (!(di == di)) atomicOr(flag, DEV_BAD_ARG);   // NaN
+        int rank = 0;
+        for (int j = 0; j < m; ++j) {
+            const double dj = d[j];
+            rank += (dj > di) || (dj == di && j < i);
+        }
+        W[rank] = di;
+        pos[i] = rank;   // eigenvector i goes to column pos[i]
     }
 }
 
@@ -1027,7 +1035,7 @@ int heev_dev(midas_gpu_ctx *c, int batch, int m, double2 *A, long long lda, long
     long long *logn = (long long *)take(sizeof(long long) * batch);
     int *pos = (int *)take(sizeof(int) * (size_t)batch * m);
     double *Z = (double *)take(sizeof(double) * (size_t)batch * m * m);
-    size_t sm = sizeof(double) * (4 * (size_t)m + 32) + sizeof(double2) * 3 * (size_t)m;
+    size_t sm = sizeof(double) * (2 * (size_t)m + 32) + sizeof(double2) * 3 * (size_t)m;
     int cb = 32;   // columns per back-transformation CTA: Z columns [m][cb] + the reflector [m]
     while (cb > 8 && sizeof(double2) * (size_t)m * (cb + 1) > 200 * 1024) cb /= 2;
     const size_t smb = sizeof(double2) * (size_t)m * (cb + 1);

@@ -157,6 +157,7 @@ struct midas_gpu_ctx {
     // lanes: child contexts (own stream and scratch pool, the cells aliased)
     // that run independent CBFM blocks concurrently
     std::vector<midas_gpu_ctx *> lanes;
+    std::vector<midas_gpu_ctx *> aux;   // the CBFM pipeline's finisher and eigen-solve contexts
     // side stream (created on first use, same priority as `stream`) for work that
     // only joins later, e.g. the solve's diagonal-block inverses during the LU
     cudaStream_t side = nullptr;

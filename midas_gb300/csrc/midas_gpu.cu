@@ -1,6 +1,7 @@
 // midas_gpu.cu -- C ABI of the GB300 MIDAS hot path (see include/midas_gpu.h).
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 
@@ -306,6 +307,12 @@ int midas_gpu_init(const midas_gpu_opts *opts, midas_gpu_ctx **out)
     if (o.index_base != 0 && o.index_base != 1) return MIDAS_ERR_ARG;
     if (o.solve_mode != MIDAS_SOLVE_MIXED && o.solve_mode != MIDAS_SOLVE_FP64) return MIDAS_ERR_ARG;
     if (o.fill_mode != MIDAS_FILL_FAITHFUL && o.fill_mode != MIDAS_FILL_FAST) return MIDAS_ERR_ARG;
+    // The CBFM pipeline drives ~20 streams (lanes, their side streams, eigen-solve and
+    // finisher streams).  With the default 8 hardware work queues streams share queues,
+    // and a long kernel (an eigen-solve, ~50 ms on one SM) holds up the kernels queued
+    // behind it from other streams.  Takes effect only if this process has no CUDA
+    // context yet; an explicit setting is kept.
+    setenv("CUDA_DEVICE_MAX_CONNECTIONS", "32", 0);
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || o.device < 0 || o.device >= ndev) {
         cudaGetLastError();

@@ -163,7 +163,7 @@ def test_errors_are_reported(gpulib):
     c.close()
 
 
-@pytest.mark.parametrize("m", [7, 64, 182])
+@pytest.mark.parametrize("m", [7, 64, 182, 380])
 def test_heev_jacobi(ctx, m):
     """Graded spectrum (singular values 1 .. 1e-9), as the Gram matrices of the CBF step."""
     rng = np.random.default_rng(m)
@@ -180,6 +180,22 @@ def test_heev_jacobi(ctx, m):
     sel = ref > 1e-8 * ref[0]
     assert np.max(np.abs(W[sel] - ref[sel]) / ref[sel]) < 4e-8
     assert np.max(np.abs(V.conj().T @ A @ V - np.diag(W))) <= 1e-12 * ref[0]
+
+
+@pytest.mark.parametrize("m,rank", [(182, 60), (96, 1)])
+def test_heev_rank_deficient(ctx, m, rank):
+    """Gram matrix of fewer independent solutions than excitations: m - rank eigenvalues at
+    the roundoff level (the split test against eps ||T|| deflates them)."""
+    rng = np.random.default_rng(m + rank)
+    X = rng.standard_normal((3 * m, rank)) + 1j * rng.standard_normal((3 * m, rank))
+    X = X @ (rng.standard_normal((rank, m)) + 1j * rng.standard_normal((rank, m)))
+    A = X.conj().T @ X
+    W, V = ctx.heev(A)
+    ref = np.sort(np.linalg.eigvalsh(A))[::-1]
+    assert np.all(np.diff(W) <= 0)
+    assert np.max(np.abs(W - ref)) <= 1e-13 * ref[0]
+    assert np.max(np.abs(V.conj().T @ V - np.eye(m))) <= 1e-12
+    assert np.max(np.abs(A @ V[:, :rank] - V[:, :rank] * W[:rank])) <= 1e-12 * ref[0]
 
 
 @pytest.mark.parametrize("M,N,K", [(130, 65, 828), (300, 40, 2000)])
