@@ -406,14 +406,14 @@ __device__ __forceinline__ float4 zd_split(double2 v)
     return r;
 }
 
-__global__ void __launch_bounds__(256) k_zgemm_df(int M, int N, int K, const double2 *__restrict__ A, long long ars,
-                                                   long long acs, const double2 *__restrict__ B, long long brs,
-                                                   long long bcs, double2 *C, long long crs, long long ccs,
-                                                   int kchunk, float4 *P)
+// one 64 x 64 tile of C (or of split partial sp in P) over k in [sp kchunk, (sp+1) kchunk)
+__device__ __forceinline__ void zgemm_df_tile(int M, int N, int K, const double2 *__restrict__ A, long long ars,
+                                              long long acs, const double2 *__restrict__ B, long long brs,
+                                              long long bcs, double2 *C, long long crs, long long ccs, int kchunk,
+                                              float4 *P, int i0, int j0, int sp)
 {
     __shared__ float4 As[ZD_TK][64], Bs[ZD_TK][64];
     const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
-    const int i0 = blockIdx.y * 64, j0 = blockIdx.x * 64, sp = blockIdx.z;
     const int kb = sp * kchunk, ke = min(K, kb + kchunk);
     float rh[4][4], rl[4][4], ih[4][4], il[4][4];
 #pragma unroll
@@ -464,6 +464,48 @@ __global__ void __launch_bounds__(256) k_zgemm_df(int M, int N, int K, const dou
         }
 }
 
+__global__ void __launch_bounds__(256) k_zgemm_df(int M, int N, int K, const double2 *__restrict__ A, long long ars,
+                                                   long long acs, const double2 *__restrict__ B, long long brs,
+                                                   long long bcs, double2 *C, long long crs, long long ccs,
+                                                   int kchunk, float4 *P)
+{
+    zgemm_df_tile(M, N, K, A, ars, acs, B, brs, bcs, C, crs, ccs, kchunk, P, blockIdx.y * 64, blockIdx.x * 64,
+                  blockIdx.z);
+}
+
+// many independent products in one launch: blockIdx.z = job * nsplit + split part
+__global__ void __launch_bounds__(256) k_zgemm_df_batched(const ZdfJob *__restrict__ jobs, int nsplit, float4 *P)
+{
+    const ZdfJob J = jobs[blockIdx.z / nsplit];
+    const int i0 = blockIdx.y * 64, j0 = blockIdx.x * 64;
+    if (i0 >= J.M || j0 >= J.N) return;   // the whole CTA: the job is smaller than the grid
+    zgemm_df_tile(J.M, J.N, J.K, J.A, J.ars, J.acs, J.B, J.brs, J.bcs, J.C, J.crs, J.ccs, J.kchunk,
+                  nsplit > 1 ? P + J.poff : nullptr, i0, j0, blockIdx.z % nsplit);
+}
+
+__global__ void k_zgemm_df_batched_reduce(const ZdfJob *__restrict__ jobs, int njobs, long long tot, int nsplit,
+                                          const float4 *P)
+{
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tot;
+         e += (long long)gridDim.x * blockDim.x) {
+        int lo = 0, hi = njobs - 1;   // the job holding output e: the last with eoff <= e
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) / 2;
+            if (jobs[mid].eoff <= e) lo = mid; else hi = mid - 1;
+        }
+        const ZdfJob &J = jobs[lo];
+        const long long q = e - J.eoff, mn = (long long)J.M * J.N;
+        double re = 0, im = 0;
+        for (int sp = 0; sp < nsplit; ++sp) {
+            const float4 p = P[J.poff + sp * mn + q];
+            re += (double)p.x + (double)p.z;
+            im += (double)p.y + (double)p.w;
+        }
+        const int i = (int)(q / J.N), j = (int)(q % J.N);
+        J.C[(long long)i * J.crs + (long long)j * J.ccs] = make_double2(re, im);
+    }
+}
+
 __global__ void k_zgemm_df_reduce(int M, int N, int nsplit, const float4 *P, double2 *C, long long crs, long long ccs)
 {
     const long long tot = (long long)M * N;
@@ -506,6 +548,56 @@ int zgemm_df(midas_gpu_ctx *c, int M, int N, int K, const double2 *A, long long 
             M, N, nsplit, P, C, crs, ccs);
     }
     kp_end(c, kp, MIDAS_KC_ZGEMM64, 8.0 * M * (double)N * K, 16.0 * ((double)M * K + (double)K * N + (double)M * N));
+    MIDAS_CUDA(c, cudaGetLastError());
+    return MIDAS_OK;
+}
+
+int zgemm_df_batched(midas_gpu_ctx *c, std::vector<ZdfJob> &jobs)
+{
+    const int nj = (int)jobs.size();
+    if (nj == 0) return MIDAS_OK;
+    long long tiles = 0;
+    int mt = 0, nt = 0, kmax = 0;
+    for (const ZdfJob &J : jobs) {
+        if (J.M <= 0 || J.N <= 0 || J.K <= 0) return c->err.set(MIDAS_ERR_ARG, "zgemm_df_batched: empty job");
+        tiles += (long long)((J.M + 63) / 64) * ((J.N + 63) / 64);
+        mt = std::max(mt, (J.M + 63) / 64);
+        nt = std::max(nt, (J.N + 63) / 64);
+        kmax = std::max(kmax, J.K);
+    }
+    // split K while the tiles of all jobs together fill less than ~4 CTAs per SM (a job
+    // with a short K leaves its trailing parts empty: they add zeros)
+    int nsplit = (int)std::min<long long>(ZD_SMAX, std::max<long long>(1, 600 / tiles));
+    nsplit = std::max(1, std::min(nsplit, kmax / 64));
+    if ((long long)nj * nsplit > 65535) return c->err.set(MIDAS_ERR_ARG, "zgemm_df_batched: too many jobs");
+    long long poff = 0, eoff = 0;
+    for (ZdfJob &J : jobs) {
+        J.kchunk = ((J.K + nsplit - 1) / nsplit + ZD_TK - 1) / ZD_TK * ZD_TK;
+        J.poff = poff;
+        J.eoff = eoff;
+        poff += (long long)nsplit * J.M * J.N;
+        eoff += (long long)J.M * J.N;
+    }
+    const size_t jb = (sizeof(ZdfJob) * nj + 255) / 256 * 256;
+    void *p;
+    MIDAS_TRY(ensure(c, S_ZDF, jb + (nsplit > 1 ? sizeof(float4) * (size_t)poff : 0) + 256, &p));
+    ZdfJob *d_jobs = (ZdfJob *)p;
+    float4 *P = (float4 *)((char *)p + jb);
+    MIDAS_CUDA(c, cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(ZdfJob) * nj, cudaMemcpyHostToDevice, c->stream));
+    double flops = 0, bytes = 0;
+    for (const ZdfJob &J : jobs) {
+        flops += 8.0 * J.M * (double)J.N * J.K;
+        bytes += 16.0 * ((double)J.M * J.K + (double)J.K * J.N + (double)J.M * J.N);
+    }
+    ++c->launches;
+    int kp = kp_begin(c);
+    k_zgemm_df_batched<<<dim3(nt, mt, nj * nsplit), 256, 0, c->stream>>>(d_jobs, nsplit, P);
+    if (nsplit > 1) {
+        ++c->launches;
+        k_zgemm_df_batched_reduce<<<(unsigned)std::min<long long>((eoff + 255) / 256, 4096), 256, 0, c->stream>>>(
+            d_jobs, nj, eoff, nsplit, P);
+    }
+    kp_end(c, kp, MIDAS_KC_ZGEMM64, flops, bytes);
     MIDAS_CUDA(c, cudaGetLastError());
     return MIDAS_OK;
 }

@@ -933,7 +933,7 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
     MIDAS_TRY(ensure(c, S_Z32, sizeof(float2) * (size_t)npd * npd, &p32));
     MIDAS_TRY(ensure(c, S_RHS64, sizeof(double2) * (size_t)npd * nr, &pb));
     MIDAS_TRY(ensure(c, S_X64, sizeof(double2) * (size_t)npd * nr, &px));
-    MIDAS_TRY(ensure(c, S_EINC, sizeof(double2) * (size_t)3 * nbmax * nr, &pe));
+    MIDAS_TRY(ensure(c, S_EINC, sizeof(double2) * (size_t)3 * n * nr, &pe));
     {
         long long tot = (long long)npd * npd;
         ++c->launches;
@@ -942,12 +942,24 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
     }
     double2 *Vc = (double2 *)pb, *Einc = (double2 *)pe;
     MIDAS_CUDA(c, cudaMemsetAsync(Vc, 0, sizeof(double2) * (size_t)npd * nr, c->stream));
-    for (int b = 0; b < nb; ++b) {
-        const int nbc = bo[b + 1] - bo[b];
-        MIDAS_TRY(launch_incident4<double2>(c, nbc, d_all + bo[b], ntr, d_th, d_ph, Einc, 1, (size_t)3 * nbc));
-        // Vc[koff_b .., :] = C_b^T Einc_b  (plain transpose)
-        MIDAS_TRY(zgemm_df(c, Kb[b], nr, 3 * nbc, Call + coff[b], 3 * nbc, 1, Einc, 1, 3 * nbc, Vc + koff[b], 1, npd));
-    }
+    // the incident fields on every cell (column-major 3n x nr)
+    MIDAS_TRY(launch_incident4<double2>(c, n, d_all, ntr, d_th, d_ph, Einc, 1, (size_t)3 * n));
+    // reduced right-hand sides and residuals: rows koff_b of V = C_b^T F_b for every block,
+    // one batched launch (F column-major 3n x nr)
+    auto project = [&](const double2 *Fv, double2 *V) -> int {
+        std::vector<ZdfJob> jobs;
+        for (int b = 0; b < nb; ++b) {
+            const int nbc = bo[b + 1] - bo[b];
+            ZdfJob J{};
+            J.M = Kb[b]; J.N = nr; J.K = 3 * nbc;
+            J.A = Call + coff[b]; J.ars = 3 * nbc; J.acs = 1;
+            J.B = Fv + 3 * (size_t)bo[b]; J.brs = 1; J.bcs = 3LL * n;
+            J.C = V + koff[b]; J.crs = 1; J.ccs = npd;
+            jobs.push_back(J);
+        }
+        return zgemm_df_batched(c, jobs);
+    };
+    MIDAS_TRY(project(Einc, Vc));
     midas_gpu_info sinfo;
     memset(&sinfo, 0, sizeof(sinfo));
     DenseLU rlu;
@@ -961,12 +973,17 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
         Eout = (double2 *)peo;
     }
     auto reconstruct = [&]() -> int {
+        std::vector<ZdfJob> jobs;
         for (int b = 0; b < nb; ++b) {
             const int nbc = bo[b + 1] - bo[b];
-            MIDAS_TRY(zgemm_df(c, 3 * nbc, nr, Kb[b], Call + coff[b], 1, 3 * nbc, (const double2 *)px + koff[b], 1,
-                               npd, Eout + 3 * (size_t)bo[b], 1, 3LL * n));
+            ZdfJob J{};
+            J.M = 3 * nbc; J.N = nr; J.K = Kb[b];
+            J.A = Call + coff[b]; J.ars = 1; J.acs = 3 * nbc;
+            J.B = (const double2 *)px + koff[b]; J.brs = 1; J.bcs = npd;
+            J.C = Eout + 3 * (size_t)bo[b]; J.crs = 1; J.ccs = 3LL * n;
+            jobs.push_back(J);
         }
-        return MIDAS_OK;
+        return zgemm_df_batched(c, jobs);
     };
     MIDAS_TRY(reconstruct());
     // One correction against the FP64 reduced residual.  The reduced matrix above
@@ -980,18 +997,13 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
     if (!use_aca && lattice_fft_fits(c)) {
         const size_t nf = (size_t)3 * n * nr;
         void *pf;
-        MIDAS_TRY(ensure(c, S_CREF, sizeof(double2) * 2 * nf + sizeof(float2) * (size_t)npd * nr + 1024, &pf));
-        double2 *Ef = (double2 *)pf, *Rf = Ef + nf;
+        MIDAS_TRY(ensure(c, S_CREF, sizeof(double2) * nf + sizeof(float2) * (size_t)npd * nr + 1024, &pf));
+        double2 *Rf = (double2 *)pf;
         float2 *d32 = (float2 *)(((uintptr_t)(Rf + nf) + 255) & ~(uintptr_t)255);
-        MIDAS_TRY(launch_incident4<double2>(c, n, d_all, ntr, d_th, d_ph, Ef, 1, (size_t)3 * n));
-        MIDAS_TRY(lattice_matvec(c, nr, Eout, 3LL * n, Ef, 3LL * n, Rf, 3LL * n, S_LFFT, true));
+        MIDAS_TRY(lattice_matvec(c, nr, Eout, 3LL * n, Einc, 3LL * n, Rf, 3LL * n, S_LFFT, true));
         double2 *rho = Vc;   // Vc is no longer needed: the reduced residual takes its place
         MIDAS_CUDA(c, cudaMemsetAsync(rho, 0, sizeof(double2) * (size_t)npd * nr, c->stream));
-        for (int b = 0; b < nb; ++b) {
-            const int nbc = bo[b + 1] - bo[b];
-            MIDAS_TRY(zgemm_df(c, Kb[b], nr, 3 * nbc, Call + coff[b], 3 * nbc, 1, Rf + 3 * (size_t)bo[b], 1, 3LL * n,
-                               rho + koff[b], 1, npd));
-        }
+        MIDAS_TRY(project(Rf, rho));
         const long long tot = (long long)npd * nr;
         ++c->launches;
         k_c64_to_c32<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(tot, rho, d32);

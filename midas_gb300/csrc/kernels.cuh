@@ -38,6 +38,21 @@ int aca_run(midas_gpu_ctx *c, int row0, int nrows, int col0, int ncols, double e
 // cbfm.cu: release the CBFM lanes of a context
 void free_lanes(midas_gpu_ctx *c);
 
+// blas.cu: one product C = A B of a batched double-float complex GEMM (element (i, k)
+// of A at A[i ars + k acs], and likewise B and C); zgemm_df_batched sets kchunk, poff
+// and eoff
+struct ZdfJob {
+    int M, N, K, kchunk;
+    const double2 *A;
+    long long ars, acs;
+    const double2 *B;
+    long long brs, bcs;
+    double2 *C;
+    long long crs, ccs;
+    long long poff, eoff;
+};
+int zgemm_df_batched(midas_gpu_ctx *c, std::vector<ZdfJob> &jobs);
+
 // sparse.cu: CSR matrix (0-based, columns ascending within a row)
 struct Csr {
     int n = 0, nnz = 0;
