@@ -411,16 +411,19 @@ void free_lanes(midas_gpu_ctx *c)
 }
 
 // Auxiliary contexts of the streamed CBFM pipeline (own stream and scratch pool, the
-// cells aliased): aux[0] finishes blocks (K_b, C_b and the reduced-assembly column of
-// block b) at the lowest stream priority, aux[1 + l] runs the eigen-solves of lane l's
-// blocks at the highest (one CTA each, on the tail of the step).
+// cells aliased): aux[0 .. CBF_FINISHERS) finish blocks (K_b, C_b and the
+// reduced-assembly column of block b) at the lowest stream priority (a second stream,
+// overlapping one column's fill with another's product, measured no faster: both are
+// bandwidth-bound); aux[CBF_FINISHERS + l] runs the eigen-solves of lane l's blocks at
+// the highest (one CTA each, on the tail of the step).
+constexpr int CBF_FINISHERS = 1;
 static int get_aux(midas_gpu_ctx *c, int na)
 {
     while ((int)c->aux.size() < na) {
         midas_gpu_ctx *A = new midas_gpu_ctx;
         A->device = c->device;
         A->pool.resize(S_NSLOTS);
-        const bool finisher = c->aux.empty();
+        const bool finisher = (int)c->aux.size() < CBF_FINISHERS;
         c->aux.push_back(A);
         int least = 0, greatest = 0;
         MIDAS_CUDA(c, cudaDeviceGetStreamPriorityRange(&least, &greatest));
@@ -747,14 +750,17 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
     }
     if (streamed) {
         const int nl = std::min(nb, cbf_lanes());
-        MIDAS_TRY(get_aux(c, 1 + nl));
-        midas_gpu_ctx *F = c->aux[0];
-        for (int a = 0; a <= nl; ++a) {
+        constexpr int NF = CBF_FINISHERS;
+        const int na = NF + nl;
+        MIDAS_TRY(get_aux(c, na));
+        midas_gpu_ctx *F = c->aux[0];   // the finisher thread's error state
+        for (int a = 0; a < na; ++a) {
             lane_sync_cells(c->aux[a], c);
             c->aux[a]->allow_side = false;
         }
-        std::vector<long long> a0(nl + 1);
-        for (int a = 0; a <= nl; ++a) a0[a] = c->aux[a]->launches;
+        std::vector<long long> a0(na);
+        for (int a = 0; a < na; ++a) a0[a] = c->aux[a]->launches;
+        std::vector<int> fidx(nb, 0);   // the finisher stream of block b (C_b and its column)
         double *hW = nullptr;
         MIDAS_CUDA(c, cudaMallocHost(&hW, sizeof(double) * (size_t)m * nb));
         std::vector<cudaEvent_t> ev_gram(nb), ev_eig(nb);
@@ -767,7 +773,7 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
         std::deque<int> q;
         bool lanes_over = false;
         std::function<int(midas_gpu_ctx *, int, int)> on_done = [&](midas_gpu_ctx *L, int l, int b) -> int {
-            midas_gpu_ctx *E = c->aux[1 + l];
+            midas_gpu_ctx *E = c->aux[NF + l];
             int st = [&]() -> int {
                 MIDAS_CUDA(L, cudaEventRecord(ev_gram[b], L->stream));
                 MIDAS_CUDA(E, cudaStreamWaitEvent(E->stream, ev_gram[b], 0));
@@ -794,16 +800,32 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
         // latency-bound chains they would otherwise hold up, and then run under the
         // eigen-solves still in flight.
         int fst = MIDAS_OK;
+        // verbose: device times of the finisher's steps ('C' C_b built, 'T' column of T done)
+        std::vector<std::pair<int, cudaEvent_t>> fin_ev;
+        auto fin_mark = [&](midas_gpu_ctx *X, int tag) {
+            if (c->opts.verbose < 1) return;
+            cudaEvent_t ev;
+            cudaEventCreate(&ev);
+            cudaEventRecord(ev, X->stream);
+            fin_ev.push_back({tag, ev});
+        };
         std::thread fin([&]() {
             cudaSetDevice(F->device);
             std::vector<int> ready;
+            int nfin = 0;
             auto over = [&] {
                 std::lock_guard<std::mutex> g(qm);
                 return lanes_over;
             };
             auto flush = [&] {
-                for (int j : ready)
-                    if (fst == MIDAS_OK) fst = assemble_column(F, j);
+                for (int j : ready) {
+                    midas_gpu_ctx *X = c->aux[fidx[j]];
+                    if (fst == MIDAS_OK) {
+                        fst = assemble_column(X, j);
+                        if (fst != MIDAS_OK && X != F) F->err = X->err;
+                    }
+                    fin_mark(X, 1000 + j);
+                }
                 ready.clear();
             };
             for (int done = 0; done < nb; ++done) {
@@ -829,7 +851,11 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
                     fst = F->err.set(MIDAS_ERR_CUDA, "cbf eigen-solve: stream failed");
                     continue;
                 }
-                fst = finish_block(F, b, hW + (size_t)m * b);
+                fidx[b] = nfin++ % NF;
+                midas_gpu_ctx *X = c->aux[fidx[b]];
+                fst = finish_block(X, b, hW + (size_t)m * b);
+                if (fst != MIDAS_OK && X != F) F->err = X->err;
+                fin_mark(X, b);
                 ready.push_back(b);
                 if (over()) flush();
             }
@@ -843,22 +869,35 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
         }
         qcv.notify_one();
         fin.join();
-        cudaEvent_t ef;
-        cudaEventCreateWithFlags(&ef, cudaEventDisableTiming);
-        cudaEventRecord(ef, F->stream);
-        cudaStreamWaitEvent(c->stream, ef, 0);
-        cudaEventDestroy(ef);
-        for (int a = 1; a <= nl; ++a) cudaStreamSynchronize(c->aux[a]->stream);
+        for (int a = 0; a < NF; ++a) {
+            cudaEvent_t ef;
+            cudaEventCreateWithFlags(&ef, cudaEventDisableTiming);
+            cudaEventRecord(ef, c->aux[a]->stream);
+            cudaStreamWaitEvent(c->stream, ef, 0);
+            cudaEventDestroy(ef);
+        }
+        for (int a = NF; a < na; ++a) cudaStreamSynchronize(c->aux[a]->stream);
+        if (!fin_ev.empty()) {
+            for (int a = 0; a < NF; ++a) cudaStreamSynchronize(c->aux[a]->stream);
+            fprintf(stderr, "[midas] cbf finisher (C:block / T:block @ ms):");
+            for (auto &fe : fin_ev) {
+                float t = 0;
+                cudaEventElapsedTime(&t, e0, fe.second);
+                fprintf(stderr, " %c%d@%.0f", fe.first >= 1000 ? 'T' : 'C', fe.first % 1000, t);
+                cudaEventDestroy(fe.second);
+            }
+            fprintf(stderr, "\n");
+        }
         for (int b = 0; b < nb; ++b) {
             cudaEventDestroy(ev_gram[b]);
             cudaEventDestroy(ev_eig[b]);
         }
         cudaFreeHost(hW);
-        for (int a = 0; a <= nl; ++a) c->launches += c->aux[a]->launches - a0[a];
+        for (int a = 0; a < na; ++a) c->launches += c->aux[a]->launches - a0[a];
         MIDAS_TRY(st);
         if (fst != MIDAS_OK) return c->err.set(fst, F->err.msg);
-        for (int a = 0; a <= nl; ++a) {
-            const int fs = check_flag(c->aux[a], a ? "cbf eigen-solve" : "cbf reduced assembly");
+        for (int a = 0; a < na; ++a) {
+            const int fs = check_flag(c->aux[a], a >= NF ? "cbf eigen-solve" : "cbf reduced assembly");
             if (fs != MIDAS_OK) return c->err.set(fs, c->aux[a]->err.msg);
         }
         for (int b = 0; b < nb; ++b) ir_max = std::max(ir_max, srefine[b]);

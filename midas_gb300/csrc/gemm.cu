@@ -215,10 +215,15 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float v[32])
 // (coarser than an FMA chain) then only spans 64 products, which brings long-K
 // products with cancellation (the CBF reduced matrix) to FP32-FMA accuracy.
 // With H16 the operands are fp16 (the same 11-bit significands as TF32, half the
-// bytes, twice the MMA rate): a k-block is 64 elements, so a chunk of two
-// k-blocks spans 128 products; alpha may be read from device memory (the
-// inverse of the operands' power-of-two scales).
+// bytes, twice the MMA rate): a k-block is 64 elements, and a chunk of four
+// k-blocks spans 256 products (two k-blocks measured 16 % slower on the CBF
+// residual updates, the drain then holding up the MMA; the CBFM field error against
+// the FP64 reference stays 7.3e-8 on the 41k-cell scene); alpha may be read from
+// device memory (the inverse of the operands' power-of-two scales).
 constexpr int TC_PROMOTE_KB = 2;
+constexpr int TC_PROMOTE_KB_H16 = 4;
+constexpr int TC_H16_STAGES = 6;
+
 
 template <bool PROMOTE, int TC_STAGES, bool H16 = false>
 __global__ void __launch_bounds__(TC_THREADS, TC_STAGES == 2 ? 2 : 1)
@@ -239,7 +244,7 @@ __global__ void __launch_bounds__(TC_THREADS, TC_STAGES == 2 ? 2 : 1)
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
     const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * TC_BN;
     const int nk = (K + BKE - 1) / BKE;
-    const int KC = PROMOTE ? TC_PROMOTE_KB : (nk > 0 ? nk : 1);
+    const int KC = PROMOTE ? (H16 ? TC_PROMOTE_KB_H16 : TC_PROMOTE_KB) : (nk > 0 ? nk : 1);
     const int nchunk = (nk + KC - 1) / KC;
 
     if (threadIdx.x == 0) {
@@ -721,10 +726,12 @@ static int gemm_tc(midas_gpu_ctx *c, const GemmArgs &g, bool precise)
     if ((((uintptr_t)g.A) & 15) || (((uintptr_t)g.Bt) & 15) || (g.lda & ldm) || (g.ldb & ldm))
         return c->err.set(MIDAS_ERR_ARG, "gemm_tf32: operands must be 16-byte aligned with 16-byte row strides");
     if (g.h16 && precise) {   // fp16 operands, every k-block promoted to FP32 registers
+        // 6 stages (192 KB): the long-K split products (K = 6 x 3 n_j halves) keep the
+        // MMA warp fed while the epilogue warps promote
         static PerDeviceOnce once_h;
         MIDAS_CUDA(c, once_h.run(c->device, [] {
-            return cudaFuncSetAttribute(k_gemm_tc<true, 4, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        tc_smem(4));
+            return cudaFuncSetAttribute(k_gemm_tc<true, TC_H16_STAGES, true>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, tc_smem(TC_H16_STAGES));
         }));
         CUtensorMap ma, mb;
         MIDAS_TRY(make_map(c, &ma, g.A, g.M, g.K, g.lda, TC_BM, true));
@@ -732,8 +739,8 @@ static int gemm_tc(midas_gpu_ctx *c, const GemmArgs &g, bool precise)
         dim3 grd((g.N + TC_BN - 1) / TC_BN, (g.M + TC_BM - 1) / TC_BM);
         ++c->launches;
         int kp = kp_begin(c);
-        k_gemm_tc<true, 4, true><<<grd, TC_THREADS, tc_smem(4), c->stream>>>(ma, mb, g.M, g.N, g.K, g.D, g.ldd, g.alpha,
-                                                                             g.beta, 0, c->d_flag, g.alpha_dev);
+        k_gemm_tc<true, TC_H16_STAGES, true><<<grd, TC_THREADS, tc_smem(TC_H16_STAGES), c->stream>>>(
+            ma, mb, g.M, g.N, g.K, g.D, g.ldd, g.alpha, g.beta, 0, c->d_flag, g.alpha_dev);
         kp_end(c, kp, g.kclass, 2.0 * g.M * g.N * g.K,
                2.0 * ((double)g.M * g.K + (double)g.N * g.K) + 4.0 * (double)g.M * g.N * (g.beta != 0.f ? 2 : 1));
         MIDAS_CUDA(c, cudaGetLastError());
