@@ -435,9 +435,11 @@ static int get_aux(midas_gpu_ctx *c, int na)
 }
 
 // on_done(L, l, b), when given, runs on lane l's host thread after block b's
-// Gram matrix is enqueued on L's stream
+// Gram matrix is enqueued on L's stream; *idle, when given, counts the lanes whose
+// work has drained (no block left to take, their stream idle)
 static int cbf_generate(midas_gpu_ctx *c, int nb, const CbfShared &S,
-                        const std::function<int(midas_gpu_ctx *, int, int)> *on_done = nullptr)
+                        const std::function<int(midas_gpu_ctx *, int, int)> *on_done = nullptr,
+                        std::atomic<int> *idle = nullptr)
 {
     // with kernel-class profiling on, one lane: each launch's event interval then
     // covers that kernel alone
@@ -495,7 +497,9 @@ static int cbf_generate(midas_gpu_ctx *c, int nb, const CbfShared &S,
                         std::chrono::duration<double, std::milli>(te - t0).count());
             }
         }
-        if (cudaStreamSynchronize(L->stream) != cudaSuccess && status[l] == MIDAS_OK) {
+        const cudaError_t se = cudaStreamSynchronize(L->stream);
+        if (idle) ++*idle;
+        if (se != cudaSuccess && status[l] == MIDAS_OK) {
             status[l] = L->err.set(MIDAS_ERR_CUDA, "cbf lane: stream failed");
             fail = 1;
         }
@@ -772,6 +776,10 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
         std::condition_variable qcv;
         std::deque<int> q;
         bool lanes_over = false;
+        // the columns of T start once a lane has drained (no block left for it): the tail
+        // of the CBF generation then shares the GPU with them (measured over 12 steps:
+        // 1013 ms waiting for every lane, 1000 ms from the first drained lane)
+        std::atomic<int> lanes_idle{0};
         std::function<int(midas_gpu_ctx *, int, int)> on_done = [&](midas_gpu_ctx *L, int l, int b) -> int {
             midas_gpu_ctx *E = c->aux[NF + l];
             int st = [&]() -> int {
@@ -796,9 +804,10 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
             return MIDAS_OK;
         };
         // The finisher builds C_b as each eigen-solve ends (small products); the columns of
-        // T (full-GPU fills and products) wait for the end of the lanes, whose
-        // latency-bound chains they would otherwise hold up, and then run under the
-        // eigen-solves still in flight.
+        // T (full-GPU fills and products) wait for the tail of the lanes, whose
+        // latency-bound chains they would otherwise hold up (started with the first block
+        // they made the CBF generation 30 % slower), and then run under the eigen-solves
+        // still in flight.
         int fst = MIDAS_OK;
         // verbose: device times of the finisher's steps ('C' C_b built, 'T' column of T done)
         std::vector<std::pair<int, cudaEvent_t>> fin_ev;
@@ -814,6 +823,7 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
             std::vector<int> ready;
             int nfin = 0;
             auto over = [&] {
+                if (lanes_idle.load() > 0) return true;
                 std::lock_guard<std::mutex> g(qm);
                 return lanes_over;
             };
@@ -829,14 +839,21 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
                 ready.clear();
             };
             for (int done = 0; done < nb; ++done) {
-                int b;
-                {
-                    std::unique_lock<std::mutex> g(qm);
-                    qcv.wait(g, [&] { return !q.empty() || lanes_over; });
-                    if (q.empty()) return;   // a lane failed: the remaining blocks never come
-                    b = q.front();
-                    q.pop_front();
+                int b = -1;
+                for (;;) {
+                    {
+                        std::unique_lock<std::mutex> g(qm);
+                        qcv.wait_for(g, std::chrono::microseconds(200), [&] { return !q.empty() || lanes_over; });
+                        if (!q.empty()) {
+                            b = q.front();
+                            q.pop_front();
+                            break;
+                        }
+                        if (lanes_over) break;
+                    }
+                    if (!ready.empty() && over()) flush();
                 }
+                if (b < 0) return;   // a lane failed: the remaining blocks never come
                 if (fst != MIDAS_OK) continue;
                 // wait for block b's eigen-solve, launching the ready columns once the lanes end
                 bool bad = false;
@@ -861,7 +878,7 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
             }
             flush();
         });
-        int st = cbf_generate(c, nb, S, &on_done);
+        int st = cbf_generate(c, nb, S, &on_done, &lanes_idle);
         if (e_lanes) cudaEventRecord(e_lanes, c->stream);
         {
             std::lock_guard<std::mutex> g(qm);
