@@ -233,6 +233,43 @@ __global__ void k_split_expand_b_h16(int K, int N, const T *src, long long rs, l
     }
 }
 
+// The same split and expansion of a row-major B (element (k, j) at src[k rs + j]),
+// through a 32 x 32 tile in shared memory so that the reads (along j) and the writes
+// (along k) both coalesce.  Block (j tile, k tile), 256 threads.
+template <typename T>
+__global__ void __launch_bounds__(256) k_split_expand_b_h16_t(int K, int N, const T *src, long long rs,
+                                                              const float *sc, __half *B3, long long ldb3)
+{
+    using V = typename SplitIn<T>::V;
+    __shared__ V tile[32][33];   // [k][j]
+    const int j0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+    const int tx = threadIdx.x % 32, ty = threadIdx.x / 32;
+    for (int r = ty; r < 32; r += 8) {
+        const int k = k0 + r, j = j0 + tx;
+        V v;
+        v.x = 0; v.y = 0;
+        if (k < K && j < N) v = SplitIn<T>::ld(src, (long long)k * rs + j);
+        tile[r][tx] = v;
+    }
+    __syncthreads();
+    const float s = sc[1];
+    for (int r = ty; r < 32; r += 8) {
+        const int j = j0 + r, k = k0 + tx;
+        if (j >= N || k >= K) continue;
+        const V v = tile[tx][r];
+        __half hr, lr, hi_, li;
+        split_h16(v.x, s, hr, lr);
+        split_h16(v.y, s, hi_, li);
+        const __half nhi = __hneg(hi_), nli = __hneg(li);
+        __half *r0 = B3 + (long long)(2 * j) * ldb3, *r1 = r0 + ldb3;
+        r0[2 * k] = hr; r0[2 * k + 1] = nhi; r1[2 * k] = hi_; r1[2 * k + 1] = hr;
+        r0[2 * K + 2 * k] = lr; r0[2 * K + 2 * k + 1] = nli; r1[2 * K + 2 * k] = li; r1[2 * K + 2 * k + 1] = lr;
+        r0[4 * K + 2 * k] = hr; r0[4 * K + 2 * k + 1] = nhi; r1[4 * K + 2 * k] = hi_; r1[4 * K + 2 * k + 1] = hr;
+        if (k == K - 1)
+            for (long long p = 6LL * K; p < ldb3; ++p) { r0[p] = __float2half(0.f); r1[p] = __float2half(0.f); }
+    }
+}
+
 // A3h (fp16 hi | hi | lo rows of K6h = 6K halves rounded up to 8) of a row-major complex64
 // M x K matrix, with its scale in sc[0] (sc: 4 floats of device memory after the split)
 int zsplit_a3_h16(midas_gpu_ctx *c, int M, int K, const float2 *A, long long lda, __half *A3, long long K6h,
@@ -258,7 +295,7 @@ int zsplit_a3_h16(midas_gpu_ctx *c, int M, int K, const float2 *A, long long lda
 // multiplies by 1 / (sA sB) (sc[2]); sc[3] is scratch.
 template <typename TB>
 int zgemm_x3h_a3(midas_gpu_ctx *c, int M, int N, int K, const __half *A3h, long long K6h, float *sc, const TB *B,
-                 long long brs, long long bcs, float *D, long long ldd, int kclass)
+                 long long brs, long long bcs, float *D, long long ldd, int kclass, int promote_kb)
 {
     if (M <= 0 || N <= 0 || K <= 0) return MIDAS_OK;
     if (K6h != (6LL * K + 7) / 8 * 8) return c->err.set(MIDAS_ERR_ARG, "zgemm_x3h_a3: bad A3 stride");
@@ -270,17 +307,48 @@ int zgemm_x3h_a3(midas_gpu_ctx *c, int M, int N, int K, const __half *A3h, long 
     MIDAS_CUDA(c, cudaMemsetAsync(sc + 3, 0, sizeof(unsigned), c->stream));
     k_cabsmax<TB><<<std::min(K, 4096), 256, 0, c->stream>>>(K, N, B, brs, bcs, (unsigned *)(sc + 3));
     k_h16_scale<<<1, 1, 0, c->stream>>>((const unsigned *)(sc + 3), sc, 1);
-    k_split_expand_b_h16<TB><<<dim3((K + 127) / 128, std::min(N, 65535)), 128, 0, c->stream>>>(K, N, B, brs, bcs, sc,
-                                                                                               B3, K6h);
+    if (bcs == 1 && brs != 1)   // row-major B: the transposing split
+        k_split_expand_b_h16_t<TB><<<dim3((N + 31) / 32, (K + 31) / 32), 256, 0, c->stream>>>(K, N, B, brs, sc, B3,
+                                                                                             K6h);
+    else
+        k_split_expand_b_h16<TB><<<dim3((K + 127) / 128, std::min(N, 65535)), 128, 0, c->stream>>>(K, N, B, brs, bcs,
+                                                                                                   sc, B3, K6h);
     kp_end(c, kp, MIDAS_KC_SPLIT, 0.0, (double)sizeof(TB) * K * N + 4.0 * N * K6h);
     MIDAS_CUDA(c, cudaGetLastError());
     GemmArgs g{M, 2 * N, (int)K6h, (const float *)A3h, K6h, (const float *)B3, K6h, D, ldd, 1.f, 0.f, 0, kclass};
     g.h16 = 1;
     g.alpha_dev = sc + 2;
+    g.promote_kb = promote_kb;
     return gemm_tf32(c, g, true);
 }
 template int zgemm_x3h_a3<double2>(midas_gpu_ctx *, int, int, int, const __half *, long long, float *,
-                                   const double2 *, long long, long long, float *, long long, int);
+                                   const double2 *, long long, long long, float *, long long, int, int);
+
+// D (M x 2N floats) = A B on fp16 split pieces, both operands split here: A (M x K
+// complex, element (i, k) at A[i ars + k acs]) scaled by sc[0], B as in zgemm_x3h_a3
+template <typename TA, typename TB>
+int zgemm_x3h(midas_gpu_ctx *c, int M, int N, int K, const TA *A, long long ars, long long acs, const TB *B,
+              long long brs, long long bcs, float *D, long long ldd, int kclass, int promote_kb)
+{
+    if (M <= 0 || N <= 0 || K <= 0) return MIDAS_OK;
+    const long long K6h = (6LL * K + 7) / 8 * 8;
+    void *pa;
+    MIDAS_TRY(ensure(c, S_CBF8, sizeof(__half) * (size_t)M * K6h + 256, &pa));
+    __half *A3h = (__half *)pa;
+    float *sc = (float *)(A3h + (size_t)M * K6h);
+    ++c->launches;
+    int kp = kp_begin(c);
+    MIDAS_CUDA(c, cudaMemsetAsync(sc + 3, 0, sizeof(unsigned), c->stream));
+    k_cabsmax<TA><<<std::min(M, 4096), 256, 0, c->stream>>>(M, K, A, ars, acs, (unsigned *)(sc + 3));
+    k_h16_scale<<<1, 1, 0, c->stream>>>((const unsigned *)(sc + 3), sc, 0);
+    k_split_a_h16<TA><<<dim3((K + 127) / 128, std::min(M, 65535)), 128, 0, c->stream>>>(M, K, A, ars, acs, sc, A3h,
+                                                                                         K6h);
+    kp_end(c, kp, MIDAS_KC_SPLIT, 0.0, (double)sizeof(TA) * M * K + 2.0 * M * K6h);
+    MIDAS_CUDA(c, cudaGetLastError());
+    return zgemm_x3h_a3<TB>(c, M, N, K, A3h, K6h, sc, B, brs, bcs, D, ldd, kclass, promote_kb);
+}
+template int zgemm_x3h<double2, float2>(midas_gpu_ctx *, int, int, int, const double2 *, long long, long long,
+                                        const float2 *, long long, long long, float *, long long, int, int);
 
 // sc[0] = s (a power of two) for a split written by a kernel that knew its scale
 __global__ void k_set_scale(float *sc, float s) { sc[0] = s; }
@@ -311,7 +379,8 @@ __global__ void k_sub_rowmajor(int n, int m, const float *P, double2 *R)
 int resid_update_x3(midas_gpu_ctx *c, int n, int m, const __half *A3h, long long K6h, float *sc, const float2 *D,
                     float *P, double2 *R)
 {
-    MIDAS_TRY(zgemm_x3h_a3<float2>(c, n, m, n, A3h, K6h, sc, D, m, 1, P, 2LL * m, MIDAS_KC_RESID32));
+    // four-block chunks: the refinement's double-float residual checks the updates
+    MIDAS_TRY(zgemm_x3h_a3<float2>(c, n, m, n, A3h, K6h, sc, D, m, 1, P, 2LL * m, MIDAS_KC_RESID32, 4));
     ++c->launches;
     int kp = kp_begin(c);
     const long long tot = (long long)n * m;

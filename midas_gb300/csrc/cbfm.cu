@@ -55,8 +55,11 @@ int resid_update_x3(midas_gpu_ctx *c, int n, int m, const __half *A3h, long long
                     float *P, double2 *R);
 template <typename TB>
 int zgemm_x3h_a3(midas_gpu_ctx *c, int M, int N, int K, const __half *A3h, long long K6h, float *sc, const TB *B,
-                 long long brs, long long bcs, float *D, long long ldd, int kclass);
+                 long long brs, long long bcs, float *D, long long ldd, int kclass, int promote_kb = 2);
 int set_h16_scale(midas_gpu_ctx *c, float *sc, float s);
+template <typename TA, typename TB>
+int zgemm_x3h(midas_gpu_ctx *c, int M, int N, int K, const TA *A, long long ars, long long acs, const TB *B,
+              long long brs, long long bcs, float *D, long long ldd, int kclass, int promote_kb = 2);
 int residual_df32(midas_gpu_ctx *c, int n, int nrhs, const float2 *Z, long long ldz, const float2 *Xh,
                   const float2 *Xl, const float2 *B, double2 *R);
 int heev_dev(midas_gpu_ctx *c, int batch, int m, double2 *A, long long lda, long long sa, double2 *H, double2 *V,
@@ -654,6 +657,8 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
     double zbound = 0.0;
     MIDAS_TRY(fill4_bound(c, &zbound));
     const bool h16 = zbound > 0.0;
+    // an FFT reduced residual corrects alpha after the reduced solve (lattice cells, no ACA)
+    const bool fft_correction = !use_aca && lattice_fft_fits(c);
     const float hsA = h16 ? ldexpf(1.f, 12 - (int)std::ceil(std::log2(zbound))) : 1.f;
     // ACA of every off-diagonal pair (i, j), pair index i * (nb - 1) + (j < i ? j : j - 1)
     const int npairs = use_aca ? nb * (nb - 1) : 0;
@@ -713,7 +718,8 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
                 MIDAS_TRY(launch_block_fill4_a3(X, nr, d_all + r0, nj, d_all + bo[j], nullptr, K6h, A3h, hsA));
                 MIDAS_TRY(set_h16_scale(X, sc, hsA));
                 MIDAS_TRY(zgemm_x3h_a3<double2>(X, 3 * nr, Kb[j], 3 * nj, A3h, K6h, sc, Cj, 1, 3LL * nj,
-                                                T + (size_t)3 * r0 * ldT + tc, ldT, MIDAS_KC_GEMM_PROD));
+                                                T + (size_t)3 * r0 * ldT + tc, ldT, MIDAS_KC_GEMM_PROD,
+                                                fft_correction ? 4 : 2));
             } else {
                 const long long K6 = (6LL * 3 * nj + 3) / 4 * 4;
                 MIDAS_TRY(ensure(X, S_CBF8, sizeof(float) * (size_t)3 * nr * K6, &pa));
@@ -973,13 +979,21 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
             for (int k = 0; k < Kb[b]; ++k) colmap[koff[b] + k] = b * m + k;
         MIDAS_CUDA(c, cudaMemcpyAsync(d_colmap, colmap.data(), sizeof(int) * Kt, cudaMemcpyHostToDevice, c->stream));
     }
-    // Zc rows of block i = C_i^T T_i (FP32-grade split-TF32 products)
+    // Zc rows of block i = C_i^T T_i, FP32-grade split products.  With the lattice-table
+    // fill (the FFT reduced residual below then corrects alpha) on fp16 pieces, each
+    // operand scaled by a power of two from its largest entry; otherwise on TF32 pieces,
+    // whose exponent range keeps the small entries of T (far pairs, ACA terms) at full
+    // relative precision (fp16 pieces moved C_abs of the ACA trimer by 1.5e-6).
     for (int i = 0; i < nb; ++i) {
         const int ni = bo[i + 1] - bo[i];
         const double2 *Ci = Call + coff[i];
         const float2 *Ti = (const float2 *)(T + (size_t)3 * bo[i] * ldT);
-        MIDAS_TRY(zgemm_x3<double2, float2>(c, Kb[i], ncolp, 3 * ni, Ci, 3 * ni, 1, 0, Ti, ncolp, 1,
-                                            Zcf + (size_t)koff[i] * ldT, ldT, 1.f, 0.f));
+        if (h16 && fft_correction)
+            MIDAS_TRY(zgemm_x3h<double2, float2>(c, Kb[i], ncolp, 3 * ni, Ci, 3 * ni, 1, Ti, ncolp, 1,
+                                                 Zcf + (size_t)koff[i] * ldT, ldT, MIDAS_KC_GEMM_PROD, 4));
+        else
+            MIDAS_TRY(zgemm_x3<double2, float2>(c, Kb[i], ncolp, 3 * ni, Ci, 3 * ni, 1, 0, Ti, ncolp, 1,
+                                                Zcf + (size_t)koff[i] * ldT, ldT, 1.f, 0.f));
     }
     cudaEventRecord(e2, c->stream);
     // ---- 3. Vc, reduced solve, E -----------------------------------------------
@@ -1050,7 +1064,7 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
     // products with f_kapChe and E in FP64); alpha += Zc^-1 rho with the TF32
     // factors then leaves ~1e-3.5 of the error.  With ACA the reduced matrix is
     // itself an approximation of these blocks, so no correction is made.
-    if (!use_aca && lattice_fft_fits(c)) {
+    if (fft_correction) {
         const size_t nf = (size_t)3 * n * nr;
         void *pf;
         MIDAS_TRY(ensure(c, S_CREF, sizeof(double2) * nf + sizeof(float2) * (size_t)npd * nr + 1024, &pf));

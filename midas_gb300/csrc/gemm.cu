@@ -215,20 +215,21 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float v[32])
 // (coarser than an FMA chain) then only spans 64 products, which brings long-K
 // products with cancellation (the CBF reduced matrix) to FP32-FMA accuracy.
 // With H16 the operands are fp16 (the same 11-bit significands as TF32, half the
-// bytes, twice the MMA rate): a k-block is 64 elements, and a chunk of four
-// k-blocks spans 256 products (two k-blocks measured 16 % slower on the CBF
-// residual updates, the drain then holding up the MMA; the CBFM field error against
-// the FP64 reference stays 7.3e-8 on the 41k-cell scene); alpha may be read from
-// device memory (the inverse of the operands' power-of-two scales).
+// bytes, twice the MMA rate): a k-block is 64 elements, and the caller sets the chunk
+// (promote_kb k-blocks): two (128 products) where the product is final, four where an
+// FP64-grade correction follows (the CBF residual updates under refinement, the
+// reduced matrix before its FFT residual correction), which measured 16 % faster (the
+// drain of two-block chunks holds up the MMA); alpha may be read from device memory
+// (the inverse of the operands' power-of-two scales).
 constexpr int TC_PROMOTE_KB = 2;
-constexpr int TC_PROMOTE_KB_H16 = 4;
 constexpr int TC_H16_STAGES = 6;
 
 
 template <bool PROMOTE, int TC_STAGES, bool H16 = false>
 __global__ void __launch_bounds__(TC_THREADS, TC_STAGES == 2 ? 2 : 1)
     k_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int M, int N, int K,
-              float *D, long long ldd, float alpha, float beta, int rnd, int *gflag, const float *alpha_dev = nullptr)
+              float *D, long long ldd, float alpha, float beta, int rnd, int *gflag, const float *alpha_dev = nullptr,
+              int promote_kb = TC_PROMOTE_KB)
 {
     constexpr int BKE = H16 ? 2 * TC_BK : TC_BK;   // elements per k-block (128 bytes of a row)
     extern __shared__ uint8_t smem_raw[];
@@ -244,7 +245,7 @@ __global__ void __launch_bounds__(TC_THREADS, TC_STAGES == 2 ? 2 : 1)
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
     const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * TC_BN;
     const int nk = (K + BKE - 1) / BKE;
-    const int KC = PROMOTE ? (H16 ? TC_PROMOTE_KB_H16 : TC_PROMOTE_KB) : (nk > 0 ? nk : 1);
+    const int KC = PROMOTE ? promote_kb : (nk > 0 ? nk : 1);
     const int nchunk = (nk + KC - 1) / KC;
 
     if (threadIdx.x == 0) {
@@ -740,7 +741,8 @@ static int gemm_tc(midas_gpu_ctx *c, const GemmArgs &g, bool precise)
         ++c->launches;
         int kp = kp_begin(c);
         k_gemm_tc<true, TC_H16_STAGES, true><<<grd, TC_THREADS, tc_smem(TC_H16_STAGES), c->stream>>>(
-            ma, mb, g.M, g.N, g.K, g.D, g.ldd, g.alpha, g.beta, 0, c->d_flag, g.alpha_dev);
+            ma, mb, g.M, g.N, g.K, g.D, g.ldd, g.alpha, g.beta, 0, c->d_flag, g.alpha_dev,
+            std::max(1, std::min(g.promote_kb, 16)));
         kp_end(c, kp, g.kclass, 2.0 * g.M * g.N * g.K,
                2.0 * ((double)g.M * g.K + (double)g.N * g.K) + 4.0 * (double)g.M * g.N * (g.beta != 0.f ? 2 : 1));
         MIDAS_CUDA(c, cudaGetLastError());

@@ -103,6 +103,7 @@ struct GemmArgs {
     int kclass = MIDAS_KC_GEMM_TC;   // kernel class for the profiler
     int h16 = 0;                     // A, Bt are fp16 (__half*, ld in fp16 elements): kind::f16 MMAs
     const float *alpha_dev = nullptr;   // when set, alpha is read from device memory at launch
+    int promote_kb = 2;   // h16 precise products: k-blocks (64 products each) per FP32 promotion
 };
 bool gemm_tc_engine();   // the tcgen05 engine is selected (required for h16 operands)
 // precise = periodic promotion of the tensor-core partial sums to FP32 registers
