@@ -119,7 +119,10 @@ int csr_from_dense(midas_gpu_ctx *c, int n, const float2 *Z, long long ldz, int 
 // r = B - Z (Xh + Xl) with Z in CSR form.  Xh, Xl row-major (n rows of ldx, ldx a
 // multiple of CSR_RESID_COLS), B column-major float (ld n), r column-major FP64
 // (ld n).  A warp per row; the lanes run over CSR_RESID_COLS right-hand sides
-// (blockIdx.y selects the group), CSR_T per lane, so the per-nonzero work (the
+// (blockIdx.y selects the group: one group's X, gathered by column index, then stays
+// in L2 beside the streamed CSR entries -- with the groups of a row block side by side
+// the X of both groups thrashed L2, DRAM reads 3.8 -> 34 GB on a 15k-row block, at the
+// same issue-bound time), CSR_T per lane, so the per-nonzero work (the
 // shuffle broadcast of the column offset and the value) is shared by 6 complex
 // multiply-adds.  The products with Xh are exact (FMA TwoProduct) and summed by
 // TwoSum; the products with Xl (2^-24 smaller) are added in FP32 into the same
