@@ -414,12 +414,13 @@ def run_ours(args, wl, world, rank, local, pg):
     ms = ev0.elapsed_time(ev1)
     launches = ctx.launch_count() - l0
     phases = ctx.info.as_dict()
-    # the same steps again with per-kernel-class CUDA events around every launch
-    # (a second timed region: the events themselves cost a few % of the step)
+    # up to three of the steps again with per-kernel-class CUDA events around every
+    # launch (a second timed region: the events themselves cost a few % of the step)
+    nprof = min(args.steps, 3)
     ctx.profile(True)
     torch.cuda.synchronize()
     ev0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(nprof):
         step_resident()
     ev1.record(stream)
     ev1.synchronize()
@@ -489,7 +490,7 @@ def run_ours(args, wl, world, rank, local, pg):
                  "algorithmic_bytes_per_launch": kp["bytes"] / max(1, kp["launches"]),
                  "algorithmic_flops_per_launch": kp["flops"] / max(1, kp["launches"]),
                  "share_of_step": kp["ms"] / ms_prof if ms_prof > 0 else None, "tflops": tf_ach, "gbs": gb_ach,
-                 "profiled_ms_per_step": ms_prof / args.steps, "ncu": NCU_COUNTERS.get(top)})
+                 "profiled_ms_per_step": ms_prof / nprof, "ncu": NCU_COUNTERS.get(top)})
     if top == "diag_lu":
         roof["note"] = ("the 64 x 64 diagonal-block LUs and their inverses: one CTA per block (1 of 152 SMs), "
                         "128 barrier-separated pivot phases -- latency-bound; in the timed six-lane step their "
@@ -505,7 +506,7 @@ def run_ours(args, wl, world, rank, local, pg):
         roof["fp32_issue"] = {"achieved_ops_per_s": ops, "peak_ops_per_s": peak_ops, "frac": ops / peak_ops,
                               "ops_per_complex_mac": 44, "sm_mhz": mhz,
                               "peak_src": f"{props.multi_processor_count} SMs x 128 FP32 lanes x SM clock"}
-    classes = {k: {"ms_per_step": v["ms"] / args.steps, "launches_per_step": v["launches"] / args.steps,
+    classes = {k: {"ms_per_step": v["ms"] / nprof, "launches_per_step": v["launches"] / nprof,
                    "gbs": v["bytes"] / (v["ms"] * 1e-3) / 1e9 if v["ms"] > 0 else None,
                    "tflops": v["flops"] / (v["ms"] * 1e-3) / 1e12 if v["ms"] > 0 else None}
                for k, v in kprof.items()}
@@ -804,7 +805,8 @@ def ctypes_byref(x):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default 10; 5 for the batch workloads, whose step is ~25 s)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="cbfm_c2", choices=sorted(WORKLOADS))
@@ -814,6 +816,8 @@ def main():
     ap.add_argument("--fp64-measure", action="store_true",
                     help="time the plain FP64 MoM (cuSOLVER) on the workload itself, whatever its size")
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 5 if args.workload in ("c4", "c4_small") else 10
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     world, rank, local, pg = dist_setup(args)
