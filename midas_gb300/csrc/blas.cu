@@ -190,24 +190,42 @@ template <> struct SplitIn<double2> {
     static __device__ __forceinline__ double2 ld(const double2 *p, long long i) { return p[i]; }
 };
 
+// Rows 2j, 2j+1 of B3 for element (k, j) = (hr + lr) + i (hi + li): the real 2 x 2 form
+// [re -im; im re] of each piece, pieces [hi | lo | hi] of pw halves; the thread of the
+// last k zeroes the pieces' tails.
+__device__ __forceinline__ void h16_b3_store(__half *r0, long long ldb3, int k, int K, long long pw, __half hr,
+                                             __half hi_, __half lr, __half li)
+{
+    __half *r1 = r0 + ldb3;
+    const __half nhi = __hneg(hi_), nli = __hneg(li);
+    r0[2 * k] = hr; r0[2 * k + 1] = nhi; r1[2 * k] = hi_; r1[2 * k + 1] = hr;
+    r0[pw + 2 * k] = lr; r0[pw + 2 * k + 1] = nli; r1[pw + 2 * k] = li; r1[pw + 2 * k + 1] = lr;
+    r0[2 * pw + 2 * k] = hr; r0[2 * pw + 2 * k + 1] = nhi; r1[2 * pw + 2 * k] = hi_; r1[2 * pw + 2 * k + 1] = hr;
+    if (k == K - 1)
+        for (long long p = 2LL * K; p < pw; ++p)
+            for (int q = 0; q < 3; ++q) { r0[q * pw + p] = __float2half(0.f); r1[q * pw + p] = __float2half(0.f); }
+}
+
+// A in the two-piece layout: row i = [hi | lo], each piece 2 h16_piece(K) halves
+// (the thread of the last column zeroes the pieces' tails)
 template <typename T>
-__global__ void k_split_a_h16(int M, int K, const T *src, long long rs, long long cs, const float *sc, __half *A3,
-                              long long lda3)
+__global__ void k_split_a_h16(int M, int K, const T *src, long long rs, long long cs, const float *sc, __half *A2,
+                              long long lda2)
 {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= K) return;
     const float s = sc[0];
+    const long long pw = 2 * h16_piece(K);   // halves per piece
     for (int i = blockIdx.y; i < M; i += gridDim.y) {
         const auto v = SplitIn<T>::ld(src, (long long)i * rs + (long long)k * cs);
         __half hr, lr, hi_, li;
         split_h16(v.x, s, hr, lr);
         split_h16(v.y, s, hi_, li);
-        __half *row = A3 + (long long)i * lda3;
+        __half *row = A2 + (long long)i * lda2;
         row[2 * k] = hr; row[2 * k + 1] = hi_;
-        row[2 * K + 2 * k] = hr; row[2 * K + 2 * k + 1] = hi_;
-        row[4 * K + 2 * k] = lr; row[4 * K + 2 * k + 1] = li;
+        row[pw + 2 * k] = lr; row[pw + 2 * k + 1] = li;
         if (k == K - 1)
-            for (long long p = 6LL * K; p < lda3; ++p) row[p] = __float2half(0.f);
+            for (long long p = 2LL * K; p < pw; ++p) { row[p] = __float2half(0.f); row[pw + p] = __float2half(0.f); }
     }
 }
 
@@ -218,18 +236,13 @@ __global__ void k_split_expand_b_h16(int K, int N, const T *src, long long rs, l
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= K) return;
     const float s = sc[1];
+    const long long pw = 2 * h16_piece(K);   // halves per piece: [hi | lo | hi]
     for (int j = blockIdx.y; j < N; j += gridDim.y) {
         const auto v = SplitIn<T>::ld(src, (long long)k * rs + (long long)j * cs);
         __half hr, lr, hi_, li;
         split_h16(v.x, s, hr, lr);
         split_h16(v.y, s, hi_, li);
-        const __half nhi = __hneg(hi_), nli = __hneg(li);
-        __half *r0 = B3 + (long long)(2 * j) * ldb3, *r1 = r0 + ldb3;
-        r0[2 * k] = hr; r0[2 * k + 1] = nhi; r1[2 * k] = hi_; r1[2 * k + 1] = hr;
-        r0[2 * K + 2 * k] = lr; r0[2 * K + 2 * k + 1] = nli; r1[2 * K + 2 * k] = li; r1[2 * K + 2 * k + 1] = lr;
-        r0[4 * K + 2 * k] = hr; r0[4 * K + 2 * k + 1] = nhi; r1[4 * K + 2 * k] = hi_; r1[4 * K + 2 * k + 1] = hr;
-        if (k == K - 1)
-            for (long long p = 6LL * K; p < ldb3; ++p) { r0[p] = __float2half(0.f); r1[p] = __float2half(0.f); }
+        h16_b3_store(B3 + (long long)(2 * j) * ldb3, ldb3, k, K, pw, hr, hi_, lr, li);
     }
 }
 
@@ -260,23 +273,17 @@ __global__ void __launch_bounds__(256) k_split_expand_b_h16_t(int K, int N, cons
         __half hr, lr, hi_, li;
         split_h16(v.x, s, hr, lr);
         split_h16(v.y, s, hi_, li);
-        const __half nhi = __hneg(hi_), nli = __hneg(li);
-        __half *r0 = B3 + (long long)(2 * j) * ldb3, *r1 = r0 + ldb3;
-        r0[2 * k] = hr; r0[2 * k + 1] = nhi; r1[2 * k] = hi_; r1[2 * k + 1] = hr;
-        r0[2 * K + 2 * k] = lr; r0[2 * K + 2 * k + 1] = nli; r1[2 * K + 2 * k] = li; r1[2 * K + 2 * k + 1] = lr;
-        r0[4 * K + 2 * k] = hr; r0[4 * K + 2 * k + 1] = nhi; r1[4 * K + 2 * k] = hi_; r1[4 * K + 2 * k + 1] = hr;
-        if (k == K - 1)
-            for (long long p = 6LL * K; p < ldb3; ++p) { r0[p] = __float2half(0.f); r1[p] = __float2half(0.f); }
+        h16_b3_store(B3 + (long long)(2 * j) * ldb3, ldb3, k, K, 2 * h16_piece(K), hr, hi_, lr, li);
     }
 }
 
-// A3h (fp16 hi | hi | lo rows of K6h = 6K halves rounded up to 8) of a row-major complex64
-// M x K matrix, with its scale in sc[0] (sc: 4 floats of device memory after the split)
+// A3h (fp16 [hi | lo] rows of K6h = h16_arow(K) halves) of a row-major complex64 M x K
+// matrix, with its scale in sc[0] (sc: 4 floats of device memory after the split)
 int zsplit_a3_h16(midas_gpu_ctx *c, int M, int K, const float2 *A, long long lda, __half *A3, long long K6h,
                   float *sc)
 {
     if (M <= 0 || K <= 0) return MIDAS_OK;
-    if (K6h != (6LL * K + 7) / 8 * 8) return c->err.set(MIDAS_ERR_ARG, "zsplit_a3_h16: bad A3 stride");
+    if (K6h != h16_arow(K)) return c->err.set(MIDAS_ERR_ARG, "zsplit_a3_h16: bad A row stride");
     ++c->launches;
     int kp = kp_begin(c);
     MIDAS_CUDA(c, cudaMemsetAsync(sc + 3, 0, sizeof(unsigned), c->stream));
@@ -290,17 +297,19 @@ int zsplit_a3_h16(midas_gpu_ctx *c, int M, int K, const float2 *A, long long lda
 }
 
 // D (M x 2N floats, row-major, ld ldd) = A B with A given as its fp16 split A3h
-// (M rows of K6h = 6K halves rounded up to 8, scale sA in sc[0]) and B (K x N complex, element
-// (k, j) at B[k brs + j bcs]): B is scaled (sc[1]) and split here, the GEMM
-// multiplies by 1 / (sA sB) (sc[2]); sc[3] is scratch.
+// (M rows of K6h = h16_arow(K) halves: the [hi | lo] pieces, scale sA in sc[0]) and B
+// (K x N complex, element (k, j) at B[k brs + j bcs]): B is scaled (sc[1]) and split here
+// into [hi | lo | hi] rows, the GEMM reads A's hi piece twice and multiplies by
+// 1 / (sA sB) (sc[2]); sc[3] is scratch.
 template <typename TB>
 int zgemm_x3h_a3(midas_gpu_ctx *c, int M, int N, int K, const __half *A3h, long long K6h, float *sc, const TB *B,
                  long long brs, long long bcs, float *D, long long ldd, int kclass, int promote_kb)
 {
     if (M <= 0 || N <= 0 || K <= 0) return MIDAS_OK;
-    if (K6h != (6LL * K + 7) / 8 * 8) return c->err.set(MIDAS_ERR_ARG, "zgemm_x3h_a3: bad A3 stride");
+    if (K6h != h16_arow(K)) return c->err.set(MIDAS_ERR_ARG, "zgemm_x3h_a3: bad A row stride");
+    const long long KB = h16_brow(K);   // halves per B3 row, the GEMM's K
     void *pb;
-    MIDAS_TRY(ensure(c, S_CBF9, sizeof(__half) * (size_t)2 * N * K6h + 256, &pb));
+    MIDAS_TRY(ensure(c, S_CBF9, sizeof(__half) * (size_t)2 * N * KB + 256, &pb));
     __half *B3 = (__half *)pb;
     ++c->launches;
     int kp = kp_begin(c);
@@ -309,16 +318,17 @@ int zgemm_x3h_a3(midas_gpu_ctx *c, int M, int N, int K, const __half *A3h, long 
     k_h16_scale<<<1, 1, 0, c->stream>>>((const unsigned *)(sc + 3), sc, 1);
     if (bcs == 1 && brs != 1)   // row-major B: the transposing split
         k_split_expand_b_h16_t<TB><<<dim3((N + 31) / 32, (K + 31) / 32), 256, 0, c->stream>>>(K, N, B, brs, sc, B3,
-                                                                                             K6h);
+                                                                                             KB);
     else
         k_split_expand_b_h16<TB><<<dim3((K + 127) / 128, std::min(N, 65535)), 128, 0, c->stream>>>(K, N, B, brs, bcs,
-                                                                                                   sc, B3, K6h);
-    kp_end(c, kp, MIDAS_KC_SPLIT, 0.0, (double)sizeof(TB) * K * N + 4.0 * N * K6h);
+                                                                                                   sc, B3, KB);
+    kp_end(c, kp, MIDAS_KC_SPLIT, 0.0, (double)sizeof(TB) * K * N + 4.0 * N * KB);
     MIDAS_CUDA(c, cudaGetLastError());
-    GemmArgs g{M, 2 * N, (int)K6h, (const float *)A3h, K6h, (const float *)B3, K6h, D, ldd, 1.f, 0.f, 0, kclass};
+    GemmArgs g{M, 2 * N, (int)KB, (const float *)A3h, K6h, (const float *)B3, KB, D, ldd, 1.f, 0.f, 0, kclass};
     g.h16 = 1;
     g.alpha_dev = sc + 2;
     g.promote_kb = promote_kb;
+    g.a_piece = 2 * h16_piece(K);
     return gemm_tf32(c, g, true);
 }
 template int zgemm_x3h_a3<double2>(midas_gpu_ctx *, int, int, int, const __half *, long long, float *,
@@ -331,7 +341,7 @@ int zgemm_x3h(midas_gpu_ctx *c, int M, int N, int K, const TA *A, long long ars,
               long long brs, long long bcs, float *D, long long ldd, int kclass, int promote_kb)
 {
     if (M <= 0 || N <= 0 || K <= 0) return MIDAS_OK;
-    const long long K6h = (6LL * K + 7) / 8 * 8;
+    const long long K6h = h16_arow(K);
     void *pa;
     MIDAS_TRY(ensure(c, S_CBF8, sizeof(__half) * (size_t)M * K6h + 256, &pa));
     __half *A3h = (__half *)pa;

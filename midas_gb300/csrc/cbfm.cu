@@ -260,7 +260,7 @@ static int cbf_block(midas_gpu_ctx *c, const CbfShared &S, int b)
         Csr zcsr;
         __half *A3z = nullptr;
         float *A3sc = nullptr;   // the split's scales (4 floats after it)
-        const long long K6z = 6LL * sp;
+        const long long K6z = h16_arow(sp);
         if (sr) {
             MIDAS_TRY(csr_from_dense(c, sp, Zlu, sp, S_CSR, &zcsr));
             MIDAS_TRY(ensure(c, S_CBF2, sizeof(__half) * (size_t)sp * (size_t)K6z + 256, &p2));
@@ -711,7 +711,7 @@ int cbfm_run(midas_gpu_ctx *c, int nb, const int *blk_offsets, const int *ext_of
             const int r0 = bo[i], nr = bo[i1] - bo[i];
             void *pa;
             if (h16) {
-                const long long K6h = (6LL * 3 * nj + 7) / 8 * 8;
+                const long long K6h = h16_arow(3LL * nj);
                 MIDAS_TRY(ensure(X, S_CBF8, sizeof(__half) * (size_t)3 * nr * K6h + 256, &pa));
                 __half *A3h = (__half *)pa;
                 float *sc = (float *)(A3h + (size_t)3 * nr * K6h);

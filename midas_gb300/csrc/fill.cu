@@ -366,7 +366,9 @@ __global__ void k_block_fill4(int n1, const int *idx1, int n2, const int *idx2, 
 // row r of A3 holds (hi | hi | lo) of the complex(4) entries Z(r, 0..K), hi =
 // TF32(z), lo = TF32(z - hi) (the layout zgemm_x3 builds), so the complex(4)
 // block is never stored on its own.  Entries are those of mode 0 of
-// k_block_fill4; the padding columns 6K..lda3 of each row are zeroed.
+// k_block_fill4; the padding columns 6K..lda3 of each row are zeroed.  With A3h
+// the row is the fp16 [hi | lo] operand of the fp16 split product (pieces of
+// h16_piece(K) complex entries, their tails zeroed).
 // ---------------------------------------------------------------------------
 template <bool LAT>
 __global__ void k_block_fill4_a3(int n1, const int *idx1, int n2, const int *idx2, const double *x, const double *y,
@@ -438,10 +440,8 @@ __global__ void k_block_fill4_a3(int n1, const int *idx1, int n2, const int *idx
         const float2 h = sh[rr][cc];
         if (A3h) {
             __half2 *row = (__half2 *)(A3h + (3LL * io0 + rr) * lda3);
-            const __half2 hh = __floats2half2_rn(h.x, h.y);
-            row[kc0 + cc] = hh;
-            row[K + kc0 + cc] = hh;
-            row[2 * K + kc0 + cc] = __floats2half2_rn(sl[rr][cc].x, sl[rr][cc].y);
+            row[kc0 + cc] = __floats2half2_rn(h.x, h.y);
+            row[h16_piece(K) + kc0 + cc] = __floats2half2_rn(sl[rr][cc].x, sl[rr][cc].y);
         } else {
             float2 *row = (float2 *)(A3 + (3LL * io0 + rr) * lda3);
             row[kc0 + cc] = h;
@@ -452,8 +452,12 @@ __global__ void k_block_fill4_a3(int n1, const int *idx1, int n2, const int *idx
     if (js0 + 64 >= n2)   // the CTA holding the last columns zeroes the row padding
         for (int t = threadIdx.y * blockDim.x + threadIdx.x; t < nrow; t += blockDim.x * blockDim.y) {
             if (A3h) {
-                __half *row = A3h + (3LL * io0 + t) * lda3;
-                for (long long pad = 6 * K; pad < lda3; ++pad) row[pad] = __float2half(0.f);
+                __half2 *row = (__half2 *)(A3h + (3LL * io0 + t) * lda3);
+                const long long P = h16_piece(K);
+                for (long long pad = K; pad < P; ++pad) {
+                    row[pad] = __floats2half2_rn(0.f, 0.f);
+                    row[P + pad] = __floats2half2_rn(0.f, 0.f);
+                }
             } else {
                 float *row = A3 + (3LL * io0 + t) * lda3;
                 for (long long pad = 6 * K; pad < lda3; ++pad) row[pad] = 0.f;
@@ -685,6 +689,7 @@ int launch_block_fill4(midas_gpu_ctx *c, int n1, const int *idx1, int n2, const 
 int launch_block_fill4_a3(midas_gpu_ctx *c, int n1, const int *idx1, int n2, const int *idx2, float *A3,
                           long long lda3, __half *A3h, float hscale)
 {
+    if (A3h && lda3 != h16_arow(3LL * n2)) return c->err.set(MIDAS_ERR_ARG, "block fill: bad fp16 operand stride");
     dim3 blk(64, 2);
     dim3 grd((n2 + 63) / 64, (n1 + 1) / 2);
     Lat l = make_lat(c);

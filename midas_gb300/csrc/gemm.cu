@@ -229,7 +229,7 @@ template <bool PROMOTE, int TC_STAGES, bool H16 = false>
 __global__ void __launch_bounds__(TC_THREADS, TC_STAGES == 2 ? 2 : 1)
     k_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int M, int N, int K,
               float *D, long long ldd, float alpha, float beta, int rnd, int *gflag, const float *alpha_dev = nullptr,
-              int promote_kb = TC_PROMOTE_KB)
+              int promote_kb = TC_PROMOTE_KB, int a_piece = 0)
 {
     constexpr int BKE = H16 ? 2 * TC_BK : TC_BK;   // elements per k-block (128 bytes of a row)
     extern __shared__ uint8_t smem_raw[];
@@ -276,8 +276,11 @@ __global__ void __launch_bounds__(TC_THREADS, TC_STAGES == 2 ? 2 : 1)
                 uint8_t *sa = smem + s * TC_STAGE_BYTES;
                 uint8_t *sb = sa + TC_A_BYTES;
                 mbar_arrive_tx(&full[s], TC_STAGE_BYTES);
-                tma_load_2d(sa, &tmA, &full[s], kb * BKE, m0);
-                tma_load_2d(sb, &tmB, &full[s], kb * BKE, n0);
+                // two-piece A ([hi | lo], a_piece elements each): k >= a_piece reads A at k - a_piece,
+                // so the hi piece serves the first two thirds of K (a_piece is a multiple of BKE)
+                const int ka = kb * BKE;
+                tma_load_2d(sa, &tmA, &full[s], (a_piece && ka >= a_piece) ? ka - a_piece : ka, m0);
+                tma_load_2d(sb, &tmB, &full[s], ka, n0);
             }
         }
     } else if (warp == 1) {
@@ -734,15 +737,17 @@ static int gemm_tc(midas_gpu_ctx *c, const GemmArgs &g, bool precise)
             return cudaFuncSetAttribute(k_gemm_tc<true, TC_H16_STAGES, true>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize, tc_smem(TC_H16_STAGES));
         }));
+        if (g.a_piece && (g.a_piece % (2 * TC_BK) || 3LL * g.a_piece != g.K))
+            return c->err.set(MIDAS_ERR_ARG, "gemm_tf32: two-piece A needs K = 3 pieces of whole k-blocks");
         CUtensorMap ma, mb;
-        MIDAS_TRY(make_map(c, &ma, g.A, g.M, g.K, g.lda, TC_BM, true));
+        MIDAS_TRY(make_map(c, &ma, g.A, g.M, g.a_piece ? (int)(2 * g.a_piece) : g.K, g.lda, TC_BM, true));
         MIDAS_TRY(make_map(c, &mb, g.Bt, g.N, g.K, g.ldb, TC_BN, true));
         dim3 grd((g.N + TC_BN - 1) / TC_BN, (g.M + TC_BM - 1) / TC_BM);
         ++c->launches;
         int kp = kp_begin(c);
         k_gemm_tc<true, TC_H16_STAGES, true><<<grd, TC_THREADS, tc_smem(TC_H16_STAGES), c->stream>>>(
             ma, mb, g.M, g.N, g.K, g.D, g.ldd, g.alpha, g.beta, 0, c->d_flag, g.alpha_dev,
-            std::max(1, std::min(g.promote_kb, 16)));
+            std::max(1, std::min(g.promote_kb, 16)), (int)g.a_piece);
         kp_end(c, kp, g.kclass, 2.0 * g.M * g.N * g.K,
                2.0 * ((double)g.M * g.K + (double)g.N * g.K) + 4.0 * (double)g.M * g.N * (g.beta != 0.f ? 2 : 1));
         MIDAS_CUDA(c, cudaGetLastError());

@@ -82,7 +82,8 @@ int launch_incident_sph(midas_gpu_ctx *c, int ncell, const int *idx, int ntr, co
 template <typename T>
 int launch_block_fill4(midas_gpu_ctx *c, int n1, const int *idx1, int n2, const int *idx2, int mode, double thr,
                        int homog, T *out, size_t rs, size_t cs);
-// Z(idx1 rows, idx2 cols) (mode 0) written as the split-TF32 A operand (hi | hi | lo)
+// Z(idx1 rows, idx2 cols) (mode 0) written as the split-TF32 A operand (hi | hi | lo), or
+// with A3h as the fp16 [hi | lo] operand (lda3 = h16_arow(3 n2) halves, pieces scaled by hscale)
 int launch_block_fill4_a3(midas_gpu_ctx *c, int n1, const int *idx1, int n2, const int *idx2, float *A3,
                           long long lda3, __half *A3h = nullptr, float hscale = 1.f);
 // upper bound of |Z| over the lattice-table fill (0 when the fill is direct)
@@ -104,7 +105,17 @@ struct GemmArgs {
     int h16 = 0;                     // A, Bt are fp16 (__half*, ld in fp16 elements): kind::f16 MMAs
     const float *alpha_dev = nullptr;   // when set, alpha is read from device memory at launch
     int promote_kb = 2;   // h16 precise products: k-blocks (64 products each) per FP32 promotion
+    long long a_piece = 0;   // h16 precise products: A is [hi | lo] of a_piece elements each, K = 3 a_piece
 };
+
+// fp16 split operands.  A row of the A operand holds the hi piece, then the lo piece, of
+// its K complex entries (re, im interleaved), each piece h16_piece(K) complex entries (a
+// multiple of 32, so that a piece is whole 64-half k-blocks; the tail is zero).  B3 rows
+// hold [hi | lo | hi] pieces of the same width, and the GEMM reads A's hi piece twice:
+// hi.hi + hi.lo + lo.hi.
+__host__ __device__ inline long long h16_piece(long long K) { return (K + 31) / 32 * 32; }
+__host__ __device__ inline long long h16_arow(long long K) { return 4 * h16_piece(K); }   // halves per A row
+__host__ __device__ inline long long h16_brow(long long K) { return 6 * h16_piece(K); }   // halves per B3 row: the GEMM's K
 bool gemm_tc_engine();   // the tcgen05 engine is selected (required for h16 operands)
 // precise = periodic promotion of the tensor-core partial sums to FP32 registers
 int gemm_tf32(midas_gpu_ctx *c, const GemmArgs &g, bool precise = false);
