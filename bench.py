@@ -94,14 +94,15 @@ class ClockSampler:
 
 # ncu counters of the kernel that leads the CBFM step: ncu --set full --clock-control none
 # of the double-float CSR residual on the 15k-unknown extended block of the Gaussian sphere
-# at a/d = 16 (56.7 M nonzeros, 380 right-hand sides, one lane: the regime of the benchmark
+# at a/d = 16 (113 M nonzeros, 380 right-hand sides, one lane: the regime of the benchmark
 # scene's largest blocks).  Traffic is dram__bytes_read.sum + dram__bytes_write.sum per
 # algorithmic byte of the launch (3.94 GB measured against 1.00 GB algorithmic: X rows come
 # back from DRAM while the CSR values stream through L2).
 NCU_COUNTERS = {
     "resid": {"kernel": "k_resid_csr_df32", "issue_active_pct": 79.4, "fma_pipe_pct": 71.3, "dram_pct": 0.85,
-              "l2_hit_pct": 99.1, "instructions_per_complex_mac": 99, "note": "FP32-issue bound (double-float "
-              "arithmetic on the CUDA cores, 44 FP32 operations per complex multiply-add); X rows served by L2"},
+              "l2_hit_pct": 99.1, "instructions_per_complex_mac": 49, "note": "FP32-issue bound (double-float "
+              "arithmetic on the CUDA cores: 44 FP32 operations per complex multiply-add, 32 FADD + 8 FFMA + 4 FMUL "
+              "by the opcode counters, 90 % of the issued instructions); X rows served by L2"},
 }
 NCU_TRAFFIC_PER_ALG_BYTE = {"resid": 3.94}
 
