@@ -494,7 +494,7 @@ def run_ours(args, wl, world, rank, local, pg):
                  "profiled_ms_per_step": ms_prof / nprof, "ncu": NCU_COUNTERS.get(top)})
     if top == "diag_lu":
         roof["note"] = ("the 64 x 64 diagonal-block LUs and their inverses: one CTA per block (1 of 152 SMs), "
-                        "128 barrier-separated pivot phases -- latency-bound; in the timed six-lane step their "
+                        "128 barrier-separated pivot phases -- latency-bound; in the timed seven-lane step their "
                         "launches overlap the other lanes' throughput-bound kernels")
     if top == "resid":
         # The double-float CSR residual is bound by FP32 instruction issue, not by HBM: its

@@ -350,7 +350,9 @@ static int cbf_block(midas_gpu_ctx *c, const CbfShared &S, int b)
 // refinement) then overlap the bandwidth-bound parts of another.  The lanes
 // live as long as the context.
 // ---------------------------------------------------------------------------
-constexpr int CBF_LANES = 6;   // default (measured best of 1-8 on GB300); MIDAS_CBFM_LANES (1..16) overrides
+// default lanes; MIDAS_CBFM_LANES (1..16) overrides.  Measured on the 41k-cell scene with the
+// eigen-solves streamed (12-step means): 5 lanes 1026 ms, 6 989-1000 ms, 7 962-973 ms, 8 964 ms
+constexpr int CBF_LANES = 7;
 
 static int cbf_lanes()
 {
